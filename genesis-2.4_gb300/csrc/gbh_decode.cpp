@@ -1,0 +1,600 @@
+// gbh_decode.cpp -- turns the reference hsolve arrays into per-neuron
+// micro-programs.
+//
+// ops[] is walked exactly like do_chip_hh4_update walks it
+// (genesis/src/hines/hines_chip.c:157-600): one compartment per
+// FCOMPT/COMPT sentinel, chip[] and givals[] consumed sequentially. Every
+// chip value a compartment reads becomes a field row of its neuron; the
+// sequential state the reference carries from one compartment to the next
+// (the Ek of a CHAN_OP, the selected conc of a CONC_VAL_OP) is resolved here
+// into explicit operands, so the device sees self-contained programs.
+//
+// funcs[] is executed symbolically, as do_euler_hsolve runs it
+// (hines_solve.c:223-296), to recover each row's parent and the three
+// off-diagonal coefficients it uses, in the order the reference applies them.
+#include "gbh_decode.h"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+
+namespace gbh {
+
+namespace {
+
+struct Ctx {
+    const gbh_batch_desc *d;
+    gbh_error *err;
+    int solver;
+};
+
+int fail(Ctx &c, int code, int row, int opcode, int64_t pos, const char *fmt, ...)
+    __attribute__((format(printf, 6, 7)));
+
+int fail(Ctx &c, int code, int row, int opcode, int64_t pos, const char *fmt, ...)
+{
+    if (c.err) {
+        c.err->code = code;
+        c.err->solver = c.solver;
+        c.err->row = row;
+        c.err->opcode = opcode;
+        c.err->position = (int)pos;
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c.err->message, sizeof(c.err->message), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+// Per-neuron builder helpers ------------------------------------------------
+struct NB {
+    Neuron *n;
+    std::unordered_map<int64_t, int> chip_field, cchip_field, giv_row, pool_row, int_row;
+    std::map<double, int> const_field;
+    int fld(int kind, int64_t idx, double val, bool state = false)
+    {
+        std::unordered_map<int64_t, int> *m = nullptr;
+        if (kind == FS_CHIP) m = &chip_field;
+        else if (kind == FS_CCHIP) m = &cchip_field;
+        if (m) {
+            auto it = m->find(idx);
+            if (it != m->end()) {
+                if (state) n->fsrc[it->second].state = true;
+                return it->second;
+            }
+        }
+        int f = (int)n->fsrc.size();
+        n->fsrc.push_back({kind, idx, state});
+        n->fval.push_back(val);
+        if (m) (*m)[idx] = f;
+        return f;
+    }
+    int cfield(double v)
+    {
+        auto it = const_field.find(v);
+        if (it != const_field.end()) return it->second;
+        int f = fld(FS_CONST, -1, v);
+        const_field[v] = f;
+        return f;
+    }
+    int giv(int64_t gi)
+    {
+        auto it = giv_row.find(gi);
+        if (it != giv_row.end()) return it->second;
+        int g = (int)n->giv_ref.size();
+        n->giv_ref.push_back(gi);
+        giv_row[gi] = g;
+        return g;
+    }
+    // three consecutive givals rows starting at gi
+    int giv3(int64_t gi)
+    {
+        int g = giv(gi);
+        giv(gi + 1);
+        giv(gi + 2);
+        return g;
+    }
+    int pool(int k)
+    {
+        auto it = pool_row.find(k);
+        if (it != pool_row.end()) return it->second;
+        int p = (int)n->pool_conc.size();
+        n->pool_conc.push_back(k);
+        pool_row[k] = p;
+        return p;
+    }
+    int introw(int opidx, int val)
+    {
+        auto it = int_row.find(opidx);
+        if (it != int_row.end()) return it->second;
+        int r = (int)n->iops.size();
+        n->iops.push_back(opidx);
+        n->ival.push_back(val);
+        int_row[opidx] = r;
+        return r;
+    }
+};
+
+// Symbolic execution of funcs[] (asymmetric compartments).
+int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra, int n,
+                std::vector<int> &parent, std::vector<double> &A, std::vector<double> &B,
+                std::vector<double> &Cc)
+{
+    parent.assign(n, -1);
+    A.assign(n, 0.0);
+    B.assign(n, 0.0);
+    Cc.assign(n, 0.0);
+    std::vector<int> fcount(n, 0), bcount(n, 0), lastkid(n, -1);
+    int64_t fi = 0, ri = 0;
+    if (n == 1) return GBH_OK;
+    if (nf < 1) return fail(c, GBH_ERR_FUNCS, -1, 0, 0, "empty funcs[] for %d compartments", n);
+    int cur = 1;
+    for (;;) {
+        if (fi >= nf) return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "funcs[] ends inside the forward pass");
+        const int op = f[fi++];
+        if (op == F_ELIM) {
+            if (fi >= nf || ri + 2 > nra)
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi, "truncated FORWARD_ELIM");
+            const int kid = f[fi++] / 2;
+            if (kid < 0 || kid >= cur || cur >= n)
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "FORWARD_ELIM row %d not below %d", kid, cur);
+            if (parent[kid] != -1 || fcount[kid])
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "row %d eliminated twice", kid);
+            if (kid <= lastkid[cur])
+                return fail(c, GBH_ERR_UNSUPPORTED, cur, op, fi - 1,
+                            "children of row %d are not in ascending row order", cur);
+            lastkid[cur] = kid;
+            parent[kid] = cur;
+            A[kid] = ra[ri++];
+            B[kid] = ra[ri++];
+            fcount[kid]++;
+        } else if (op == F_SET_DIAG) {
+            cur += 1;
+        } else if (op == F_SKIP_DIAG) {
+            cur += 2;
+        } else if (op == F_FINISH) {
+            break;
+        } else {
+            return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1,
+                        "funcs token %d (symmetric-compartment elimination) is not implemented", op);
+        }
+        if (cur >= n) return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "forward cursor past the last row");
+    }
+    if (cur != n - 1)
+        return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "forward pass ends at row %d, expected %d", cur, n - 1);
+    cur = n - 2;
+    for (;;) {
+        if (fi >= nf) return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "funcs[] ends inside the backward pass");
+        const int op = f[fi++];
+        if (op == F_ELIM) {
+            if (fi >= nf || ri + 1 > nra) return fail(c, GBH_ERR_FUNCS, cur, op, fi, "truncated BACKWARD_ELIM");
+            const int p = f[fi++] / 2;
+            if (cur < 0 || p != parent[cur] || bcount[cur])
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "BACKWARD_ELIM of row %d does not match its parent", cur);
+            Cc[cur] = ra[ri++];
+            bcount[cur]++;
+        } else if (op == F_CALC) {
+            if (cur < 0) return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "CALC_RESULTS below row 0");
+            if (parent[cur] >= 0 && !bcount[cur])
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "row %d solved before its parent term", cur);
+            cur -= 1;
+        } else if (op == F_FINISH) {
+            break;
+        } else {
+            return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1,
+                        "funcs token %d (symmetric-compartment elimination) is not implemented", op);
+        }
+    }
+    if (cur != -1) return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "backward pass stops at row %d", cur);
+    return GBH_OK;
+}
+
+}  // namespace
+
+int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
+{
+    Ctx c{d, err, -1};
+    if (!d || d->abi_version != GBH_ABI_VERSION)
+        return fail(c, GBH_ERR_ARG, -1, 0, -1, "descriptor missing or ABI version mismatch");
+    if (d->nsolvers <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "no solvers");
+    out.neurons.clear();
+    out.solver_first_neuron.assign(d->nsolvers + 1, 0);
+    for (int si = 0; si < d->nsolvers; ++si) {
+        c.solver = si;
+        out.solver_first_neuron[si] = (int)out.neurons.size();
+        const int *ops = d->ops + d->ops_start[si];
+        const int64_t nops = d->ops_start[si + 1] - d->ops_start[si];
+        const double *chip = d->chip + d->chip_start[si];
+        const int64_t nchip = d->chip_start[si + 1] - d->chip_start[si];
+        const int n = (int)(d->vm_start[si + 1] - d->vm_start[si]);
+        const double *giv = d->givals + d->givals_start[si];
+        const int64_t ngiv = d->givals_start[si + 1] - d->givals_start[si];
+        const int method = d->method[si], cm = d->chanmode[si], calc = d->calcmode[si];
+        const int ts = d->table_set ? d->table_set[si] : 0;
+        if (n <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "solver without compartments");
+        if (cm != 4 && cm != 5) return fail(c, GBH_ERR_UNSUPPORTED, -1, cm, -1, "chanmode %d (engine runs 4 and 5)", cm);
+        if (ts < 0 || ts >= d->ntables) return fail(c, GBH_ERR_ARG, -1, 0, -1, "table set %d out of range", ts);
+
+        // elimination structure
+        std::vector<int> parent;
+        std::vector<double> A, B, Cc;
+        int rc = parse_funcs(c, d->funcs + d->funcs_start[si], d->funcs_start[si + 1] - d->funcs_start[si],
+                             d->ravals + d->ravals_start[si], d->ravals_start[si + 1] - d->ravals_start[si],
+                             n, parent, A, B, Cc);
+        if (rc) return rc;
+        // trees: parents always have higher rows (Hines numbering)
+        std::vector<int> tree(n, -1);
+        std::vector<int> tmin, tmax;
+        for (int r = n - 1; r >= 0; --r) {
+            if (parent[r] < 0) {
+                tree[r] = (int)tmin.size();
+                tmin.push_back(r);
+                tmax.push_back(r);
+            } else {
+                if (parent[r] <= r) return fail(c, GBH_ERR_FUNCS, r, 0, -1, "parent row not above child");
+                tree[r] = tree[parent[r]];
+                if (r < tmin[tree[r]]) tmin[tree[r]] = r;
+            }
+        }
+        const int ntrees = (int)tmin.size();
+        std::vector<int> cnt(ntrees, 0);
+        for (int r = 0; r < n; ++r) cnt[tree[r]]++;
+        // neurons in ascending row order
+        std::vector<int> order(ntrees);
+        for (int t = 0; t < ntrees; ++t) {
+            if (tmax[t] - tmin[t] + 1 != cnt[t])
+                return fail(c, GBH_ERR_UNSUPPORTED, tmin[t], 0, -1, "tree rows are not contiguous");
+            order[ntrees - 1 - t] = t;  // trees were found from the top row down
+        }
+        std::vector<int> tree_neuron(ntrees);
+        const int nbase = (int)out.neurons.size();
+        for (int k = 0; k < ntrees; ++k) {
+            Neuron nn;
+            nn.solver = si;
+            nn.row0 = tmin[order[k]];
+            nn.nrows = cnt[order[k]];
+            nn.table_set = ts;
+            nn.crank = method == 11;
+            nn.c5 = cm == 5;
+            nn.interp = calc != 0;
+            for (int r = nn.row0; r < nn.row0 + nn.nrows; ++r) {
+                nn.parent.push_back(parent[r] < 0 ? -1 : parent[r] - nn.row0);
+                nn.A.push_back(A[r]);
+                nn.B.push_back(B[r]);
+                nn.C.push_back(Cc[r]);
+            }
+            tree_neuron[order[k]] = nbase + k;
+            out.neurons.push_back(std::move(nn));
+        }
+        std::vector<NB> nbs(ntrees);
+        for (int k = 0; k < ntrees; ++k) nbs[k].n = &out.neurons[nbase + k];
+
+        // ---- walk ops[] ----
+        int64_t o = 0, ch = 0, g = 1;   // givals[0] is unused
+        int row = 0;
+        // sequential state carried by the reference between compartments
+        int ek_kind = 0;         // 0 none, 1 static chip index, 2 dynamic in row ek_row
+        int64_t ek_chip = -1;
+        int ek_row = -1;
+        int sel = -1, sel_row = -1;
+        bool doghk = false;
+        auto need = [&](int64_t k) { return o + k <= nops; };
+        while (true) {
+            if (o >= nops) return fail(c, GBH_ERR_OPCODE, row, 0, o, "ops[] ends without LCOMPT_OP");
+            const int sentinel = ops[o++];
+            if (sentinel == R_LCOMPT) break;
+            if (sentinel != R_COMPT && sentinel != R_FCOMPT)
+                return fail(c, GBH_ERR_OPCODE, row, sentinel, o - 1, "expected a compartment sentinel, found %d", sentinel);
+            if (row >= n) return fail(c, GBH_ERR_OPCODE, row, sentinel, o - 1, "more compartments in ops[] than rows");
+            NB &nb = nbs[tree_neuron[tree[row]] - nbase];
+            Neuron &N = *nb.n;
+            const int nrow0 = tree_neuron[tree[row]];
+            std::vector<int> &P = N.prog;
+            if (ch + 2 > nchip || g + 2 > ngiv) return fail(c, GBH_ERR_ARG, row, 0, o, "chip[]/givals[] too short");
+            P.push_back(M_BEGIN);
+            P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+            P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+            P.push_back(nb.fld(FS_GIV, g, giv[g]));
+            P.push_back(nb.giv(g + 1));
+            ch += 2;
+            g += 2;
+            auto sel_pool = [&](int64_t at) -> int {
+                if (sel < 0 || tree[sel_row] != tree[row]) {
+                    fail(c, GBH_ERR_UNSUPPORTED, row, ops[at], at,
+                         "conc selected in another neuron (CONC_VAL_OP missing)");
+                    return -1;
+                }
+                return nb.pool(sel);
+            };
+            while (o < nops && ops[o] > R_LCOMPT) {
+                const int code = ops[o++];
+                bool current = false;
+                switch (code) {
+                case R_NEWVOLT:
+                    P.push_back(M_NEWVOLT);
+                    break;
+                case R_CONC_VAL: {
+                    if (!need(1)) return fail(c, GBH_ERR_OPCODE, row, code, o, "truncated CONC_VAL_OP");
+                    const int k = ops[o++];
+                    const int64_t nconc = d->conc_start[si + 1] - d->conc_start[si];
+                    if (k < 0 || k >= nconc) return fail(c, GBH_ERR_ARG, row, code, o - 1, "conc index %d out of range", k);
+                    sel = k;
+                    sel_row = row;
+                    P.push_back(M_CONCVAL);
+                    P.push_back(nb.pool(k));
+                    break;
+                }
+                case R_DOMAIN:
+                    P.push_back(M_DOMAIN);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    ch++;
+                    break;
+                case R_NEWCONC2: {
+                    const int k = ops[o++];
+                    P.push_back(M_NEWCONC2);
+                    P.push_back(nb.pool(k));
+                    break;
+                }
+                case R_NEWCONC1: {
+                    int p = sel_pool(o - 1);
+                    if (p < 0) return GBH_ERR_UNSUPPORTED;
+                    P.push_back(M_NEWCONC1);
+                    break;
+                }
+                case R_SPIKE: {
+                    if (!need(2)) return fail(c, GBH_ERR_OPCODE, row, code, o, "truncated SPIKE_OP");
+                    if (N.spike_op >= 0)
+                        return fail(c, GBH_ERR_UNSUPPORTED, row, code, o - 1, "second spikegen in one neuron");
+                    N.spike_op = (int)(o - 1);
+                    P.push_back(M_SPIKE);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    P.push_back(nb.introw((int)o, ops[o]));
+                    P.push_back(nb.introw((int)o + 1, ops[o + 1]));
+                    o += 2;
+                    ch++;
+                    break;
+                }
+                case R_ELMMPUMP: {
+                    int p = sel_pool(o - 1);
+                    if (p < 0) return GBH_ERR_UNSUPPORTED;
+                    P.push_back(M_ELMMPUMP);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+                    P.push_back(nb.fld(FS_CHIP, ch + 2, chip[ch + 2]));
+                    P.push_back(nb.giv(g));
+                    ch += 3;
+                    g += 1;
+                    break;
+                }
+                case R_FLUX: {
+                    int p = sel_pool(o - 1);
+                    if (p < 0) return GBH_ERR_UNSUPPORTED;
+                    P.push_back(M_FLUX);
+                    break;
+                }
+                case R_SCALE_FLUX: {
+                    int p = sel_pool(o - 1);
+                    if (p < 0) return GBH_ERR_UNSUPPORTED;
+                    P.push_back(M_SCALE_FLUX);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    ch++;
+                    break;
+                }
+                case R_STORE_ALLI:
+                case R_STORE_ALLC:
+                    return fail(c, GBH_ERR_UNSUPPORTED, row, code, o - 1,
+                                "storemode (itotal accumulation) is not supported by the engine");
+                case R_GHK:
+                case R_NERNST: {
+                    int p = sel_pool(o - 1);
+                    if (p < 0) return GBH_ERR_UNSUPPORTED;
+                    if (nb.pool(sel + 1) != p + 1)
+                        return fail(c, GBH_ERR_UNSUPPORTED, row, code, o - 1, "Cin/Cout pools not adjacent");
+                    if (code == R_GHK) {
+                        P.push_back(M_GHK);
+                        P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                        P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+                        P.push_back(nb.fld(FS_CHIP, ch + 2, chip[ch + 2]));
+                        ch += 3;
+                    } else {
+                        P.push_back(M_NERNST);
+                        P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                        P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+                        ch += 2;
+                    }
+                    ek_kind = 2;
+                    ek_row = row;
+                    current = true;
+                    break;
+                }
+                case R_SAME_GHK:
+                    P.push_back(M_SAME_GHK);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    ch++;
+                    current = true;
+                    break;
+                case R_DO_TABGHK:
+                    P.push_back(M_DO_TABGHK);
+                    doghk = true;
+                    current = true;
+                    break;
+                case R_CHAN_EK:
+                    P.push_back(M_CHAN);
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+                    ek_kind = 1;
+                    ek_chip = ch;
+                    ch += 2;
+                    current = true;
+                    break;
+                case R_CHAN:
+                    if (ek_kind == 2 && ek_row == row) {
+                        P.push_back(M_CHAN_G);
+                    } else if (ek_kind == 1) {
+                        P.push_back(M_CHAN);
+                        P.push_back(nb.fld(FS_CHIP, ek_chip, d->chip[d->chip_start[si] + ek_chip]));
+                    } else if (ek_kind == 0) {
+                        P.push_back(M_CHAN);
+                        P.push_back(nb.cfield(0.0));
+                    } else {
+                        return fail(c, GBH_ERR_UNSUPPORTED, row, code, o - 1,
+                                    "CHAN_OP uses an Ek computed in another compartment");
+                    }
+                    P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                    ch++;
+                    current = true;
+                    break;
+                default:
+                    return fail(c, GBH_ERR_OPCODE, row, code, o - 1, "ops[] opcode %d is not implemented", code);
+                }
+                if (!current) continue;
+                // conductance sub-program (hines_chip.c:412-590)
+                for (;;) {
+                    if (o >= nops) return fail(c, GBH_ERR_OPCODE, row, 0, o, "ops[] ends inside a channel");
+                    const int k = ops[o++];
+                    if (k == R_IPOL1V || k == R_IPOL1C || k == R_IPOL2V || k == R_IPOL2C) {
+                        if (!need(2)) return fail(c, GBH_ERR_OPCODE, row, k, o, "truncated gate op");
+                        const int kind = k == R_IPOL1V ? GK_1V : k == R_IPOL1C ? GK_1C : k == R_IPOL2V ? GK_2V : GK_2C;
+                        const int col = ops[o++];
+                        const int pw = ops[o++];
+                        if (pw > 6 || pw < -6)
+                            return fail(c, GBH_ERR_OPCODE, row, k, o - 1, "gate power %d outside -6..6", pw);
+                        if ((kind == GK_1C || kind == GK_2C) && sel < 0 && kind == GK_1C) {
+                            // C1 cursor comes from NEWCONC1/DOMAIN; nothing to check here
+                        }
+                        P.push_back(M_GATE);
+                        P.push_back(kind);
+                        P.push_back(col);
+                        P.push_back(pw);
+                        if (pw == 0) {
+                            P.push_back(-1);
+                            ek_kind = 2;
+                            ek_row = row;
+                            if (doghk) {
+                                doghk = false;
+                                break;
+                            }
+                            P.push_back(M_ADDCURR);
+                            P.push_back(nb.giv3(g));
+                            g += 3;
+                            break;
+                        }
+                        P.push_back(nb.fld(FS_CHIP, ch, chip[ch], true));
+                        ch++;
+                        continue;
+                    } else if (k >= R_SYN2) {
+                        if (k != R_SYN2 && k != R_SYN3)
+                            return fail(c, GBH_ERR_OPCODE, row, k, o - 1, "conductance opcode %d is not implemented", k);
+                        if (!need(3)) return fail(c, GBH_ERR_OPCODE, row, k, o, "truncated SYN op");
+                        int ffreq = -1;
+                        if (k == R_SYN3) {
+                            ffreq = nb.fld(FS_CHIP, ch, chip[ch]);
+                            ch++;
+                        }
+                        const int stab = ops[o];
+                        const int64_t nstab = d->stab_start[si + 1] - d->stab_start[si];
+                        if (stab < 0 || stab + 4 > nstab)
+                            return fail(c, GBH_ERR_ARG, row, k, o, "stablist index %d out of range", stab);
+                        const int srow = (int)N.syn_op.size();
+                        N.syn_op.push_back((int)(o - 1));
+                        P.push_back(M_SYN);
+                        P.push_back(ffreq);
+                        P.push_back((int)(d->stab_start[si] + stab));
+                        P.push_back(srow);
+                        P.push_back(nb.fld(FS_CHIP, ch, chip[ch], true));
+                        P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1], true));
+                        P.push_back(nb.fld(FS_WDT, srow, 0.0));
+                        ch += 2;
+                        o += 3;
+                        if (o < nops && ops[o] == R_MGBLOCK) {
+                            o++;
+                            P.push_back(M_MGBLOCK);
+                            P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                            P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+                            P.push_back(nb.fld(FS_CHIP, ch + 2, chip[ch + 2]));
+                            P.push_back(nb.giv3(g));
+                            ch += 3;
+                            g += 3;
+                        }
+                        P.push_back(M_ADDCURR);
+                        P.push_back(nb.giv3(g));
+                        g += 3;
+                        break;
+                    } else if (k == R_ADD_CURR) {
+                        P.push_back(M_ADDCURR);
+                        P.push_back(nb.giv3(g));
+                        g += 3;
+                        break;
+                    } else {
+                        return fail(c, GBH_ERR_OPCODE, row, k, o - 1, "conductance opcode %d is not implemented", k);
+                    }
+                }
+            }
+            if (ch + 2 > nchip || g + 1 > ngiv) return fail(c, GBH_ERR_ARG, row, 0, o, "chip[]/givals[] too short");
+            P.push_back(M_END);
+            P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+            P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
+            P.push_back(nb.giv(g));
+            ch += 2;
+            g += 1;
+            (void)nrow0;
+            row++;
+        }
+        if (row != n) return fail(c, GBH_ERR_OPCODE, row, 0, o, "ops[] has %d compartments for %d rows", row, n);
+
+        // ---- concops (hines_conc_chip.c:79-219) ----
+        {
+            const int *cops = d->concops + d->concops_start[si];
+            const int64_t ncops = d->concops_start[si + 1] - d->concops_start[si];
+            const int64_t ccbase = d->concchip_start[si];
+            int64_t co = 0, cc = 0;
+            std::vector<int> pool_owner(d->conc_start[si + 1] - d->conc_start[si], -1);
+            for (int k = 0; k < ntrees; ++k)
+                for (int pc : nbs[k].n->pool_conc) pool_owner[pc] = k;
+            while (co < ncops) {
+                const int op = cops[co++];
+                if (op == R_LCACONC) break;
+                if (op == R_CACONC) {
+                    const int k = cops[co++];
+                    if (k < 0 || k >= (int)pool_owner.size())
+                        return fail(c, GBH_ERR_ARG, -1, op, co - 1, "conc index %d out of range", k);
+                    if (pool_owner[k] < 0)
+                        return fail(c, GBH_ERR_UNSUPPORTED, -1, op, co - 1,
+                                    "Ca pool %d is not used by any compartment program", k);
+                    NB &nb = nbs[pool_owner[k]];
+                    std::vector<int> &PP = nb.n->pool_prog;
+                    PP.push_back(PO_CACONC);
+                    PP.push_back(nb.pool(k));
+                    PP.push_back(nb.fld(FS_CCHIP, cc, d->concchip[ccbase + cc]));
+                    PP.push_back(nb.fld(FS_CCHIP, cc + 1, d->concchip[ccbase + cc + 1]));
+                    PP.push_back(nb.fld(FS_CCHIP, cc + 2, d->concchip[ccbase + cc + 2]));
+                    cc += 3;
+                } else {
+                    return fail(c, GBH_ERR_OPCODE, -1, op, co - 1,
+                                "concops opcode %d (diffusion shells, pumps, buffers) is not implemented", op);
+                }
+            }
+        }
+        for (int k = 0; k < ntrees; ++k) {
+            Neuron &N = *nbs[k].n;
+            N.pool_prog.push_back(0);
+            // grouping key: everything the kernel's control flow depends on
+            std::string key;
+            auto put = [&](int v) { key.append(reinterpret_cast<const char *>(&v), sizeof(int)); };
+            put(N.nrows); put(N.table_set); put(N.crank); put(N.c5); put(N.interp);
+            put((int)N.fsrc.size()); put((int)N.iops.size()); put((int)N.pool_conc.size());
+            put((int)N.giv_ref.size()); put((int)N.syn_op.size()); put(N.spike_op >= 0);
+            put((int)N.prog.size());
+            for (int v : N.prog) put(v);
+            for (int v : N.pool_prog) put(v);
+            N.key = std::move(key);
+        }
+    }
+    out.solver_first_neuron[d->nsolvers] = (int)out.neurons.size();
+    return GBH_OK;
+}
+
+}  // namespace gbh

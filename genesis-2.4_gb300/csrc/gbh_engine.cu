@@ -1,0 +1,704 @@
+// gbh_engine.cu -- the GB300 hsolve engine: tile layout, device memory,
+// launches, and the C ABI declared in include/gbhsolve.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "gbh_decode.h"
+#include "gbh_kernels.cuh"
+#include "gbhsolve.h"
+
+using namespace gbh;
+
+namespace {
+
+thread_local char g_last_error[320] = "no error";
+
+void set_last(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            set_last("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return GBH_ERR_CUDA;                                                          \
+        }                                                                                 \
+    } while (0)
+
+template <typename T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        n = count;
+        if (count == 0) count = 1;
+        if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+            set_last("cudaMalloc of %zu bytes failed", count * sizeof(T));
+            return GBH_ERR_CUDA;
+        }
+        return GBH_OK;
+    }
+    int upload(const std::vector<T> &h)
+    {
+        if (alloc(h.size())) return GBH_ERR_CUDA;
+        if (!h.empty()) CK(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return GBH_OK;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+struct Launch {
+    int tile0, tile1, smax, warps;
+};
+
+}  // namespace
+
+struct gbh_engine {
+    gbh_options opt{};
+    int device = 0;
+    int nsolvers = 0;
+    double dt = 0.0;
+    Decoded dec;
+    std::vector<TileType> types;
+    std::vector<Tile> tiles;
+    std::vector<int> neuron_tile, neuron_lane;   // placement of every neuron
+    std::vector<int64_t> chip_start, conc_start, ops_start, vm_start, giv_start;
+    std::vector<double> chip_orig;              // reference chip[] for sync copies
+    std::vector<int> ops_orig;
+    int64_t ngiv_total = 0;
+    // device buffers
+    DBuf<Tile> d_tiles;
+    DBuf<TileType> d_types;
+    DBuf<int> d_prog;
+    DBuf<TableGeom> d_tgeom;
+    DBuf<double> d_tab64, d_xy;
+    DBuf<float> d_tab32;
+    DBuf<double> d_P, d_V, d_C, d_F, d_A, d_B, d_Cb, d_giv, d_stab;
+    DBuf<int> d_I, d_par;
+    DBuf<unsigned> d_ring;
+    DBuf<int64_t> d_out_start, d_out_base;
+    DBuf<int> d_out_delay;
+    DBuf<unsigned long long> d_spikes;
+    DBuf<int> d_status;
+    int ring_len = 2;
+    int64_t rows_fld = 0, rows_int = 0, rows_pool = 0, rows_giv = 0, rows_vm = 0, rows_topo = 0,
+            rows_syn = 0;
+    std::vector<Launch> launches;
+    int steps_per_launch = 1;
+    bool has_network = false;
+    bool givals_enabled = false;
+    bool givals_valid = false;
+    long long step = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    gbh_stats stats{};
+};
+
+namespace {
+
+int fail_err(gbh_error *err, int code, const char *fmt, ...)
+{
+    char buf[256];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (err) {
+        err->code = code;
+        err->solver = err->row = -1;
+        err->opcode = 0;
+        err->position = -1;
+        snprintf(err->message, sizeof(err->message), "%s", buf);
+    }
+    set_last("%s", buf);
+    return code;
+}
+
+// Shared-memory budget per block for the elimination columns.
+constexpr int kSmemPerBlock = 96 * 1024;
+
+int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn, gbh_error *err)
+{
+    Decoded &dec = e->dec;
+    const int nneu = (int)dec.neurons.size();
+    // ---- group neurons by program signature ----
+    std::map<std::string, int> type_of_key;
+    std::vector<std::vector<int>> members;
+    std::vector<int> prog_pool;
+    for (int i = 0; i < nneu; ++i) {
+        auto it = type_of_key.find(dec.neurons[i].key);
+        if (it == type_of_key.end()) {
+            const Neuron &N = dec.neurons[i];
+            TileType tt{};
+            tt.nslots = N.nrows;
+            tt.nfields = (int)N.fsrc.size();
+            tt.nints = (int)N.iops.size();
+            tt.npools = (int)N.pool_conc.size();
+            tt.ngiv = (int)N.giv_ref.size();
+            tt.prog_off = (int)prog_pool.size();
+            prog_pool.insert(prog_pool.end(), N.prog.begin(), N.prog.end());
+            tt.pool_off = (int)prog_pool.size();
+            prog_pool.insert(prog_pool.end(), N.pool_prog.begin(), N.pool_prog.end());
+            tt.table_set = N.table_set;
+            tt.crank = N.crank;
+            tt.chanmode5 = N.c5;
+            tt.interp = N.interp;
+            tt.has_spike = N.spike_op >= 0;
+            tt.nsyn = (int)N.syn_op.size();
+            type_of_key[N.key] = (int)e->types.size();
+            e->types.push_back(tt);
+            members.emplace_back();
+            it = type_of_key.find(N.key);
+        }
+        members[it->second].push_back(i);
+    }
+    // ---- event ring length from the synapse delays ----
+    e->has_network = syn && syn->nsynapses > 0;
+    int maxd = 1;
+    if (e->has_network) {
+        for (int64_t s = 0; s < syn->nsynapses; ++s) {
+            if (syn->delay_steps[s] < 1)
+                return fail_err(err, GBH_ERR_UNSUPPORTED, "synapse %lld has a delay below one step",
+                                (long long)s);
+            maxd = std::max(maxd, syn->delay_steps[s] + 1);
+        }
+    }
+    e->ring_len = maxd + 1;
+    // ---- tiles: types ordered by slot count (descending) ----
+    std::vector<int> torder(e->types.size());
+    for (size_t i = 0; i < torder.size(); ++i) torder[i] = (int)i;
+    std::stable_sort(torder.begin(), torder.end(),
+                     [&](int a, int b) { return e->types[a].nslots > e->types[b].nslots; });
+    e->neuron_tile.assign(nneu, -1);
+    e->neuron_lane.assign(nneu, -1);
+    int64_t gneuron = 0;
+    for (int ti : torder) {
+        const TileType &tt = e->types[ti];
+        const std::vector<int> &m = members[ti];
+        for (size_t k = 0; k < m.size(); k += LANES) {
+            Tile t{};
+            t.type = ti;
+            t.nlanes = (int)std::min<size_t>(LANES, m.size() - k);
+            t.fld = e->rows_fld; e->rows_fld += tt.nfields;
+            t.ints = e->rows_int; e->rows_int += tt.nints;
+            t.pools = e->rows_pool; e->rows_pool += tt.npools;
+            t.giv = e->rows_giv; e->rows_giv += tt.ngiv;
+            t.vm = e->rows_vm; e->rows_vm += tt.nslots;
+            t.topo = e->rows_topo; e->rows_topo += tt.nslots;
+            t.syn = e->rows_syn; e->rows_syn += (int64_t)tt.nsyn * e->ring_len;
+            t.first_neuron = gneuron;
+            gneuron += LANES;
+            for (int l = 0; l < t.nlanes; ++l) {
+                e->neuron_tile[m[k + l]] = (int)e->tiles.size();
+                e->neuron_lane[m[k + l]] = l;
+            }
+            e->tiles.push_back(t);
+        }
+    }
+    // ---- host images of the device arrays ----
+    const size_t L = LANES;
+    std::vector<double> P(e->rows_fld * L, 0.0), V(e->rows_vm * L, 0.0), C(e->rows_pool * L, 0.0),
+        A(e->rows_topo * L, 0.0), B(e->rows_topo * L, 0.0), Cb(e->rows_topo * L, 0.0);
+    std::vector<int> I(e->rows_int * L, 0), par(e->rows_topo * L, -1);
+    // padding lanes: a passive row that solves to zero and never spikes
+    for (const Tile &t : e->tiles) {
+        const TileType &tt = e->types[t.type];
+        for (int l = t.nlanes; l < LANES; ++l) {
+            for (int f = 0; f < tt.nfields; ++f) P[(t.fld + f) * L + l] = 1.0;
+            for (int s = 0; s < tt.nslots; ++s) V[(t.vm + s) * L + l] = 0.0;
+        }
+    }
+    // synapse weights per synchan (must be uniform per target synchan)
+    std::unordered_map<int64_t, double> wdt;  // key: global neuron * 4096 + syn row
+    for (int i = 0; i < nneu; ++i) {
+        const Neuron &N = dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        const int64_t vbase = d->vm_start[N.solver] + N.row0;
+        for (int s = 0; s < N.nrows; ++s) {
+            V[(t.vm + s) * L + l] = d->vm[vbase + s];
+            par[(t.topo + s) * L + l] = N.parent[s];
+            A[(t.topo + s) * L + l] = N.A[s];
+            B[(t.topo + s) * L + l] = N.B[s];
+            Cb[(t.topo + s) * L + l] = N.C[s];
+        }
+        for (size_t f = 0; f < N.fsrc.size(); ++f) P[(t.fld + f) * L + l] = N.fval[f];
+        for (size_t r = 0; r < N.iops.size(); ++r) I[(t.ints + r) * L + l] = N.ival[r];
+        for (size_t p = 0; p < N.pool_conc.size(); ++p)
+            C[(t.pools + p) * L + l] = d->conc[d->conc_start[N.solver] + N.pool_conc[p]];
+    }
+    // ---- synapses: CSR over global neuron index ----
+    std::vector<int64_t> out_start(gneuron + 1, 0), out_base;
+    std::vector<int> out_delay;
+    if (e->has_network) {
+        // synchan lookup: (solver, op) -> (neuron, syn row)
+        std::unordered_map<int64_t, std::pair<int, int>> syn_at;
+        for (int i = 0; i < nneu; ++i) {
+            const Neuron &N = dec.neurons[i];
+            for (size_t r = 0; r < N.syn_op.size(); ++r)
+                syn_at[(int64_t)N.solver * (1LL << 32) + N.syn_op[r]] = {i, (int)r};
+        }
+        std::vector<int> src_neuron(e->nsolvers, -1);
+        for (int i = 0; i < nneu; ++i)
+            if (dec.neurons[i].spike_op >= 0) src_neuron[dec.neurons[i].solver] = i;
+        std::vector<std::vector<std::pair<int64_t, int>>> per(gneuron);
+        std::unordered_map<int64_t, double> wset;
+        for (int s = 0; s < e->nsolvers; ++s) {
+            for (int64_t k = syn->src_start[s]; k < syn->src_start[s + 1]; ++k) {
+                if (src_neuron[s] < 0)
+                    return fail_err(err, GBH_ERR_ARG, "synapse %lld leaves solver %d, which has no spikegen",
+                                    (long long)k, s);
+                const int ts = syn->target_solver[k];
+                if (ts < 0 || ts >= e->nsolvers)
+                    return fail_err(err, GBH_ERR_ARG, "synapse %lld targets solver %d", (long long)k, ts);
+                auto it = syn_at.find((int64_t)ts * (1LL << 32) + syn->target_op[k]);
+                if (it == syn_at.end())
+                    return fail_err(err, GBH_ERR_ARG, "synapse %lld: ops[%d] of solver %d is not a SYN2/SYN3 op",
+                                    (long long)k, syn->target_op[k], ts);
+                const int tn = it->second.first, srow = it->second.second;
+                const double w = syn->weight[k] / e->dt;
+                const int64_t wkey = (int64_t)tn * 4096 + srow;
+                auto wi = wset.find(wkey);
+                if (wi == wset.end()) wset[wkey] = w;
+                else if (wi->second != w)
+                    return fail_err(err, GBH_ERR_UNSUPPORTED,
+                                    "synapses into one synchan (solver %d, ops[%d]) carry different weights", ts,
+                                    syn->target_op[k]);
+                const Neuron &SN = dec.neurons[src_neuron[s]];
+                int dl = syn->delay_steps[k];
+                // a target whose SYN2 op runs before the source's SPIKE op in the
+                // same step sees the event one step later (the countdown of this
+                // step is already spent)
+                if (ts < s || (ts == s && syn->target_op[k] < SN.spike_op)) dl += 1;
+                const Tile &tt = e->tiles[e->neuron_tile[tn]];
+                const int64_t base = (tt.syn + (int64_t)srow * e->ring_len) * LANES + e->neuron_lane[tn];
+                const int64_t gsrc = e->tiles[e->neuron_tile[src_neuron[s]]].first_neuron +
+                                     e->neuron_lane[src_neuron[s]];
+                per[gsrc].push_back({base, dl});
+            }
+        }
+        for (int64_t g = 0; g < gneuron; ++g) {
+            out_start[g + 1] = out_start[g] + (int64_t)per[g].size();
+            for (auto &pr : per[g]) {
+                out_base.push_back(pr.first);
+                out_delay.push_back(pr.second);
+            }
+        }
+        for (auto &kv : wset) {
+            const int tn = (int)(kv.first / 4096), srow = (int)(kv.first % 4096);
+            const Neuron &N = dec.neurons[tn];
+            const Tile &t = e->tiles[e->neuron_tile[tn]];
+            for (size_t f = 0; f < N.fsrc.size(); ++f)
+                if (N.fsrc[f].kind == FS_WDT && N.fsrc[f].idx == srow)
+                    P[(t.fld + f) * L + e->neuron_lane[tn]] = kv.second;
+        }
+    }
+    // ---- tables ----
+    std::vector<TableGeom> tg(d->ntables);
+    std::vector<double> tab64, xy;
+    std::vector<float> tab32;
+    for (int k = 0; k < d->ntables; ++k) {
+        const gbh_tables &T = d->tables[k];
+        TableGeom g{};
+        g.ncols = T.ncols;
+        g.xdivs = T.xdivs;
+        g.ydivs = T.ydivs;
+        g.xmin = T.xmin;
+        g.invdx = T.invdx;
+        g.ymin = T.ymin;
+        g.invdy = T.invdy;
+        g.tab_off = (int64_t)tab64.size();
+        const int64_t rows = T.ncols ? (int64_t)T.xdivs + 1 : 0;
+        for (int64_t r = 0; r < rows; ++r)
+            for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(T.tablist[r * T.ncols + cc]);
+        // one padding row: the clamped top row reads row xdivs+1
+        for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(rows ? T.tablist[(rows - 1) * T.ncols + cc] : 0.0);
+        g.xv_off = (int64_t)xy.size();
+        for (int64_t r = 0; r < rows; ++r) xy.push_back(T.xvals[r]);
+        xy.push_back(rows ? T.xvals[rows - 1] : 0.0);   // empty top bracket: always relocate
+        xy.push_back(0.0);
+        g.yv_off = -1;
+        if (T.ydivs > 0 && T.yvals) {
+            g.yv_off = (int64_t)xy.size();
+            for (int r = 0; r <= T.ydivs; ++r) xy.push_back(T.yvals[r]);
+            xy.push_back(T.yvals[T.ydivs]);
+            xy.push_back(0.0);
+        }
+        tg[k] = g;
+    }
+    tab32.resize(tab64.size());
+    for (size_t i = 0; i < tab64.size(); ++i) tab32[i] = (float)tab64[i];
+    std::vector<double> stab(d->stablist, d->stablist + d->stab_start[d->nsolvers]);
+
+    // ---- upload ----
+    int rc = 0;
+    rc |= e->d_tiles.upload(e->tiles);
+    rc |= e->d_types.upload(e->types);
+    rc |= e->d_prog.upload(prog_pool);
+    rc |= e->d_tgeom.upload(tg);
+    rc |= e->d_tab64.upload(tab64);
+    rc |= e->d_tab32.upload(tab32);
+    rc |= e->d_xy.upload(xy);
+    rc |= e->d_P.upload(P);
+    rc |= e->d_V.upload(V);
+    rc |= e->d_C.upload(C);
+    rc |= e->d_F.upload(std::vector<double>(C.size(), 0.0));
+    rc |= e->d_A.upload(A);
+    rc |= e->d_B.upload(B);
+    rc |= e->d_Cb.upload(Cb);
+    rc |= e->d_I.upload(I);
+    rc |= e->d_par.upload(par);
+    rc |= e->d_giv.upload(std::vector<double>(e->rows_giv * L, 0.0));
+    rc |= e->d_stab.upload(stab);
+    rc |= e->d_ring.upload(std::vector<unsigned>(e->rows_syn * L, 0u));
+    rc |= e->d_out_start.upload(out_start);
+    rc |= e->d_out_base.upload(out_base);
+    rc |= e->d_out_delay.upload(out_delay);
+    rc |= e->d_spikes.upload(std::vector<unsigned long long>(gneuron + 1, 0ULL));
+    rc |= e->d_status.upload(std::vector<int>(1, 0));
+    if (rc) return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
+
+    // ---- launch plan: consecutive tiles bucketed by slot count ----
+    size_t t0 = 0;
+    while (t0 < e->tiles.size()) {
+        const int smax = e->types[e->tiles[t0].type].nslots;
+        // bucket: tiles whose slot count is above half of smax
+        size_t t1 = t0;
+        while (t1 < e->tiles.size() && e->types[e->tiles[t1].type].nslots * 2 > smax) ++t1;
+        const int per_warp = 2 * smax * LANES * (int)sizeof(double);
+        int warps = e->opt.warps_per_block > 0 ? e->opt.warps_per_block : 4;
+        warps = std::max(1, std::min(warps, kSmemPerBlock / per_warp));
+        if (per_warp > 200 * 1024)
+            return fail_err(err, GBH_ERR_UNSUPPORTED, "neuron with %d compartments exceeds the shared-memory sweep",
+                            smax);
+        e->launches.push_back({(int)t0, (int)t1, smax, warps});
+        t0 = t1;
+    }
+    return GBH_OK;
+}
+
+DevView view_of(gbh_engine *e)
+{
+    DevView v{};
+    v.tiles = e->d_tiles.p;
+    v.types = e->d_types.p;
+    v.prog = e->d_prog.p;
+    v.tgeom = e->d_tgeom.p;
+    v.tab64 = e->d_tab64.p;
+    v.tab32 = e->d_tab32.p;
+    v.xyvals = e->d_xy.p;
+    v.P = e->d_P.p;
+    v.I = e->d_I.p;
+    v.V = e->d_V.p;
+    v.C = e->d_C.p;
+    v.F = e->d_F.p;
+    v.parent = e->d_par.p;
+    v.A = e->d_A.p;
+    v.B = e->d_B.p;
+    v.Cb = e->d_Cb.p;
+    v.giv = e->d_giv.p;
+    v.ring = e->d_ring.p;
+    v.ring_len = e->ring_len;
+    v.syn_out_start = e->d_out_start.p;
+    v.syn_out_base = e->d_out_base.p;
+    v.syn_out_delay = e->d_out_delay.p;
+    v.spikes = e->d_spikes.p;
+    v.stablist = e->d_stab.p;
+    v.status = e->d_status.p;
+    v.dt = e->dt;
+    return v;
+}
+
+int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long long step, bool mixed,
+               bool giv, cudaStream_t st)
+{
+    cudaError_t ce = mixed ? launch_mixed(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st)
+                           : launch_fp64(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st);
+    if (ce != cudaSuccess) {
+        set_last("kernel launch failed: %s", cudaGetErrorString(ce));
+        return GBH_ERR_CUDA;
+    }
+    e->stats.launches++;
+    return GBH_OK;
+}
+
+int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
+{
+    const DevView v = view_of(e);
+    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+    int done = 0;
+    while (done < nsteps) {
+        int k = std::min(e->steps_per_launch, nsteps - done);
+        const bool last = done + k == nsteps;
+        const bool giv = e->givals_enabled && last;
+        if (giv && k > 1) k -= 1;  // the recorded step runs on its own
+        const bool giv_now = giv && done + k == nsteps;
+        for (const Launch &L : e->launches) {
+            const int rc = launch_one(e, v, L, k, e->step, mixed, giv_now, st);
+            if (rc) return rc;
+        }
+        e->step += k;
+        done += k;
+    }
+    if (e->givals_enabled) e->givals_valid = true;
+    return GBH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gbh_last_error(void) { return g_last_error; }
+
+int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons, int64_t *n_types)
+{
+    gbh_error local{};
+    if (!err) err = &local;
+    memset(err, 0, sizeof(*err));
+    Decoded dec;
+    int rc = decode_batch(desc, dec, err);
+    if (rc) {
+        set_last("%s", err->message);
+        return rc;
+    }
+    std::map<std::string, int> keys;
+    for (const Neuron &N : dec.neurons) keys[N.key] = 1;
+    if (n_neurons) *n_neurons = (int64_t)dec.neurons.size();
+    if (n_types) *n_types = (int64_t)keys.size();
+    return GBH_OK;
+}
+
+gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_options *opt,
+                       gbh_error *err)
+{
+    gbh_error local{};
+    if (!err) err = &local;
+    memset(err, 0, sizeof(*err));
+    if (!desc) {
+        fail_err(err, GBH_ERR_ARG, "NULL descriptor");
+        return nullptr;
+    }
+    gbh_engine *e = new gbh_engine();
+    if (opt) e->opt = *opt;
+    e->nsolvers = desc->nsolvers;
+    e->dt = desc->dt;
+    if (cudaSetDevice(e->opt.device) != cudaSuccess) {
+        fail_err(err, GBH_ERR_CUDA, "cudaSetDevice(%d) failed", e->opt.device);
+        delete e;
+        return nullptr;
+    }
+    int rc = decode_batch(desc, e->dec, err);
+    if (rc) {
+        set_last("%s", err->message);
+        delete e;
+        return nullptr;
+    }
+    // keep the reference layout for state sync
+    const int ns = desc->nsolvers;
+    e->chip_start.assign(desc->chip_start, desc->chip_start + ns + 1);
+    e->conc_start.assign(desc->conc_start, desc->conc_start + ns + 1);
+    e->ops_start.assign(desc->ops_start, desc->ops_start + ns + 1);
+    e->vm_start.assign(desc->vm_start, desc->vm_start + ns + 1);
+    e->giv_start.assign(desc->givals_start, desc->givals_start + ns + 1);
+    e->chip_orig.assign(desc->chip, desc->chip + desc->chip_start[ns]);
+    e->ops_orig.assign(desc->ops, desc->ops + desc->ops_start[ns]);
+    rc = build_layout(e, desc, syn, err);
+    if (rc) {
+        gbh_destroy(e);
+        return nullptr;
+    }
+    e->steps_per_launch = e->opt.steps_per_launch > 0 ? e->opt.steps_per_launch : 64;
+    if (e->has_network) e->steps_per_launch = 1;  // spikes cross tiles every step
+    cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    cudaEventCreate(&e->ev0);
+    cudaEventCreate(&e->ev1);
+    int64_t comps = 0;
+    for (const Neuron &N : e->dec.neurons) comps += N.nrows;
+    e->stats.compartments = comps;
+    e->stats.tiles = (int64_t)e->tiles.size();
+    e->stats.precision = e->opt.precision;
+    e->stats.steps_per_launch = e->steps_per_launch;
+    e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
+    return e;
+}
+
+int gbh_run_async(gbh_engine *e, int nsteps, void *stream)
+{
+    if (!e || nsteps < 0) return GBH_ERR_ARG;
+    if (nsteps == 0) return GBH_OK;
+    return run_steps(e, nsteps, (cudaStream_t)stream);
+}
+
+int gbh_run(gbh_engine *e, int nsteps)
+{
+    if (!e || nsteps < 0) return GBH_ERR_ARG;
+    if (nsteps == 0) return GBH_OK;
+    CK(cudaEventRecord(e->ev0, e->stream));
+    int rc = run_steps(e, nsteps, e->stream);
+    if (rc) return rc;
+    CK(cudaEventRecord(e->ev1, e->stream));
+    CK(cudaEventSynchronize(e->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    e->stats.device_ms += ms;
+    e->stats.steps += nsteps;
+    int status = 0;
+    CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status) {
+        set_last("device status word 0x%x (unimplemented micro-op reached)", status);
+        return GBH_ERR_DEVICE;
+    }
+    return GBH_OK;
+}
+
+int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *ops)
+{
+    if (!e) return GBH_ERR_ARG;
+    const size_t L = LANES;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<double> V(e->rows_vm * L), P(e->rows_fld * L), C(e->rows_pool * L);
+    std::vector<int> I(e->rows_int * L);
+    if (!V.empty()) CK(cudaMemcpy(V.data(), e->d_V.p, V.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!P.empty()) CK(cudaMemcpy(P.data(), e->d_P.p, P.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!C.empty()) CK(cudaMemcpy(C.data(), e->d_C.p, C.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!I.empty()) CK(cudaMemcpy(I.data(), e->d_I.p, I.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    if (chip) memcpy(chip, e->chip_orig.data(), e->chip_orig.size() * sizeof(double));
+    if (ops) memcpy(ops, e->ops_orig.data(), e->ops_orig.size() * sizeof(int));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        if (vm)
+            for (int s = 0; s < N.nrows; ++s) vm[e->vm_start[N.solver] + N.row0 + s] = V[(t.vm + s) * L + l];
+        if (chip)
+            for (size_t f = 0; f < N.fsrc.size(); ++f)
+                if (N.fsrc[f].state && N.fsrc[f].kind == FS_CHIP)
+                    chip[e->chip_start[N.solver] + N.fsrc[f].idx] = P[(t.fld + f) * L + l];
+        if (conc)
+            for (size_t p = 0; p < N.pool_conc.size(); ++p)
+                conc[e->conc_start[N.solver] + N.pool_conc[p]] = C[(t.pools + p) * L + l];
+        if (ops)
+            for (size_t r = 0; r < N.iops.size(); ++r)
+                ops[e->ops_start[N.solver] + N.iops[r]] = I[(t.ints + r) * L + l];
+    }
+    return GBH_OK;
+}
+
+int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const double *conc)
+{
+    if (!e) return GBH_ERR_ARG;
+    const size_t L = LANES;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<double> V(e->rows_vm * L), P(e->rows_fld * L), C(e->rows_pool * L);
+    if (!V.empty()) CK(cudaMemcpy(V.data(), e->d_V.p, V.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!P.empty()) CK(cudaMemcpy(P.data(), e->d_P.p, P.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (!C.empty()) CK(cudaMemcpy(C.data(), e->d_C.p, C.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        if (vm)
+            for (int s = 0; s < N.nrows; ++s) V[(t.vm + s) * L + l] = vm[e->vm_start[N.solver] + N.row0 + s];
+        if (chip)
+            for (size_t f = 0; f < N.fsrc.size(); ++f)
+                if (N.fsrc[f].kind == FS_CHIP)
+                    P[(t.fld + f) * L + l] = chip[e->chip_start[N.solver] + N.fsrc[f].idx];
+        if (conc)
+            for (size_t p = 0; p < N.pool_conc.size(); ++p)
+                C[(t.pools + p) * L + l] = conc[e->conc_start[N.solver] + N.pool_conc[p]];
+    }
+    if (chip) e->chip_orig.assign(chip, chip + e->chip_orig.size());
+    if (!V.empty()) CK(cudaMemcpy(e->d_V.p, V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!P.empty()) CK(cudaMemcpy(e->d_P.p, P.data(), P.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (!C.empty()) CK(cudaMemcpy(e->d_C.p, C.data(), C.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return GBH_OK;
+}
+
+int gbh_enable_givals(gbh_engine *e, int enable)
+{
+    if (!e) return GBH_ERR_ARG;
+    e->givals_enabled = enable != 0;
+    e->givals_valid = false;
+    return GBH_OK;
+}
+
+int gbh_get_givals(gbh_engine *e, double *givals)
+{
+    if (!e || !givals) return GBH_ERR_ARG;
+    if (!e->givals_valid) {
+        set_last("givals were not recorded: enable them before gbh_run");
+        return GBH_ERR_ARG;
+    }
+    const size_t L = LANES;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<double> Gv(e->rows_giv * L);
+    if (!Gv.empty()) CK(cudaMemcpy(Gv.data(), e->d_giv.p, Gv.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        for (size_t r = 0; r < N.giv_ref.size(); ++r)
+            givals[e->giv_start[N.solver] + N.giv_ref[r]] = Gv[(t.giv + r) * L + l];
+    }
+    return GBH_OK;
+}
+
+int gbh_get_spike_counts(gbh_engine *e, int64_t *counts)
+{
+    if (!e || !counts) return GBH_ERR_ARG;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<unsigned long long> s(e->d_spikes.n);
+    if (!s.empty()) CK(cudaMemcpy(s.data(), e->d_spikes.p, s.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < e->nsolvers; ++k) counts[k] = 0;
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        if (N.spike_op < 0) continue;
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        counts[N.solver] += (int64_t)s[t.first_neuron + e->neuron_lane[i]];
+    }
+    return GBH_OK;
+}
+
+int gbh_get_stats(const gbh_engine *e, gbh_stats *st)
+{
+    if (!e || !st) return GBH_ERR_ARG;
+    *st = e->stats;
+    return GBH_OK;
+}
+
+void gbh_destroy(gbh_engine *e)
+{
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
+    e->d_tab64.release(); e->d_tab32.release(); e->d_xy.release(); e->d_P.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_A.release(); e->d_B.release();
+    e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
+    e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
+    e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
+    if (e->ev0) cudaEventDestroy(e->ev0);
+    if (e->ev1) cudaEventDestroy(e->ev1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// gbh_internal.h -- shared definitions between the host decoder and the
+// device kernels of the GB300 hsolve engine.
+#pragma once
+#include <stdint.h>
+
+namespace gbh {
+
+// ---- reference opcode values (genesis/src/hines/hines_defs.h:120-222) ----
+enum RefOp {
+    R_TABCURR = 0, R_COMPT = 100, R_FCOMPT = 101, R_LCOMPT = 102, R_SPIKE = 200,
+    R_ELMMPUMP = 500, R_CONC_VAL = 1000, R_NERNST = 2000, R_GHK = 2010, R_CHAN = 3000,
+    R_CHAN_EK = 3001, R_SAME_GHK = 3002, R_DO_TABGHK = 3003, R_ADD_CURR = 3200,
+    R_FLUX = 3300, R_SCALE_FLUX = 3301, R_STORE_ALLI = 3501, R_STORE_ALLC = 3502,
+    R_IPOL1V = 4001, R_IPOL1C = 4002, R_IPOL2V = 4003, R_IPOL2C = 4004, R_SYN2 = 4100,
+    R_SYN3 = 4101, R_MGBLOCK = 4200, R_NEWVOLT = 5100, R_NEWCONC1 = 5110,
+    R_NEWCONC2 = 5111, R_DOMAIN = 5112,
+    R_CONC = 10100, R_FCONC = 10101, R_LCONC = 10102, R_FLUXCONC = 10103,
+    R_CACONC = 10200, R_LCACONC = 10202
+};
+enum RefFunc { F_ELIM = 0, F_SET_DIAG = 1, F_SKIP_DIAG = 2, F_FASTSIB = 3, F_COPY = 4,
+               F_SIB = 5, F_CALC = 6, F_FINISH = 7 };
+
+// ---- engine micro-ops: one compartment program is a list of these ----
+// Operands named f* are field rows of the tile's parameter block; p* are pool
+// rows; i* are rows of the integer-state block; g* are givals rows (or -1).
+enum MicroOp {
+    M_BEGIN = 1,     // fEmRm fInject fRm gIleak                       (row start)
+    M_NEWVOLT,       //                                                 (locate V)
+    M_CONCVAL,       // pConc                                           (select pool, flux=0)
+    M_DOMAIN,        // fScale                                          (locate C at scale*Ik)
+    M_NEWCONC2,      // pConc                                           (save C1, locate C2)
+    M_NEWCONC1,      //                                                 (locate C at conc[sel])
+    M_SPIKE,         // fThresh iCounter iRefract                       (spike detect)
+    M_ELMMPUMP,      // fKd fVmax fDiag gOut                            (electrogenic pump)
+    M_FLUX,          //                                                 (flux[sel] += Ik)
+    M_SCALE_FLUX,    // fScale
+    M_GHK,           // fZFRT fZF fGmax                                 (GHK + SAME_GHK)
+    M_SAME_GHK,      // fGmax
+    M_DO_TABGHK,     //
+    M_NERNST,        // fConst fGmax
+    M_CHAN,          // fEk fGmax                                       (CHAN_EK / CHAN with Ek)
+    M_CHAN_G,        // fGmax                                           (CHAN keeping Ek)
+    M_GATE,          // kind col power fState                           (IPOL* + DOPOWER)
+    M_SYN,           // fFreq stab sRow fX fY fWdt                      (SYN2/SYN3)
+    M_MGBLOCK,       // fKA fKBinv fCMg gOut                            (after M_SYN)
+    M_ADDCURR,       // gOut
+    M_STORE,         // kind(0 I, 1 G) name                              (storemode itotal)
+    M_END            // fTbyc fDiag gIm
+};
+enum GateKind { GK_1V = 0, GK_1C = 1, GK_2V = 2, GK_2C = 3 };
+enum PoolOp { PO_CACONC = 1 };   // pConc fBase fItau fDtB
+
+// Lanes per tile: one neuron per lane of a warp.
+constexpr int LANES = 32;
+
+struct TableGeom {
+    int ncols, xdivs, ydivs, pad;
+    double xmin, invdx, ymin, invdy;
+    int64_t tab_off;   // offset into the table pool (doubles / floats)
+    int64_t xv_off;    // offset into the value pool (xvals)
+    int64_t yv_off;    // offset into the value pool (yvals), -1 if none
+};
+
+struct TileType {
+    int nslots;      // compartments per neuron
+    int nfields;     // double rows in the parameter block
+    int nints;       // int rows
+    int npools;      // conc rows
+    int ngiv;        // givals rows
+    int prog_off;    // offset of slot 0's program in the micro-op pool
+    int pool_off;    // offset of the pool program
+    int table_set;
+    int crank;       // 1 = Crank-Nicolson
+    int chanmode5;
+    int interp;      // calcmode
+    int has_spike;
+    int nsyn;        // synchan rows
+};
+
+struct Tile {
+    int type;
+    int nlanes;      // active lanes
+    int64_t fld;     // row offsets (x32 elements) into the pools below
+    int64_t topo;    // parent / A / B / C rows (nslots each)
+    int64_t ints;
+    int64_t pools;
+    int64_t giv;
+    int64_t vm;      // nslots rows
+    int64_t syn;     // event-ring rows (nsyn * ring_len)
+    int64_t first_neuron; // global neuron index of lane 0
+};
+
+// Device status word bits
+enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2 };
+
+}  // namespace gbh

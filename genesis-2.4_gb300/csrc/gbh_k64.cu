@@ -1,0 +1,11 @@
+// gbh_k64.cu -- FP64 step kernels (compiled with --fmad=false so the
+// arithmetic matches the reference's CPU solver bit for bit).
+#include "gbh_kernels.cuh"
+
+namespace gbh {
+cudaError_t launch_fp64(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
+                        long long step, bool giv, cudaStream_t st)
+{
+    return launch_impl<double>(v, tile0, tile1, smax, warps, nsteps, step, giv, st);
+}
+}  // namespace gbh

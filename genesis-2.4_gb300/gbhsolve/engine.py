@@ -1,0 +1,317 @@
+"""ctypes binding of the C ABI in include/gbhsolve.h (libgbhsolve.so).
+
+This is the host-side mirror of the reference's accelerator interface for
+the hsolve chanmode 4/5 step (genesis/src/hines/cuda/cuda_hsolve.h:22-25):
+``Engine(solvers)`` plays ``cuda_init``, ``Engine.run`` plays the multiloop
+``cuda_chip_update`` returning "vm ready", ``get_state`` plays
+``cuda_sync_chip``, and ``close`` plays ``cuda_cleanup``. There is no CPU
+fallback: if the library cannot be loaded or the model uses something the
+engine does not implement, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lp = C.POINTER(C.c_int64)
+
+ABI_VERSION = 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class GbhError(C.Structure):
+    _fields_ = [("code", C.c_int), ("solver", C.c_int), ("row", C.c_int), ("opcode", C.c_int),
+                ("position", C.c_int), ("message", C.c_char * 256)]
+
+
+class GbhTables(C.Structure):
+    _fields_ = [("ncols", C.c_int), ("xdivs", C.c_int), ("ydivs", C.c_int),
+                ("xmin", C.c_double), ("invdx", C.c_double), ("ymin", C.c_double),
+                ("invdy", C.c_double), ("tablist", _dp), ("xvals", _dp), ("yvals", _dp)]
+
+
+class GbhBatchDesc(C.Structure):
+    _fields_ = [("abi_version", C.c_int), ("nsolvers", C.c_int), ("dt", C.c_double),
+                ("method", _ip), ("chanmode", _ip), ("calcmode", _ip), ("table_set", _ip),
+                ("ntables", C.c_int), ("tables", C.POINTER(GbhTables)),
+                ("ops_start", _lp), ("ops", _ip),
+                ("chip_start", _lp), ("chip", _dp),
+                ("funcs_start", _lp), ("funcs", _ip),
+                ("ravals_start", _lp), ("ravals", _dp),
+                ("vm_start", _lp), ("vm", _dp),
+                ("givals_start", _lp), ("givals", _dp),
+                ("stab_start", _lp), ("stablist", _dp),
+                ("conc_start", _lp), ("conc", _dp),
+                ("concops_start", _lp), ("concops", _ip),
+                ("concchip_start", _lp), ("concchip", _dp)]
+
+
+class GbhSynapses(C.Structure):
+    _fields_ = [("nsynapses", C.c_int64), ("src_start", _lp), ("target_solver", _ip),
+                ("target_op", _ip), ("weight", _dp), ("delay_steps", _ip)]
+
+
+class GbhOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("steps_per_launch", C.c_int),
+                ("warps_per_block", C.c_int), ("use_graph", C.c_int), ("device", C.c_int)]
+
+
+class GbhStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("device_ms", C.c_double), ("compartments", C.c_int64),
+                ("tiles", C.c_int64), ("launches", C.c_int64), ("bytes_per_step", C.c_double),
+                ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int)]
+
+
+EXPORTED = ["gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
+            "gbh_enable_givals", "gbh_get_givals", "gbh_get_spike_counts", "gbh_get_stats",
+            "gbh_destroy", "gbh_last_error"]
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads libgbhsolve.so (building it first when sources are newer)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError("libgbhsolve.so is missing; run gbhsolve.build.build()")
+    lib = C.CDLL(_build.LIB)
+    lib.gbh_create.restype = C.c_void_p
+    lib.gbh_create.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhSynapses), C.POINTER(GbhOptions),
+                               C.POINTER(GbhError)]
+    lib.gbh_validate.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhError), _lp, _lp]
+    lib.gbh_run.argtypes = [C.c_void_p, C.c_int]
+    lib.gbh_run_async.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.gbh_get_state.argtypes = [C.c_void_p, _dp, _dp, _dp, _ip]
+    lib.gbh_set_state.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    lib.gbh_enable_givals.argtypes = [C.c_void_p, C.c_int]
+    lib.gbh_get_givals.argtypes = [C.c_void_p, _dp]
+    lib.gbh_get_spike_counts.argtypes = [C.c_void_p, _lp]
+    lib.gbh_get_stats.argtypes = [C.c_void_p, C.POINTER(GbhStats)]
+    lib.gbh_destroy.argtypes = [C.c_void_p]
+    lib.gbh_last_error.restype = C.c_char_p
+    _LIB = lib
+    return lib
+
+
+def _cat(arrays, dtype):
+    starts = np.zeros(len(arrays) + 1, dtype=np.int64)
+    for i, a in enumerate(arrays):
+        starts[i + 1] = starts[i] + len(a)
+    flat = np.concatenate([np.asarray(a, dtype=dtype) for a in arrays]) if starts[-1] else \
+        np.zeros(1, dtype=dtype)
+    return starts, np.ascontiguousarray(flat)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+class EngineError(RuntimeError):
+    def __init__(self, err: GbhError):
+        self.code = err.code
+        self.solver = err.solver
+        self.row = err.row
+        self.opcode = err.opcode
+        self.position = err.position
+        super().__init__("gbh_create failed (code %d, solver %d, row %d, opcode %d, pos %d): %s" % (
+            err.code, err.solver, err.row, err.opcode, err.position, err.message.decode()))
+
+
+class Batch:
+    """Concatenated reference arrays of many hsolve elements (plain numpy)."""
+
+    def __init__(self, solvers: Sequence, synapses: Optional[dict] = None):
+        self.solvers = list(solvers)
+        s0 = self.solvers[0]
+        dt = s0.dt
+        for s in self.solvers:
+            if s.dt != dt:
+                raise ValueError("all solvers of a batch share dt")
+        self.dt = dt
+        self.n = len(self.solvers)
+        # table sets: share identical tables
+        self.table_keys = {}
+        self.table_list = []
+        ts = []
+        for s in self.solvers:
+            key = id(s.tablist)
+            if key not in self.table_keys:
+                self.table_keys[key] = len(self.table_list)
+                self.table_list.append(s)
+            ts.append(self.table_keys[key])
+        self.table_set = np.array(ts, dtype=np.int32)
+        self.method = np.array([s.method for s in self.solvers], dtype=np.int32)
+        self.chanmode = np.array([s.chanmode for s in self.solvers], dtype=np.int32)
+        self.calcmode = np.array([s.calcmode for s in self.solvers], dtype=np.int32)
+        self.ops_start, self.ops = _cat([s.ops for s in self.solvers], np.int32)
+        self.chip_start, self.chip = _cat([s.chip for s in self.solvers], np.float64)
+        self.funcs_start, self.funcs = _cat([s.funcs for s in self.solvers], np.int32)
+        self.ravals_start, self.ravals = _cat([s.ravals for s in self.solvers], np.float64)
+        self.vm_start, self.vm = _cat([s.vm for s in self.solvers], np.float64)
+        self.givals_start, self.givals = _cat([s.givals for s in self.solvers], np.float64)
+        self.stab_start, self.stablist = _cat([s.stablist for s in self.solvers], np.float64)
+        self.conc_start, self.conc = _cat([s.conc for s in self.solvers], np.float64)
+        self.concops_start, self.concops = _cat([s.concops for s in self.solvers], np.int32)
+        self.concchip_start, self.concchip = _cat([s.concchip for s in self.solvers], np.float64)
+        self._tables = (GbhTables * max(1, len(self.table_list)))()
+        self._keep = []
+        for k, s in enumerate(self.table_list):
+            t = self._tables[k]
+            t.ncols, t.xdivs, t.ydivs = s.ncols, s.xdivs, s.ydivs
+            t.xmin, t.invdx, t.ymin, t.invdy = s.xmin, s.invdx, s.ymin, s.invdy
+            tab = np.ascontiguousarray(s.tablist, dtype=np.float64)
+            xv = np.ascontiguousarray(s.xvals, dtype=np.float64)
+            yv = np.ascontiguousarray(s.yvals, dtype=np.float64)
+            self._keep += [tab, xv, yv]
+            t.tablist = _ptr(tab, _dp) if tab.size else C.cast(0, _dp)
+            t.xvals = _ptr(xv, _dp) if xv.size else C.cast(0, _dp)
+            t.yvals = _ptr(yv, _dp) if yv.size else C.cast(0, _dp)
+        d = GbhBatchDesc()
+        d.abi_version = ABI_VERSION
+        d.nsolvers = self.n
+        d.dt = dt
+        d.method, d.chanmode = _ptr(self.method, _ip), _ptr(self.chanmode, _ip)
+        d.calcmode, d.table_set = _ptr(self.calcmode, _ip), _ptr(self.table_set, _ip)
+        d.ntables = len(self.table_list)
+        d.tables = self._tables
+        for name, t in (("ops", _ip), ("chip", _dp), ("funcs", _ip), ("ravals", _dp), ("vm", _dp),
+                        ("givals", _dp), ("stablist", _dp), ("conc", _dp), ("concops", _ip),
+                        ("concchip", _dp)):
+            start = "stab_start" if name == "stablist" else name + "_start"
+            setattr(d, start, _ptr(getattr(self, start), _lp))
+            setattr(d, name, _ptr(getattr(self, name), t))
+        self.desc = d
+        self.syn = None
+        if synapses is not None:
+            self._syn = {k: np.ascontiguousarray(v) for k, v in synapses.items()}
+            sy = GbhSynapses()
+            sy.nsynapses = len(self._syn["target_solver"])
+            sy.src_start = _ptr(self._syn["src_start"].astype(np.int64), _lp)
+            self._syn["src_start"] = self._syn["src_start"].astype(np.int64)
+            sy.src_start = _ptr(self._syn["src_start"], _lp)
+            self._syn["target_solver"] = self._syn["target_solver"].astype(np.int32)
+            self._syn["target_op"] = self._syn["target_op"].astype(np.int32)
+            self._syn["weight"] = self._syn["weight"].astype(np.float64)
+            self._syn["delay_steps"] = self._syn["delay_steps"].astype(np.int32)
+            sy.target_solver = _ptr(self._syn["target_solver"], _ip)
+            sy.target_op = _ptr(self._syn["target_op"], _ip)
+            sy.weight = _ptr(self._syn["weight"], _dp)
+            sy.delay_steps = _ptr(self._syn["delay_steps"], _ip)
+            self.syn = sy
+
+    def split(self, flat, starts):
+        return [flat[starts[i]:starts[i + 1]] for i in range(self.n)]
+
+
+def validate(solvers: Sequence):
+    """Host-only decode of a batch; returns (neurons, tile types) or raises."""
+    lib = load()
+    b = Batch(solvers)
+    err = GbhError()
+    nn = C.c_int64(0)
+    nt = C.c_int64(0)
+    rc = lib.gbh_validate(C.byref(b.desc), C.byref(err), C.byref(nn), C.byref(nt))
+    if rc != 0:
+        raise EngineError(err)
+    return nn.value, nt.value
+
+
+class Engine:
+    """A device engine over a batch of hsolve elements."""
+
+    def __init__(self, solvers: Sequence, synapses: Optional[dict] = None, precision: int = PREC_FP64,
+                 steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0):
+        self.lib = load()
+        self.batch = Batch(solvers, synapses)
+        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 0, device)
+        err = GbhError()
+        h = self.lib.gbh_create(C.byref(self.batch.desc),
+                                C.byref(self.batch.syn) if self.batch.syn is not None else None,
+                                C.byref(opt), C.byref(err))
+        if not h:
+            raise EngineError(err)
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError("gbhsolve error %d: %s" % (rc, self.lib.gbh_last_error().decode()))
+
+    def run(self, nsteps: int) -> None:
+        self._check(self.lib.gbh_run(self.h, int(nsteps)))
+
+    def run_async(self, nsteps: int, stream_handle: int) -> None:
+        self._check(self.lib.gbh_run_async(self.h, int(nsteps), C.c_void_p(stream_handle)))
+
+    def get_state(self):
+        b = self.batch
+        vm = np.empty_like(b.vm)
+        chip = np.empty_like(b.chip)
+        conc = np.array(b.conc, copy=True)
+        ops = np.empty_like(b.ops)
+        self._check(self.lib.gbh_get_state(self.h, _ptr(vm, _dp), _ptr(chip, _dp), _ptr(conc, _dp),
+                                           _ptr(ops, _ip)))
+        return dict(vm=b.split(vm, b.vm_start), chip=b.split(chip, b.chip_start),
+                    conc=b.split(conc, b.conc_start), ops=b.split(ops, b.ops_start))
+
+    def vm(self) -> np.ndarray:
+        b = self.batch
+        vm = np.empty_like(b.vm)
+        self._check(self.lib.gbh_get_state(self.h, _ptr(vm, _dp), None, None, None))
+        return vm
+
+    def set_state(self, vm=None, chip=None, conc=None):
+        b = self.batch
+        args = []
+        for arr, dt in ((vm, np.float64), (chip, np.float64), (conc, np.float64)):
+            if arr is None:
+                args.append(None)
+            else:
+                a = np.ascontiguousarray(np.concatenate(arr) if isinstance(arr, list) else arr, dtype=dt)
+                self._tmp = getattr(self, "_tmp", []) + [a]
+                args.append(_ptr(a, _dp))
+        self._check(self.lib.gbh_set_state(self.h, *args))
+
+    def enable_givals(self, on: bool = True):
+        self._check(self.lib.gbh_enable_givals(self.h, 1 if on else 0))
+
+    def givals(self):
+        b = self.batch
+        g = np.array(b.givals, copy=True)
+        self._check(self.lib.gbh_get_givals(self.h, _ptr(g, _dp)))
+        return b.split(g, b.givals_start)
+
+    def spike_counts(self) -> np.ndarray:
+        c = np.zeros(self.batch.n, dtype=np.int64)
+        self._check(self.lib.gbh_get_spike_counts(self.h, _ptr(c, _lp)))
+        return c
+
+    def stats(self) -> GbhStats:
+        st = GbhStats()
+        self._check(self.lib.gbh_get_stats(self.h, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gbh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

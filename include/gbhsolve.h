@@ -1,0 +1,181 @@
+/*
+ * gbhsolve.h -- C ABI of the GB300 hsolve chanmode 4/5 step engine.
+ *
+ * Drop-in for the accelerator boundary of GENESIS hsolve (the reference's
+ * genesis/src/hines/cuda/cuda_hsolve.h:22-25 and the array-level API of
+ * genesis/src/hines/cuda/cuda_backend.cu:157-259, 396-444). The engine takes
+ * the arrays the reference SETUP builds -- ops[], chip[], funcs[], ravals[],
+ * tablist[], concops[], concchip[] ... -- for one or many hsolve elements,
+ * copies them to the GPU, and advances them by whole PROCESS steps: channel
+ * program, Ca pools and Hines elimination, all on the device. There is no CPU
+ * fallback: an opcode or elimination token the engine does not implement is a
+ * setup error naming the solver, compartment row and opcode.
+ *
+ * Plain pointers and sizes only; no GENESIS or CUDA types cross this header.
+ * All arrays are read during gbh_create and not retained.
+ */
+#ifndef GBHSOLVE_H
+#define GBHSOLVE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBH_ABI_VERSION 1
+
+/* precision of gate/table arithmetic (elimination, Vm and Ca are always FP64) */
+#define GBH_PREC_FP64 0
+#define GBH_PREC_MIXED 1 /* gates, tables, interpolation in FP32 */
+
+/* error codes */
+#define GBH_OK 0
+#define GBH_ERR_ARG -1        /* bad argument or size                        */
+#define GBH_ERR_OPCODE -2     /* ops[]/concops[] opcode not implemented      */
+#define GBH_ERR_FUNCS -3      /* funcs[] token not implemented / malformed   */
+#define GBH_ERR_CUDA -4       /* CUDA runtime failure                        */
+#define GBH_ERR_DEVICE -5     /* device-side status word (e.g. event ring)   */
+#define GBH_ERR_UNSUPPORTED -6 /* model feature outside the engine's scope   */
+
+typedef struct gbh_error {
+    int code;
+    int solver;     /* solver index, or -1                           */
+    int row;        /* compartment row (Hines order), or -1          */
+    int opcode;     /* offending ops[]/funcs[] value, or 0           */
+    int position;   /* index into ops[]/funcs[]/concops[], or -1     */
+    char message[256];
+} gbh_error;
+
+/*
+ * One composite table set: hsolve->tablist/xvals/yvals and their geometry
+ * (hines_struct.h:352-378). tablist has (xdivs+1)*ncols doubles; xvals has
+ * xdivs+1 entries, yvals ydivs+1 (or NULL).
+ */
+typedef struct gbh_tables {
+    int ncols, xdivs, ydivs;
+    double xmin, invdx, ymin, invdy;
+    const double *tablist;
+    const double *xvals;
+    const double *yvals;
+} gbh_tables;
+
+/*
+ * A batch of hsolve elements, arrays concatenated solver after solver with
+ * CSR offsets (length nsolvers+1). Per-solver arrays are exactly the
+ * reference's: ops (hsolve->ops, nops), chip (nchips), funcs (nfuncs), ravals
+ * (nravals), vm (ncompts), givals (ngivals, only the Rm entries are read),
+ * stablist (4*sntab), conc (nconcs), concops (nconcops), concchip (nconcchips).
+ * Empty ranges are allowed for concops/concchip/stablist/conc.
+ */
+typedef struct gbh_batch_desc {
+    int abi_version;            /* GBH_ABI_VERSION */
+    int nsolvers;
+    double dt;                  /* hsolve->dt, common to the batch           */
+    const int *method;          /* [nsolvers] 10 BEULER, 11 CRANK_INT        */
+    const int *chanmode;        /* [nsolvers] 4 or 5                          */
+    const int *calcmode;        /* [nsolvers] 1 interpolate, 0 nearest row    */
+    const int *table_set;       /* [nsolvers] index into tables[]             */
+    int ntables;
+    const gbh_tables *tables;   /* [ntables]                                  */
+    const int64_t *ops_start;    const int *ops;
+    const int64_t *chip_start;   const double *chip;
+    const int64_t *funcs_start;  const int *funcs;
+    const int64_t *ravals_start; const double *ravals;
+    const int64_t *vm_start;     const double *vm;
+    const int64_t *givals_start; const double *givals;
+    const int64_t *stab_start;   const double *stablist;
+    const int64_t *conc_start;   const double *conc;
+    const int64_t *concops_start;  const int *concops;
+    const int64_t *concchip_start; const double *concchip;
+} gbh_batch_desc;
+
+/*
+ * Spike -> synchan connectivity between solvers of the batch (what
+ * h_dospike_event / synchan EVENT / HSEVENT do through GENESIS messages,
+ * hines_conn.c:44-108, newconn/synchan.c:160-313). CSR over source solvers
+ * (the solver holding the spikegen). Each synapse targets the SYN2_OP whose
+ * ops[] index (within the target solver) is target_op, with weight and delay
+ * in steps ((int)(delay/dt + 0.9), synchan.c:199-200). All synapses into one
+ * synchan must carry the same weight; delays must be >= 1 step.
+ */
+typedef struct gbh_synapses {
+    int64_t nsynapses;
+    const int64_t *src_start;  /* [nsolvers+1] */
+    const int *target_solver;  /* [nsynapses]  */
+    const int *target_op;      /* [nsynapses]  */
+    const double *weight;      /* [nsynapses]  */
+    const int *delay_steps;    /* [nsynapses]  */
+} gbh_synapses;
+
+typedef struct gbh_options {
+    int precision;       /* GBH_PREC_FP64 or GBH_PREC_MIXED                  */
+    int steps_per_launch;/* 0 = autotune; otherwise steps fused per launch     */
+    int warps_per_block; /* 0 = autotune                                      */
+    int use_graph;       /* capture multi-launch runs in a CUDA graph         */
+    int device;          /* CUDA device ordinal                                */
+} gbh_options;
+
+typedef struct gbh_stats {
+    int64_t steps;
+    double device_ms;          /* device time of gbh_run calls (CUDA events) */
+    int64_t compartments;
+    int64_t tiles;             /* warps of 32 neurons                          */
+    int64_t launches;          /* kernel launches issued                       */
+    double bytes_per_step;     /* algorithmic bytes streamed per step          */
+    int steps_per_launch;
+    int warps_per_block;
+    int precision;
+} gbh_stats;
+
+typedef struct gbh_engine gbh_engine;
+
+/* Builds the device engine; returns NULL and fills *err on failure. */
+gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn,
+                       const gbh_options *opt, gbh_error *err);
+
+/*
+ * Runs only the host-side decoder (no GPU needed): checks that every opcode
+ * and elimination token is implemented and reports the layout the engine
+ * would use. Returns GBH_OK or the error gbh_create would return.
+ * n_neurons / n_tiles / n_types may be NULL.
+ */
+int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons, int64_t *n_types);
+
+/* Advances every solver by nsteps PROCESS steps. Returns GBH_OK or an error. */
+int gbh_run(gbh_engine *e, int nsteps);
+
+/* Same, on a caller-owned CUDA stream (cudaStream_t passed as void*). */
+int gbh_run_async(gbh_engine *e, int nsteps, void *stream);
+
+/*
+ * Copies state back into reference-layout arrays (concatenated like the
+ * batch desc; any pointer may be NULL to skip): vm, chip (gate states and
+ * synchan X/Y updated in place over a copy of the original chip), conc,
+ * and ops (spike refractory counters and synchan countdowns).
+ */
+int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *ops);
+
+/* Writes vm / chip / conc back into the engine (HPUT / RESTORE2 path). */
+int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const double *conc);
+
+/*
+ * Copies the givals of the last completed step into a reference-layout array
+ * (the kernel records them on the final step of a gbh_run when enabled).
+ */
+int gbh_enable_givals(gbh_engine *e, int enable);
+int gbh_get_givals(gbh_engine *e, double *givals);
+
+/* Per-solver spike counts since creation (int64[nsolvers]). */
+int gbh_get_spike_counts(gbh_engine *e, int64_t *counts);
+
+int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
+void gbh_destroy(gbh_engine *e);
+
+/* Static description of the last error on this thread (never NULL). */
+const char *gbh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBHSOLVE_H */
