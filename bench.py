@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hsolve step engine (one JSON line on rank 0).
+
+Workload: 100,000 identical neurons x 16 compartments (1.6 M compartments),
+config-0 morphology (soma 30x30 um + 15 dendrites 20x2 um) with somatic HH
+Na/K and a dendritic K tabchannel at 36 S/m^2, seeded per-neuron inject
+U(0.1, 0.5) nA, dt = 20 us, backward Euler. One step = one hsolve PROCESS
+step over all compartments (channel program, elimination, Vm update).
+
+  value    compartment-steps/s of the mixed-precision form, device-timed
+           (CUDA events around the launches, inputs resident in HBM; the
+           1.6 M-compartment state is larger than L2)
+  forms    the same for the plain FP64 form, plus the mixed form's max|dVm|
+           against the FP64 CPU oracle over 10,000 steps of a neuron sample
+  e2e      the same metric through the C ABI with host buffers: every step
+           copies the per-neuron inject currents host->device (h_in_msgs) and
+           the somatic Vm of every neuron device->host (h_out_msgs)
+  roofline HBM roofline of the step kernel (algorithmic bytes per
+           compartment-step x compartment-steps per launch / launch time)
+
+``--impl reference`` times the CPU restatement of the reference solver (the
+oracle port: the reference's own C step code cannot be built on this host)
+on every host core over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "genesis-2.4_gb300"))
+
+import numpy as np  # noqa: E402
+
+N_NEURONS = 100_000
+NCOMP = 16
+GK_DEND = 36.0
+DT = 20e-6
+SEED = 3
+# algorithmic bytes per compartment-step for this workload (one streaming
+# pass over per-compartment state and coefficients, tables on chip):
+# FP64 (16+32)*16 + 28*15 + 17*16 + 18*16 = 1748 B per neuron; mixed 1469 B
+ALG_BYTES = {"fp64": 1748.0 / NCOMP, "mixed": 1469.0 / NCOMP}
+ACC_STEPS = 10_000
+ACC_SAMPLE = 32
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return ws, rank, local, dist
+    return 1, 0, 0, None
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", "gbh_clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+            sm = [float(r[0]) for r in rows]
+            mx = float(rows[0][1])
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i].strip() == "Active"})
+            return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons,
+                    "samples": len(sm)}
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def build_workload(n_neurons):
+    from gbhsolve import configs
+    t = time.time()
+    hs, injects = configs.cables_replicated(n_neurons, NCOMP, seed=SEED, dt=DT, gk_dend=GK_DEND)
+    log("workload built: %d neurons in %.1fs" % (n_neurons, time.time() - t))
+    return hs, injects
+
+
+def time_engine(eng, steps, warmup):
+    eng.run(warmup)
+    st0 = eng.stats()
+    ms0, l0 = st0.device_ms, st0.launches
+    eng.run(steps)
+    st1 = eng.stats()
+    return st1.device_ms - ms0, st1.launches - l0, st1
+
+
+def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE, chunk=500):
+    """max|dVm| of the engine against the FP64 oracle over nsteps steps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    from gbhsolve import engine
+    idx = np.linspace(0, len(hs) - 1, nsample).astype(int)
+    sample = [hs[i] for i in idx]
+    eng = engine.Engine(sample, precision=precision)
+    orc = [pyoracle.Solver(h) for h in sample]
+    worst = 0.0
+    done = 0
+    while done < nsteps:
+        k = min(chunk, nsteps - done)
+        eng.run(k)
+        for s in orc:
+            s.run(k)
+        vm = eng.vm()
+        ref = np.concatenate([s.vm for s in orc])
+        worst = max(worst, float(np.max(np.abs(vm - ref))))
+        done += k
+    eng.close()
+    return worst
+
+
+def cpu_sample_rate(hs, seconds=12.0):
+    """Oracle (one core) compartment-steps/s over a bounded sample."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    pyoracle.ensure_built(with_reference=False)
+    solvers = [pyoracle.Solver(h) for h in hs[:256]]
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for s in solvers:
+            s.run(20)
+        steps += 20
+    el = time.perf_counter() - t0
+    cs = steps * len(solvers) * NCOMP
+    return cs / el, "%d neurons x %d compartments x %d steps (%.1f s)" % (len(solvers), NCOMP, steps, el)
+
+
+def _cpu_worker(args):
+    n, steps, seed = args
+    sys.path.insert(0, os.path.join(REPO, "genesis-2.4_gb300"))
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    from gbhsolve import configs
+    hs, _ = configs.cables_replicated(n, NCOMP, seed=seed, dt=DT, gk_dend=GK_DEND)
+    solvers = [pyoracle.Solver(h) for h in hs]
+    t0 = time.perf_counter()
+    for s in solvers:
+        s.run(steps)
+    return n * NCOMP * steps, time.perf_counter() - t0
+
+
+def run_reference(args, ws, rank, dist):
+    """CPU restatement of the reference solver on every host core."""
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import multiprocessing as mp
+    import pyoracle
+    pyoracle.ensure_built(with_reference=False)
+    cores = os.cpu_count() or 1
+    per = 96                       # neurons per worker per step batch
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_cpu_worker, [(8, 5, k) for k in range(cores)])   # warm the workers
+        vals = []
+        for _ in range(args.warmup):
+            pool.map(_cpu_worker, [(per, 10, k) for k in range(cores)])
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(per, 10, k) for k in range(cores)])
+            wall = time.perf_counter() - t0
+            cs = sum(r[0] for r in res)
+            vals.append(cs / max(max(r[1] for r in res), 1e-9))
+    value = float(np.median(vals))
+    line = {
+        "metric": "compartment-steps/s", "value": value, "unit": "compartment-steps/s",
+        "impl": "reference", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "cables-100k-x16 (config 3 morphology, dendritic K)", "sample_neurons":
+                   per * cores, "steps_per_sample": 10},
+        "cpu_baseline": {"value": value, "unit": "compartment-steps/s", "cores": cores, "kind": "port",
+                         "sample": "%d workers x %d neurons x 16 compartments x 10 steps per timed step"
+                                   % (cores, per)},
+        "e2e": {"value": value, "unit": "compartment-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--neurons", type=int, default=N_NEURONS)
+    ap.add_argument("--steps-per-launch", type=int, default=0)
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank, dist)
+
+    import torch
+    torch.cuda.set_device(local)
+    from gbhsolve import engine
+
+    hs, injects = build_workload(args.neurons)
+    M = args.neurons * NCOMP
+    results = {}
+    for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
+        eng = engine.Engine(hs, precision=prec, steps_per_launch=args.steps_per_launch, device=local)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            ms, launches, st = time_engine(eng, args.steps, args.warmup)
+        torch.cuda.synchronize()
+        if dist:
+            t = torch.tensor([ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        results[form] = dict(ms=ms, launches=launches, spl=st.steps_per_launch,
+                             value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng)
+        log("%s: %.3f ms for %d steps, %d launches -> %.3e cs/s" % (form, ms, args.steps, launches,
+                                                                   results[form]["value"]))
+        if form == "fp64":
+            eng.close()
+
+    # end to end through the C ABI with host buffers (mixed form)
+    eng = results["mixed"]["eng"]
+    nh = len(hs)
+    eng.register_inputs(np.arange(nh, dtype=np.int32),
+                        np.full(nh, int(hs[0].compchips[NCOMP - 1]) + 1, dtype=np.int64))
+    eng.register_outputs(np.arange(nh, dtype=np.int32), np.full(nh, NCOMP - 1, dtype=np.int32))
+    pin_in = torch.empty(nh, dtype=torch.float64, pin_memory=True)
+    pin_out = torch.empty(nh, dtype=torch.float64, pin_memory=True)
+    pin_in.numpy()[:] = np.array([float(np.float32(x)) for x in injects])
+    stream = torch.cuda.Stream()
+    h_in, h_out = pin_in.numpy(), pin_out.numpy()
+    sh = stream.cuda_stream
+    for _ in range(args.warmup):
+        eng.set_inputs_async(h_in, sh)
+        eng.run_async(1, sh)
+        eng.get_outputs_async(h_out, sh)
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        eng.set_inputs_async(h_in, sh)
+        eng.run_async(1, sh)
+        eng.get_outputs_async(h_out, sh)
+    e1.record(stream)
+    stream.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([e2e_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_val = M * ws * args.steps / (e2e_ms / 1e3)
+    eng.close()
+
+    # accuracy of the mixed form against the FP64 oracle
+    acc = None
+    if rank == 0 and not args.skip_accuracy:
+        acc = accuracy_sample(hs, engine.PREC_MIXED)
+        log("mixed max|dVm| over %d steps: %.3e V" % (ACC_STEPS, acc))
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        v, sample = cpu_sample_rate(hs)
+        cpu = {"value": v, "unit": "compartment-steps/s", "cores": 1, "kind": "port", "sample": sample}
+
+    peak, peak_kind = peaks()
+    r = results["mixed"]
+    launch_ms = r["ms"] / max(r["launches"], 1)
+    units = M * r["spl"]
+    achieved = ALG_BYTES["mixed"] * units / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "k_steps_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tj = json.load(f)
+        if "bytes_per_compartment_step_mixed" in tj:
+            traffic = tj["bytes_per_compartment_step_mixed"] * units
+    if rank == 0:
+        line = {
+            "metric": "compartment-steps/s", "value": r["value"], "unit": "compartment-steps/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-gates/f64-elimination", "data": "synthetic",
+            "config": {"workload": "cables-100k-x16: 100,000 neurons x 16 compartments, somatic HH Na/K, "
+                                   "dendritic K 36 S/m^2, dt 20 us, backward Euler",
+                       "compartments": M, "form": "batched mixed precision",
+                       "steps_per_launch": r["spl"], "l2": "state 1.6M compartments > L2, no flush"},
+            "forms": {"fp64": {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
+                               "dtype": "f64"},
+                      "mixed": {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
+                                "max_abs_dvm_vs_fp64_oracle_V": acc, "accuracy_steps": ACC_STEPS,
+                                "accuracy_sample_neurons": ACC_SAMPLE}},
+            "speedup_mixed_over_fp64": r["value"] / results["fp64"]["value"],
+            "e2e": {"value": e2e_val, "unit": "compartment-steps/s", "h2d_bytes_per_step": nh * 8,
+                    "d2h_bytes_per_step": nh * 8},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "gbh::k_steps<float>", "launch_ms": launch_ms,
+                         "alg_bytes_per_compartment_step": ALG_BYTES["mixed"]},
+            "cpu_baseline": cpu,
+            "gpu_launches": int(r["launches"]),
+            "clocks": r["clocks"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -111,6 +111,10 @@ struct gbh_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gbh_stats stats{};
+    // per-step I/O (h_in_msgs / h_out_msgs)
+    int n_in = 0, n_out = 0;
+    DBuf<double> d_in_vals, d_out_vals;
+    DBuf<int64_t> d_in_start, d_in_addr, d_out_addr;
 };
 
 namespace {
@@ -465,9 +469,108 @@ int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 
 }  // namespace
 
+__global__ void k_scatter_inputs(const double *vals, const int64_t *start, const int64_t *addr, int n,
+                                 double *P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = vals[i];
+    for (int64_t k = start[i]; k < start[i + 1]; ++k) P[addr[k]] = v;
+}
+
+__global__ void k_gather_outputs(const double *V, const int64_t *addr, int n, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = V[addr[i]];
+}
+
 extern "C" {
 
 const char *gbh_last_error(void) { return g_last_error; }
+
+int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index)
+{
+    if (!e || n < 0 || (n && (!solver || !chip_index))) return GBH_ERR_ARG;
+    // chip index -> every field row that copies it
+    std::vector<std::vector<int64_t>> addrs(n);
+    std::unordered_map<int64_t, int> want;
+    for (int i = 0; i < n; ++i) {
+        if (solver[i] < 0 || solver[i] >= e->nsolvers) return GBH_ERR_ARG;
+        want[e->chip_start[solver[i]] + chip_index[i]] = i;
+    }
+    for (size_t k = 0; k < e->dec.neurons.size(); ++k) {
+        const Neuron &N = e->dec.neurons[k];
+        const Tile &t = e->tiles[e->neuron_tile[k]];
+        const int l = e->neuron_lane[k];
+        for (size_t f = 0; f < N.fsrc.size(); ++f) {
+            if (N.fsrc[f].kind != FS_CHIP) continue;
+            auto it = want.find(e->chip_start[N.solver] + N.fsrc[f].idx);
+            if (it != want.end()) addrs[it->second].push_back((t.fld + (int64_t)f) * LANES + l);
+        }
+    }
+    std::vector<int64_t> start(n + 1, 0), flat;
+    for (int i = 0; i < n; ++i) {
+        if (addrs[i].empty()) {
+            set_last("input %d (solver %d, chip[%lld]) is not read by any compartment program", i, solver[i],
+                     (long long)chip_index[i]);
+            return GBH_ERR_ARG;
+        }
+        start[i + 1] = start[i] + (int64_t)addrs[i].size();
+        flat.insert(flat.end(), addrs[i].begin(), addrs[i].end());
+    }
+    e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
+    if (e->d_in_vals.alloc(n) || e->d_in_start.upload(start) || e->d_in_addr.upload(flat)) return GBH_ERR_CUDA;
+    e->n_in = n;
+    return GBH_OK;
+}
+
+int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream)
+{
+    if (!e || !host_values) return GBH_ERR_ARG;
+    if (e->n_in == 0) return GBH_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(e->d_in_vals.p, host_values, e->n_in * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_scatter_inputs<<<(e->n_in + 255) / 256, 256, 0, st>>>(e->d_in_vals.p, e->d_in_start.p, e->d_in_addr.p,
+                                                           e->n_in, e->d_P.p);
+    CK(cudaGetLastError());
+    return GBH_OK;
+}
+
+int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row)
+{
+    if (!e || n < 0 || (n && (!solver || !row))) return GBH_ERR_ARG;
+    // (solver, row) -> neuron: neurons of a solver are contiguous in row order
+    std::vector<int64_t> addr(n);
+    for (int i = 0; i < n; ++i) {
+        const int s = solver[i];
+        if (s < 0 || s >= e->nsolvers) return GBH_ERR_ARG;
+        int found = -1;
+        for (int k = e->dec.solver_first_neuron[s]; k < e->dec.solver_first_neuron[s + 1]; ++k) {
+            const Neuron &N = e->dec.neurons[k];
+            if (row[i] >= N.row0 && row[i] < N.row0 + N.nrows) { found = k; break; }
+        }
+        if (found < 0) return GBH_ERR_ARG;
+        const Neuron &N = e->dec.neurons[found];
+        const Tile &t = e->tiles[e->neuron_tile[found]];
+        addr[i] = (t.vm + (row[i] - N.row0)) * LANES + e->neuron_lane[found];
+    }
+    e->d_out_vals.release(); e->d_out_addr.release();
+    if (e->d_out_vals.alloc(n) || e->d_out_addr.upload(addr)) return GBH_ERR_CUDA;
+    e->n_out = n;
+    return GBH_OK;
+}
+
+int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
+{
+    if (!e || !host_values) return GBH_ERR_ARG;
+    if (e->n_out == 0) return GBH_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_gather_outputs<<<(e->n_out + 255) / 256, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, e->n_out,
+                                                             e->d_out_vals.p);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host_values, e->d_out_vals.p, e->n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return GBH_OK;
+}
 
 int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons, int64_t *n_types)
 {
@@ -695,6 +798,8 @@ void gbh_destroy(gbh_engine *e)
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
+    e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
+    e->d_out_vals.release(); e->d_out_addr.release();
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->stream) cudaStreamDestroy(e->stream);

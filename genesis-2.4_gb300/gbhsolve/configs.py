@@ -226,3 +226,45 @@ def hh_network(n_cells=4000, frac_exc=0.8, p_conn=0.02, seed=1, dt=1e-4, delay=1
                child_pos=np.array(chan, np.int32),
                weight=np.full(len(tgt), f32(weight)), delay_steps=np.full(len(tgt), dsteps, np.int32))
     return models, syn
+
+
+# --------------------------------------------------------------------------
+# Fast construction of many identical neurons
+# --------------------------------------------------------------------------
+def replicate(h, n, inject=None, vm=None):
+    """``n`` one-neuron hsolves that share every array of ``h`` except chip[]
+    (per-neuron inject current, compartment row 0's chip[1] slot of the soma)
+    and vm. Equivalent to building each copy with :func:`model.build`.
+
+    ``inject``: per-neuron values written into the soma's inject slot."""
+    import copy
+    soma = h.ncompts - 1                      # the root is the last row
+    slot = int(h.compchips[soma]) + 1         # chip layout: Em/Rm, inject, ...
+    out = []
+    for i in range(n):
+        c = copy.copy(h)
+        if inject is not None:
+            chip = h.chip.copy()
+            chip[slot] = f32(inject[i])
+            c.chip = chip
+        if vm is not None:
+            c.vm = np.full_like(h.vm, vm[i]) if np.ndim(vm[i]) == 0 else np.asarray(vm[i])
+        out.append(c)
+    return out
+
+
+def inject_slot(h):
+    """chip[] index of the soma's inject current in a one-neuron hsolve."""
+    return int(h.compchips[h.ncompts - 1]) + 1
+
+
+def cables_replicated(n_neurons, ncomp=16, seed=0, dt=20e-6, method=BEULER, gk_dend=0.0,
+                      inject_range=(0.1e-9, 0.5e-9), erest=-0.065):
+    """Configs 0/3 as one hsolve per neuron, built once and replicated."""
+    rng = np.random.default_rng(seed)
+    injects = rng.uniform(inject_range[0], inject_range[1], size=n_neurons)
+    na, k = hh_channels(erest)
+    from .model import build
+    h = build(Model(cable_neuron(na, k, float(injects[0]), ncomp, erest=erest, gk_dend=gk_dend),
+                    dt=sli(dt), method=method))
+    return replicate(h, n_neurons, inject=[sli(x) for x in injects]), injects

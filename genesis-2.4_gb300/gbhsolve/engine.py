@@ -70,7 +70,8 @@ class GbhStats(C.Structure):
 
 
 EXPORTED = ["gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
-            "gbh_enable_givals", "gbh_get_givals", "gbh_get_spike_counts", "gbh_get_stats",
+            "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
+            "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error"]
 
 _LIB = None
@@ -101,6 +102,10 @@ def load(build_if_missing: bool = True):
     lib.gbh_enable_givals.argtypes = [C.c_void_p, C.c_int]
     lib.gbh_get_givals.argtypes = [C.c_void_p, _dp]
     lib.gbh_get_spike_counts.argtypes = [C.c_void_p, _lp]
+    lib.gbh_register_inputs.argtypes = [C.c_void_p, C.c_int, _ip, _lp]
+    lib.gbh_set_inputs_async.argtypes = [C.c_void_p, _dp, C.c_void_p]
+    lib.gbh_register_outputs.argtypes = [C.c_void_p, C.c_int, _ip, _ip]
+    lib.gbh_get_outputs_async.argtypes = [C.c_void_p, _dp, C.c_void_p]
     lib.gbh_get_stats.argtypes = [C.c_void_p, C.POINTER(GbhStats)]
     lib.gbh_destroy.argtypes = [C.c_void_p]
     lib.gbh_last_error.restype = C.c_char_p
@@ -294,6 +299,24 @@ class Engine:
         g = np.array(b.givals, copy=True)
         self._check(self.lib.gbh_get_givals(self.h, _ptr(g, _dp)))
         return b.split(g, b.givals_start)
+
+    def register_inputs(self, solver, chip_index):
+        self._in_s = np.ascontiguousarray(solver, dtype=np.int32)
+        self._in_c = np.ascontiguousarray(chip_index, dtype=np.int64)
+        self._check(self.lib.gbh_register_inputs(self.h, len(self._in_s), _ptr(self._in_s, _ip),
+                                                 _ptr(self._in_c, _lp)))
+
+    def set_inputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
+        self._check(self.lib.gbh_set_inputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))
+
+    def register_outputs(self, solver, row):
+        self._out_s = np.ascontiguousarray(solver, dtype=np.int32)
+        self._out_r = np.ascontiguousarray(row, dtype=np.int32)
+        self._check(self.lib.gbh_register_outputs(self.h, len(self._out_s), _ptr(self._out_s, _ip),
+                                                  _ptr(self._out_r, _ip)))
+
+    def get_outputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
+        self._check(self.lib.gbh_get_outputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))
 
     def spike_counts(self) -> np.ndarray:
         c = np.zeros(self.batch.n, dtype=np.int64)

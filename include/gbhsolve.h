@@ -166,6 +166,25 @@ int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const dou
 int gbh_enable_givals(gbh_engine *e, int enable);
 int gbh_get_givals(gbh_engine *e, double *givals);
 
+/*
+ * Per-step inputs and outputs, the engine side of h_in_msgs / h_out_msgs
+ * (genesis/src/hines/hines_msgs.c:351-405, 423-486).
+ *
+ * gbh_register_inputs names n chip[] entries (solver, index within that
+ * solver's chip[]) that the caller rewrites between steps -- INJECT, BASE or
+ * THRESH message targets. gbh_set_inputs_async copies n values from host
+ * memory (pinned for full speed) and scatters them into the engine on the
+ * given stream, ordered before the next gbh_run_async on that stream.
+ *
+ * gbh_register_outputs names n compartments (solver, Hines row) whose Vm the
+ * caller records; gbh_get_outputs_async gathers them and copies n doubles to
+ * host memory on the stream (complete after a stream synchronize).
+ */
+int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index);
+int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream);
+int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row);
+int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream);
+
 /* Per-solver spike counts since creation (int64[nsolvers]). */
 int gbh_get_spike_counts(gbh_engine *e, int64_t *counts);
 
