@@ -469,6 +469,34 @@ int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 
 }  // namespace
 
+// Internal: the step loop of run_steps with the flux scratch supplied by the
+// caller (used by gbh_run_noalloc). Reports the flux elements the engine needs.
+int64_t gbh_internal_flux_elems(const gbh_engine *e) { return e->rows_pool * (int64_t)LANES; }
+int gbh_internal_device(const gbh_engine *e) { return e->opt.device; }
+
+int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, double *flux)
+{
+    DevView v = view_of(e);
+    v.F = flux;
+    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+    int done = 0;
+    while (done < nsteps) {
+        int k = std::min(e->steps_per_launch, nsteps - done);
+        const bool last = done + k == nsteps;
+        const bool giv = e->givals_enabled && last;
+        if (giv && k > 1) k -= 1;
+        const bool giv_now = giv && done + k == nsteps;
+        for (const Launch &L : e->launches) {
+            const int rc = launch_one(e, v, L, k, e->step, mixed, giv_now, st);
+            if (rc) return rc;
+        }
+        e->step += k;
+        done += k;
+    }
+    if (e->givals_enabled) e->givals_valid = true;
+    return GBH_OK;
+}
+
 __global__ void k_scatter_inputs(const double *vals, const int64_t *start, const int64_t *addr, int n,
                                  double *P)
 {

@@ -55,6 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         ("gbh_k64.cu", ["--fmad=false", "-Xptxas", "-v"] if verbose else ["--fmad=false"]),
         ("gbh_k32.cu", ["-Xptxas", "-v"] if verbose else []),
         ("gbh_engine.cu", []),
+        ("gbh_noalloc.cu", []),
         ("gbh_decode.cpp", []),
     ]
 

@@ -72,7 +72,7 @@ class GbhStats(C.Structure):
 EXPORTED = ["gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
-            "gbh_destroy", "gbh_last_error"]
+            "gbh_destroy", "gbh_last_error", "gbh_run_noalloc"]
 
 _LIB = None
 
@@ -109,6 +109,7 @@ def load(build_if_missing: bool = True):
     lib.gbh_get_stats.argtypes = [C.c_void_p, C.POINTER(GbhStats)]
     lib.gbh_destroy.argtypes = [C.c_void_p]
     lib.gbh_last_error.restype = C.c_char_p
+    lib.gbh_run_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     _LIB = lib
     return lib
 
@@ -258,6 +259,10 @@ class Engine:
 
     def run(self, nsteps: int) -> None:
         self._check(self.lib.gbh_run(self.h, int(nsteps)))
+
+    def run_noalloc(self, nsteps: int, stream_handle: int = 0) -> None:
+        """gbh_run_noalloc: the step with the library's fixed flux scratch."""
+        self._check(self.lib.gbh_run_noalloc(self.h, int(nsteps), C.c_void_p(stream_handle)))
 
     def run_async(self, nsteps: int, stream_handle: int) -> None:
         self._check(self.lib.gbh_run_async(self.h, int(nsteps), C.c_void_p(stream_handle)))

@@ -189,6 +189,32 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream);
 int gbh_get_spike_counts(gbh_engine *e, int64_t *counts);
 
 int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
+
+/*
+ * gbh_run_noalloc -- advance the engine by nsteps with no device allocation.
+ *
+ * No counterpart in the reference: its CUDA backend allocates per solver.
+ * This exists for hosts that are not allowed to allocate device memory while
+ * the simulation steps, for example a GENESIS build that issues the step
+ * inside CUDA stream capture (allocation calls are not permitted there) or
+ * one that sizes a device memory pool once at start-up. Results equal
+ * gbh_run's on the same engine.
+ *
+ * The step kernel's per-step scratch -- the Ca flux rows, one double per Ca
+ * pool per neuron slot, padded to 32 lanes -- comes from a fixed array of
+ * GBH_NOALLOC_FLUX_MAX doubles (8 MiB) compiled into the library, which every
+ * GPU that loads the library keeps until the process exits. Engines that need
+ * more are rejected with GBH_ERR_ARG. The call makes no cudaMalloc/cudaFree
+ * or other allocating call; it clears the part of the array it uses before
+ * stepping. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls that may overlap on the GPU (other
+ * streams, other engines) race on it and must be serialised by the caller.
+ * stream is a cudaStream_t passed as void* (NULL = default stream); the call
+ * returns once the work is queued.
+ */
+#define GBH_NOALLOC_FLUX_MAX (1 << 20)
+int gbh_run_noalloc(gbh_engine *e, int nsteps, void *stream);
 void gbh_destroy(gbh_engine *e);
 
 /* Static description of the last error on this thread (never NULL). */
