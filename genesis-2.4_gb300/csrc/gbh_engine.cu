@@ -14,6 +14,7 @@
 
 #include "gbh_decode.h"
 #include "gbh_kernels.cuh"
+#include "gbh_df.cuh"
 #include "gbhsolve.h"
 
 using namespace gbh;
@@ -92,6 +93,8 @@ struct gbh_engine {
     DBuf<TableGeom> d_tgeom;
     DBuf<double> d_tab64, d_xy;
     DBuf<float> d_tab32;
+    DBuf<float4> d_tabdf;
+    std::vector<std::vector<char>> type_df;     // mixed: field rows stored as packed double-float
     DBuf<double> d_P, d_V, d_C, d_F, d_A, d_B, d_Cb, d_giv, d_stab;
     DBuf<int> d_I, d_par;
     DBuf<unsigned> d_ring;
@@ -135,6 +138,62 @@ int fail_err(gbh_error *err, int code, const char *fmt, ...)
     }
     set_last("%s", buf);
     return code;
+}
+
+// Operand counts of the engine micro-ops (see gbh_internal.h).
+int micro_operands(int code)
+{
+    switch (code) {
+    case M_BEGIN: return 4;
+    case M_NEWVOLT: case M_NEWCONC1: case M_FLUX: case M_DO_TABGHK: return 0;
+    case M_CONCVAL: case M_DOMAIN: case M_NEWCONC2: case M_SCALE_FLUX: case M_SAME_GHK:
+    case M_CHAN_G: case M_ADDCURR: return 1;
+    case M_NERNST: case M_CHAN: case M_STORE: return 2;
+    case M_SPIKE: case M_GHK: case M_END: return 3;
+    case M_ELMMPUMP: case M_GATE: case M_MGBLOCK: return 4;
+    case M_SYN: return 6;
+    default: return -1;
+    }
+}
+
+// Fields the mixed-precision kernel reads as packed double-float pairs.
+std::vector<char> df_fields_of(const TileType &tt, const std::vector<int> &prog)
+{
+    std::vector<char> m(tt.nfields, 0);
+    size_t pc = tt.prog_off;
+    for (int s = 0; s < tt.nslots; ++s) {
+        for (;;) {
+            const int code = prog[pc];
+            const int n = micro_operands(code);
+            if (n < 0) return m;
+            const int *o = &prog[pc + 1];
+            if (code == M_BEGIN) { m[o[0]] = 1; m[o[1]] = 1; }
+            else if (code == M_CHAN) { m[o[0]] = 1; m[o[1]] = 1; }
+            else if (code == M_CHAN_G) { m[o[0]] = 1; }
+            else if (code == M_GATE && o[2] != 0) { m[o[3]] = 1; }
+            else if (code == M_END) { m[o[0]] = 1; m[o[1]] = 1; }
+            pc += 1 + n;
+            if (code == M_END) break;
+        }
+    }
+    return m;
+}
+
+double pack_df(double x)
+{
+    const float hi = (float)x;
+    const float lo = (float)(x - (double)hi);
+    float2 f = make_float2(hi, lo);
+    double d;
+    memcpy(&d, &f, sizeof(d));
+    return d;
+}
+
+double unpack_df(double d)
+{
+    float2 f;
+    memcpy(&f, &d, sizeof(d));
+    return (double)f.x + (double)f.y;
 }
 
 // Shared-memory budget per block for the elimination columns.
@@ -250,6 +309,18 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         for (size_t p = 0; p < N.pool_conc.size(); ++p)
             C[(t.pools + p) * L + l] = d->conc[d->conc_start[N.solver] + N.pool_conc[p]];
     }
+    // ---- mixed precision: double-float packing of the fields read as df ----
+    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+    e->type_df.assign(e->types.size(), std::vector<char>());
+    if (mixed) {
+        for (size_t ti = 0; ti < e->types.size(); ++ti) e->type_df[ti] = df_fields_of(e->types[ti], prog_pool);
+        for (const Tile &t : e->tiles) {
+            const std::vector<char> &m = e->type_df[t.type];
+            for (int f = 0; f < (int)m.size(); ++f)
+                if (m[f])
+                    for (int l = 0; l < LANES; ++l) P[(t.fld + f) * L + l] = pack_df(P[(t.fld + f) * L + l]);
+        }
+    }
     // ---- synapses: CSR over global neuron index ----
     std::vector<int64_t> out_start(gneuron + 1, 0), out_base;
     std::vector<int> out_delay;
@@ -351,6 +422,26 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     }
     tab32.resize(tab64.size());
     for (size_t i = 0; i < tab64.size(); ++i) tab32[i] = (float)tab64[i];
+    // double-float entries (value, difference to the next row) for the mixed kernel
+    std::vector<float4> tabdf(tab64.size());
+    for (int k = 0; k < d->ntables; ++k) {
+        TableGeom &g = tg[k];
+        const int nc = g.ncols;
+        const int64_t rows = nc ? (int64_t)g.xdivs + 2 : 0;   // including the padding row
+        for (int64_t r = 0; r < rows; ++r)
+            for (int cc = 0; cc < nc; ++cc) {
+                const int64_t i = g.tab_off + r * nc + cc;
+                const double t0 = tab64[i];
+                const double dlt = (r + 1 < rows) ? tab64[i + nc] - t0 : 0.0;
+                const float th = (float)t0, dh = (float)dlt;
+                tabdf[i] = make_float4(th, (float)(t0 - (double)th), dh, (float)(dlt - (double)dh));
+            }
+        auto split = [](double x, float &h, float &l) { h = (float)x; l = (float)(x - (double)h); };
+        split(g.xmin, g.xmin_hi, g.xmin_lo);
+        split(g.invdx, g.invdx_hi, g.invdx_lo);
+        split(g.ymin, g.ymin_hi, g.ymin_lo);
+        split(g.invdy, g.invdy_hi, g.invdy_lo);
+    }
     std::vector<double> stab(d->stablist, d->stablist + d->stab_start[d->nsolvers]);
 
     // ---- upload ----
@@ -361,6 +452,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_tgeom.upload(tg);
     rc |= e->d_tab64.upload(tab64);
     rc |= e->d_tab32.upload(tab32);
+    rc |= e->d_tabdf.upload(tabdf);
     rc |= e->d_xy.upload(xy);
     rc |= e->d_P.upload(P);
     rc |= e->d_V.upload(V);
@@ -388,7 +480,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         // bucket: tiles whose slot count is above half of smax
         size_t t1 = t0;
         while (t1 < e->tiles.size() && e->types[e->tiles[t1].type].nslots * 2 > smax) ++t1;
-        const int per_warp = 2 * smax * LANES * (int)sizeof(double);
+        const int per_warp = (mixed ? 3 : 2) * smax * LANES * (int)sizeof(double);
         int warps = e->opt.warps_per_block > 0 ? e->opt.warps_per_block : 4;
         warps = std::max(1, std::min(warps, kSmemPerBlock / per_warp));
         if (per_warp > 200 * 1024)
@@ -409,6 +501,7 @@ DevView view_of(gbh_engine *e)
     v.tgeom = e->d_tgeom.p;
     v.tab64 = e->d_tab64.p;
     v.tab32 = e->d_tab32.p;
+    v.tabdf = e->d_tabdf.p;
     v.xyvals = e->d_xy.p;
     v.P = e->d_P.p;
     v.I = e->d_I.p;
@@ -497,13 +590,24 @@ int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, doubl
     return GBH_OK;
 }
 
+constexpr int64_t kPackedFlag = 1LL << 62;   // input address holds a packed double-float
+
 __global__ void k_scatter_inputs(const double *vals, const int64_t *start, const int64_t *addr, int n,
                                  double *P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double v = vals[i];
-    for (int64_t k = start[i]; k < start[i + 1]; ++k) P[addr[k]] = v;
+    for (int64_t k = start[i]; k < start[i + 1]; ++k) {
+        const int64_t a = addr[k];
+        if (a & kPackedFlag) {
+            const float hi = __double2float_rn(v);
+            const float lo = __double2float_rn(v - (double)hi);
+            *reinterpret_cast<float2 *>(&P[a & ~kPackedFlag]) = make_float2(hi, lo);
+        } else {
+            P[a] = v;
+        }
+    }
 }
 
 __global__ void k_gather_outputs(const double *V, const int64_t *addr, int n, double *out)
@@ -533,7 +637,10 @@ int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *
         for (size_t f = 0; f < N.fsrc.size(); ++f) {
             if (N.fsrc[f].kind != FS_CHIP) continue;
             auto it = want.find(e->chip_start[N.solver] + N.fsrc[f].idx);
-            if (it != want.end()) addrs[it->second].push_back((t.fld + (int64_t)f) * LANES + l);
+            if (it != want.end()) {
+                const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
+                addrs[it->second].push_back(((t.fld + (int64_t)f) * LANES + l) | (packed ? kPackedFlag : 0));
+            }
         }
     }
     std::vector<int64_t> start(n + 1, 0), flat;
@@ -720,10 +827,13 @@ int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *op
         const int l = e->neuron_lane[i];
         if (vm)
             for (int s = 0; s < N.nrows; ++s) vm[e->vm_start[N.solver] + N.row0 + s] = V[(t.vm + s) * L + l];
+        const std::vector<char> &dfm = e->type_df[t.type];
         if (chip)
             for (size_t f = 0; f < N.fsrc.size(); ++f)
-                if (N.fsrc[f].state && N.fsrc[f].kind == FS_CHIP)
-                    chip[e->chip_start[N.solver] + N.fsrc[f].idx] = P[(t.fld + f) * L + l];
+                if (N.fsrc[f].state && N.fsrc[f].kind == FS_CHIP) {
+                    const double raw = P[(t.fld + f) * L + l];
+                    chip[e->chip_start[N.solver] + N.fsrc[f].idx] = (!dfm.empty() && dfm[f]) ? unpack_df(raw) : raw;
+                }
         if (conc)
             for (size_t p = 0; p < N.pool_conc.size(); ++p)
                 conc[e->conc_start[N.solver] + N.pool_conc[p]] = C[(t.pools + p) * L + l];
@@ -749,10 +859,13 @@ int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const dou
         const int l = e->neuron_lane[i];
         if (vm)
             for (int s = 0; s < N.nrows; ++s) V[(t.vm + s) * L + l] = vm[e->vm_start[N.solver] + N.row0 + s];
+        const std::vector<char> &dfm = e->type_df[t.type];
         if (chip)
             for (size_t f = 0; f < N.fsrc.size(); ++f)
-                if (N.fsrc[f].kind == FS_CHIP)
-                    P[(t.fld + f) * L + l] = chip[e->chip_start[N.solver] + N.fsrc[f].idx];
+                if (N.fsrc[f].kind == FS_CHIP) {
+                    const double val = chip[e->chip_start[N.solver] + N.fsrc[f].idx];
+                    P[(t.fld + f) * L + l] = (!dfm.empty() && dfm[f]) ? pack_df(val) : val;
+                }
         if (conc)
             for (size_t p = 0; p < N.pool_conc.size(); ++p)
                 C[(t.pools + p) * L + l] = conc[e->conc_start[N.solver] + N.pool_conc[p]];
@@ -821,7 +934,7 @@ void gbh_destroy(gbh_engine *e)
     if (!e) return;
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
-    e->d_tab64.release(); e->d_tab32.release(); e->d_xy.release(); e->d_P.release();
+    e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
     e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_A.release(); e->d_B.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();

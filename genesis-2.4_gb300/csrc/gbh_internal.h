@@ -59,6 +59,9 @@ struct TableGeom {
     int64_t tab_off;   // offset into the table pool (doubles / floats)
     int64_t xv_off;    // offset into the value pool (xvals)
     int64_t yv_off;    // offset into the value pool (yvals), -1 if none
+    // double-float copies of the axis constants for the mixed-precision kernel
+    float xmin_hi, xmin_lo, invdx_hi, invdx_lo;
+    float ymin_hi, ymin_lo, invdy_hi, invdy_lo;
 };
 
 struct TileType {

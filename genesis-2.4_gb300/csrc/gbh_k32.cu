@@ -1,11 +1,11 @@
 // gbh_k32.cu -- mixed-precision step kernels: gate and table arithmetic in
-// FP32, Vm, elimination and Ca pools in FP64.
-#include "gbh_kernels.cuh"
+// double-float on FP32 instructions; Vm, elimination and Ca pools in FP64.
+#include "gbh_kmixed.cuh"
 
 namespace gbh {
 cudaError_t launch_mixed(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
                          long long step, bool giv, cudaStream_t st)
 {
-    return launch_impl<float>(v, tile0, tile1, smax, warps, nsteps, step, giv, st);
+    return launch_mixed_impl(v, tile0, tile1, smax, warps, nsteps, step, giv, st);
 }
 }  // namespace gbh

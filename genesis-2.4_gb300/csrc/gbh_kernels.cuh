@@ -29,6 +29,7 @@ struct DevView {
     const TableGeom *tgeom;
     const double *tab64;
     const float *tab32;
+    const float4 *tabdf;     // per entry: table value and next-row difference, double-float
     const double *xyvals;
     double *P;        // parameter / state fields
     int *I;           // integer state (spike counters)

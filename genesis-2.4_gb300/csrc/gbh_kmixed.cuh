@@ -1,0 +1,436 @@
+// gbh_kmixed.cuh -- the mixed-precision step kernel.
+//
+// Same tile layout and decoded programs as k_steps (gbh_kernels.cuh), with
+//   * gate and table arithmetic -- table interpolation, the trapezoid /
+//     instantaneous gate update, gate powers, conductance and current sums --
+//     in double-float on FP32 instructions (gbh_df.cuh), tables stored as
+//     (value, next-row difference) double-float pairs;
+//   * Vm, the rhs/diagonal of each row, the Hines elimination and the Ca pools
+//     in FP64, the elimination dividing through a reciprocal refined by one
+//     Newton step from an FP32 seed (one reciprocal per row instead of two
+//     IEEE divisions);
+//   * conversions between the two representations on the integer pipe.
+// It does not reproduce the reference bit for bit; its error against the
+// FP64 CPU solver is measured and reported instead.
+#pragma once
+#include "gbh_df.cuh"
+#include "gbh_kernels.cuh"
+
+namespace gbh {
+
+struct DCursor {
+    int row, base;
+    df frac;
+};
+
+// table position of value v on an axis (min, inv) with divs rows, clamped
+__device__ __forceinline__ void locate_df(DCursor &c, df v, df nmin, df inv, int divs, int ncols)
+{
+    df f = df_mul(df_add(v, nmin), inv);
+    int row;
+    if (f.hi <= 0.0f) {
+        row = 0;
+        f = df_make(0.f, 0.f);
+    } else if (f.hi >= (float)divs) {
+        row = divs;
+        f = df_make(0.f, 0.f);
+    } else {
+        row = (int)floorf(f.hi);
+        f = df_add_f(f, -(float)row);
+        if (f.hi < 0.0f) {
+            row -= 1;
+            f = df_add_f(f, 1.0f);
+        } else if (f.hi >= 1.0f) {
+            row += 1;
+            f = df_add_f(f, -1.0f);
+        }
+    }
+    c.row = row;
+    c.base = row * ncols;
+    c.frac = f;
+}
+
+__device__ __forceinline__ df ld_df(const double *p)
+{
+    const float2 v = *reinterpret_cast<const float2 *>(p);
+    return df_make(v.x, v.y);
+}
+
+__device__ __forceinline__ void st_df(double *p, df x)
+{
+    *reinterpret_cast<float2 *>(p) = make_float2(x.hi, x.lo);
+}
+
+// interpolated value of table entry e at fraction fr: value + fr*difference
+__device__ __forceinline__ df interp_df(const float4 *tab, int e, df fr)
+{
+    const float4 t = tab[e];
+    return df_add(df_make(t.x, t.y), df_mul(df_make(t.z, t.w), fr));
+}
+
+__device__ __forceinline__ df val_df(const float4 *tab, int e)
+{
+    const float4 t = tab[e];
+    return df_make(t.x, t.y);
+}
+
+__device__ __forceinline__ df dpow(df g, df x, int p)
+{
+    switch (p) {
+    case 1: return df_mul(g, x);
+    case 2: return df_mul(g, df_mul(x, x));
+    case 3: return df_mul(g, df_mul(df_mul(x, x), x));
+    case 4: x = df_mul(x, x); return df_mul(g, df_mul(x, x));
+    case 5: g = df_mul(g, x); x = df_mul(x, x); x = df_mul(x, x); return df_mul(g, x);
+    default: x = df_mul(x, x); g = df_mul(g, x); x = df_mul(x, x); return df_mul(g, x);
+    }
+}
+
+template <bool GIV>
+__global__ void __launch_bounds__(256)
+k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
+{
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib;
+    if (t >= tile1) return;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const float4 *tab = v.tabdf + tg.tab_off;
+    const int ncols = tg.ncols;
+    const df xnmin = df_make(-tg.xmin_hi, -tg.xmin_lo), xinv = df_make(tg.invdx_hi, tg.invdx_lo);
+    const df ynmin = df_make(-tg.ymin_hi, -tg.ymin_lo), yinv = df_make(tg.invdy_hi, tg.invdy_lo);
+    const bool c5 = ty.chanmode5 != 0;
+    const bool active = lane < tl.nlanes;
+
+    double *Pw = v.P + tl.fld * LANES + lane;
+    int *Iw = v.I + tl.ints * LANES + lane;
+    double *Vw = v.V + tl.vm * LANES + lane;
+    double *Cw = v.C + tl.pools * LANES + lane;
+    double *Fw = v.F + tl.pools * LANES + lane;
+    double *Gw = v.giv + tl.giv * LANES + lane;
+    const int *par = v.parent + tl.topo * LANES + lane;
+    const double *Aw = v.A + tl.topo * LANES + lane;
+    const double *Bw = v.B + tl.topo * LANES + lane;
+    const double *Cbw = v.Cb + tl.topo * LANES + lane;
+    double *Dcol = sm + (size_t)wib * 3 * smax * LANES + lane;
+    double *Rcol = Dcol + (size_t)smax * LANES;
+    double *Icol = Rcol + (size_t)smax * LANES;   // reciprocal of each eliminated diagonal
+    const int S = ty.nslots;
+    const int64_t neuron = tl.first_neuron + lane;
+
+    for (int it = 0; it < nsteps; ++it) {
+        const long long step = step0 + it;
+        DCursor vc, cc, c1;
+        vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f);
+        cc = vc;
+        c1 = vc;
+        int sel = 0;
+        df Ek = df_make(0.f, 0.f), Gk = Ek, gmax = Ek;
+        double GHK = 0.0, Ik = 0.0;
+        int doGHK = 0;
+        const int *pc = v.prog + ty.prog_off;
+        for (int s = 0; s < S; ++s) {
+            const double Vm = Vw[s * LANES];
+            const df vmd = d2df(Vm);
+            df sumg = df_make(0.f, 0.f), ichan = sumg;
+            double Im = 0.0;
+            for (;;) {
+                const int code = pc[0];
+                if (code == M_BEGIN) {
+                    const df emrm = ld_df(&Pw[pc[1] * LANES]);
+                    ichan = df_add(emrm, ld_df(&Pw[pc[2] * LANES]));
+                    if (GIV) {
+                        Im = df2d(emrm) - Vm / Pw[pc[3] * LANES];
+                        Gw[pc[4] * LANES] = Im;
+                    }
+                    pc += 5;
+                } else if (code == M_NEWVOLT) {
+                    locate_df(vc, vmd, xnmin, xinv, tg.xdivs, ncols);
+                    pc += 1;
+                } else if (code == M_CONCVAL) {
+                    sel = pc[1];
+                    Fw[sel * LANES] = 0.0;
+                    pc += 2;
+                } else if (code == M_DOMAIN) {
+                    locate_df(cc, d2df(Pw[pc[1] * LANES] * Ik), ynmin, yinv, tg.ydivs, ncols);
+                    pc += 2;
+                } else if (code == M_NEWCONC2) {
+                    c1 = cc;
+                    locate_df(cc, d2df(Cw[pc[1] * LANES]), ynmin, yinv, tg.ydivs, ncols);
+                    pc += 2;
+                } else if (code == M_NEWCONC1) {
+                    locate_df(cc, d2df(Cw[sel * LANES]), ynmin, yinv, tg.ydivs, ncols);
+                    pc += 1;
+                } else if (code == M_SPIKE) {
+                    int cnt = Iw[pc[2] * LANES] - 1;
+                    if (Vm > Pw[pc[1] * LANES]) {
+                        if (cnt <= 0 && active) {
+                            const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
+                            for (int64_t e = e0; e < e1; ++e) {
+                                const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
+                                atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
+                            }
+                            v.spikes[neuron] += 1ULL;
+                            cnt = Iw[pc[3] * LANES];
+                        }
+                    }
+                    Iw[pc[2] * LANES] = cnt;
+                    pc += 4;
+                } else if (code == M_ELMMPUMP) {
+                    const double cx = Cw[sel * LANES];
+                    const double X = 1.0 / (cx + Pw[pc[1] * LANES]);
+                    const double vmax = Pw[pc[2] * LANES];
+                    Ik = vmax * cx * X;
+                    ichan = df_add(ichan, d2df(Ik));
+                    if (GIV) Gw[pc[4] * LANES] = c5 ? Ik / vmax : Ik;
+                    Im += Ik;
+                    pc += 5;
+                } else if (code == M_FLUX) {
+                    Fw[sel * LANES] += Ik;
+                    pc += 1;
+                } else if (code == M_SCALE_FLUX) {
+                    Fw[sel * LANES] += Pw[pc[1] * LANES] * Ik;
+                    pc += 2;
+                } else if (code == M_STORE) {
+                    pc += 3;
+                } else if (code == M_END) {
+                    const df tbyc = ld_df(&Pw[pc[1] * LANES]);
+                    const df dv = df_mul(ichan, tbyc);
+                    Rcol[s * LANES] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);
+                    Dcol[s * LANES] = df2d(df_add(df_mul(sumg, tbyc), ld_df(&Pw[pc[2] * LANES])));
+                    if (GIV) Gw[pc[3] * LANES] = Im;
+                    pc += 4;
+                    break;
+                } else {
+                    if (code == M_GHK) {
+                        const double cin = Cw[sel * LANES], cout = Cw[(sel + 1) * LANES];
+                        double g = Pw[pc[1] * LANES];
+                        const double X = Vm * g;
+                        const double Y = exp(-X);
+                        double e = Pw[pc[2] * LANES];
+                        double ik = e * (cin - (Y * cout));
+                        double gk;
+                        if (fabs(X) < 1.0e-6) {
+                            gk = 1.0 - 0.5 * X;
+                            g = 0.5 * g * e * (cin + cout);
+                            ik = -ik / gk;
+                        } else {
+                            gk = 1.0 - Y;
+                            g = g * (ik / gk - e * g * (cin - cout) * Vm * Y / (gk * gk));
+                            ik = -X * ik / gk;
+                        }
+                        GHK = g;
+                        Ek = d2df((ik + g * Vm) / g);
+                        gmax = d2df(Pw[pc[3] * LANES]);
+                        Gk = d2df(Pw[pc[3] * LANES] * GHK);
+                        pc += 4;
+                    } else if (code == M_SAME_GHK) {
+                        gmax = d2df(Pw[pc[1] * LANES]);
+                        Gk = d2df(Pw[pc[1] * LANES] * GHK);
+                        pc += 2;
+                    } else if (code == M_DO_TABGHK) {
+                        doGHK = 1;
+                        pc += 1;
+                    } else if (code == M_NERNST) {
+                        Ek = d2df(log(Cw[(sel + 1) * LANES] / Cw[sel * LANES]) * Pw[pc[1] * LANES]);
+                        gmax = Gk = d2df(Pw[pc[2] * LANES]);
+                        pc += 3;
+                    } else if (code == M_CHAN) {
+                        Ek = ld_df(&Pw[pc[1] * LANES]);
+                        gmax = Gk = ld_df(&Pw[pc[2] * LANES]);
+                        pc += 3;
+                    } else if (code == M_CHAN_G) {
+                        gmax = Gk = ld_df(&Pw[pc[1] * LANES]);
+                        pc += 2;
+                    } else {
+                        if (v.status) atomicOr(v.status, ST_BAD_OP);
+                        return;
+                    }
+                    for (;;) {
+                        const int k = pc[0];
+                        if (k == M_GATE) {
+                            const int kind = pc[1];
+                            df X, Y;
+                            if (kind == GK_1V || kind == GK_1C) {
+                                const DCursor &cu = (kind == GK_1V) ? vc : cc;
+                                const int b = cu.base + pc[2];
+                                X = interp_df(tab, b, cu.frac);
+                                Y = interp_df(tab, b + 1, cu.frac);
+                            } else {
+                                // 2-D tables: rows from the voltage (or first conc) cursor,
+                                // columns from the conc cursor
+                                const DCursor &ru = (kind == GK_2V) ? vc : c1;
+                                const int b = ru.base + cc.row + cc.row + pc[2];
+                                const df cf = cc.frac, rf = ru.frac;
+                                const df one_c = df_add_f(df_neg(cf), 1.0f), one_r = df_add_f(df_neg(rf), 1.0f);
+                                df q[2];
+                                for (int h = 0; h < 2; ++h) {
+                                    const df t00 = val_df(tab, b + h), t01 = val_df(tab, b + 2 + h);
+                                    const df t10 = interp_df(tab, b + h, df_make(1.f, 0.f));
+                                    const df t11 = interp_df(tab, b + 2 + h, df_make(1.f, 0.f));
+                                    const df lo = df_add(df_mul(one_c, t00), df_mul(cf, t01));
+                                    const df hi = df_add(df_mul(one_c, t10), df_mul(cf, t11));
+                                    q[h] = df_add(df_mul(one_r, lo), df_mul(rf, hi));
+                                }
+                                X = q[0];
+                                Y = q[1];
+                            }
+                            const int p = pc[3];
+                            if (p == 0) {
+                                Ek = Y;
+                                pc += 5;
+                                if (doGHK) {
+                                    GHK = df2d(X);
+                                    doGHK = 0;
+                                    break;
+                                }
+                                Gk = df_mul(Gk, X);
+                                continue;
+                            }
+                            double *st = &Pw[pc[4] * LANES];
+                            df x;
+                            int pw = p;
+                            if (p > 0) {
+                                x = df_div(df_add(df_mul(ld_df(st), df_add_f(df_neg(X), 2.0f)), Y), X);
+                            } else {
+                                x = df_div(Y, X);
+                                pw = -p;
+                            }
+                            st_df(st, x);
+                            Gk = dpow(Gk, x, pw);
+                            pc += 5;
+                            continue;
+                        } else if (k == M_SYN) {
+                            const double *sl = v.stablist + pc[2];
+                            double *px = &Pw[pc[4] * LANES];
+                            double *py = &Pw[pc[5] * LANES];
+                            if (pc[1] >= 0) {
+                                const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^
+                                                     (uint64_t)pc[4];
+                                if (syn3_uniform(key) <= Pw[pc[1] * LANES]) *px += sl[3];
+                            }
+                            double X = *px * sl[0];
+                            unsigned *cell = v.ring + ((tl.syn + (int64_t)pc[3] * v.ring_len +
+                                                        (int64_t)(step % v.ring_len)) * LANES + lane);
+                            const unsigned n = *cell;
+                            if (n) {
+                                const double wdt = Pw[pc[6] * LANES];
+                                double act = 0.0;
+                                for (unsigned q = 0; q < n; ++q) act += wdt;
+                                X += v.dt * act * sl[3];
+                                *cell = 0u;
+                            }
+                            *px = X;
+                            const double Y = X * sl[1] + *py * sl[2];
+                            *py = Y;
+                            Gk = df_mul(Gk, d2df(Y));
+                            pc += 7;
+                            continue;
+                        } else if (k == M_MGBLOCK) {
+                            const double gk = df2d(Gk), ek = df2d(Ek);
+                            if (GIV) {
+                                const int g = pc[4];
+                                const double gm = c5 ? df2d(gmax) : 1.0;
+                                Gw[g * LANES] = gk / gm;
+                                Gw[(g + 1) * LANES] = gk * (ek - Vm) / gm;
+                                Gw[(g + 2) * LANES] = ek;
+                            }
+                            const double X = Pw[pc[1] * LANES] * exp(Vm * Pw[pc[2] * LANES]);
+                            Gk = d2df(gk * (X / (X + Pw[pc[3] * LANES])));
+                            pc += 5;
+                            continue;
+                        } else if (k == M_ADDCURR) {
+                            const int g = pc[1];
+                            sumg = df_add(sumg, Gk);
+                            ichan = df_add(ichan, df_mul(Ek, Gk));
+                            const double gk = df2d(Gk), ek = df2d(Ek);
+                            Ik = gk * (ek - Vm);
+                            if (GIV) {
+                                const double gm = c5 ? df2d(gmax) : 1.0;
+                                Gw[g * LANES] = gk / gm;
+                                Gw[(g + 1) * LANES] = Ik / gm;
+                                Gw[(g + 2) * LANES] = ek;
+                            }
+                            Im += Ik;
+                            pc += 2;
+                            break;
+                        } else {
+                            if (v.status) atomicOr(v.status, ST_BAD_OP);
+                            return;
+                        }
+                    }
+                }
+            }
+        }
+
+        // Ca pools (FP64)
+        {
+            const int *pp = v.prog + ty.pool_off;
+            while (pp[0] != 0) {
+                if (pp[0] == PO_CACONC) {
+                    double *cx = &Cw[pp[1] * LANES];
+                    const double base = Pw[pp[2] * LANES];
+                    const double itau = Pw[pp[3] * LANES];
+                    *cx = base + ((*cx - base) * (2.0 - itau) + (Fw[pp[1] * LANES] * Pw[pp[4] * LANES])) / itau;
+                    pp += 5;
+                } else {
+                    if (v.status) atomicOr(v.status, ST_BAD_OP);
+                    return;
+                }
+            }
+        }
+
+        // elimination (FP64, one refined reciprocal per row)
+        for (int s = 0; s < S; ++s) {
+            const int p = par[s * LANES];
+            const double ri = rcp_newton(Dcol[s * LANES]);
+            Icol[s * LANES] = ri;
+            if (p >= 0) {
+                const double temp = Aw[s * LANES] * ri;
+                Dcol[p * LANES] = fma(-Bw[s * LANES], temp, Dcol[p * LANES]);
+                Rcol[p * LANES] = fma(-Rcol[s * LANES], temp, Rcol[p * LANES]);
+            }
+        }
+        for (int s = S - 1; s >= 0; --s) {
+            const int p = par[s * LANES];
+            double r = Rcol[s * LANES];
+            if (p >= 0) r = fma(-Cbw[s * LANES], Rcol[p * LANES], r);
+            r = r * Icol[s * LANES];
+            Rcol[s * LANES] = r;
+            if (ty.crank) {
+                const double old = Vw[s * LANES];
+                Vw[s * LANES] = fma(2.0, r, -old);
+            } else {
+                Vw[s * LANES] = r;
+            }
+        }
+    }
+}
+
+inline cudaError_t launch_mixed_impl(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
+                                     long long step, bool giv, cudaStream_t st)
+{
+    const int ntiles = tile1 - tile0;
+    const int blocks = (ntiles + warps - 1) / warps;
+    const size_t smem = (size_t)warps * 3 * smax * LANES * sizeof(double);
+    cudaError_t ce;
+    if (giv) {
+        if (smem > 48 * 1024) {
+            ce = cudaFuncSetAttribute(k_steps_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (ce != cudaSuccess) return ce;
+        }
+        k_steps_mixed<true><<<blocks, warps * LANES, smem, st>>>(v, tile0, tile1, smax, nsteps, step);
+    } else {
+        if (smem > 48 * 1024) {
+            ce = cudaFuncSetAttribute(k_steps_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (ce != cudaSuccess) return ce;
+        }
+        k_steps_mixed<false><<<blocks, warps * LANES, smem, st>>>(v, tile0, tile1, smax, nsteps, step);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace gbh
