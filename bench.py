@@ -266,8 +266,8 @@ def main():
             ms = float(t.item())
         results[form] = dict(ms=ms, launches=launches, spl=st.steps_per_launch,
                              value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng)
-        log("%s: %.3f ms for %d steps, %d launches -> %.3e cs/s" % (form, ms, args.steps, launches,
-                                                                   results[form]["value"]))
+        log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels -> %.3e cs/s" % (
+            form, ms, args.steps, launches, st.jit_kernels, results[form]["value"]))
         if form == "fp64":
             eng.close()
 

@@ -15,6 +15,8 @@
 #include "gbh_decode.h"
 #include "gbh_kernels.cuh"
 #include "gbh_df.cuh"
+#include "gbh_jit.h"
+#include <thread>
 #include "gbhsolve.h"
 
 using namespace gbh;
@@ -69,6 +71,8 @@ struct DBuf {
 
 struct Launch {
     int tile0, tile1, smax, warps;
+    int jit = -1;        // index of a specialised kernel, or -1 to interpret
+    size_t jit_smem = 0;
 };
 
 }  // namespace
@@ -114,6 +118,9 @@ struct gbh_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gbh_stats stats{};
+    std::vector<JitKernel> jits;
+    int jit_compiled = 0;
+    std::string jit_log;
     // per-step I/O (h_in_msgs / h_out_msgs)
     int n_in = 0, n_out = 0;
     DBuf<double> d_in_vals, d_out_vals;
@@ -198,6 +205,50 @@ double unpack_df(double d)
 
 // Shared-memory budget per block for the elimination columns.
 constexpr int kSmemPerBlock = 96 * 1024;
+
+// Composite tables on the device: FP64 copy (plus one padding row), axis
+// value pools and their geometry.
+void build_tables(const gbh_batch_desc *d, std::vector<TableGeom> &tg, std::vector<double> &tab64,
+                  std::vector<double> &xy)
+{
+    tg.assign(d->ntables, TableGeom{});
+    for (int k = 0; k < d->ntables; ++k) {
+        const gbh_tables &T = d->tables[k];
+        TableGeom g{};
+        g.ncols = T.ncols;
+        g.xdivs = T.xdivs;
+        g.ydivs = T.ydivs;
+        g.xmin = T.xmin;
+        g.invdx = T.invdx;
+        g.ymin = T.ymin;
+        g.invdy = T.invdy;
+        g.tab_off = (int64_t)tab64.size();
+        const int64_t rows = T.ncols ? (int64_t)T.xdivs + 1 : 0;
+        for (int64_t r = 0; r < rows; ++r)
+            for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(T.tablist[r * T.ncols + cc]);
+        // one padding row: the clamped top row reads row xdivs+1
+        for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(rows ? T.tablist[(rows - 1) * T.ncols + cc] : 0.0);
+        g.xv_off = (int64_t)xy.size();
+        for (int64_t r = 0; r < rows; ++r) xy.push_back(T.xvals[r]);
+        xy.push_back(rows ? T.xvals[rows - 1] : 0.0);   // empty top bracket: always relocate
+        xy.push_back(0.0);
+        g.yv_off = -1;
+        if (T.ydivs > 0 && T.yvals) {
+            g.yv_off = (int64_t)xy.size();
+            for (int r = 0; r <= T.ydivs; ++r) xy.push_back(T.yvals[r]);
+            xy.push_back(T.yvals[T.ydivs]);
+            xy.push_back(0.0);
+        }
+        tg[k] = g;
+    }
+    for (TableGeom &g : tg) {
+        auto split = [](double x, float &h, float &l) { h = (float)x; l = (float)(x - (double)h); };
+        split(g.xmin, g.xmin_hi, g.xmin_lo);
+        split(g.invdx, g.invdx_hi, g.invdx_lo);
+        split(g.ymin, g.ymin_hi, g.ymin_lo);
+        split(g.invdy, g.invdy_hi, g.invdy_lo);
+    }
+}
 
 int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn, gbh_error *err)
 {
@@ -388,38 +439,10 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         }
     }
     // ---- tables ----
-    std::vector<TableGeom> tg(d->ntables);
+    std::vector<TableGeom> tg;
     std::vector<double> tab64, xy;
     std::vector<float> tab32;
-    for (int k = 0; k < d->ntables; ++k) {
-        const gbh_tables &T = d->tables[k];
-        TableGeom g{};
-        g.ncols = T.ncols;
-        g.xdivs = T.xdivs;
-        g.ydivs = T.ydivs;
-        g.xmin = T.xmin;
-        g.invdx = T.invdx;
-        g.ymin = T.ymin;
-        g.invdy = T.invdy;
-        g.tab_off = (int64_t)tab64.size();
-        const int64_t rows = T.ncols ? (int64_t)T.xdivs + 1 : 0;
-        for (int64_t r = 0; r < rows; ++r)
-            for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(T.tablist[r * T.ncols + cc]);
-        // one padding row: the clamped top row reads row xdivs+1
-        for (int cc = 0; cc < T.ncols; ++cc) tab64.push_back(rows ? T.tablist[(rows - 1) * T.ncols + cc] : 0.0);
-        g.xv_off = (int64_t)xy.size();
-        for (int64_t r = 0; r < rows; ++r) xy.push_back(T.xvals[r]);
-        xy.push_back(rows ? T.xvals[rows - 1] : 0.0);   // empty top bracket: always relocate
-        xy.push_back(0.0);
-        g.yv_off = -1;
-        if (T.ydivs > 0 && T.yvals) {
-            g.yv_off = (int64_t)xy.size();
-            for (int r = 0; r <= T.ydivs; ++r) xy.push_back(T.yvals[r]);
-            xy.push_back(T.yvals[T.ydivs]);
-            xy.push_back(0.0);
-        }
-        tg[k] = g;
-    }
+    build_tables(d, tg, tab64, xy);
     tab32.resize(tab64.size());
     for (size_t i = 0; i < tab64.size(); ++i) tab32[i] = (float)tab64[i];
     // double-float entries (value, difference to the next row) for the mixed kernel
@@ -436,11 +459,6 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 const float th = (float)t0, dh = (float)dlt;
                 tabdf[i] = make_float4(th, (float)(t0 - (double)th), dh, (float)(dlt - (double)dh));
             }
-        auto split = [](double x, float &h, float &l) { h = (float)x; l = (float)(x - (double)h); };
-        split(g.xmin, g.xmin_hi, g.xmin_lo);
-        split(g.invdx, g.invdx_hi, g.invdx_lo);
-        split(g.ymin, g.ymin_hi, g.ymin_lo);
-        split(g.invdy, g.invdy_hi, g.invdy_lo);
     }
     std::vector<double> stab(d->stablist, d->stablist + d->stab_start[d->nsolvers]);
 
@@ -473,15 +491,89 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_status.upload(std::vector<int>(1, 0));
     if (rc) return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
 
-    // ---- launch plan: consecutive tiles bucketed by slot count ----
+    // ---- specialised kernels (one per tile type with enough tiles) ----
+    std::vector<int> type_t0(e->types.size(), -1), type_t1(e->types.size(), -1);
+    for (size_t ti = 0; ti < e->tiles.size(); ++ti) {
+        const int ty = e->tiles[ti].type;
+        if (type_t0[ty] < 0) type_t0[ty] = (int)ti;
+        type_t1[ty] = (int)ti + 1;
+    }
+    std::vector<int> type_jit(e->types.size(), -1);
+    std::vector<char> type_uniform(e->types.size(), 0);
+    std::string why;
+    const bool jit_on = e->opt.jit >= 0 && jit_available(&why);
+    if (!jit_on && e->opt.jit >= 0) e->jit_log = "JIT unavailable: " + why;
+    if (jit_on) {
+        // types in tile order, largest first
+        std::vector<int> cand;
+        for (int ti : torder)
+            if (type_t0[ti] >= 0) cand.push_back(ti);
+        std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
+            return (type_t1[a] - type_t0[a]) > (type_t1[b] - type_t0[b]);
+        });
+        const int max_jit = 24;
+        if ((int)cand.size() > max_jit) cand.resize(max_jit);
+        std::vector<std::string> srcs(cand.size());
+        std::vector<std::vector<int>> upar(cand.size());
+        for (size_t c = 0; c < cand.size(); ++c) {
+            const int ti = cand[c];
+            // is every neuron of this type the same tree?
+            bool uni = true;
+            std::vector<int> ref;
+            for (int i = 0; i < nneu && uni; ++i) {
+                if (e->tiles[e->neuron_tile[i]].type != ti) continue;
+                if (ref.empty()) ref = dec.neurons[i].parent;
+                else if (dec.neurons[i].parent != ref) uni = false;
+            }
+            if (uni && !ref.empty()) upar[c] = ref;
+            srcs[c] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
+                                 upar[c].empty() ? nullptr : &upar[c]);
+        }
+        int dev = e->opt.device, major = 10, minor = 3;
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+        std::vector<JitKernel> ks(cand.size());
+        std::vector<int> ok(cand.size(), 0);
+        std::vector<std::string> logs(cand.size());
+        std::vector<std::thread> th;
+        for (size_t c = 0; c < cand.size(); ++c)
+            th.emplace_back([&, c]() {
+                cudaSetDevice(dev);
+                if (!srcs[c].empty())
+                    ok[c] = jit_compile(srcs[c], !mixed, major, minor, &ks[c], &logs[c]) == 0;
+            });
+        for (auto &x : th) x.join();
+        for (size_t c = 0; c < cand.size(); ++c) {
+            if (ok[c]) {
+                type_jit[cand[c]] = (int)e->jits.size();
+                type_uniform[cand[c]] = !upar[c].empty();
+                e->jits.push_back(ks[c]);
+                e->jit_compiled++;
+            } else if (!logs[c].empty() && e->jit_log.size() < 4000) {
+                e->jit_log += logs[c];
+            }
+        }
+    }
+    // ---- launch plan: specialised types alone, the rest bucketed by slot count ----
     size_t t0 = 0;
     while (t0 < e->tiles.size()) {
-        const int smax = e->types[e->tiles[t0].type].nslots;
-        // bucket: tiles whose slot count is above half of smax
+        const int ty0 = e->tiles[t0].type;
+        if (type_jit[ty0] >= 0) {
+            const int S = e->types[ty0].nslots;
+            Launch L{(int)t0, type_t1[ty0], S, 4};
+            L.jit = type_jit[ty0];
+            L.jit_smem = type_uniform[ty0] ? 0 : (size_t)L.warps * 2 * S * LANES * sizeof(double);
+            e->launches.push_back(L);
+            t0 = type_t1[ty0];
+            continue;
+        }
+        const int smax = e->types[ty0].nslots;
         size_t t1 = t0;
-        while (t1 < e->tiles.size() && e->types[e->tiles[t1].type].nslots * 2 > smax) ++t1;
-        const int per_warp = (mixed ? 3 : 2) * smax * LANES * (int)sizeof(double);
-        int warps = e->opt.warps_per_block > 0 ? e->opt.warps_per_block : 4;
+        while (t1 < e->tiles.size() && type_jit[e->tiles[t1].type] < 0 &&
+               e->types[e->tiles[t1].type].nslots * 2 > smax)
+            ++t1;
+        const int per_warp = 2 * smax * LANES * (int)sizeof(double);
+        int warps = e->opt.warps_per_block > 0 ? std::min(e->opt.warps_per_block, 4) : 4;
         warps = std::max(1, std::min(warps, kSmemPerBlock / per_warp));
         if (per_warp > 200 * 1024)
             return fail_err(err, GBH_ERR_UNSUPPORTED, "neuron with %d compartments exceeds the shared-memory sweep",
@@ -528,6 +620,15 @@ DevView view_of(gbh_engine *e)
 int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long long step, bool mixed,
                bool giv, cudaStream_t st)
 {
+    if (L.jit >= 0 && !giv) {
+        const cudaError_t je = jit_launch(e->jits[L.jit], v, L.tile0, L.tile1, L.smax, L.warps, k, step, L.jit_smem, st);
+        if (je != cudaSuccess) {
+            set_last("specialised kernel launch failed: %s", cudaGetErrorString(je));
+            return GBH_ERR_CUDA;
+        }
+        e->stats.launches++;
+        return GBH_OK;
+    }
     cudaError_t ce = mixed ? launch_mixed(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st)
                            : launch_fp64(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st);
     if (ce != cudaSuccess) {
@@ -707,6 +808,59 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
     return GBH_OK;
 }
 
+int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, char *buf, int64_t buflen)
+{
+    gbh_error err{};
+    Decoded dec;
+    if (decode_batch(desc, dec, &err)) {
+        set_last("%s", err.message);
+        return err.code;
+    }
+    std::map<std::string, int> keys;
+    std::vector<TileType> types;
+    std::vector<int> prog_pool;
+    std::vector<std::vector<int>> parents;
+    std::vector<char> uniform;
+    for (const Neuron &N : dec.neurons) {
+        auto it = keys.find(N.key);
+        if (it == keys.end()) {
+            TileType tt{};
+            tt.nslots = N.nrows;
+            tt.nfields = (int)N.fsrc.size();
+            tt.nints = (int)N.iops.size();
+            tt.npools = (int)N.pool_conc.size();
+            tt.ngiv = (int)N.giv_ref.size();
+            tt.prog_off = (int)prog_pool.size();
+            prog_pool.insert(prog_pool.end(), N.prog.begin(), N.prog.end());
+            tt.pool_off = (int)prog_pool.size();
+            prog_pool.insert(prog_pool.end(), N.pool_prog.begin(), N.pool_prog.end());
+            tt.table_set = N.table_set;
+            tt.crank = N.crank;
+            tt.chanmode5 = N.c5;
+            tt.interp = N.interp;
+            keys[N.key] = (int)types.size();
+            types.push_back(tt);
+            parents.push_back(N.parent);
+            uniform.push_back(1);
+        } else if (parents[it->second] != N.parent) {
+            uniform[it->second] = 0;
+        }
+    }
+    if (type_index < 0 || type_index >= (int)types.size()) return GBH_ERR_ARG;
+    std::vector<TableGeom> tg;
+    std::vector<double> tab64, xy;
+    build_tables(desc, tg, tab64, xy);
+    const std::string src = jit_source(types[type_index], prog_pool, tg[types[type_index].table_set],
+                                       precision == GBH_PREC_MIXED, false,
+                                       uniform[type_index] ? &parents[type_index] : nullptr);
+    if (buf && buflen > 0) {
+        const int64_t n = std::min<int64_t>(buflen - 1, (int64_t)src.size());
+        memcpy(buf, src.data(), (size_t)n);
+        buf[n] = 0;
+    }
+    return (int64_t)src.size();
+}
+
 int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons, int64_t *n_types)
 {
     gbh_error local{};
@@ -776,6 +930,10 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->stats.precision = e->opt.precision;
     e->stats.steps_per_launch = e->steps_per_launch;
     e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
+    e->stats.jit_kernels = e->jit_compiled;
+    if (getenv("GBH_VERBOSE") && !e->jit_log.empty())
+        fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
+                e->jit_log.c_str());
     return e;
 }
 
@@ -941,6 +1099,7 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_out_vals.release(); e->d_out_addr.release();
+    for (JitKernel &k : e->jits) jit_release(k);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->stream) cudaStreamDestroy(e->stream);

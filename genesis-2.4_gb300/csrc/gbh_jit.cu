@@ -1,0 +1,651 @@
+// gbh_jit.cu -- per-program kernel specialisation at setup.
+//
+// The interpreting kernels (k_steps, k_steps_mixed) read each compartment's
+// micro-ops from memory, so every load of a compartment waits for the
+// opcode before it and little memory-level parallelism is exposed. For a
+// tile type (all neurons sharing one program) this file emits the same
+// computation as straight-line CUDA -- every slot unrolled, every field row,
+// table column, power and stablist index a literal, the elimination unrolled
+// in registers when all neurons of the type share one tree -- and compiles
+// it with NVRTC for the running GPU. The arithmetic of each micro-op is
+// emitted exactly as the interpreter performs it, so the FP64 form stays
+// bit-identical (it is compiled without multiply-add contraction).
+//
+// NVRTC is loaded with dlopen and the driver calls are resolved through
+// cudaGetDriverEntryPointByVersion, so the library links neither.
+#include "gbh_jit.h"
+
+#include <cuda.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+
+#include "gbh_internal.h"
+#include "gbh_jit_sources.h"   // generated at build time: header texts
+
+namespace gbh {
+
+namespace {
+
+// ---- NVRTC and driver entry points ----------------------------------------
+struct Api {
+    bool ok = false;
+    std::string why;
+    nvrtcResult (*create)(nvrtcProgram *, const char *, const char *, int, const char *const *,
+                          const char *const *) = nullptr;
+    nvrtcResult (*compile)(nvrtcProgram, int, const char *const *) = nullptr;
+    nvrtcResult (*logsize)(nvrtcProgram, size_t *) = nullptr;
+    nvrtcResult (*getlog)(nvrtcProgram, char *) = nullptr;
+    nvrtcResult (*cubinsize)(nvrtcProgram, size_t *) = nullptr;
+    nvrtcResult (*getcubin)(nvrtcProgram, char *) = nullptr;
+    nvrtcResult (*destroy)(nvrtcProgram *) = nullptr;
+    CUresult (*load)(CUmodule *, const void *) = nullptr;
+    CUresult (*getfn)(CUfunction *, CUmodule, const char *) = nullptr;
+    CUresult (*launch)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                       CUstream, void **, void **) = nullptr;
+    CUresult (*setattr)(CUfunction, CUfunction_attribute, int) = nullptr;
+    CUresult (*unload)(CUmodule) = nullptr;
+};
+
+Api g_api;
+std::once_flag g_api_once;
+
+template <typename F>
+bool sym(void *h, const char *name, F &fn)
+{
+    fn = reinterpret_cast<F>(dlsym(h, name));
+    return fn != nullptr;
+}
+
+template <typename F>
+bool drv(const char *name, F &fn)
+{
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &p, 13000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !p)
+        return false;
+    fn = reinterpret_cast<F>(p);
+    return true;
+}
+
+void init_api()
+{
+    const char *cands[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13",
+                           "/usr/local/cuda/lib64/libnvrtc.so"};
+    void *h = nullptr;
+    for (const char *c : cands)
+        if ((h = dlopen(c, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) {
+        g_api.why = "libnvrtc not found";
+        return;
+    }
+    bool ok = sym(h, "nvrtcCreateProgram", g_api.create) && sym(h, "nvrtcCompileProgram", g_api.compile) &&
+              sym(h, "nvrtcGetProgramLogSize", g_api.logsize) && sym(h, "nvrtcGetProgramLog", g_api.getlog) &&
+              sym(h, "nvrtcGetCUBINSize", g_api.cubinsize) && sym(h, "nvrtcGetCUBIN", g_api.getcubin) &&
+              sym(h, "nvrtcDestroyProgram", g_api.destroy);
+    ok = ok && drv("cuModuleLoadData", g_api.load) && drv("cuModuleGetFunction", g_api.getfn) &&
+         drv("cuLaunchKernel", g_api.launch) && drv("cuFuncSetAttribute", g_api.setattr) &&
+         drv("cuModuleUnload", g_api.unload);
+    if (!ok) {
+        g_api.why = "NVRTC or driver entry points missing";
+        return;
+    }
+    g_api.ok = true;
+}
+
+// ---- source emission -------------------------------------------------------
+std::string lit(double x)
+{
+    char b[64];
+    snprintf(b, sizeof(b), "%a", x);
+    return b;
+}
+std::string litf(float x)
+{
+    char b[64];
+    snprintf(b, sizeof(b), "%af", (double)x);
+    return b;
+}
+
+struct Emit {
+    std::ostringstream o;
+    bool mixed, giv;
+    std::string P(int f) const { return "Pw[" + std::to_string(f * LANES) + "]"; }
+    std::string I(int r) const { return "Iw[" + std::to_string(r * LANES) + "]"; }
+    std::string C(int p) const { return "Cw[" + std::to_string(p * LANES) + "]"; }
+    std::string F(int p) const { return "Fw[" + std::to_string(p * LANES) + "]"; }
+    std::string G(int g) const { return "Gw[" + std::to_string(g * LANES) + "]"; }
+    std::string pP(int f) const { return "&Pw[" + std::to_string(f * LANES) + "]"; }
+};
+
+int nops_of(int code)
+{
+    switch (code) {
+    case M_BEGIN: return 4;
+    case M_NEWVOLT: case M_NEWCONC1: case M_FLUX: case M_DO_TABGHK: return 0;
+    case M_CONCVAL: case M_DOMAIN: case M_NEWCONC2: case M_SCALE_FLUX: case M_SAME_GHK:
+    case M_CHAN_G: case M_ADDCURR: return 1;
+    case M_NERNST: case M_CHAN: case M_STORE: return 2;
+    case M_SPIKE: case M_GHK: case M_END: return 3;
+    case M_ELMMPUMP: case M_GATE: case M_MGBLOCK: return 4;
+    case M_SYN: return 6;
+    default: return -1;
+    }
+}
+
+// One compartment's channel program. Returns false on an unknown op.
+bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
+{
+    std::ostringstream &o = E.o;
+    const bool mx = E.mixed, giv = E.giv;
+    const int ncols = tg.ncols;
+    o << "    { // slot " << s << "\n";
+    o << "      const double Vm = Vw[" << s * LANES << "];\n";
+    if (mx) o << "      const df vmd = d2df(Vm);\n      df sumg = df_make(0.f, 0.f), ichan = sumg;\n";
+    else o << "      double sumg = 0.0, ichan = 0.0;\n";
+    o << "      double Im = 0.0; (void)Im;\n";
+    // state carried inside the compartment
+    for (;;) {
+        const int code = pc[0];
+        const int n = nops_of(code);
+        if (n < 0) return false;
+        const int *a = pc + 1;
+        switch (code) {
+        case M_BEGIN:
+            if (mx) {
+                o << "      { const df emrm = ld_df(" << E.pP(a[0]) << "); ichan = df_add(emrm, ld_df(" << E.pP(a[1])
+                  << "));";
+                if (giv) o << " Im = df2d(emrm) - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
+                o << " }\n";
+            } else {
+                o << "      { const double emrm = " << E.P(a[0]) << "; ichan = emrm + " << E.P(a[1]) << ";";
+                if (giv) o << " Im = emrm - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
+                o << " }\n";
+            }
+            break;
+        case M_NEWVOLT:
+            if (mx)
+                o << "      locate_df(vc, vmd, xnmin, xinv, " << tg.xdivs << ", " << ncols << ");\n";
+            else
+                o << "      locate(vc, Vm, " << lit(tg.xmin) << ", " << lit(tg.invdx) << ", " << tg.xdivs
+                  << ", xvals, " << ncols << ", interp);\n";
+            break;
+        case M_CONCVAL:
+            o << "      sel = " << a[0] << "; " << E.F(a[0]) << " = 0.0;\n";
+            break;
+        case M_DOMAIN:
+            if (mx)
+                o << "      locate_df(cc, d2df(" << E.P(a[0]) << " * Ik), ynmin, yinv, " << tg.ydivs << ", " << ncols
+                  << ");\n";
+            else
+                o << "      locate(cc, " << E.P(a[0]) << " * Ik, " << lit(tg.ymin) << ", " << lit(tg.invdy) << ", "
+                  << tg.ydivs << ", yvals, " << ncols << ", interp); ctab_base = cc.base;\n";
+            break;
+        case M_NEWCONC2:
+            if (mx)
+                o << "      c1 = cc; locate_df(cc, d2df(" << E.C(a[0]) << "), ynmin, yinv, " << tg.ydivs << ", "
+                  << ncols << ");\n";
+            else
+                o << "      tab_base = ctab_base; save_frac = cc.frac; locate(cc, " << E.C(a[0]) << ", "
+                  << lit(tg.ymin) << ", " << lit(tg.invdy) << ", " << tg.ydivs << ", yvals, " << ncols
+                  << ", interp); ctab_base = cc.base;\n";
+            break;
+        case M_NEWCONC1:
+            if (mx)
+                o << "      locate_df(cc, d2df(Cw[sel * 32]), ynmin, yinv, " << tg.ydivs << ", " << ncols << ");\n";
+            else
+                o << "      locate(cc, Cw[sel * 32], " << lit(tg.ymin) << ", " << lit(tg.invdy) << ", " << tg.ydivs
+                  << ", yvals, " << ncols << ", interp); ctab_base = cc.base;\n";
+            break;
+        case M_SPIKE:
+            o << "      { int cnt = " << E.I(a[1]) << " - 1;\n"
+              << "        if (Vm > " << E.P(a[0]) << " && cnt <= 0 && active) {\n"
+              << "          const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];\n"
+              << "          for (int64_t e = e0; e < e1; ++e) {\n"
+              << "            const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);\n"
+              << "            atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * 32], 1u); }\n"
+              << "          v.spikes[neuron] += 1ULL; cnt = " << E.I(a[2]) << "; }\n"
+              << "        " << E.I(a[1]) << " = cnt; }\n";
+            break;
+        case M_ELMMPUMP:
+            o << "      { const double cx = Cw[sel * 32]; const double X = 1.0 / (cx + " << E.P(a[0])
+              << "); const double vmax = " << E.P(a[1]) << "; Ik = vmax * cx * X;";
+            if (mx) o << " ichan = df_add(ichan, d2df(Ik));";
+            else o << " ichan += Ik;";
+            if (giv) o << " " << E.G(a[3]) << " = c5 ? Ik / vmax : Ik;";
+            o << " Im += Ik; }\n";
+            break;
+        case M_FLUX:
+            o << "      Fw[sel * 32] += Ik;\n";
+            break;
+        case M_SCALE_FLUX:
+            o << "      Fw[sel * 32] += " << E.P(a[0]) << " * Ik;\n";
+            break;
+        case M_STORE:
+            break;
+        case M_END:
+            if (mx) {
+                o << "      { const df tbyc = ld_df(" << E.pP(a[0]) << "); const df dv = df_mul(ichan, tbyc);\n"
+                  << "        R[" << s << "] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);\n"
+                  << "        D[" << s << "] = df2d(df_add(df_mul(sumg, tbyc), ld_df(" << E.pP(a[1]) << "))); }\n";
+            } else {
+                o << "      { const double tbyc = " << E.P(a[0]) << "; R[" << s << "] = Vm + ichan * tbyc; D[" << s
+                  << "] = sumg * tbyc + " << E.P(a[1]) << "; }\n";
+            }
+            if (giv) o << "      " << E.G(a[2]) << " = Im;\n";
+            pc += 1 + n;
+            o << "    }\n";
+            return true;
+        default: {
+            // current-producing op then its conductance sub-program
+            if (code == M_GHK) {
+                o << "      { const double cin = Cw[sel * 32], cout = Cw[(sel + 1) * 32]; double g = " << E.P(a[0])
+                  << "; const double X = Vm * g; const double Y = exp(-X); double e = " << E.P(a[1])
+                  << "; double ik = e * (cin - (Y * cout)); double gk;\n"
+                  << "        if (fabs(X) < 1.0e-6) { gk = 1.0 - 0.5 * X; g = 0.5 * g * e * (cin + cout); ik = -ik / gk; }\n"
+                  << "        else { gk = 1.0 - Y; g = g * (ik / gk - e * g * (cin - cout) * Vm * Y / (gk * gk)); ik = -X * ik / gk; }\n"
+                  << "        GHK = g;";
+                if (mx)
+                    o << " Ek = d2df((ik + g * Vm) / g); gmax = d2df(" << E.P(a[2]) << "); Gk = d2df(" << E.P(a[2])
+                      << " * GHK); }\n";
+                else
+                    o << " Ek = (ik + g * Vm) / g; gmax = " << E.P(a[2]) << "; Gk = gmax * GHK; }\n";
+            } else if (code == M_SAME_GHK) {
+                if (mx) o << "      gmax = d2df(" << E.P(a[0]) << "); Gk = d2df(" << E.P(a[0]) << " * GHK);\n";
+                else o << "      gmax = " << E.P(a[0]) << "; Gk = gmax * GHK;\n";
+            } else if (code == M_DO_TABGHK) {
+                o << "      doGHK = 1;\n";
+            } else if (code == M_NERNST) {
+                if (mx)
+                    o << "      Ek = d2df(log(Cw[(sel + 1) * 32] / Cw[sel * 32]) * " << E.P(a[0]) << "); gmax = Gk = d2df("
+                      << E.P(a[1]) << ");\n";
+                else
+                    o << "      Ek = log(Cw[(sel + 1) * 32] / Cw[sel * 32]) * " << E.P(a[0]) << "; gmax = Gk = "
+                      << E.P(a[1]) << ";\n";
+            } else if (code == M_CHAN) {
+                if (mx) o << "      Ek = ld_df(" << E.pP(a[0]) << "); gmax = Gk = ld_df(" << E.pP(a[1]) << ");\n";
+                else o << "      Ek = " << E.P(a[0]) << "; gmax = Gk = " << E.P(a[1]) << ";\n";
+            } else if (code == M_CHAN_G) {
+                if (mx) o << "      gmax = Gk = ld_df(" << E.pP(a[0]) << ");\n";
+                else o << "      gmax = Gk = " << E.P(a[0]) << ";\n";
+            } else {
+                return false;
+            }
+            pc += 1 + n;
+            for (;;) {
+                const int k = pc[0];
+                const int m = nops_of(k);
+                if (m < 0) return false;
+                const int *b = pc + 1;
+                if (k == M_GATE) {
+                    const int kind = b[0], col = b[1], p = b[2], fs = b[3];
+                    o << "      {\n";
+                    if (mx) {
+                        if (kind == GK_1V || kind == GK_1C) {
+                            const char *cu = kind == GK_1V ? "vc" : "cc";
+                            o << "        const int bb = " << cu << ".base + " << col << ";\n"
+                              << "        const df X = interp_df(tab, bb, " << cu << ".frac), Y = interp_df(tab, bb + 1, "
+                              << cu << ".frac);\n";
+                        } else {
+                            const char *ru = kind == GK_2V ? "vc" : "c1";
+                            o << "        const int bb = " << ru << ".base + cc.row + cc.row + " << col << ";\n"
+                              << "        const df cf = cc.frac, rf = " << ru << ".frac;\n"
+                              << "        const df one_c = df_add_f(df_neg(cf), 1.0f), one_r = df_add_f(df_neg(rf), 1.0f);\n"
+                              << "        df q[2];\n"
+                              << "        for (int h = 0; h < 2; ++h) { const df t00 = val_df(tab, bb + h), t01 = val_df(tab, bb + 2 + h);\n"
+                              << "          const df t10 = interp_df(tab, bb + h, df_make(1.f, 0.f)), t11 = interp_df(tab, bb + 2 + h, df_make(1.f, 0.f));\n"
+                              << "          q[h] = df_add(df_mul(one_r, df_add(df_mul(one_c, t00), df_mul(cf, t01))), df_mul(rf, df_add(df_mul(one_c, t10), df_mul(cf, t11)))); }\n"
+                              << "        const df X = q[0], Y = q[1];\n";
+                        }
+                        if (p == 0) {
+                            o << "        Ek = Y;\n";
+                            pc += 1 + m;
+                            if (pc[0] != M_ADDCURR) {   // DO_TABGHK: slope conductance, no current
+                                o << "        GHK = df2d(X); doGHK = 0;\n      }\n";
+                                break;
+                            }
+                            o << "        Gk = df_mul(Gk, X);\n      }\n";
+                            continue;
+                        }
+                        o << "        double *st = " << E.pP(fs) << ";\n";
+                        if (p > 0)
+                            o << "        const df x = df_div(df_add(df_mul(ld_df(st), df_add_f(df_neg(X), 2.0f)), Y), X);\n";
+                        else
+                            o << "        const df x = df_div(Y, X);\n";
+                        o << "        st_df(st, x); Gk = dpow(Gk, x, " << (p > 0 ? p : -p) << ");\n      }\n";
+                    } else {
+                        if (kind == GK_1V || kind == GK_1C) {
+                            o << "        const int bb = " << (kind == GK_1V ? "vc.base" : "ctab_base") << " + " << col
+                              << ";\n        double X, Y;\n"
+                              << "        if (interp) { const double fr = " << (kind == GK_1V ? "vc" : "cc")
+                              << ".frac; X = tab[bb]; X = X + fr * (tab[bb + " << ncols << "] - X); Y = tab[bb + 1]; Y = Y + fr * (tab[bb + 1 + "
+                              << ncols << "] - Y); }\n        else { X = tab[bb]; Y = tab[bb + 1]; }\n";
+                        } else {
+                            o << "        const double rf = " << (kind == GK_2V ? "vc.frac" : "save_frac")
+                              << ", cf = cc.frac;\n        const int bb = " << (kind == GK_2V ? "vc.base" : "tab_base")
+                              << " + cc.row + cc.row + " << col << ";\n        double X, Y;\n"
+                              << "        if (interp) { const int nn = bb + " << ncols
+                              << ";\n          X = (1.0 - rf) * ((1.0 - cf) * tab[bb] + cf * tab[bb + 2]) + rf * ((1.0 - cf) * tab[nn] + cf * tab[nn + 2]);\n"
+                              << "          Y = (1.0 - rf) * ((1.0 - cf) * tab[bb + 1] + cf * tab[bb + 3]) + rf * ((1.0 - cf) * tab[nn + 1] + cf * tab[nn + 3]); }\n"
+                              << "        else { X = tab[bb]; Y = tab[bb + 1]; }\n";
+                        }
+                        o << "        tab_base = bb + 1;\n";
+                        if (p == 0) {
+                            o << "        Ek = Y;\n";
+                            pc += 1 + m;
+                            if (pc[0] != M_ADDCURR) {
+                                o << "        GHK = X; doGHK = 0;\n      }\n";
+                                break;
+                            }
+                            o << "        Gk *= X;\n      }\n";
+                            continue;
+                        }
+                        o << "        double *st = " << E.pP(fs) << ";\n";
+                        if (p > 0) o << "        const double x = (*st * (2.0 - X) + Y) / X;\n";
+                        else o << "        const double x = Y / X;\n";
+                        o << "        *st = x; Gk = gpow<double>(Gk, x, " << (p > 0 ? p : -p) << ");\n      }\n";
+                    }
+                    pc += 1 + m;
+                    continue;
+                } else if (k == M_SYN) {
+                    const int ff = b[0], stab = b[1], srow = b[2], fx = b[3], fy = b[4], fw = b[5];
+                    o << "      { const double *sl = v.stablist + " << stab << "; double *px = " << E.pP(fx)
+                      << "; double *py = " << E.pP(fy) << ";\n";
+                    if (ff >= 0)
+                        o << "        { const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^ (uint64_t)"
+                          << fx << "; if (syn3_uniform(key) <= " << E.P(ff) << ") *px += sl[3]; }\n";
+                    o << "        double X = *px * sl[0];\n"
+                      << "        unsigned *cell = v.ring + ((tl.syn + (int64_t)" << srow
+                      << " * v.ring_len + (int64_t)(step % v.ring_len)) * 32 + lane);\n"
+                      << "        const unsigned n = *cell;\n"
+                      << "        if (n) { const double wdt = " << E.P(fw)
+                      << "; double act = 0.0; for (unsigned q = 0; q < n; ++q) act += wdt; X += v.dt * act * sl[3]; *cell = 0u; }\n"
+                      << "        *px = X; const double Y = X * sl[1] + *py * sl[2]; *py = Y;";
+                    if (mx) o << " Gk = df_mul(Gk, d2df(Y)); }\n";
+                    else o << " Gk *= Y; }\n";
+                    pc += 1 + m;
+                    continue;
+                } else if (k == M_MGBLOCK) {
+                    o << "      {";
+                    if (mx) {
+                        o << " const double gk = df2d(Gk), ek = df2d(Ek);";
+                        if (giv)
+                            o << " { const double gm = c5 ? df2d(gmax) : 1.0; " << E.G(b[3]) << " = gk / gm; "
+                              << E.G(b[3] + 1) << " = gk * (ek - Vm) / gm; " << E.G(b[3] + 2) << " = ek; }";
+                        o << " const double X = " << E.P(b[0]) << " * exp(Vm * " << E.P(b[1]) << "); Gk = d2df(gk * (X / (X + "
+                          << E.P(b[2]) << "))); }\n";
+                    } else {
+                        if (giv)
+                            o << " if (c5) { " << E.G(b[3]) << " = Gk / gmax; " << E.G(b[3] + 1) << " = Gk * (Ek - Vm) / gmax; } else { "
+                              << E.G(b[3]) << " = Gk; " << E.G(b[3] + 1) << " = Gk * (Ek - Vm); } " << E.G(b[3] + 2)
+                              << " = Ek;";
+                        o << " const double X = " << E.P(b[0]) << " * exp(Vm * " << E.P(b[1]) << "); Gk *= X / (X + "
+                          << E.P(b[2]) << "); }\n";
+                    }
+                    pc += 1 + m;
+                    continue;
+                } else if (k == M_ADDCURR) {
+                    const int g = b[0];
+                    if (mx) {
+                        o << "      { sumg = df_add(sumg, Gk); ichan = df_add(ichan, df_mul(Ek, Gk)); const double gk = df2d(Gk), ek = df2d(Ek); Ik = gk * (ek - Vm);";
+                        if (giv)
+                            o << " { const double gm = c5 ? df2d(gmax) : 1.0; " << E.G(g) << " = gk / gm; " << E.G(g + 1)
+                              << " = Ik / gm; " << E.G(g + 2) << " = ek; }";
+                        o << " Im += Ik; }\n";
+                    } else {
+                        o << "      { sumg += Gk; ichan += Ek * Gk; Ik = Gk * (Ek - Vm);";
+                        if (giv)
+                            o << " if (c5) { " << E.G(g) << " = Gk / gmax; " << E.G(g + 1) << " = Ik / gmax; } else { "
+                              << E.G(g) << " = Gk; " << E.G(g + 1) << " = Ik; } " << E.G(g + 2) << " = Ek;";
+                        o << " Im += Ik; }\n";
+                    }
+                    pc += 1 + m;
+                    break;
+                } else {
+                    return false;
+                }
+            }
+            break;
+        }
+        }
+        if (code != M_GHK && code != M_SAME_GHK && code != M_DO_TABGHK && code != M_NERNST && code != M_CHAN &&
+            code != M_CHAN_G)
+            pc += 1 + n;
+    }
+}
+
+}  // namespace
+
+std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
+                       const std::vector<int> *uniform_parent)
+{
+    Emit E;
+    E.mixed = mixed;
+    E.giv = giv;
+    std::ostringstream &o = E.o;
+    const int S = tt.nslots;
+    o << "#include \"gbh_devfn.cuh\"\nusing namespace gbh;\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(128, 4) gbh_jit(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)\n{\n";
+    o << "  extern __shared__ double sm[];\n"
+      << "  const int lane = threadIdx.x & 31; const int wib = threadIdx.x >> 5;\n"
+      << "  const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib; if (t >= tile1) return;\n"
+      << "  const Tile tl = v.tiles[t];\n"
+      << "  const bool active = lane < tl.nlanes; (void)active;\n"
+      << "  const bool c5 = " << (tt.chanmode5 ? "true" : "false") << "; (void)c5;\n"
+      << "  const bool interp = " << (tt.interp ? "true" : "false") << "; (void)interp;\n"
+      << "  double *Pw = v.P + tl.fld * 32 + lane; int *Iw = v.I + tl.ints * 32 + lane; (void)Iw;\n"
+      << "  double *Vw = v.V + tl.vm * 32 + lane; double *Cw = v.C + tl.pools * 32 + lane; (void)Cw;\n"
+      << "  double *Fw = v.F + tl.pools * 32 + lane; double *Gw = v.giv + tl.giv * 32 + lane; (void)Fw; (void)Gw;\n"
+      << "  const int64_t neuron = tl.first_neuron + lane; (void)neuron;\n";
+    if (mixed) {
+        o << "  const float4 *tab = v.tabdf + " << tg.tab_off << "; (void)tab;\n"
+          << "  const df xnmin = df_make(" << litf(-tg.xmin_hi) << ", " << litf(-tg.xmin_lo) << "), xinv = df_make("
+          << litf(tg.invdx_hi) << ", " << litf(tg.invdx_lo) << "); (void)xnmin; (void)xinv;\n"
+          << "  const df ynmin = df_make(" << litf(-tg.ymin_hi) << ", " << litf(-tg.ymin_lo) << "), yinv = df_make("
+          << litf(tg.invdy_hi) << ", " << litf(tg.invdy_lo) << "); (void)ynmin; (void)yinv;\n";
+    } else {
+        o << "  const double *tab = v.tab64 + " << tg.tab_off << "; (void)tab;\n"
+          << "  const double *xvals = v.xyvals + " << tg.xv_off << "; (void)xvals;\n"
+          << "  const double *yvals = v.xyvals + " << (tg.yv_off >= 0 ? tg.yv_off : tg.xv_off) << "; (void)yvals;\n";
+    }
+    if (!uniform_parent)
+        o << "  const int *par = v.parent + tl.topo * 32 + lane;\n"
+          << "  double *Dc = sm + (size_t)wib * " << 2 * S * LANES << " + lane; double *Rc = Dc + " << S * LANES << ";\n";
+    o << "  const double *Aw = v.A + tl.topo * 32 + lane; const double *Bw = v.B + tl.topo * 32 + lane; const double *Cbw = v.Cb + tl.topo * 32 + lane;\n";
+    o << "  for (int it = 0; it < nsteps; ++it) {\n"
+      << "    const long long step = step0 + it; (void)step;\n";
+    if (mixed) {
+        o << "    DCursor vc, cc, c1; vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f); cc = vc; c1 = vc;\n"
+          << "    df Ek = df_make(0.f, 0.f), Gk = Ek, gmax = Ek; (void)gmax;\n";
+    } else {
+        o << "    VCursor vc, cc;\n";
+        if (tg.ncols) o << "    vc.lo = vc.hi = 0.0;\n";
+        else o << "    vc.lo = -1e20; vc.hi = 1e20;\n";
+        o << "    vc.row = vc.base = 0; vc.frac = 0.0; cc.lo = cc.hi = 0.0; cc.row = cc.base = 0; cc.frac = 0.0;\n"
+          << "    double save_frac = 0.0; int tab_base = 0, ctab_base = 0; (void)save_frac; (void)tab_base; (void)ctab_base;\n"
+          << "    double Ek = 0.0, Gk = 0.0, gmax = 0.0; (void)gmax;\n";
+    }
+    o << "    double GHK = 0.0, Ik = 0.0; int doGHK = 0, sel = 0; (void)GHK; (void)doGHK; (void)sel; (void)Ik;\n";
+    if (uniform_parent) o << "    double D[" << S << "], R[" << S << "];\n";
+    else o << "    double *D = nullptr, *R = nullptr; (void)D; (void)R;\n";
+    std::ostringstream save;
+    const int *pc = prog.data() + tt.prog_off;
+    // in the non-uniform case rows live in shared memory columns
+    for (int s = 0; s < S; ++s) {
+        if (!emit_slot(E, s, pc, tg)) return std::string();
+    }
+    std::string body = o.str();
+    if (!uniform_parent) {
+        // rewrite D[s]/R[s] into the shared columns
+        std::string out;
+        out.reserve(body.size());
+        for (size_t i = 0; i < body.size(); ++i) {
+            if ((body[i] == 'D' || body[i] == 'R') && i + 1 < body.size() && body[i + 1] == '[' &&
+                (i == 0 || !(isalnum((unsigned char)body[i - 1]) || body[i - 1] == '_'))) {
+                size_t j = body.find(']', i);
+                const std::string idx = body.substr(i + 2, j - i - 2);
+                out += (body[i] == 'D' ? "Dc[(" : "Rc[(") + idx + ") * 32]";
+                i = j;
+            } else {
+                out += body[i];
+            }
+        }
+        body = out;
+    }
+    std::ostringstream t;
+    t << body;
+    // pools
+    const int *pp = prog.data() + tt.pool_off;
+    while (pp[0] != 0) {
+        if (pp[0] != PO_CACONC) return std::string();
+        t << "    { double *cx = &Cw[" << pp[1] * LANES << "]; const double base = Pw[" << pp[2] * LANES
+          << "]; const double itau = Pw[" << pp[3] * LANES << "];\n"
+          << "      *cx = base + ((*cx - base) * (2.0 - itau) + (Fw[" << pp[1] * LANES << "] * Pw[" << pp[4] * LANES
+          << "])) / itau; }\n";
+        pp += 5;
+    }
+    // elimination
+    const char *dv = uniform_parent ? "D[%d]" : "Dc[%d]";
+    (void)dv;
+    auto Dx = [&](int s) { return uniform_parent ? "D[" + std::to_string(s) + "]" : "Dc[" + std::to_string(s * LANES) + "]"; };
+    auto Rx = [&](int s) { return uniform_parent ? "R[" + std::to_string(s) + "]" : "Rc[" + std::to_string(s * LANES) + "]"; };
+    if (uniform_parent) {
+        const std::vector<int> &par = *uniform_parent;
+        for (int s = 0; s < S; ++s) {
+            const int p = par[s];
+            if (mixed) {
+                t << "    { const double ri = rcp_newton(" << Dx(s) << "); " << Dx(s) << " = ri;";
+                if (p >= 0)
+                    t << " const double temp = Aw[" << s * LANES << "] * ri; " << Dx(p) << " = fma(-Bw[" << s * LANES
+                      << "], temp, " << Dx(p) << "); " << Rx(p) << " = fma(-" << Rx(s) << ", temp, " << Rx(p) << ");";
+                t << " }\n";
+            } else if (p >= 0) {
+                t << "    { const double temp = Aw[" << s * LANES << "] / " << Dx(s) << "; " << Dx(p) << " -= Bw["
+                  << s * LANES << "] * temp; " << Rx(p) << " -= " << Rx(s) << " * temp; }\n";
+            }
+        }
+        for (int s = S - 1; s >= 0; --s) {
+            const int p = par[s];
+            t << "    { double r = " << Rx(s) << ";";
+            if (p >= 0) {
+                if (mixed) t << " r = fma(-Cbw[" << s * LANES << "], " << Rx(p) << ", r);";
+                else t << " r -= Cbw[" << s * LANES << "] * " << Rx(p) << ";";
+            }
+            if (mixed) t << " r = r * " << Dx(s) << ";";
+            else t << " r = r / " << Dx(s) << ";";
+            t << " " << Rx(s) << " = r;";
+            if (tt.crank) {
+                if (mixed) t << " Vw[" << s * LANES << "] = fma(2.0, r, -Vw[" << s * LANES << "]);";
+                else t << " Vw[" << s * LANES << "] = r + r - Vw[" << s * LANES << "];";
+            } else {
+                t << " Vw[" << s * LANES << "] = r;";
+            }
+            t << " }\n";
+        }
+    } else {
+        t << "    for (int s = 0; s < " << S << "; ++s) { const int p = par[s * 32];\n";
+        if (mixed)
+            t << "      const double ri = rcp_newton(Dc[s * 32]); Dc[s * 32] = ri;\n"
+              << "      if (p >= 0) { const double temp = Aw[s * 32] * ri; Dc[p * 32] = fma(-Bw[s * 32], temp, Dc[p * 32]); Rc[p * 32] = fma(-Rc[s * 32], temp, Rc[p * 32]); } }\n";
+        else
+            t << "      if (p >= 0) { const double d = Dc[s * 32]; const double temp = Aw[s * 32] / d; Dc[p * 32] -= Bw[s * 32] * temp; Rc[p * 32] -= Rc[s * 32] * temp; } }\n";
+        t << "    for (int s = " << S - 1 << "; s >= 0; --s) { const int p = par[s * 32]; double r = Rc[s * 32];\n";
+        if (mixed) t << "      if (p >= 0) r = fma(-Cbw[s * 32], Rc[p * 32], r); r = r * Dc[s * 32];\n";
+        else t << "      if (p >= 0) r -= Cbw[s * 32] * Rc[p * 32]; r = r / Dc[s * 32];\n";
+        t << "      Rc[s * 32] = r;";
+        if (tt.crank) {
+            if (mixed) t << " Vw[s * 32] = fma(2.0, r, -Vw[s * 32]);";
+            else t << " Vw[s * 32] = r + r - Vw[s * 32];";
+        } else {
+            t << " Vw[s * 32] = r;";
+        }
+        t << " }\n";
+    }
+    t << "  }\n}\n";
+    return t.str();
+}
+
+bool jit_available(std::string *why)
+{
+    std::call_once(g_api_once, init_api);
+    if (!g_api.ok && why) *why = g_api.why;
+    return g_api.ok;
+}
+
+int jit_compile(const std::string &src, bool fp64_exact, int device_major, int device_minor, JitKernel *out,
+                std::string *log)
+{
+    if (!jit_available(log)) return -1;
+    nvrtcProgram prog;
+    const char *hdr_src[] = {kSrc_gbh_internal_h, kSrc_gbh_df_cuh, kSrc_gbh_devfn_cuh, "", kStdintStub};
+    const char *hdr_name[] = {"gbh_internal.h", "gbh_df.cuh", "gbh_devfn.cuh", "cuda_runtime.h", "stdint.h"};
+    if (g_api.create(&prog, src.c_str(), "gbh_jit.cu", 5, hdr_src, hdr_name) != NVRTC_SUCCESS) {
+        if (log) *log = "nvrtcCreateProgram failed";
+        return -1;
+    }
+    char arch[64];
+    snprintf(arch, sizeof(arch), "--gpu-architecture=sm_%d%da", device_major, device_minor);
+    std::vector<const char *> opts = {arch, "--std=c++17", "-default-device", "-lineinfo"};
+    if (fp64_exact) opts.push_back("--fmad=false");
+    const nvrtcResult rc = g_api.compile(prog, (int)opts.size(), opts.data());
+    size_t ls = 0;
+    g_api.logsize(prog, &ls);
+    if (log && ls > 1) {
+        log->resize(ls);
+        g_api.getlog(prog, &(*log)[0]);
+    }
+    if (rc != NVRTC_SUCCESS) {
+        g_api.destroy(&prog);
+        return -1;
+    }
+    size_t cs = 0;
+    g_api.cubinsize(prog, &cs);
+    std::vector<char> cubin(cs);
+    g_api.getcubin(prog, cubin.data());
+    g_api.destroy(&prog);
+    CUmodule mod;
+    if (g_api.load(&mod, cubin.data()) != CUDA_SUCCESS) {
+        if (log) *log += "\ncuModuleLoadData failed";
+        return -1;
+    }
+    CUfunction fn;
+    if (g_api.getfn(&fn, mod, "gbh_jit") != CUDA_SUCCESS) {
+        g_api.unload(mod);
+        if (log) *log += "\ncuModuleGetFunction failed";
+        return -1;
+    }
+    out->module = mod;
+    out->fn = fn;
+    return 0;
+}
+
+cudaError_t jit_launch(const JitKernel &k, const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
+                       long long step, size_t smem, cudaStream_t st)
+{
+    const int ntiles = tile1 - tile0;
+    const int blocks = (ntiles + warps - 1) / warps;
+    if (smem > 48 * 1024) {
+        if (g_api.setattr((CUfunction)k.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem) != CUDA_SUCCESS)
+            return cudaErrorLaunchFailure;
+    }
+    DevView vv = v;
+    void *args[] = {&vv, &tile0, &tile1, &smax, &nsteps, &step};
+    if (g_api.launch((CUfunction)k.fn, blocks, 1, 1, warps * LANES, 1, 1, (unsigned)smem, (CUstream)st, args,
+                     nullptr) != CUDA_SUCCESS)
+        return cudaErrorLaunchFailure;
+    return cudaSuccess;
+}
+
+void jit_release(JitKernel &k)
+{
+    if (k.module && g_api.ok) g_api.unload((CUmodule)k.module);
+    k.module = nullptr;
+    k.fn = nullptr;
+}
+
+}  // namespace gbh

@@ -18,76 +18,8 @@
 
 namespace gbh {
 
-struct DCursor {
-    int row, base;
-    df frac;
-};
-
-// table position of value v on an axis (min, inv) with divs rows, clamped
-__device__ __forceinline__ void locate_df(DCursor &c, df v, df nmin, df inv, int divs, int ncols)
-{
-    df f = df_mul(df_add(v, nmin), inv);
-    int row;
-    if (f.hi <= 0.0f) {
-        row = 0;
-        f = df_make(0.f, 0.f);
-    } else if (f.hi >= (float)divs) {
-        row = divs;
-        f = df_make(0.f, 0.f);
-    } else {
-        row = (int)floorf(f.hi);
-        f = df_add_f(f, -(float)row);
-        if (f.hi < 0.0f) {
-            row -= 1;
-            f = df_add_f(f, 1.0f);
-        } else if (f.hi >= 1.0f) {
-            row += 1;
-            f = df_add_f(f, -1.0f);
-        }
-    }
-    c.row = row;
-    c.base = row * ncols;
-    c.frac = f;
-}
-
-__device__ __forceinline__ df ld_df(const double *p)
-{
-    const float2 v = *reinterpret_cast<const float2 *>(p);
-    return df_make(v.x, v.y);
-}
-
-__device__ __forceinline__ void st_df(double *p, df x)
-{
-    *reinterpret_cast<float2 *>(p) = make_float2(x.hi, x.lo);
-}
-
-// interpolated value of table entry e at fraction fr: value + fr*difference
-__device__ __forceinline__ df interp_df(const float4 *tab, int e, df fr)
-{
-    const float4 t = tab[e];
-    return df_add(df_make(t.x, t.y), df_mul(df_make(t.z, t.w), fr));
-}
-
-__device__ __forceinline__ df val_df(const float4 *tab, int e)
-{
-    const float4 t = tab[e];
-    return df_make(t.x, t.y);
-}
-
-__device__ __forceinline__ df dpow(df g, df x, int p)
-{
-    switch (p) {
-    case 1: return df_mul(g, x);
-    case 2: return df_mul(g, df_mul(x, x));
-    case 3: return df_mul(g, df_mul(df_mul(x, x), x));
-    case 4: x = df_mul(x, x); return df_mul(g, df_mul(x, x));
-    case 5: g = df_mul(g, x); x = df_mul(x, x); x = df_mul(x, x); return df_mul(g, x);
-    default: x = df_mul(x, x); g = df_mul(g, x); x = df_mul(x, x); return df_mul(g, x);
-    }
-}
-
 template <bool GIV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128, 6)
 k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
 {
     extern __shared__ double sm[];
@@ -115,9 +47,8 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
     const double *Aw = v.A + tl.topo * LANES + lane;
     const double *Bw = v.B + tl.topo * LANES + lane;
     const double *Cbw = v.Cb + tl.topo * LANES + lane;
-    double *Dcol = sm + (size_t)wib * 3 * smax * LANES + lane;
+    double *Dcol = sm + (size_t)wib * 2 * smax * LANES + lane;   // diagonal, then its reciprocal
     double *Rcol = Dcol + (size_t)smax * LANES;
-    double *Icol = Rcol + (size_t)smax * LANES;   // reciprocal of each eliminated diagonal
     const int S = ty.nslots;
     const int64_t neuron = tl.first_neuron + lane;
 
@@ -387,7 +318,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
         for (int s = 0; s < S; ++s) {
             const int p = par[s * LANES];
             const double ri = rcp_newton(Dcol[s * LANES]);
-            Icol[s * LANES] = ri;
+            Dcol[s * LANES] = ri;   // the row's diagonal is final here; keep only its reciprocal
             if (p >= 0) {
                 const double temp = Aw[s * LANES] * ri;
                 Dcol[p * LANES] = fma(-Bw[s * LANES], temp, Dcol[p * LANES]);
@@ -398,7 +329,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
             const int p = par[s * LANES];
             double r = Rcol[s * LANES];
             if (p >= 0) r = fma(-Cbw[s * LANES], Rcol[p * LANES], r);
-            r = r * Icol[s * LANES];
+            r = r * Dcol[s * LANES];
             Rcol[s * LANES] = r;
             if (ty.crank) {
                 const double old = Vw[s * LANES];
@@ -415,7 +346,7 @@ inline cudaError_t launch_mixed_impl(const DevView &v, int tile0, int tile1, int
 {
     const int ntiles = tile1 - tile0;
     const int blocks = (ntiles + warps - 1) / warps;
-    const size_t smem = (size_t)warps * 3 * smax * LANES * sizeof(double);
+    const size_t smem = (size_t)warps * 2 * smax * LANES * sizeof(double);
     cudaError_t ce;
     if (giv) {
         if (smem > 48 * 1024) {

@@ -42,6 +42,26 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
+JIT_HEADERS = ["gbh_internal.h", "gbh_df.cuh", "gbh_devfn.cuh"]
+STDINT_STUB = ("typedef signed char int8_t; typedef short int16_t; typedef int int32_t; "
+               "typedef long long int64_t; typedef unsigned char uint8_t; typedef unsigned short uint16_t; "
+               "typedef unsigned int uint32_t; typedef unsigned long long uint64_t;")
+
+
+def _write_jit_sources(path):
+    """Embeds the device headers the runtime compiler needs as C string literals."""
+    lines = ["// generated by gbhsolve/build.py: device headers for the runtime compiler", "#pragma once"]
+    for h in JIT_HEADERS:
+        text = open(os.path.join(CSRC, h)).read()
+        name = "kSrc_" + h.replace(".", "_")
+        lines.append('static const char %s[] = R"GBHSRC(%s)GBHSRC";' % (name, text))
+    lines.append('static const char kStdintStub[] = "%s";' % STDINT_STUB)
+    new = "\n".join(lines) + "\n"
+    if not os.path.exists(path) or open(path).read() != new:
+        with open(path, "w") as f:
+            f.write(new)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     if not force and up_to_date():
         return LIB
@@ -51,12 +71,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
     common = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
                      "-I" + CSRC, "-I" + INCLUDE]
+    gen_dir = os.path.join(OUT_DIR, "gen")
+    os.makedirs(gen_dir, exist_ok=True)
+    _write_jit_sources(os.path.join(gen_dir, "gbh_jit_sources.h"))
+    common = common + ["-I" + gen_dir]
     units = [
         ("gbh_k64.cu", ["--fmad=false", "-Xptxas", "-v"] if verbose else ["--fmad=false"]),
         ("gbh_k32.cu", ["-Xptxas", "-v"] if verbose else []),
         ("gbh_engine.cu", []),
         ("gbh_noalloc.cu", []),
         ("gbh_decode.cpp", []),
+        ("gbh_jit.cu", []),
     ]
 
     def compile_unit(u):
@@ -76,7 +101,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(log)
     objs = [o for o, _ in results]
     tmp = LIB + ".tmp"
-    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)

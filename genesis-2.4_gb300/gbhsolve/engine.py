@@ -60,16 +60,18 @@ class GbhSynapses(C.Structure):
 
 class GbhOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("steps_per_launch", C.c_int),
-                ("warps_per_block", C.c_int), ("use_graph", C.c_int), ("device", C.c_int)]
+                ("warps_per_block", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
+                ("jit", C.c_int)]
 
 
 class GbhStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("device_ms", C.c_double), ("compartments", C.c_int64),
                 ("tiles", C.c_int64), ("launches", C.c_int64), ("bytes_per_step", C.c_double),
-                ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int)]
+                ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int),
+                ("jit_kernels", C.c_int)]
 
 
-EXPORTED = ["gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
+EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc"]
@@ -94,6 +96,8 @@ def load(build_if_missing: bool = True):
     lib.gbh_create.restype = C.c_void_p
     lib.gbh_create.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhSynapses), C.POINTER(GbhOptions),
                                C.POINTER(GbhError)]
+    lib.gbh_jit_source.restype = C.c_int64
+    lib.gbh_jit_source.argtypes = [C.POINTER(GbhBatchDesc), C.c_int, C.c_int, C.c_char_p, C.c_int64]
     lib.gbh_validate.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhError), _lp, _lp]
     lib.gbh_run.argtypes = [C.c_void_p, C.c_int]
     lib.gbh_run_async.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -237,14 +241,26 @@ def validate(solvers: Sequence):
     return nn.value, nt.value
 
 
+def jit_source(solvers: Sequence, precision: int = PREC_FP64, type_index: int = 0) -> str:
+    """CUDA source generated for one tile type (host only, no GPU)."""
+    lib = load()
+    b = Batch(solvers)
+    n = lib.gbh_jit_source(C.byref(b.desc), precision, type_index, None, 0)
+    if n < 0:
+        raise RuntimeError("gbh_jit_source failed: %s" % lib.gbh_last_error().decode())
+    buf = C.create_string_buffer(int(n) + 1)
+    lib.gbh_jit_source(C.byref(b.desc), precision, type_index, buf, int(n) + 1)
+    return buf.value.decode()
+
+
 class Engine:
     """A device engine over a batch of hsolve elements."""
 
     def __init__(self, solvers: Sequence, synapses: Optional[dict] = None, precision: int = PREC_FP64,
-                 steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0):
+                 steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0, jit: bool = True):
         self.lib = load()
         self.batch = Batch(solvers, synapses)
-        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 0, device)
+        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 0, device, 0 if jit else -1)
         err = GbhError()
         h = self.lib.gbh_create(C.byref(self.batch.desc),
                                 C.byref(self.batch.syn) if self.batch.syn is not None else None,

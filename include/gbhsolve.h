@@ -114,6 +114,8 @@ typedef struct gbh_options {
     int warps_per_block; /* 0 = autotune                                      */
     int use_graph;       /* capture multi-launch runs in a CUDA graph         */
     int device;          /* CUDA device ordinal                                */
+    int jit;             /* 0 = specialise each neuron program at setup (NVRTC)
+                            when available, -1 = interpret the programs only   */
 } gbh_options;
 
 typedef struct gbh_stats {
@@ -126,6 +128,7 @@ typedef struct gbh_stats {
     int steps_per_launch;
     int warps_per_block;
     int precision;
+    int jit_kernels;           /* programs specialised and compiled at setup   */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
@@ -141,6 +144,14 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn,
  * n_neurons / n_tiles / n_types may be NULL.
  */
 int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons, int64_t *n_types);
+
+/*
+ * Diagnostics: writes the CUDA source the engine generates for tile type
+ * type_index (neurons sharing one program) into buf (NUL-terminated,
+ * truncated to buflen). Returns the full source length, or a negative error.
+ * Needs no GPU.
+ */
+int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, char *buf, int64_t buflen);
 
 /* Advances every solver by nsteps PROCESS steps. Returns GBH_OK or an error. */
 int gbh_run(gbh_engine *e, int nsteps);

@@ -56,3 +56,18 @@ def test_random_trees_with_ca_bitwise(oracle, gpu_engine):
         ref = _oracle_run(oracle, hs[i], 300)
         np.testing.assert_array_equal(st["vm"][i], ref.vm)
         np.testing.assert_array_equal(st["conc"][i], ref.conc[:len(hs[i].conc)])
+
+
+@pytest.mark.parametrize("jit", [True, False])
+def test_jit_and_interpreter_agree_bitwise(oracle, gpu_engine, jit):
+    """Both execution paths -- programs specialised at setup and the
+    interpreting kernel -- reproduce the oracle exactly."""
+    hs = configs.cables_replicated(50, gk_dend=36.0, seed=9)[0]
+    hs += [model.build(m) for m in configs.random_trees(20, size_range=(10, 30), seed=2)]
+    eng = gpu_engine.Engine(hs, jit=jit, steps_per_launch=40)
+    eng.run(120)
+    st = eng.get_state()
+    for i in (0, 17, 49, 50, 60, 69):
+        ref = _oracle_run(oracle, hs[i], 120)
+        np.testing.assert_array_equal(st["vm"][i], ref.vm)
+        np.testing.assert_array_equal(st["chip"][i], ref.chip)

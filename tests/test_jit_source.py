@@ -1,0 +1,58 @@
+"""The per-program kernels the engine generates at setup compile for sm_103a
+(NVRTC, no GPU needed) for every kind of program the configs produce."""
+import ctypes as C
+import os
+
+import pytest
+
+from gbhsolve import build, configs, engine, model
+
+CSRC = os.path.join(os.path.dirname(build.ROOT), "genesis-2.4_gb300", "csrc")
+
+
+def _nvrtc():
+    for name in ("libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    pytest.skip("libnvrtc not available")
+
+
+def compile_sm103a(src, fp64_exact):
+    lib = _nvrtc()
+    prog = C.c_void_p()
+    heads = ["gbh_internal.h", "gbh_df.cuh", "gbh_devfn.cuh"]
+    texts = [open(os.path.join(build.CSRC, h)).read().encode() for h in heads]
+    texts += [b"", build.STDINT_STUB.encode()]
+    names = [h.encode() for h in heads] + [b"cuda_runtime.h", b"stdint.h"]
+    arr_t = (C.c_char_p * len(texts))(*texts)
+    arr_n = (C.c_char_p * len(names))(*names)
+    assert lib.nvrtcCreateProgram(C.byref(prog), src.encode(), b"gbh_jit.cu", len(texts), arr_t, arr_n) == 0
+    opts = [b"--gpu-architecture=sm_103a", b"--std=c++17", b"-default-device"]
+    if fp64_exact:
+        opts.append(b"--fmad=false")
+    rc = lib.nvrtcCompileProgram(prog, len(opts), (C.c_char_p * len(opts))(*opts))
+    n = C.c_size_t()
+    lib.nvrtcGetProgramLogSize(prog, C.byref(n))
+    log = C.create_string_buffer(n.value + 1)
+    lib.nvrtcGetProgramLog(prog, log)
+    lib.nvrtcDestroyProgram(C.byref(prog))
+    return rc, log.value.decode(errors="replace")
+
+
+def _models():
+    yield "cables-uniform", configs.cables_replicated(4, gk_dend=36.0)[0]
+    yield "single-hsolve", [model.build(configs.cables(3, gk_dend=36.0, method=model.CRANK)[0])]
+    yield "trees-ca", [model.build(m) for m in configs.random_trees(3, size_range=(12, 12), seed=4)]
+    ms, _ = configs.hh_network(6, p_conn=0.5)
+    yield "network", [model.build(m) for m in ms]
+
+
+@pytest.mark.parametrize("prec", [engine.PREC_FP64, engine.PREC_MIXED])
+@pytest.mark.parametrize("name,hs", list(_models()))
+def test_generated_kernel_compiles(name, hs, prec):
+    src = engine.jit_source(hs, precision=prec, type_index=0)
+    assert "gbh_jit" in src
+    rc, log = compile_sm103a(src, prec == engine.PREC_FP64)
+    assert rc == 0, log[:4000]

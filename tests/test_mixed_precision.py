@@ -27,9 +27,10 @@ def _max_dev(oracle, gpu_engine, hs, nsteps, chunk=500, **kw):
     return worst
 
 
-def test_mixed_cables_10k_steps(oracle, gpu_engine):
+@pytest.mark.parametrize("jit", [True, False])
+def test_mixed_cables_10k_steps(oracle, gpu_engine, jit):
     hs, _ = configs.cables_replicated(32, gk_dend=36.0, seed=3)
-    dev = _max_dev(oracle, gpu_engine, hs, 10000)
+    dev = _max_dev(oracle, gpu_engine, hs, 10000, jit=jit)
     assert dev <= TOL_V, dev
 
 
