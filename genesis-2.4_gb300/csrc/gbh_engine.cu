@@ -526,8 +526,9 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 else if (dec.neurons[i].parent != ref) uni = false;
             }
             if (uni && !ref.empty()) upar[c] = ref;
+            const char *mb = getenv("GBH_JIT_MINB");
             srcs[c] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
-                                 upar[c].empty() ? nullptr : &upar[c]);
+                                 upar[c].empty() ? nullptr : &upar[c], mb ? atoi(mb) : 4);
         }
         int dev = e->opt.device, major = 10, minor = 3;
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);

@@ -422,7 +422,7 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
 }  // namespace
 
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent)
+                       const std::vector<int> *uniform_parent, int min_blocks)
 {
     Emit E;
     E.mixed = mixed;
@@ -430,7 +430,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     std::ostringstream &o = E.o;
     const int S = tt.nslots;
     o << "#include \"gbh_devfn.cuh\"\nusing namespace gbh;\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(128, 4) gbh_jit(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)\n{\n";
+    o << "extern \"C\" __global__ void __launch_bounds__(128, " << min_blocks
+      << ") gbh_jit(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)\n{\n";
     o << "  extern __shared__ double sm[];\n"
       << "  const int lane = threadIdx.x & 31; const int wib = threadIdx.x >> 5;\n"
       << "  const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib; if (t >= tile1) return;\n"

@@ -19,7 +19,7 @@ struct JitKernel {
 // shared by every neuron of the type (elimination unrolled in registers), or
 // null (per-neuron trees, shared-memory columns).
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent);
+                       const std::vector<int> *uniform_parent, int min_blocks = 4);
 
 bool jit_available(std::string *why);
 int jit_compile(const std::string &src, bool fp64_exact, int device_major, int device_minor, JitKernel *out,

@@ -268,3 +268,19 @@ def cables_replicated(n_neurons, ncomp=16, seed=0, dt=20e-6, method=BEULER, gk_d
     h = build(Model(cable_neuron(na, k, float(injects[0]), ncomp, erest=erest, gk_dend=gk_dend),
                     dt=sli(dt), method=method))
     return replicate(h, n_neurons, inject=[sli(x) for x in injects]), injects
+
+
+def network_synapses(hs, syn):
+    """Synapse table of :func:`hh_network` in the engine's and the oracle's
+    terms: the target is the SYN2_OP of the target cell's synchan (its ops[]
+    index), and, for the oracle, that synchan's child index."""
+    n = len(hs)
+    tgt_op = np.empty(len(syn["target"]), dtype=np.int32)
+    tgt_child = np.empty(len(syn["target"]), dtype=np.int32)
+    for k, (t, pos) in enumerate(zip(syn["target"], syn["child_pos"])):
+        h = hs[t]
+        cidx = h.syn_child[(0, int(pos))]
+        tgt_child[k] = cidx
+        tgt_op[k] = h.childops[cidx]
+    return dict(src_start=syn["start"].astype(np.int64), target_solver=syn["target"].astype(np.int32),
+                target_op=tgt_op, weight=syn["weight"], delay_steps=syn["delay_steps"]), tgt_child

@@ -71,3 +71,21 @@ def test_jit_and_interpreter_agree_bitwise(oracle, gpu_engine, jit):
         ref = _oracle_run(oracle, hs[i], 120)
         np.testing.assert_array_equal(st["vm"][i], ref.vm)
         np.testing.assert_array_equal(st["chip"][i], ref.chip)
+
+
+def test_engine_matches_reference_fixtures(gpu_engine):
+    """GPU engine against trajectories produced by the reference's own step
+    code (tests/golden/make_golden.py): Euler, Crank-Nicolson, calcmode 0,
+    a branched tree with a Ca pool."""
+    import os
+    from test_oracle_reference import _from_npz
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_trajectories.npz"))
+    for name in [str(x) for x in d["names"]]:
+        h = _from_npz(d, name)
+        for jit in (True, False):
+            eng = gpu_engine.Engine([h], jit=jit)
+            eng.run(int(d[name + "/nsteps"]))
+            st = eng.get_state()
+            np.testing.assert_array_equal(st["vm"][0], d[name + "/vm_ref"], err_msg=name)
+            np.testing.assert_array_equal(st["chip"][0], d[name + "/chip_ref"], err_msg=name)
+            eng.close()

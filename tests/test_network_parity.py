@@ -1,0 +1,55 @@
+"""Spiking network (one hsolve per cell, spikegen -> synchan events): the
+GPU engine's device-side event delivery against the CPU oracle's restatement
+of the synchan event queue. FP64: Vm bit for bit and identical spike counts."""
+import numpy as np
+import pytest
+
+from gbhsolve import configs, model
+
+pytestmark = pytest.mark.gpu
+
+
+def _network(n, p, seed, delay=1e-4, weight=1.0, inject=None):
+    ms, syn = configs.hh_network(n, p_conn=p, seed=seed, delay=delay, weight=weight)
+    if inject is not None:
+        for m, x in zip(ms, inject):
+            m.compartments[0].inject = x
+    hs = [model.build(m) for m in ms]
+    esyn, child = configs.network_synapses(hs, syn)
+    return hs, esyn, child
+
+
+def _oracle_net(oracle, hs, esyn, child, nsteps):
+    solvers = [oracle.Solver(h, i) for i, h in enumerate(hs)]
+    net = oracle.Network(solvers, esyn["src_start"], esyn["target_solver"], child, esyn["target_op"],
+                         esyn["weight"], esyn["delay_steps"])
+    net.run(nsteps)
+    return solvers, net.spikes
+
+
+@pytest.mark.parametrize("jit", [True, False])
+def test_network_spikes_and_vm_bitwise(oracle, gpu_engine, jit):
+    rng = np.random.default_rng(3)
+    n = 120
+    inj = rng.uniform(0.0, 0.3e-9, size=n)
+    hs, esyn, child = _network(n, 0.08, seed=5, inject=inj)
+    eng = gpu_engine.Engine(hs, synapses=esyn, jit=jit)
+    eng.run(3000)
+    spikes = eng.spike_counts()
+    vm = eng.vm()
+    solvers, ref_spikes = _oracle_net(oracle, hs, esyn, child, 3000)
+    assert ref_spikes.sum() > n      # the network is active
+    np.testing.assert_array_equal(spikes, ref_spikes)
+    np.testing.assert_array_equal(vm, np.concatenate([s.vm for s in solvers]))
+
+
+def test_network_longer_delays(oracle, gpu_engine):
+    rng = np.random.default_rng(4)
+    n = 60
+    hs, esyn, child = _network(n, 0.15, seed=6, delay=7.3e-4, inject=rng.uniform(0.05e-9, 0.25e-9, n))
+    assert esyn["delay_steps"].max() >= 7
+    eng = gpu_engine.Engine(hs, synapses=esyn)
+    eng.run(2500)
+    solvers, ref_spikes = _oracle_net(oracle, hs, esyn, child, 2500)
+    np.testing.assert_array_equal(eng.spike_counts(), ref_spikes)
+    np.testing.assert_array_equal(eng.vm(), np.concatenate([s.vm for s in solvers]))
