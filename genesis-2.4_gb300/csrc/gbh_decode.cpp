@@ -201,6 +201,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         return fail(c, GBH_ERR_ARG, -1, 0, -1, "descriptor missing or ABI version mismatch");
     if (d->nsolvers <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "no solvers");
     out.neurons.clear();
+    out.stablist.clear();
     out.solver_first_neuron.assign(d->nsolvers + 1, 0);
     for (int si = 0; si < d->nsolvers; ++si) {
         c.solver = si;
@@ -500,9 +501,19 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                             return fail(c, GBH_ERR_ARG, row, k, o, "stablist index %d out of range", stab);
                         const int srow = (int)N.syn_op.size();
                         N.syn_op.push_back((int)(o - 1));
+                        // identical constant sets share one entry, so identical cells
+                        // of different solvers keep identical programs
+                        const double *sv = d->stablist + d->stab_start[si] + stab;
+                        int gstab = -1;
+                        for (size_t q = 0; q + 4 <= out.stablist.size(); q += 4)
+                            if (memcmp(&out.stablist[q], sv, 4 * sizeof(double)) == 0) { gstab = (int)q; break; }
+                        if (gstab < 0) {
+                            gstab = (int)out.stablist.size();
+                            out.stablist.insert(out.stablist.end(), sv, sv + 4);
+                        }
                         P.push_back(M_SYN);
                         P.push_back(ffreq);
-                        P.push_back((int)(d->stab_start[si] + stab));
+                        P.push_back(gstab);
                         P.push_back(srow);
                         P.push_back(nb.fld(FS_CHIP, ch, chip[ch], true));
                         P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1], true));

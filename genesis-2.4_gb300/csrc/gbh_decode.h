@@ -39,6 +39,7 @@ struct Neuron {
 
 struct Decoded {
     std::vector<Neuron> neurons;
+    std::vector<double> stablist;             // deduplicated synchan constants (4 per entry)
     std::vector<int> solver_first_neuron;  // [nsolvers+1]
 };
 

@@ -131,14 +131,19 @@ __device__ __forceinline__ df d2df(double d)
 // df -> double: exact conversions, one FP64 add
 __device__ __forceinline__ double df2d(df x) { return f2d_bits(x.hi) + f2d_bits(x.lo); }
 
-// reciprocal of a positive or negative normal double to ~46 bits:
-// float seed (MUFU) then one Newton step in FP64 (two DFMA)
+// reciprocal of a normal double to ~46 bits: the mantissa m in [1,2) gets a
+// float seed (MUFU), the seed is rescaled by the exponent on the integer
+// pipe, then one Newton step in FP64 (two DFMA). Valid for any finite d with
+// 2^-1021 < |d| < 2^1021.
 __device__ __forceinline__ double rcp_newton(double d)
 {
-    const float s = rcp_approx(d2f_trunc_bits(d));
-    double r = f2d_bits(s);
-    const double e = fma(-d, r, 1.0);
-    return fma(r, e, r);
+    const int hi = __double2hiint(d), lo = __double2loint(d);
+    const int e = (hi >> 20) & 0x7ff;
+    const double m = __hiloint2double((hi & 0x800fffff) | 0x3ff00000, lo);
+    const double s = f2d_bits(rcp_approx(d2f_trunc_bits(m)));
+    const double r = __hiloint2double(__double2hiint(s) + ((1023 - e) << 20), __double2loint(s));
+    const double err = fma(-d, r, 1.0);
+    return fma(r, err, r);
 }
 
 }  // namespace gbh

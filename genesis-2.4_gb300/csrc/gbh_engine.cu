@@ -460,7 +460,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 tabdf[i] = make_float4(th, (float)(t0 - (double)th), dh, (float)(dlt - (double)dh));
             }
     }
-    std::vector<double> stab(d->stablist, d->stablist + d->stab_start[d->nsolvers]);
+    std::vector<double> stab = dec.stablist;
 
     // ---- upload ----
     int rc = 0;

@@ -158,8 +158,15 @@ class Batch:
         self.table_keys = {}
         self.table_list = []
         ts = []
+        content = {}
         for s in self.solvers:
             key = id(s.tablist)
+            if key not in content:
+                tab = np.ascontiguousarray(s.tablist)
+                content[key] = (s.ncols, s.xdivs, s.ydivs, s.xmin, s.invdx, s.ymin, s.invdy,
+                                hash(tab.tobytes()), hash(np.ascontiguousarray(s.xvals).tobytes()),
+                                hash(np.ascontiguousarray(s.yvals).tobytes()))
+            key = content[key]      # identical tables share one table set
             if key not in self.table_keys:
                 self.table_keys[key] = len(self.table_list)
                 self.table_list.append(s)

@@ -1,0 +1,80 @@
+"""Setup-time decoding on the host (no GPU): every model the configs build
+decodes; unimplemented or malformed programs are hard errors naming the
+solver, row, opcode and position (there is no CPU fallback)."""
+import numpy as np
+import pytest
+
+import ophelpers as A
+from gbhsolve import configs, engine, model
+
+
+def _err(hs):
+    with pytest.raises(engine.EngineError) as ei:
+        engine.validate(hs)
+    return ei.value
+
+
+def test_configs_decode():
+    assert engine.validate([model.build(configs.ap_verify(8))]) == (8, 1)
+    hs, _ = configs.cables_replicated(64, gk_dend=36.0)
+    assert engine.validate(hs) == (64, 1)
+    one = model.build(configs.cables(5, gk_dend=36.0, method=model.CRANK)[0])
+    n, t = engine.validate([one])
+    assert n == 5
+    trees = [model.build(m) for m in configs.random_trees(30, size_range=(8, 40), seed=1)]
+    assert engine.validate(trees)[0] == 30
+    ms, _ = configs.hh_network(20, p_conn=0.2)
+    assert engine.validate([model.build(m) for m in ms]) == (20, 1)
+
+
+def _hh():
+    c = A.Compt(-2e-10, 1e-10, 2.0, 1.01, 3e8, -0.06)
+    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.05, 1e-8]).op(A.IPOL1V, 0, 3, chips=[0.1]).op(A.ADD_CURR, giv=3)
+    return c
+
+
+def test_unknown_opcode_is_rejected():
+    c = _hh()
+    c.ops.insert(1, 7777)
+    e = _err([A.solver([c], A.tables(12, 20))])
+    assert e.code == -2 and e.opcode == 7777 and e.row == 0 and e.position == 2
+
+
+def test_unknown_conductance_opcode_is_rejected():
+    c = A.Compt(-2e-10, 1e-10, 2.0, 1.01, 3e8, -0.06)
+    c.op(A.NEWVOLT).op(A.CHAN_EK, 4099, chips=[0.05, 1e-8])
+    e = _err([A.solver([c], A.tables(12, 20))])
+    assert e.code == -2 and e.opcode == 4099
+
+
+def test_storemode_is_rejected():
+    c = _hh()
+    c.op(A.STORE_ALLI, 0)
+    e = _err([A.solver([c], A.tables(12, 20))])
+    assert e.code == -6 and e.opcode == A.STORE_ALLI
+
+
+@pytest.mark.parametrize("token", [3, 4, 5])
+def test_symmetric_compartment_elimination_is_rejected(token):
+    h = A.solver([_hh(), _hh()], A.tables(12, 20), parents=[1, -1])
+    f = list(h.funcs)
+    f.insert(0, token)
+    h.funcs = np.array(f, np.int32)
+    e = _err([h])
+    assert e.code == -3 and e.opcode == token
+
+
+def test_truncated_chip_is_rejected():
+    h = A.solver([_hh()], A.tables(12, 20))
+    h.chip = h.chip[:4]
+    e = _err([h])
+    assert e.code == -1
+
+
+def test_error_names_the_solver():
+    good = A.solver([_hh()], A.tables(12, 20))
+    c = _hh()
+    c.ops.append(9999)
+    bad = A.solver([c], A.tables(12, 20))
+    e = _err([good, good, bad])
+    assert e.solver == 2
