@@ -266,8 +266,9 @@ def main():
             ms = float(t.item())
         results[form] = dict(ms=ms, launches=launches, spl=st.steps_per_launch,
                              value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng)
-        log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels -> %.3e cs/s" % (
-            form, ms, args.steps, launches, st.jit_kernels, results[form]["value"]))
+        log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels (min blocks %d), %d steps/launch"
+            " -> %.3e cs/s" % (form, ms, args.steps, launches, st.jit_kernels, st.jit_min_blocks,
+                               st.steps_per_launch, results[form]["value"]))
         if form == "fp64":
             eng.close()
 
@@ -339,7 +340,8 @@ def main():
             "config": {"workload": "cables-100k-x16: 100,000 neurons x 16 compartments, somatic HH Na/K, "
                                    "dendritic K 36 S/m^2, dt 20 us, backward Euler",
                        "compartments": M, "form": "batched mixed precision",
-                       "steps_per_launch": r["spl"], "l2": "state 1.6M compartments > L2, no flush"},
+                       "steps_per_launch": r["spl"], "autotuned": args.steps_per_launch == 0,
+                       "l2": "state 1.6M compartments > L2, no flush"},
             "forms": {"fp64": {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
                                "dtype": "f64"},
                       "mixed": {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
@@ -350,7 +352,7 @@ def main():
                     "d2h_bytes_per_step": nh * 8},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "gbh::k_steps<float>", "launch_ms": launch_ms,
+                         "kernel": "gbh_jit (specialised mixed step)", "launch_ms": launch_ms,
                          "alg_bytes_per_compartment_step": ALG_BYTES["mixed"]},
             "cpu_baseline": cpu,
             "gpu_launches": int(r["launches"]),

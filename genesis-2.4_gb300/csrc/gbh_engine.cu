@@ -118,7 +118,10 @@ struct gbh_engine {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     gbh_stats stats{};
-    std::vector<JitKernel> jits;
+    std::vector<JitKernel> jits;                 // active kernel of each specialised type
+    std::vector<std::vector<JitKernel>> jit_var;  // compiled variants per specialised type
+    std::vector<int> jit_minb;                    // residency target of each variant
+    int jit_choice = 0;
     int jit_compiled = 0;
     std::string jit_log;
     // per-step I/O (h_in_msgs / h_out_msgs)
@@ -513,7 +516,13 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         });
         const int max_jit = 24;
         if ((int)cand.size() > max_jit) cand.resize(max_jit);
-        std::vector<std::string> srcs(cand.size());
+        // residency targets (resident blocks of 4 warps per SM) tried by the autotuner
+        e->jit_minb.clear();
+        if (const char *mb = getenv("GBH_JIT_MINB")) e->jit_minb.push_back(atoi(mb));
+        else if (e->opt.steps_per_launch > 0) e->jit_minb.push_back(6);
+        else e->jit_minb = {4, 6};
+        const int nvar = (int)e->jit_minb.size();
+        std::vector<std::string> srcs(cand.size() * nvar);
         std::vector<std::vector<int>> upar(cand.size());
         for (size_t c = 0; c < cand.size(); ++c) {
             const int ti = cand[c];
@@ -526,18 +535,18 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 else if (dec.neurons[i].parent != ref) uni = false;
             }
             if (uni && !ref.empty()) upar[c] = ref;
-            const char *mb = getenv("GBH_JIT_MINB");
-            srcs[c] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
-                                 upar[c].empty() ? nullptr : &upar[c], mb ? atoi(mb) : 4);
+            for (int vi = 0; vi < nvar; ++vi)
+                srcs[c * nvar + vi] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
+                                                 upar[c].empty() ? nullptr : &upar[c], e->jit_minb[vi]);
         }
         int dev = e->opt.device, major = 10, minor = 3;
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
-        std::vector<JitKernel> ks(cand.size());
-        std::vector<int> ok(cand.size(), 0);
-        std::vector<std::string> logs(cand.size());
+        std::vector<JitKernel> ks(srcs.size());
+        std::vector<int> ok(srcs.size(), 0);
+        std::vector<std::string> logs(srcs.size());
         std::vector<std::thread> th;
-        for (size_t c = 0; c < cand.size(); ++c)
+        for (size_t c = 0; c < srcs.size(); ++c)
             th.emplace_back([&, c]() {
                 cudaSetDevice(dev);
                 if (!srcs[c].empty())
@@ -545,13 +554,20 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             });
         for (auto &x : th) x.join();
         for (size_t c = 0; c < cand.size(); ++c) {
-            if (ok[c]) {
+            bool all = true;
+            for (int vi = 0; vi < nvar; ++vi) all = all && ok[c * nvar + vi];
+            if (all) {
                 type_jit[cand[c]] = (int)e->jits.size();
                 type_uniform[cand[c]] = !upar[c].empty();
-                e->jits.push_back(ks[c]);
+                std::vector<JitKernel> vars(ks.begin() + c * nvar, ks.begin() + (c + 1) * nvar);
+                e->jits.push_back(vars[0]);
+                e->jit_var.push_back(vars);
                 e->jit_compiled++;
-            } else if (!logs[c].empty() && e->jit_log.size() < 4000) {
-                e->jit_log += logs[c];
+            } else {
+                for (int vi = 0; vi < nvar; ++vi) {
+                    if (ok[c * nvar + vi]) jit_release(ks[c * nvar + vi]);
+                    if (!logs[c * nvar + vi].empty() && e->jit_log.size() < 4000) e->jit_log += logs[c * nvar + vi];
+                }
             }
         }
     }
@@ -663,6 +679,68 @@ int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 }
 
 }  // namespace
+
+// Autotuner: times trial steps for every (kernel variant, steps per launch)
+// candidate on the live engine, saving the mutable state first and restoring
+// it after each trial, and keeps the fastest pair. Results are unaffected.
+int autotune(gbh_engine *e)
+{
+    std::vector<int> spls;
+    if (e->has_network) spls = {1};
+    else spls = {16, 64, 256};
+    const int nvar = e->jit_var.empty() ? 1 : (int)e->jit_var[0].size();
+    if ((int)spls.size() * nvar <= 1) {
+        e->steps_per_launch = spls[0];
+        return GBH_OK;
+    }
+    struct Save { void *dst; const void *src; size_t bytes; };
+    std::vector<Save> saves;
+    auto keep = [&](void *p, size_t bytes) {
+        if (!p || !bytes) return GBH_OK;
+        void *b = nullptr;
+        if (cudaMalloc(&b, bytes) != cudaSuccess) return GBH_ERR_CUDA;
+        saves.push_back({b, p, bytes});
+        return GBH_OK;
+    };
+    int rc = 0;
+    rc |= keep(e->d_P.p, e->d_P.n * sizeof(double));
+    rc |= keep(e->d_V.p, e->d_V.n * sizeof(double));
+    rc |= keep(e->d_C.p, e->d_C.n * sizeof(double));
+    rc |= keep(e->d_I.p, e->d_I.n * sizeof(int));
+    rc |= keep(e->d_ring.p, e->d_ring.n * sizeof(unsigned));
+    rc |= keep(e->d_spikes.p, e->d_spikes.n * sizeof(unsigned long long));
+    if (rc) {
+        for (Save &s : saves) cudaFree(s.dst);
+        return GBH_ERR_CUDA;
+    }
+    for (Save &s : saves) CK(cudaMemcpy(s.dst, s.src, s.bytes, cudaMemcpyDeviceToDevice));
+    double best = 1e300;
+    int best_v = 0, best_s = spls[0];
+    for (int vi = 0; vi < nvar; ++vi) {
+        for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][vi];
+        for (int spl : spls) {
+            e->steps_per_launch = spl;
+            const int steps = e->has_network ? 32 : std::max(2 * spl, 128);
+            run_steps(e, 8, e->stream);          // warm caches and clocks
+            CK(cudaEventRecord(e->ev0, e->stream));
+            run_steps(e, steps, e->stream);
+            CK(cudaEventRecord(e->ev1, e->stream));
+            CK(cudaEventSynchronize(e->ev1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+            const double per = ms / steps;
+            if (per < best) { best = per; best_v = vi; best_s = spl; }
+            for (Save &s : saves) CK(cudaMemcpy((void *)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice));
+        }
+    }
+    for (Save &s : saves) cudaFree(s.dst);
+    for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
+    e->jit_choice = best_v;
+    e->steps_per_launch = best_s;
+    e->step = 0;
+    e->stats.launches = 0;
+    return GBH_OK;
+}
 
 // Internal: the step loop of run_steps with the flux scratch supplied by the
 // caller (used by gbh_run_noalloc). Reports the flux elements the engine needs.
@@ -924,6 +1002,11 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     cudaEventCreate(&e->ev0);
     cudaEventCreate(&e->ev1);
+    if (e->opt.steps_per_launch <= 0 && autotune(e) != GBH_OK) {
+        fail_err(err, GBH_ERR_CUDA, "autotuner: %s", g_last_error);
+        gbh_destroy(e);
+        return nullptr;
+    }
     int64_t comps = 0;
     for (const Neuron &N : e->dec.neurons) comps += N.nrows;
     e->stats.compartments = comps;
@@ -932,6 +1015,7 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->stats.steps_per_launch = e->steps_per_launch;
     e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
     e->stats.jit_kernels = e->jit_compiled;
+    e->stats.jit_min_blocks = e->jit_minb.empty() ? 0 : e->jit_minb[e->jit_choice];
     if (getenv("GBH_VERBOSE") && !e->jit_log.empty())
         fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
                 e->jit_log.c_str());
@@ -1100,7 +1184,8 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_out_vals.release(); e->d_out_addr.release();
-    for (JitKernel &k : e->jits) jit_release(k);
+    for (auto &vars : e->jit_var)
+        for (JitKernel &k : vars) jit_release(k);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
     if (e->stream) cudaStreamDestroy(e->stream);

@@ -110,7 +110,10 @@ typedef struct gbh_synapses {
 
 typedef struct gbh_options {
     int precision;       /* GBH_PREC_FP64 or GBH_PREC_MIXED                  */
-    int steps_per_launch;/* 0 = autotune; otherwise steps fused per launch     */
+    int steps_per_launch;/* 0 = autotune: gbh_create times trial steps on a saved
+                            copy of the state for each candidate kernel variant
+                            and steps-per-launch, restores the state and keeps
+                            the fastest; otherwise steps fused per launch     */
     int warps_per_block; /* 0 = autotune                                      */
     int use_graph;       /* capture multi-launch runs in a CUDA graph         */
     int device;          /* CUDA device ordinal                                */
@@ -129,6 +132,8 @@ typedef struct gbh_stats {
     int warps_per_block;
     int precision;
     int jit_kernels;           /* programs specialised and compiled at setup   */
+    int jit_min_blocks;        /* resident 4-warp blocks per SM the chosen
+                                  specialised variant was compiled for        */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
