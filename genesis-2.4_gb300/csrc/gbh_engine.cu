@@ -843,7 +843,7 @@ int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream)
 {
     if (!e || !host_values) return GBH_ERR_ARG;
     if (e->n_in == 0) return GBH_OK;
-    cudaStream_t st = (cudaStream_t)stream;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
     CK(cudaMemcpyAsync(e->d_in_vals.p, host_values, e->n_in * sizeof(double), cudaMemcpyHostToDevice, st));
     k_scatter_inputs<<<(e->n_in + 255) / 256, 256, 0, st>>>(e->d_in_vals.p, e->d_in_start.p, e->d_in_addr.p,
                                                            e->n_in, e->d_P.p);
@@ -879,7 +879,7 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
 {
     if (!e || !host_values) return GBH_ERR_ARG;
     if (e->n_out == 0) return GBH_OK;
-    cudaStream_t st = (cudaStream_t)stream;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
     k_gather_outputs<<<(e->n_out + 255) / 256, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, e->n_out,
                                                              e->d_out_vals.p);
     CK(cudaGetLastError());
@@ -1026,7 +1026,7 @@ int gbh_run_async(gbh_engine *e, int nsteps, void *stream)
 {
     if (!e || nsteps < 0) return GBH_ERR_ARG;
     if (nsteps == 0) return GBH_OK;
-    return run_steps(e, nsteps, (cudaStream_t)stream);
+    return run_steps(e, nsteps, stream ? (cudaStream_t)stream : e->stream);
 }
 
 int gbh_run(gbh_engine *e, int nsteps)

@@ -161,7 +161,8 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
 /* Advances every solver by nsteps PROCESS steps. Returns GBH_OK or an error. */
 int gbh_run(gbh_engine *e, int nsteps);
 
-/* Same, on a caller-owned CUDA stream (cudaStream_t passed as void*). */
+/* Same, on a caller-owned CUDA stream (cudaStream_t passed as void*; NULL =
+ * the engine's own stream, the one gbh_run uses). Returns once queued. */
 int gbh_run_async(gbh_engine *e, int nsteps, void *stream);
 
 /*
@@ -194,7 +195,8 @@ int gbh_get_givals(gbh_engine *e, double *givals);
  *
  * gbh_register_outputs names n compartments (solver, Hines row) whose Vm the
  * caller records; gbh_get_outputs_async gathers them and copies n doubles to
- * host memory on the stream (complete after a stream synchronize).
+ * host memory on the stream (complete after a stream synchronize). For these
+ * two, stream NULL means the engine's own stream.
  */
 int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index);
 int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream);
