@@ -47,6 +47,8 @@ SEED = 3
 ALG_BYTES = {"fp64": 1748.0 / NCOMP, "mixed": 1469.0 / NCOMP}
 ACC_STEPS = 10_000
 ACC_SAMPLE = 32
+# differentiated form (gradient of a somatic-trace loss)
+GRAD_NEURONS, GRAD_NCOMP, GRAD_STEPS, GRAD_K, GRAD_DT = 4096, 64, 10_000, 100, 25e-6
 
 
 def log(*a):
@@ -189,6 +191,58 @@ def _cpu_worker(args):
     return n * NCOMP * steps, time.perf_counter() - t0
 
 
+def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
+    """Gradient workload: 4,096 seeded random binary trees x 64 compartments
+    with Na, K and leak on every compartment, dt 25 us, backward Euler; loss =
+    summed squared somatic Vm error over 10,000 steps against traces of the
+    same trees with every gbar scaled by U(0.8, 1.2); checkpoints every 100
+    steps. Times gbh_loss_gradient against the plain FP64 forward
+    (gbh_run) of the same steps on the same engine."""
+    import torch
+    from gbhsolve import configs, engine, model
+    t0 = time.time()
+    trees, (na, k) = configs.grad_trees(n_neurons, ncomp=GRAD_NCOMP, seed=4)
+    targets = configs.grad_targets(trees, seed=5)
+    hs = [model.build(t.model(na, k, dt=GRAD_DT), exact=True) for t in trees]
+    ht = [model.build(t.model(na, k, dt=GRAD_DT), exact=True) for t in targets]
+    solver = np.arange(n_neurons, dtype=np.int32)
+    soma = np.array([h.ncompts - 1 for h in hs], dtype=np.int32)
+    log("gradient workload built in %.1f s" % (time.time() - t0))
+    # target traces from the FP64 engine (bit-identical to the CPU oracle)
+    et = engine.Engine(ht, precision=engine.PREC_FP64, device=device)
+    et.register_outputs(solver, soma)
+    trace = torch.empty((nsteps, n_neurons), dtype=torch.float64, pin_memory=True)
+    tr = trace.numpy()
+    stream = torch.cuda.Stream()
+    for n in range(nsteps):
+        et.run_async(1, stream.cuda_stream)
+        et.get_outputs_async(tr[n], stream.cuda_stream)
+    stream.synchronize()
+    et.close()
+    eng = engine.Engine(hs, precision=engine.PREC_FP64, device=device)
+    st0 = eng.get_state()
+    ms0 = eng.stats().device_ms
+    eng.run(nsteps)
+    fwd_ms = eng.stats().device_ms - ms0
+    eng.set_state(vm=st0["vm"], chip=st0["chip"])
+    t1 = time.time()
+    loss, dchip, drav, dvm = eng.loss_gradient(nsteps, solver, soma, tr, GRAD_K)
+    wall = time.time() - t1
+    st = eng.stats()
+    grad_ms = st.grad_forward_ms + st.grad_reverse_ms
+    eng.close()
+    finite = bool(np.all(np.isfinite(dchip)) and np.all(np.isfinite(drav)) and np.all(np.isfinite(dvm)))
+    log("gradient: forward %.1f ms, gradient %.1f ms (checkpoint pass %.1f, reverse %.1f), ratio %.2f, "
+        "loss %.6g" % (fwd_ms, grad_ms, st.grad_forward_ms, st.grad_reverse_ms, grad_ms / fwd_ms, loss))
+    return {"workload": "grad-trees-4096x64: %d random binary trees x %d compartments, Na/K/leak on every "
+                        "compartment, dt 25 us, backward Euler, somatic-trace loss" % (n_neurons, GRAD_NCOMP),
+            "steps": nsteps, "checkpoint_every": GRAD_K, "dtype": "f64",
+            "forward_ms": fwd_ms, "gradient_ms": grad_ms, "checkpoint_pass_ms": st.grad_forward_ms,
+            "reverse_pass_ms": st.grad_reverse_ms, "gradient_wall_s": wall,
+            "ratio_gradient_over_forward": grad_ms / fwd_ms, "loss": loss, "gradients_finite": finite,
+            "launches": 1 + 2 * ((nsteps + GRAD_K - 1) // GRAD_K)}
+
+
 def run_reference(args, ws, rank, dist):
     """CPU restatement of the reference solver on every host core."""
     if rank != 0:
@@ -239,6 +293,7 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=0)
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local, dist = dist_setup()
@@ -314,6 +369,10 @@ def main():
         acc = accuracy_sample(hs, engine.PREC_MIXED)
         log("mixed max|dVm| over %d steps: %.3e V" % (ACC_STEPS, acc))
 
+    adj = None
+    if rank == 0 and not args.skip_adjoint:
+        adj = adjoint_measure(local)
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         v, sample = cpu_sample_rate(hs)
@@ -355,6 +414,7 @@ def main():
                          "kernel": "gbh_jit (specialised mixed step)", "launch_ms": launch_ms,
                          "alg_bytes_per_compartment_step": ALG_BYTES["mixed"]},
             "cpu_baseline": cpu,
+            "adjoint": adj,
             "gpu_launches": int(r["launches"]),
             "clocks": r["clocks"],
         }

@@ -121,8 +121,9 @@ struct NB {
 // Symbolic execution of funcs[] (asymmetric compartments).
 int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra, int n,
                 std::vector<int> &parent, std::vector<double> &A, std::vector<double> &B,
-                std::vector<double> &Cc)
+                std::vector<double> &Cc, std::vector<int> &ridx)
 {
+    ridx.assign(3 * (size_t)n, -1);   // ravals index of A, B, C of each row
     parent.assign(n, -1);
     A.assign(n, 0.0);
     B.assign(n, 0.0);
@@ -148,7 +149,9 @@ int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra,
                             "children of row %d are not in ascending row order", cur);
             lastkid[cur] = kid;
             parent[kid] = cur;
+            ridx[3 * kid] = (int)ri;
             A[kid] = ra[ri++];
+            ridx[3 * kid + 1] = (int)ri;
             B[kid] = ra[ri++];
             fcount[kid]++;
         } else if (op == F_SET_DIAG) {
@@ -174,6 +177,7 @@ int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra,
             const int p = f[fi++] / 2;
             if (cur < 0 || p != parent[cur] || bcount[cur])
                 return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "BACKWARD_ELIM of row %d does not match its parent", cur);
+            ridx[3 * cur + 2] = (int)ri;
             Cc[cur] = ra[ri++];
             bcount[cur]++;
         } else if (op == F_CALC) {
@@ -220,11 +224,11 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         if (ts < 0 || ts >= d->ntables) return fail(c, GBH_ERR_ARG, -1, 0, -1, "table set %d out of range", ts);
 
         // elimination structure
-        std::vector<int> parent;
+        std::vector<int> parent, ridx;
         std::vector<double> A, B, Cc;
         int rc = parse_funcs(c, d->funcs + d->funcs_start[si], d->funcs_start[si + 1] - d->funcs_start[si],
                              d->ravals + d->ravals_start[si], d->ravals_start[si + 1] - d->ravals_start[si],
-                             n, parent, A, B, Cc);
+                             n, parent, A, B, Cc, ridx);
         if (rc) return rc;
         // trees: parents always have higher rows (Hines numbering)
         std::vector<int> tree(n, -1);
@@ -266,6 +270,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                 nn.A.push_back(A[r]);
                 nn.B.push_back(B[r]);
                 nn.C.push_back(Cc[r]);
+                for (int q = 0; q < 3; ++q) nn.ridx.push_back(ridx[3 * r + q]);
             }
             tree_neuron[order[k]] = nbase + k;
             out.neurons.push_back(std::move(nn));

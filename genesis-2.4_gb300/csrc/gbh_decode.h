@@ -33,6 +33,7 @@ struct Neuron {
     std::vector<int> syn_op;      // solver ops index of each synchan row
     std::vector<int> parent;      // per slot
     std::vector<double> A, B, C;  // per slot
+    std::vector<int> ridx;        // per slot: ravals index of A, B, C (-1: none)
     int spike_op = -1;
     std::string key;              // grouping signature
 };

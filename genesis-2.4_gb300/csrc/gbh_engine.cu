@@ -16,6 +16,7 @@
 #include "gbh_kernels.cuh"
 #include "gbh_df.cuh"
 #include "gbh_jit.h"
+#include "gbh_adjoint.h"
 #include <thread>
 #include "gbhsolve.h"
 
@@ -86,7 +87,7 @@ struct gbh_engine {
     std::vector<TileType> types;
     std::vector<Tile> tiles;
     std::vector<int> neuron_tile, neuron_lane;   // placement of every neuron
-    std::vector<int64_t> chip_start, conc_start, ops_start, vm_start, giv_start;
+    std::vector<int64_t> chip_start, conc_start, ops_start, vm_start, giv_start, rav_start;
     std::vector<double> chip_orig;              // reference chip[] for sync copies
     std::vector<int> ops_orig;
     int64_t ngiv_total = 0;
@@ -990,6 +991,7 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->ops_start.assign(desc->ops_start, desc->ops_start + ns + 1);
     e->vm_start.assign(desc->vm_start, desc->vm_start + ns + 1);
     e->giv_start.assign(desc->givals_start, desc->givals_start + ns + 1);
+    e->rav_start.assign(desc->ravals_start, desc->ravals_start + ns + 1);
     e->chip_orig.assign(desc->chip, desc->chip + desc->chip_start[ns]);
     e->ops_orig.assign(desc->ops, desc->ops + desc->ops_start[ns]);
     rc = build_layout(e, desc, syn, err);
@@ -1169,6 +1171,240 @@ int gbh_get_stats(const gbh_engine *e, gbh_stats *st)
 {
     if (!e || !st) return GBH_ERR_ARG;
     *st = e->stats;
+    return GBH_OK;
+}
+
+int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh_loss_spec *spec,
+                      double *loss, double *dchip, double *dravals, double *dvm0)
+{
+    if (!e || nsteps < 0 || !spec || spec->ntargets < 0 ||
+        (spec->ntargets > 0 && (!spec->solver || !spec->row || !spec->trace)))
+        return fail_err(nullptr, GBH_ERR_ARG, "gbh_loss_gradient: bad arguments");
+    if (e->opt.precision != GBH_PREC_FP64)
+        return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient needs an FP64 engine");
+    if (e->has_network)
+        return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: synaptic networks are not differentiated");
+    const size_t L = LANES;
+    // ---- supported programs; gate count per tile type ----
+    std::vector<int> ngates(e->types.size(), 0);
+    std::vector<int> prog;
+    {
+        prog.resize(e->d_prog.n);
+        if (!prog.empty()) CK(cudaMemcpy(prog.data(), e->d_prog.p, prog.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    for (size_t ti = 0; ti < e->types.size(); ++ti) {
+        const TileType &tt = e->types[ti];
+        if (tt.npools || tt.nsyn || tt.has_spike)
+            return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
+                            "gbh_loss_gradient: Ca pools, synchans and spike detectors are not differentiated");
+        int pc = tt.prog_off, s = 0, in_chan = 0;
+        while (s < tt.nslots) {
+            const int code = prog[pc];
+            switch (code) {
+            case M_BEGIN: pc += 5; break;
+            case M_NEWVOLT: pc += 1; break;
+            case M_CHAN: pc += 3; in_chan = 0; break;
+            case M_CHAN_G: pc += 2; in_chan = 0; break;
+            case M_ADDCURR: pc += 2; break;
+            case M_END: pc += 4; ++s; break;
+            case M_GATE:
+                if (prog[pc + 1] != GK_1V || prog[pc + 3] == 0)
+                    return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
+                                    "gbh_loss_gradient: only voltage-table gates with a nonzero power are "
+                                    "differentiated (kind %d, power %d)", prog[pc + 1], prog[pc + 3]);
+                if (++in_chan > ADJ_MAX_GATES)
+                    return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: more than %d gates in a channel",
+                                    ADJ_MAX_GATES);
+                ngates[ti]++;
+                pc += 5;
+                break;
+            default:
+                return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
+                                "gbh_loss_gradient: micro-op %d (concentration, GHK, synaptic or pump terms) is "
+                                "not differentiated", code);
+            }
+        }
+    }
+    if (nsteps == 0) {
+        if (loss) *loss = 0.0;
+        if (dchip) memset(dchip, 0, e->chip_start.back() * sizeof(double));
+        if (dravals) memset(dravals, 0, e->rav_start.back() * sizeof(double));
+        if (dvm0) memset(dvm0, 0, e->vm_start.back() * sizeof(double));
+        return GBH_OK;
+    }
+    const int K = std::max(1, std::min(checkpoint_every > 0 ? checkpoint_every : 100, nsteps));
+    const int nseg = (nsteps + K - 1) / K;
+    // ---- target rows ----
+    std::vector<int> tgt(e->rows_topo * L, -1);
+    {
+        std::unordered_map<int64_t, int> at;   // (solver, row) -> neuron
+        for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+            const Neuron &N = e->dec.neurons[i];
+            for (int s = 0; s < N.nrows; ++s) at[(int64_t)N.solver * (1LL << 32) + N.row0 + s] = (int)i;
+        }
+        for (int j = 0; j < spec->ntargets; ++j) {
+            auto it = at.find((int64_t)spec->solver[j] * (1LL << 32) + spec->row[j]);
+            if (it == at.end())
+                return fail_err(nullptr, GBH_ERR_ARG, "target %d: solver %d has no row %d", j, spec->solver[j],
+                                spec->row[j]);
+            const Neuron &N = e->dec.neurons[it->second];
+            const Tile &t = e->tiles[e->neuron_tile[it->second]];
+            int &cell = tgt[(t.topo + spec->row[j] - N.row0) * L + e->neuron_lane[it->second]];
+            if (cell >= 0) return fail_err(nullptr, GBH_ERR_ARG, "target %d repeats target %d", j, cell);
+            cell = j;
+        }
+    }
+    // ---- checkpoint and tape layout ----
+    std::vector<int64_t> ck_off(e->tiles.size()), tp_off(e->tiles.size());
+    int64_t ck_stride = 0, tp_stride = 0;
+    int smax = 1;
+    for (size_t t = 0; t < e->tiles.size(); ++t) {
+        const TileType &tt = e->types[e->tiles[t].type];
+        ck_off[t] = ck_stride;
+        tp_off[t] = tp_stride;
+        ck_stride += tt.nslots + ngates[e->tiles[t].type];
+        tp_stride += 4 * tt.nslots + ngates[e->tiles[t].type];
+        smax = std::max(smax, tt.nslots);
+    }
+    if ((size_t)2 * smax * L * sizeof(double) > 227 * 1024)
+        return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: %d compartments per neuron exceed shared memory",
+                        smax);
+    // ---- device buffers (released on every return path) ----
+    struct Bufs {
+        DBuf<double> P, V, ck, tape, Vb, Xb, Gf, GA, GB, GC, trace, loss;
+        DBuf<int> tgt;
+        DBuf<int64_t> ck_off, tp_off;
+        ~Bufs()
+        {
+            P.release(); V.release(); ck.release(); tape.release(); Vb.release(); Xb.release(); Gf.release();
+            GA.release(); GB.release(); GC.release(); trace.release(); loss.release(); tgt.release();
+            ck_off.release(); tp_off.release();
+        }
+    } b;
+    const int64_t nfld = e->rows_fld * L, nvm = e->rows_vm * L, ntopo = e->rows_topo * L;
+    if (b.P.alloc(nfld) || b.V.alloc(nvm) || b.ck.alloc((size_t)nseg * ck_stride * L) ||
+        b.tape.alloc((size_t)K * tp_stride * L) || b.Vb.alloc(nvm) || b.Xb.alloc(nfld) || b.Gf.alloc(nfld) ||
+        b.GA.alloc(ntopo) || b.GB.alloc(ntopo) || b.GC.alloc(ntopo) || b.loss.alloc(e->tiles.size() * L) ||
+        b.trace.alloc(std::max<size_t>(1, (size_t)nsteps * spec->ntargets)))
+        return GBH_ERR_CUDA;
+    if (b.tgt.upload(tgt) || b.ck_off.upload(ck_off) || b.tp_off.upload(tp_off)) return GBH_ERR_CUDA;
+    cudaStream_t st = e->stream;
+    CK(cudaStreamSynchronize(st));
+    if (spec->ntargets)
+        CK(cudaMemcpy(b.trace.p, spec->trace, (size_t)nsteps * spec->ntargets * sizeof(double),
+                      cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(b.P.p, e->d_P.p, nfld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(b.V.p, e->d_V.p, nvm * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemsetAsync(b.Vb.p, 0, nvm * sizeof(double), st));
+    CK(cudaMemsetAsync(b.Xb.p, 0, nfld * sizeof(double), st));
+    CK(cudaMemsetAsync(b.Gf.p, 0, nfld * sizeof(double), st));
+    CK(cudaMemsetAsync(b.GA.p, 0, ntopo * sizeof(double), st));
+    CK(cudaMemsetAsync(b.GB.p, 0, ntopo * sizeof(double), st));
+    CK(cudaMemsetAsync(b.GC.p, 0, ntopo * sizeof(double), st));
+    CK(cudaMemsetAsync(b.loss.p, 0, e->tiles.size() * L * sizeof(double), st));
+    AdjView v{};
+    v.tiles = e->d_tiles.p;
+    v.types = e->d_types.p;
+    v.prog = e->d_prog.p;
+    v.tgeom = e->d_tgeom.p;
+    v.tab64 = e->d_tab64.p;
+    v.xyvals = e->d_xy.p;
+    v.parent = e->d_par.p;
+    v.A = e->d_A.p;
+    v.B = e->d_B.p;
+    v.Cb = e->d_Cb.p;
+    v.P = b.P.p;
+    v.V = b.V.p;
+    v.ckpt = b.ck.p;
+    v.ck_off = b.ck_off.p;
+    v.ck_stride = ck_stride;
+    v.tape = b.tape.p;
+    v.tp_off = b.tp_off.p;
+    v.tp_stride = tp_stride;
+    v.Vbar = b.Vb.p;
+    v.Xbar = b.Xb.p;
+    v.Gf = b.Gf.p;
+    v.GA = b.GA.p;
+    v.GB = b.GB.p;
+    v.GC = b.GC.p;
+    v.tgt = b.tgt.p;
+    v.trace = b.trace.p;
+    v.ntargets = spec->ntargets;
+    v.loss = b.loss.p;
+    v.status = e->d_status.p;
+    const int ntiles = (int)e->tiles.size();
+    auto ck_launch = [&](cudaError_t ce) {
+        if (ce != cudaSuccess) {
+            set_last("adjoint kernel launch failed: %s", cudaGetErrorString(ce));
+            return GBH_ERR_CUDA;
+        }
+        return GBH_OK;
+    };
+    // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed)
+    CK(cudaEventRecord(e->ev0, st));
+    if (ck_launch(launch_adj_forward(v, 0, ntiles, smax, (nseg - 1) * K, K, 0, 0, st))) return GBH_ERR_CUDA;
+    CK(cudaEventRecord(e->ev1, st));
+    CK(cudaEventSynchronize(e->ev1));
+    float ms_fwd = 0.f;
+    CK(cudaEventElapsedTime(&ms_fwd, e->ev0, e->ev1));
+    // reverse pass, segment by segment
+    CK(cudaEventRecord(e->ev0, st));
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int nk = std::min(K, nsteps - seg * K);
+        if (ck_launch(launch_adj_forward(v, 0, ntiles, smax, nk, K, 1, seg, st))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reverse(v, 0, ntiles, smax, nk, seg * K, st))) return GBH_ERR_CUDA;
+    }
+    CK(cudaEventRecord(e->ev1, st));
+    CK(cudaEventSynchronize(e->ev1));
+    float ms_rev = 0.f;
+    CK(cudaEventElapsedTime(&ms_rev, e->ev0, e->ev1));
+    e->stats.grad_forward_ms = ms_fwd;
+    e->stats.grad_reverse_ms = ms_rev;
+    e->stats.launches += 1 + 2 * nseg;
+    int status = 0;
+    CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status) {
+        set_last("device status word 0x%x in the adjoint kernels", status);
+        return GBH_ERR_DEVICE;
+    }
+    // ---- gather ----
+    std::vector<double> Vb(nvm), Xb(nfld), Gf(nfld), GA(ntopo), GB(ntopo), GC(ntopo), ls(e->tiles.size() * L);
+    CK(cudaMemcpy(Vb.data(), b.Vb.p, nvm * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(Xb.data(), b.Xb.p, nfld * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(Gf.data(), b.Gf.p, nfld * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(GA.data(), b.GA.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(GB.data(), b.GB.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(GC.data(), b.GC.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ls.data(), b.loss.p, ls.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if (loss) {
+        double sum = 0.0;
+        for (size_t t = 0; t < e->tiles.size(); ++t)
+            for (int l = 0; l < e->tiles[t].nlanes; ++l) sum += ls[t * L + l];
+        *loss = sum;
+    }
+    if (dchip) memset(dchip, 0, e->chip_start.back() * sizeof(double));
+    if (dravals) memset(dravals, 0, e->rav_start.back() * sizeof(double));
+    if (dvm0) memset(dvm0, 0, e->vm_start.back() * sizeof(double));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        if (dvm0)
+            for (int s = 0; s < N.nrows; ++s) dvm0[e->vm_start[N.solver] + N.row0 + s] = Vb[(t.vm + s) * L + l];
+        if (dchip)
+            for (size_t f = 0; f < N.fsrc.size(); ++f)
+                if (N.fsrc[f].kind == FS_CHIP)
+                    dchip[e->chip_start[N.solver] + N.fsrc[f].idx] +=
+                        Gf[(t.fld + f) * L + l] + Xb[(t.fld + f) * L + l];
+        if (dravals)
+            for (int s = 0; s < N.nrows; ++s) {
+                const double g[3] = {GA[(t.topo + s) * L + l], GB[(t.topo + s) * L + l], GC[(t.topo + s) * L + l]};
+                for (int q = 0; q < 3; ++q) {
+                    const int r = N.ridx[3 * s + q];
+                    if (r >= 0) dravals[e->rav_start[N.solver] + r] += g[q];
+                }
+            }
+    }
     return GBH_OK;
 }
 

@@ -1,8 +1,9 @@
 """Builds the engine library libgbhsolve.so in-tree for sm_103a (GB300).
 
-Three CUDA/C++ translation units are compiled in parallel:
+The CUDA/C++ translation units are compiled in parallel:
   gbh_k64.cu    FP64 kernels, --fmad=false (bit-level parity with the CPU solver)
   gbh_k32.cu    mixed-precision kernels (FP32 gates), contraction allowed
+  gbh_adjoint.cu adjoint (gradient) kernels of the FP64 form, --fmad=false
   gbh_engine.cu host layout, launches and the C ABI
   gbh_decode.cpp ops[]/funcs[] decoder
 """
@@ -78,6 +79,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     units = [
         ("gbh_k64.cu", ["--fmad=false", "-Xptxas", "-v"] if verbose else ["--fmad=false"]),
         ("gbh_k32.cu", ["-Xptxas", "-v"] if verbose else []),
+        ("gbh_adjoint.cu", ["--fmad=false", "-Xptxas", "-v"] if verbose else ["--fmad=false"]),
         ("gbh_engine.cu", []),
         ("gbh_noalloc.cu", []),
         ("gbh_decode.cpp", []),

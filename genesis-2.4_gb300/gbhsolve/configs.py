@@ -284,3 +284,175 @@ def network_synapses(hs, syn):
         tgt_op[k] = h.childops[cidx]
     return dict(src_start=syn["start"].astype(np.int64), target_solver=syn["target"].astype(np.int32),
                 target_op=tgt_op, weight=syn["weight"], delay_steps=syn["delay_steps"]), tgt_child
+
+
+# --------------------------------------------------------------------------
+# Adjoint gradients (config 4)
+# --------------------------------------------------------------------------
+class GradTree:
+    """Physical parameters of one config-4 neuron: a seeded random binary
+    tree whose every compartment carries HH Na and K tabchannels and a leak
+    (conductance gl through the membrane resistance). Parameters: per
+    compartment gna, gk, gl (S/m^2); per neuron cm (F/m^2) and ra (ohm m).
+    Geometry, inject and reversal potentials are fixed."""
+
+    def __init__(self, parents, length, diam, gna, gk, gl, cm, ra, inject, erest=-0.065):
+        self.parents = list(parents)
+        self.length = np.asarray(length, dtype=np.float64)
+        self.diam = np.asarray(diam, dtype=np.float64)
+        self.gna = np.array(gna, dtype=np.float64)
+        self.gk = np.array(gk, dtype=np.float64)
+        self.gl = np.array(gl, dtype=np.float64)
+        self.cm = float(cm)
+        self.ra = float(ra)
+        self.inject = float(inject)
+        self.erest = float(erest)
+
+    @property
+    def area(self):
+        return self.length * PI * self.diam
+
+    @property
+    def xarea(self):
+        return PI * (self.diam / 2) ** 2
+
+    def copy(self):
+        return GradTree(self.parents, self.length, self.diam, self.gna, self.gk, self.gl, self.cm, self.ra,
+                        self.inject, self.erest)
+
+    def vector(self):
+        """Parameters as one flat vector: gna, gk, gl (per compartment), cm, ra."""
+        return np.concatenate([self.gna, self.gk, self.gl, [self.cm, self.ra]])
+
+    def with_vector(self, v):
+        n = len(self.parents)
+        return GradTree(self.parents, self.length, self.diam, v[:n], v[n:2 * n], v[2 * n:3 * n], v[3 * n],
+                        v[3 * n + 1], self.inject, self.erest)
+
+    def model(self, na, k, dt=25e-6, method=BEULER) -> Model:
+        """Compartments with fields computed in double (no SLI or float
+        rounding): build with ``model.build(m, exact=True)``."""
+        area, xarea = self.area, self.xarea
+        comps = []
+        for c, p in enumerate(self.parents):
+            comp = Compartment(Em=self.erest, Rm=1.0 / (self.gl[c] * area[c]), Cm=self.cm * area[c],
+                               Ra=self.ra * self.length[c] / xarea[c], initVm=self.erest,
+                               inject=self.inject if c == 0 else 0.0, parent=p)
+            comp.children = [TabChannel(na, Gbar=self.gna[c] * area[c]), TabChannel(k, Gbar=self.gk[c] * area[c])]
+            comps.append(comp)
+        return Model(comps, dt=dt, method=method)
+
+
+def grad_trees(n_neurons=4096, ncomp=64, seed=4, soma=(30e-6, 30e-6), dend_len=20e-6,
+               dia_range=(0.5e-6, 3e-6), inject_range=(0.2e-9, 0.6e-9)):
+    """Config 4 neurons (seeded). Soma gna 1200, gk 360 S/m^2, dendrites a
+    tenth of that, gl = 1/0.33 S/m^2, each scaled by U(0.8, 1.2) per
+    compartment; cm = 0.01 F/m^2 x U(0.9, 1.1), ra = 0.3 ohm m x U(0.9, 1.1)
+    per neuron. Returns (trees, (na, k) channel types)."""
+    rng = np.random.default_rng(seed)
+    na, k = hh_channels(-0.065)
+    trees = []
+    for _ in range(n_neurons):
+        parents = random_binary_tree(rng, ncomp)
+        length = np.full(ncomp, dend_len)
+        diam = rng.uniform(*dia_range, size=ncomp)
+        length[0], diam[0] = soma
+        scale = np.where(np.arange(ncomp) == 0, 1.0, 0.1)
+        gna = 1200.0 * scale * rng.uniform(0.8, 1.2, ncomp)
+        gk = 360.0 * scale * rng.uniform(0.8, 1.2, ncomp)
+        gl = (1.0 / 0.33) * rng.uniform(0.8, 1.2, ncomp)
+        cm = 0.01 * rng.uniform(0.9, 1.1)
+        ra = 0.3 * rng.uniform(0.9, 1.1)
+        trees.append(GradTree(parents, length, diam, gna, gk, gl, cm, ra, rng.uniform(*inject_range)))
+    return trees, (na, k)
+
+
+def grad_targets(trees, seed=5, spread=0.2):
+    """Target models: every gbar (Na, K, leak) scaled by U(1-spread, 1+spread)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for t in trees:
+        u = t.copy()
+        n = len(t.parents)
+        u.gna = t.gna * (1.0 + rng.uniform(-spread, spread, n))
+        u.gk = t.gk * (1.0 + rng.uniform(-spread, spread, n))
+        u.gl = t.gl * (1.0 + rng.uniform(-spread, spread, n))
+        out.append(u)
+    return out
+
+
+def chip_roles(h):
+    """Role of every chip[] entry of a one-tree solver built from
+    :class:`GradTree`: ('emrm'|'inject'|'tbyc'|'diag', compt) or
+    ('ek'|'gbar'|'state', compt, reversal potential of the channel). SETUP
+    orders a compartment's channels by its own rules; the reversal potential
+    identifies the channel."""
+    from .model import (ADD_CURR_OP, CHAN_EK_OP, CHAN_OP, IPOL1V_OP, LCOMPT_OP, NEWVOLT_OP)
+    roles = [None] * len(h.chip)
+    ops = h.ops
+    o = c = row = 0
+    ek = 0.0
+    while True:
+        code = int(ops[o])
+        o += 1
+        if code == LCOMPT_OP:
+            break
+        elm = int(h.elmnum[row])
+        roles[c], roles[c + 1] = ("emrm", elm), ("inject", elm)
+        c += 2
+        while int(ops[o]) > LCOMPT_OP:
+            k = int(ops[o])
+            o += 1
+            if k == NEWVOLT_OP or k == ADD_CURR_OP:
+                continue
+            if k == CHAN_EK_OP:
+                ek = float(h.chip[c])
+                roles[c], roles[c + 1] = ("ek", elm, ek), ("gbar", elm, ek)
+                c += 2
+            elif k == CHAN_OP:   # keeps the previous channel's Ek
+                roles[c] = ("gbar", elm, ek)
+                c += 1
+            elif k == IPOL1V_OP:
+                o += 2
+                roles[c] = ("state", elm, ek)
+                c += 1
+            else:
+                raise ValueError("opcode %d outside the config-4 program" % k)
+        roles[c], roles[c + 1] = ("tbyc", elm), ("diag", elm)
+        c += 2
+        row += 1
+    return roles
+
+
+def param_gradient(tree: GradTree, h, dchip, dravals, ena, dt=25e-6, method=BEULER):
+    """Chain rule from the gradient with respect to one solver's chip[] and
+    ravals[] to the tree's physical parameters (same order as
+    ``GradTree.vector``), for arrays built with ``exact=True``:
+      Gbar = g*area;  Em/Rm = Em*gl*area;  dt'/Cm = dt'/(cm*area);
+      diag = 1 + dt'*gl/cm + coupling,  coupling and every ravals entry
+      proportional to 1/(cm*ra);  dt' = dt/2 for Crank-Nicolson.
+    ``ena`` is the Na channel's reversal potential (the other channel is K)."""
+    n = len(tree.parents)
+    dtc = dt / 2.0 if method == CRANK else dt
+    area = tree.area
+    g = np.zeros(3 * n + 2)
+    for idx, role in enumerate(chip_roles(h)):
+        kind, elm = role[0], role[1]
+        d = float(dchip[idx])
+        if kind == "gbar":
+            g[(0 if abs(role[2] - ena) < 1e-12 else 1) * n + elm] += d * area[elm]
+        elif kind == "emrm":
+            g[2 * n + elm] += d * tree.erest * area[elm]
+        elif kind == "tbyc":
+            g[3 * n] += d * (-h.chip[idx] / tree.cm)
+        elif kind == "diag":
+            leak = dtc * tree.gl[elm] / tree.cm
+            coupling = h.chip[idx] - 1.0 - leak
+            g[2 * n + elm] += d * dtc / tree.cm
+            g[3 * n] += d * (-(h.chip[idx] - 1.0) / tree.cm)
+            g[3 * n + 1] += d * (-coupling / tree.ra)
+    r = np.asarray(h.ravals, dtype=np.float64)
+    dr = np.asarray(dravals[:len(r)], dtype=np.float64)
+    g[3 * n] += float(np.dot(dr, -r / tree.cm))
+    g[3 * n + 1] += float(np.dot(dr, -r / tree.ra))
+    return g

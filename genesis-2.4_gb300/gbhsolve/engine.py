@@ -64,17 +64,22 @@ class GbhOptions(C.Structure):
                 ("jit", C.c_int)]
 
 
+class GbhLossSpec(C.Structure):
+    _fields_ = [("ntargets", C.c_int), ("solver", _ip), ("row", _ip), ("trace", _dp)]
+
+
 class GbhStats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("device_ms", C.c_double), ("compartments", C.c_int64),
                 ("tiles", C.c_int64), ("launches", C.c_int64), ("bytes_per_step", C.c_double),
                 ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int),
-                ("jit_kernels", C.c_int), ("jit_min_blocks", C.c_int)]
+                ("jit_kernels", C.c_int), ("jit_min_blocks", C.c_int),
+                ("grad_forward_ms", C.c_double), ("grad_reverse_ms", C.c_double)]
 
 
 EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
-            "gbh_destroy", "gbh_last_error", "gbh_run_noalloc"]
+            "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient"]
 
 _LIB = None
 
@@ -114,6 +119,7 @@ def load(build_if_missing: bool = True):
     lib.gbh_destroy.argtypes = [C.c_void_p]
     lib.gbh_last_error.restype = C.c_char_p
     lib.gbh_run_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.gbh_loss_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(GbhLossSpec), _dp, _dp, _dp, _dp]
     _LIB = lib
     return lib
 
@@ -345,6 +351,23 @@ class Engine:
 
     def get_outputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
         self._check(self.lib.gbh_get_outputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))
+
+    def loss_gradient(self, nsteps: int, solver, row, trace, checkpoint_every: int = 100):
+        """gbh_loss_gradient: loss = sum over steps and targets of (Vm - trace)^2
+        and its gradient with respect to chip[], ravals[] and the initial vm[]
+        (flat arrays in the batch layout). The engine state is unchanged."""
+        b = self.batch
+        s = np.ascontiguousarray(solver, dtype=np.int32)
+        r = np.ascontiguousarray(row, dtype=np.int32)
+        tr = np.ascontiguousarray(trace, dtype=np.float64).reshape(int(nsteps), len(s))
+        spec = GbhLossSpec(len(s), _ptr(s, _ip), _ptr(r, _ip), _ptr(tr, _dp))
+        loss = C.c_double(0.0)
+        dchip = np.zeros(int(b.chip_start[-1]) or 1)
+        drav = np.zeros(int(b.ravals_start[-1]) or 1)
+        dvm = np.zeros(int(b.vm_start[-1]) or 1)
+        self._check(self.lib.gbh_loss_gradient(self.h, int(nsteps), int(checkpoint_every), C.byref(spec),
+                                               C.byref(loss), _ptr(dchip, _dp), _ptr(drav, _dp), _ptr(dvm, _dp)))
+        return loss.value, dchip, drav, dvm
 
     def spike_counts(self) -> np.ndarray:
         c = np.zeros(self.batch.n, dtype=np.int64)

@@ -56,6 +56,9 @@ def f32(x: float) -> float:
     return float(np.float32(x))
 
 
+_f32_field = f32
+
+
 def sli(x: float) -> float:
     """Value after an SLI expression is passed as a command argument: SLI
     formats floats with ``%0.10g`` (sim/sim_main.c:372, ss/eval.c:1075)."""
@@ -319,8 +322,14 @@ def _belongs_before(a, b):
     return False
 
 
-def build(model: Model) -> HsolveArrays:
-    """SETUP + RESET of one hsolve over ``model``; returns the flat arrays."""
+def build(model: Model, exact: bool = False) -> HsolveArrays:
+    """SETUP + RESET of one hsolve over ``model``; returns the flat arrays.
+
+    ``exact=True`` skips the rounding of element fields to float storage, so
+    the arrays are smooth functions of the model's parameters (used by the
+    differentiated form's finite-difference checks); the default reproduces
+    the reference's arrays."""
+    f32 = (lambda x: float(x)) if exact else _f32_field
     comps = model.compartments
     n = len(comps)
     dt = float(model.dt)
@@ -530,7 +539,7 @@ def build(model: Model) -> HsolveArrays:
         compchips[i] = len(chip)
         ops.append(FCOMPT_OP if i == 0 else COMPT_OP)
         Em, Rm, Cm = f32(cp.Em), f32(cp.Rm), f32(cp.Cm)
-        chip += [float(np.float32(np.float32(Em) / np.float32(Rm))), f32(cp.inject)]
+        chip += [f32(f32(Em) / f32(Rm)), f32(cp.inject)]
         vm[i] = f32(cp.initVm)  # compartment RESET: Vm = initVm
         has_volt = any(isinstance(ch, TabChannel) and
                        any(not g[3] for g in chan_gates[(i, p)])
@@ -647,7 +656,7 @@ def build(model: Model) -> HsolveArrays:
             ravals.append(t)
             diagterms[i] -= t
             # float*float: the product is formed in float (hines_init.c:734)
-            t = -dtc / float(np.float32(np.float32(link.Cm) * np.float32(link.Ra)))
+            t = -dtc / f32(f32(link.Cm) * f32(link.Ra))
             ravals.append(t)
             diagterms[row] -= t
     funcs.append(FINISH)
@@ -684,7 +693,7 @@ def build(model: Model) -> HsolveArrays:
                 conc[k] = float(ch.Ca_base)
                 concops += [CACONC_OP, k]
                 tau = f32(ch.tau)
-                concchip += [float(ch.Ca_base), 1.0 + dt / float(np.float32(2 * np.float32(tau))),
+                concchip += [float(ch.Ca_base), 1.0 + dt / f32(2 * f32(tau)),
                              dt * f32(ch.B)]
     if nconcs:
         concops.append(LCACONC_OP)

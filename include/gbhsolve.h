@@ -134,6 +134,10 @@ typedef struct gbh_stats {
     int jit_kernels;           /* programs specialised and compiled at setup   */
     int jit_min_blocks;        /* resident 4-warp blocks per SM the chosen
                                   specialised variant was compiled for        */
+    double grad_forward_ms;    /* last gbh_loss_gradient: checkpointed forward
+                                  pass (device time, CUDA events)             */
+    double grad_reverse_ms;    /* last gbh_loss_gradient: segment recomputation
+                                  + adjoint steps (device time)               */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
@@ -233,6 +237,48 @@ int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
  */
 #define GBH_NOALLOC_FLUX_MAX (1 << 20)
 int gbh_run_noalloc(gbh_engine *e, int nsteps, void *stream);
+
+/*
+ * gbh_loss_gradient -- differentiated form (FP64 engines only).
+ *
+ * No counterpart in the reference (GENESIS computes no gradients). From the
+ * engine's current state it runs nsteps steps and returns
+ *   loss = sum_n sum_j (Vm[solver_j, row_j] after step n+1 - trace[n][j])^2
+ * for n = 0 .. nsteps-1, and its gradient with respect to every input of the
+ * step (each output may be NULL):
+ *   dchip   [total chip]   parameters read from chip[] (Em/Rm, inject, Ek,
+ *                          gbar, dt/Cm, diagonal term) and the initial gate
+ *                          states held there;
+ *   dravals [total ravals] the elimination coefficients of every row;
+ *   dvm0    [total vm]     the initial membrane potentials;
+ * laid out like the arrays of the gbh_batch_desc given to gbh_create (solvers
+ * concatenated through the *_start offsets). Entries the step does not read
+ * are zero. The engine's own state is left unchanged.
+ *
+ * Method: hand-written adjoint (reverse-mode) kernels. A forward pass stores
+ * Vm and the gate states every checkpoint_every steps (<= 0: 100); the
+ * reverse pass recomputes each segment from its checkpoint, recording Vm,
+ * the elimination's diagonals and right-hand sides, the solution and the
+ * gate states of every step, and runs the transposed Hines sweep (reverse
+ * elimination order) and the reverse of the gate updates and table
+ * interpolations step by step back to the start. Device memory held during
+ * the call: checkpoints ~ (nsteps / checkpoint_every) x (rows + gates) and
+ * the tape ~ checkpoint_every x (4 rows + gates) doubles per neuron.
+ *
+ * Supported programs (GBH_ERR_UNSUPPORTED otherwise): compartments with
+ * voltage-tabulated channels (TABCHAN with IPOL1V gates of nonzero power,
+ * leak through Em/Rm), chanmode 4 or 5, either calcmode, backward Euler or
+ * Crank-Nicolson; no Ca pools, concentration gates, GHK, synchans, spike
+ * detectors or output-only opcodes. Each target row may appear once.
+ */
+typedef struct gbh_loss_spec {
+    int ntargets;
+    const int *solver;      /* [ntargets] */
+    const int *row;         /* [ntargets] Hines row within the solver */
+    const double *trace;    /* [nsteps][ntargets] target Vm after each step, host memory */
+} gbh_loss_spec;
+int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh_loss_spec *spec,
+                      double *loss, double *dchip, double *dravals, double *dvm0);
 void gbh_destroy(gbh_engine *e);
 
 /* Static description of the last error on this thread (never NULL). */

@@ -582,6 +582,21 @@ int orc_process(orc_solver *s)
     return 0;
 }
 
+int orc_run_loss(orc_solver *s, int nsteps, int ntargets, const int *rows, const double *trace, double *loss)
+{
+    int i, j;
+    double sum = 0.0;
+    for (i = 0; i < nsteps; i++) {
+        if (orc_process(s)) return -1;
+        for (j = 0; j < ntargets; j++) {
+            const double d = s->vm[rows[j]] - trace[(long)i * ntargets + j];
+            sum += d * d;
+        }
+    }
+    *loss = sum;
+    return 0;
+}
+
 int orc_run(orc_solver *s, int nsteps)
 {
     int i;

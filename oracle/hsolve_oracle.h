@@ -90,6 +90,10 @@ void orc_solve(orc_solver *s);
 int orc_process(orc_solver *s);
 /* n PROCESS steps of one solver with no network; returns 0 or -1. */
 int orc_run(orc_solver *s, int nsteps);
+/* Runs nsteps steps and returns sum_n sum_j (vm[rows[j]] after step n+1 -
+ * trace[n*ntargets + j])^2 in *loss: the loss of the engine's differentiated
+ * form, for finite-difference checks. */
+int orc_run_loss(orc_solver *s, int nsteps, int ntargets, const int *rows, const double *trace, double *loss);
 
 /* ---- network of solvers with spike -> synchan event delivery ---- */
 typedef struct orc_net orc_net;

@@ -72,6 +72,7 @@ def _lib(which: str):
         if which == "oracle":
             lib.orc_process.argtypes = [C.POINTER(OrcSolver)]
             lib.orc_run.argtypes = [C.POINTER(OrcSolver), C.c_int]
+            lib.orc_run_loss.argtypes = [C.POINTER(OrcSolver), C.c_int, C.c_int, _ip, _dp, _dp]
             lib.orc_net_create.restype = C.c_void_p
             lib.orc_net_create.argtypes = [C.c_int, C.POINTER(C.POINTER(OrcSolver)), _ip, _ip, _ip,
                                            _ip, _dp, _ip]
@@ -153,6 +154,19 @@ class Solver:
         rc = fn(C.byref(self.s), int(nsteps))
         if rc != 0:
             raise RuntimeError("%s step failed at op %d" % (impl, self.s.err_op))
+
+
+    def run_loss(self, nsteps: int, rows, trace) -> float:
+        """Runs nsteps steps; returns sum over steps and targets of
+        (vm[row] after the step - trace[step][target])^2 (orc_run_loss)."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        tr = np.ascontiguousarray(trace, dtype=np.float64).reshape(int(nsteps), len(r))
+        out = C.c_double(0.0)
+        rc = _lib("oracle").orc_run_loss(C.byref(self.s), int(nsteps), len(r), _p(r, _ip), _p(tr, _dp),
+                                         C.byref(out))
+        if rc != 0:
+            raise RuntimeError("oracle step failed at op %d" % self.s.err_op)
+        return out.value
 
 
 class Network:
