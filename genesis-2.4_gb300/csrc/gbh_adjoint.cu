@@ -1,6 +1,6 @@
 // gbh_adjoint.cu -- launchers of the adjoint kernels (compiled with
-// --fmad=false so the forward recomputation reproduces the FP64 step
-// bit for bit).
+// --fmad=false so the per-step recomputation reproduces the FP64 step bit
+// for bit).
 #include "gbh_adjoint.cuh"
 
 namespace gbh {
@@ -13,23 +13,39 @@ cudaError_t smem_attr(const void *fn, size_t smem)
 }
 }  // namespace
 
-cudaError_t launch_adj_forward(const AdjView &v, int tile0, int tile1, int smax, int nsteps, int K, int mode,
-                               int seg, cudaStream_t st)
+cudaError_t launch_adj_copy(const AdjView &v, int ntiles, int maxrows, int c, int dir, bool to_tape,
+                            cudaStream_t st)
 {
-    const size_t smem = (size_t)2 * smax * LANES * sizeof(double);
-    cudaError_t ce = smem_attr((const void *)k_adj_forward, smem);
-    if (ce != cudaSuccess) return ce;
-    k_adj_forward<<<tile1 - tile0, LANES, smem, st>>>(v, tile0, tile1, smax, nsteps, K, mode, seg);
+    if (ntiles <= 0 || maxrows <= 0) return cudaSuccess;
+    const dim3 grid(ntiles, (maxrows + 31) / 32);
+    k_adj_copy<<<grid, LANES, 0, st>>>(v, c, dir, to_tape ? 1 : 0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adj_reverse(const AdjView &v, int tile0, int tile1, int smax, int nk, int step0,
-                               cudaStream_t st)
+cudaError_t launch_adj_linearize(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st)
 {
+    if (ntiles <= 0 || nk <= 0) return cudaSuccess;
+    const size_t smem = (size_t)2 * smax * LANES * sizeof(double);
+    cudaError_t ce = smem_attr((const void *)k_adj_linearize, smem);
+    if (ce != cudaSuccess) return ce;
+    k_adj_linearize<<<dim3(ntiles, nk), LANES, smem, st>>>(v, smax);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_reverse(const AdjView &v, int ntiles, int smax, int nk, int step0, cudaStream_t st)
+{
+    if (ntiles <= 0 || nk <= 0) return cudaSuccess;
     const size_t smem = (size_t)2 * smax * LANES * sizeof(double);
     cudaError_t ce = smem_attr((const void *)k_adj_reverse, smem);
     if (ce != cudaSuccess) return ce;
-    k_adj_reverse<<<tile1 - tile0, LANES, smem, st>>>(v, tile0, tile1, smax, nk, step0);
+    k_adj_reverse<<<ntiles, LANES, smem, st>>>(v, smax, nk, step0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_reduce(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st)
+{
+    if (ntiles <= 0 || nk <= 0) return cudaSuccess;
+    k_adj_reduce<<<dim3(ntiles, smax), LANES, 0, st>>>(v, nk);
     return cudaGetLastError();
 }
 

@@ -5,30 +5,37 @@
 // (do_chip_hh4_update, genesis/src/hines/hines_chip.c:157-600, followed by
 // do_euler_hsolve / do_crank_hsolve, genesis/src/hines/hines_solve.c:140-296).
 //
-// Checkpointed reverse sweep. k_adj_forward runs the forward step on work
-// copies of the state; in checkpoint mode it stores Vm and the gate states
-// every K steps, in tape mode it restarts from one checkpoint and records, for
-// each of the next K steps, the values the reverse step needs: Vm before the
-// step, each row's diagonal D' and rhs R' after forward elimination, the
-// solution x, and the gate states before the step. k_adj_reverse then walks
-// those steps backwards:
-//   1. seed: the adjoint of Vm after the step gains 2*(Vm - target) at target
-//      rows (Crank-Nicolson: Vm_after = 2x - Vm_before);
-//   2. back substitution reversed, rows ascending (a row's adjoint is final
-//      once its children, the lower rows, have pushed into it):
-//      x_s = (R'_s - C_s x_p) / D'_s;
-//   3. forward elimination reversed, rows descending:
-//      t_s = A_s / D'_s, D'_p -= B_s t_s, R'_p -= R'_s t_s;
-//   4. channel program reversed per compartment: rhs = Vm + ichan*tbyc,
-//      diag = sumg*tbyc + diagterm, ichan = Em/Rm + inject + sum Ek*G,
-//      G = gmax * prod x^p, the trapezoid gate update x' = (x(2-B') + A')/B'
-//      (x' = A'/B' for instantaneous gates) and the linear table
-//      interpolation, whose derivative in Vm is the interval slope times
-//      1/dx (zero where the lookup clamps at either end of the table, and
-//      zero without interpolation).
-// Outputs: adjoints of Vm and of the gate states before the first step, and
-// accumulated gradients of every parameter field (Em/Rm, inject, Ek, gmax,
-// tbyc, diagterm) and of the three elimination coefficients of every row.
+// FP64 arithmetic on GB300 is bound by each SM sub-partition's FP64 unit,
+// and a warp occupies it for all 32 lanes whether they are active or not: a
+// batch of a few thousand neurons (one warp per 32) reaches a quarter of the
+// GPU's FP64 rate in any kernel that walks the steps one after another. The
+// sweep therefore keeps the sequential kernels lean and moves the rest into
+// kernels that are parallel over steps as well as neurons:
+//
+//   forward   the engine's own step kernel advances work copies of Vm and the
+//             gate states; k_adj_copy stores them every K steps (checkpoints)
+//             and, when a segment is recomputed, before every step (snapshot);
+//   k_adj_linearize   (parallel over steps) recomputes each step of a segment
+//             from its snapshot with the step's exact arithmetic and stores
+//             the local derivatives the reverse needs: 1/D', A/D', R' and x of
+//             every row, ichan and sumg of every compartment, the gate product
+//             of every channel, and per gate d prod/dx, dx'/dVm (table slope,
+//             zero where the lookup clamps or without interpolation) and
+//             dx'/dx (the trapezoid factor (2-B')/B', zero for instant gates);
+//   k_adj_reverse   (sequential over steps, one lane per neuron) the adjoint
+//             recurrence of Vm and the gate states:
+//               seed      Vm-bar += 2 (Vm after - target) at target rows
+//                         (Crank-Nicolson: Vm after = 2x - Vm before);
+//               back substitution reversed, rows ascending:
+//                         x_s = (R'_s - C_s x_p) / D'_s;
+//               forward elimination reversed, rows descending:
+//                         t_s = A_s / D'_s, D'_p -= B_s t_s, R'_p -= R'_s t_s;
+//               channels  rhs = Vm + ichan*tbyc, diag = sumg*tbyc + diagterm,
+//                         G = gmax prod x^p, x' = (x(2-B') + A')/B';
+//             it stores the adjoints of R, D and of the back substitution;
+//   k_adj_reduce   (parallel over rows) sums the parameter gradients of a
+//             segment from those adjoints and the tape, steps descending so
+//             the totals do not depend on the checkpoint interval.
 // Supported programs: compartments with voltage-table gated channels
 // (M_BEGIN, M_NEWVOLT, M_CHAN, M_CHAN_G, M_GATE of kind GK_1V with a nonzero
 // power, M_ADDCURR, M_END); the host rejects anything else.
@@ -39,54 +46,9 @@
 
 namespace gbh {
 
-struct AdjLane {
-    const int *prog;
-    int S;
-    bool interp, crank;
-    const double *tab, *xvals;
-    TableGeom tg;
-    double *P, *V;
-    const int *par;
-    const double *A, *B, *C;
-};
-
-__device__ __forceinline__ AdjLane adj_lane(const AdjView &v, const Tile &tl, int lane)
+__device__ __forceinline__ double *adj_tape(const AdjView &v, int k, int t, int lane)
 {
-    const TileType ty = v.types[tl.type];
-    AdjLane a;
-    a.prog = v.prog + ty.prog_off;
-    a.S = ty.nslots;
-    a.interp = ty.interp != 0;
-    a.crank = ty.crank != 0;
-    a.tg = v.tgeom[ty.table_set];
-    a.tab = v.tab64 + a.tg.tab_off;
-    a.xvals = v.xyvals + a.tg.xv_off;
-    a.P = v.P + tl.fld * LANES + lane;
-    a.V = v.V + tl.vm * LANES + lane;
-    a.par = v.parent + tl.topo * LANES + lane;
-    a.A = v.A + tl.topo * LANES + lane;
-    a.B = v.B + tl.topo * LANES + lane;
-    a.C = v.Cb + tl.topo * LANES + lane;
-    return a;
-}
-
-__device__ __forceinline__ void adj_cursor_reset(VCursor &vc, int ncols)
-{
-    if (ncols) { vc.lo = vc.hi = 0.0; } else { vc.lo = -1e20; vc.hi = 1e20; }
-    vc.row = vc.base = 0;
-    vc.frac = 0.0;
-}
-
-// Operand count + 1 of the micro-ops the differentiated form accepts.
-__device__ __forceinline__ int adj_op_len(int code)
-{
-    switch (code) {
-    case M_BEGIN: case M_GATE: return 5;
-    case M_END: return 4;
-    case M_CHAN: return 3;
-    case M_NEWVOLT: return 1;
-    default: return 2;   // M_CHAN_G, M_ADDCURR
-    }
+    return v.tape + ((int64_t)k * v.tp_stride + v.tp_off[t]) * LANES + lane;
 }
 
 // locate() of the interpolating lookup, also reporting whether the fraction
@@ -115,358 +77,338 @@ __device__ __forceinline__ bool locate_lin(VCursor &c, double v, const TableGeom
     return lin;
 }
 
-// One forward step of the lane's neuron on the work arrays; arithmetic and
-// operand order as the engine's FP64 step. With tp != nullptr it records the
-// step's tape rows (Vm, D', R', x, gate states before the update).
-__device__ __forceinline__ bool adj_forward_step(const AdjLane &a, double *Dc, double *Rc, double *tp)
+// ---------------------------------------------------------------- copies
+// grid (tiles, row chunks of 32), 32 threads: one lane each.
+__global__ void __launch_bounds__(32)
+k_adj_copy(AdjView v, int c, int dir, int to_tape)
 {
-    const int S = a.S;
-    const int ncols = a.tg.ncols;
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x;
+    const Tile tl = v.tiles[t];
+    const AdjType at = v.atypes[tl.type];
+    const int rows = at.nslots + at.ngates;
+    const int r0 = blockIdx.y * 32;
+    const int r1 = min(rows, r0 + 32);
+    double *blk = to_tape ? adj_tape(v, c, t, lane)
+                          : v.ckpt + ((int64_t)c * v.ck_stride + v.ck_off[t]) * LANES + lane;
+    for (int r = r0; r < r1; ++r) {
+        double *w = r < at.nslots ? v.V + (tl.vm + r) * LANES + lane
+                                  : v.P + (tl.fld + v.snap_field[at.snap_off + r - at.nslots]) * LANES + lane;
+        if (dir == 0) blk[r * LANES] = *w;
+        else *w = blk[r * LANES];
+    }
+}
+
+// ---------------------------------------------------------------- linearisation
+// grid (tiles, steps), 32 threads. Shared memory: 2 * smax * 32 doubles.
+__global__ void __launch_bounds__(32)
+k_adj_linearize(AdjView v, int smax)
+{
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x;
+    const int k = blockIdx.y;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const AdjType at = v.atypes[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const double *tab = v.tab64 + tg.tab_off;
+    const double *xvals = v.xyvals + tg.xv_off;
+    const int ncols = tg.ncols;
+    const bool interp = ty.interp != 0;
+    const int S = at.nslots;
+    const AdjRows R = adj_rows(S, at.ngates, at.nchans);
+    const double *P = v.P + tl.fld * LANES + lane;
+    const int *par = v.parent + tl.topo * LANES + lane;
+    const double *Aw = v.A + tl.topo * LANES + lane;
+    const double *Bw = v.B + tl.topo * LANES + lane;
+    const double *Cw = v.Cb + tl.topo * LANES + lane;
+    double *tp = adj_tape(v, k, t, lane);
+    double *Dc = sm + lane;
+    double *Rc = Dc + (size_t)smax * LANES;
+
     VCursor vc;
-    adj_cursor_reset(vc, ncols);
+    if (ncols) { vc.lo = vc.hi = 0.0; } else { vc.lo = -1e20; vc.hi = 1e20; }
+    vc.row = vc.base = 0;
+    vc.frac = 0.0;
+    double dfdv = 0.0;
     double Ek = 0.0, Gk = 0.0;
-    int gi = 0;
-    const int *pc = a.prog;
+    int gi = 0, ci = -1, cg0 = 0;
+    double gx[ADJ_MAX_GATES];
+    int gp[ADJ_MAX_GATES];
+    const int *pc = v.prog + ty.prog_off;
     for (int s = 0; s < S; ++s) {
-        const double Vm = a.V[s * LANES];
-        if (tp) tp[s * LANES] = Vm;
+        const double Vm = tp[(R.V + s) * LANES];
         double sumg = 0.0, ichan = 0.0;
         for (;;) {
             const int code = pc[0];
             if (code == M_BEGIN) {
-                ichan = a.P[pc[1] * LANES] + a.P[pc[2] * LANES];
+                ichan = P[pc[1] * LANES] + P[pc[2] * LANES];
                 pc += 5;
             } else if (code == M_NEWVOLT) {
-                locate(vc, Vm, a.tg.xmin, a.tg.invdx, a.tg.xdivs, a.xvals, ncols, a.interp);
+                if (interp) {
+                    dfdv = locate_lin(vc, Vm, tg, xvals) ? tg.invdx : 0.0;
+                } else {
+                    locate(vc, Vm, tg.xmin, tg.invdx, tg.xdivs, xvals, ncols, false);
+                    dfdv = 0.0;
+                }
                 pc += 1;
-            } else if (code == M_CHAN) {
-                Ek = a.P[pc[1] * LANES];
-                Gk = a.P[pc[2] * LANES];
-                pc += 3;
-            } else if (code == M_CHAN_G) {
-                Gk = a.P[pc[1] * LANES];
-                pc += 2;
+            } else if (code == M_CHAN || code == M_CHAN_G) {
+                if (code == M_CHAN) {
+                    Ek = P[pc[1] * LANES];
+                    Gk = P[pc[2] * LANES];
+                    pc += 3;
+                } else {
+                    Gk = P[pc[1] * LANES];
+                    pc += 2;
+                }
+                ++ci;
+                cg0 = gi;
             } else if (code == M_GATE) {
                 const int b = vc.base + pc[2];
-                double X, Y;
-                if (a.interp) {
+                double X, Y, sX = 0.0, sY = 0.0;
+                if (interp) {
                     const double fr = vc.frac;
-                    X = a.tab[b];
-                    X = X + fr * (a.tab[b + ncols] - X);
-                    Y = a.tab[b + 1];
-                    Y = Y + fr * (a.tab[b + 1 + ncols] - Y);
+                    X = tab[b];
+                    sX = tab[b + ncols] - X;
+                    X = X + fr * sX;
+                    Y = tab[b + 1];
+                    sY = tab[b + 1 + ncols] - Y;
+                    Y = Y + fr * sY;
                 } else {
-                    X = a.tab[b];
-                    Y = a.tab[b + 1];
+                    X = tab[b];
+                    Y = tab[b + 1];
                 }
                 const int p = pc[3];
-                double *st = &a.P[pc[4] * LANES];
-                if (tp) tp[(4 * S + gi) * LANES] = *st;
-                ++gi;
+                const double st = tp[(R.ST + gi) * LANES];
                 double x;
                 int pw = p;
                 if (p > 0) {
-                    x = (*st * (2.0 - X) + Y) / X;
+                    x = (st * (2.0 - X) + Y) / X;
                 } else {
                     x = Y / X;
                     pw = -p;
                 }
-                *st = x;
                 Gk = gpow<double>(Gk, x, pw);
+                const double rX = 1.0 / X;
+                const double along = p > 0 ? st + x : x;   // -(dx'/dB') * B'
+                tp[(R.DXDV + gi) * LANES] = rX * dfdv * (sY - along * sX);
+                tp[(R.DXDST + gi) * LANES] = p > 0 ? (2.0 - X) * rX : 0.0;
+                const int j = gi - cg0;
+                if (j < ADJ_MAX_GATES) {
+                    gx[j] = x;
+                    gp[j] = pw;
+                } else if (v.status) {
+                    atomicOr(v.status, ST_BAD_OP);
+                }
+                ++gi;
                 pc += 5;
             } else if (code == M_ADDCURR) {
                 sumg += Gk;
                 ichan += Ek * Gk;
+                const int ng = min(gi - cg0, ADJ_MAX_GATES);
+                double prod = 1.0;
+                for (int g = 0; g < ng; ++g) prod = gpow<double>(prod, gx[g], gp[g]);
+                tp[(R.PROD + ci) * LANES] = prod;
+                for (int g = 0; g < ng; ++g) {
+                    double q = (double)gp[g];
+                    for (int e = 1; e < gp[g]; ++e) q *= gx[g];
+                    for (int h = 0; h < ng; ++h)
+                        if (h != g) q = gpow<double>(q, gx[h], gp[h]);
+                    tp[(R.Q + cg0 + g) * LANES] = q;
+                }
                 pc += 2;
             } else if (code == M_END) {
-                const double tbyc = a.P[pc[1] * LANES];
+                const double tbyc = P[pc[1] * LANES];
                 Rc[s * LANES] = Vm + ichan * tbyc;
-                Dc[s * LANES] = sumg * tbyc + a.P[pc[2] * LANES];
+                Dc[s * LANES] = sumg * tbyc + P[pc[2] * LANES];
+                tp[(R.ICH + s) * LANES] = ichan;
+                tp[(R.SG + s) * LANES] = sumg;
                 pc += 4;
                 break;
             } else {
-                return false;
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
             }
         }
     }
     for (int s = 0; s < S; ++s) {
-        const int p = a.par[s * LANES];
-        if (tp) {
-            tp[(S + s) * LANES] = Dc[s * LANES];
-            tp[(2 * S + s) * LANES] = Rc[s * LANES];
-        }
+        const int p = par[s * LANES];
+        const double d = Dc[s * LANES];
+        tp[(R.RD + s) * LANES] = 1.0 / d;
+        tp[(R.RP + s) * LANES] = Rc[s * LANES];
+        double temp = 0.0;
         if (p >= 0) {
-            const double temp = a.A[s * LANES] / Dc[s * LANES];
-            Dc[p * LANES] -= a.B[s * LANES] * temp;
+            temp = Aw[s * LANES] / d;
+            Dc[p * LANES] -= Bw[s * LANES] * temp;
             Rc[p * LANES] -= Rc[s * LANES] * temp;
         }
+        tp[(R.T + s) * LANES] = temp;
     }
     for (int s = S - 1; s >= 0; --s) {
-        const int p = a.par[s * LANES];
+        const int p = par[s * LANES];
         double r = Rc[s * LANES];
-        if (p >= 0) r -= a.C[s * LANES] * Rc[p * LANES];
+        if (p >= 0) r -= Cw[s * LANES] * Rc[p * LANES];
         r = r / Dc[s * LANES];
         Rc[s * LANES] = r;
-        if (tp) tp[(3 * S + s) * LANES] = r;
-        if (a.crank) {
-            const double old = a.V[s * LANES];
-            a.V[s * LANES] = r + r - old;
-        } else {
-            a.V[s * LANES] = r;
-        }
-    }
-    return true;
-}
-
-// Copies Vm and the gate states between the work arrays and a checkpoint block.
-__device__ __forceinline__ void adj_checkpoint(const AdjLane &a, double *ck, bool save)
-{
-    const int S = a.S;
-    for (int s = 0; s < S; ++s) {
-        if (save) ck[s * LANES] = a.V[s * LANES];
-        else a.V[s * LANES] = ck[s * LANES];
-    }
-    int gi = 0;
-    const int *pc = a.prog;
-    for (int s = 0; s < S; ++s) {
-        for (;;) {
-            const int code = pc[0];
-            if (code == M_GATE) {
-                double *st = &a.P[pc[4] * LANES];
-                if (save) ck[(S + gi) * LANES] = *st;
-                else *st = ck[(S + gi) * LANES];
-                ++gi;
-            }
-            pc += adj_op_len(code);
-            if (code == M_END) break;
-        }
+        tp[(R.X + s) * LANES] = r;
     }
 }
 
-// mode 0: run nsteps steps from the work state, saving checkpoint c before
-//         every step with step % K == 0 and after the last one when nsteps
-//         is a multiple of K (c = step / K);
-// mode 1: restore checkpoint seg, then run nsteps (<= K) steps recording the tape.
+// ---------------------------------------------------------------- reverse
+// grid (tiles), 32 threads. Shared memory: 2 * smax * 32 doubles.
 __global__ void __launch_bounds__(32)
-k_adj_forward(AdjView v, int tile0, int tile1, int smax, int nsteps, int K, int mode, int seg)
+k_adj_reverse(AdjView v, int smax, int nk, int step0)
 {
     extern __shared__ double sm[];
-    const int lane = threadIdx.x & 31;
-    const int t = tile0 + blockIdx.x;
-    if (t >= tile1) return;
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x;
     const Tile tl = v.tiles[t];
-    const AdjLane a = adj_lane(v, tl, lane);
-    double *Dc = sm + lane;
-    double *Rc = Dc + (size_t)smax * LANES;
-    if (mode == 1) adj_checkpoint(a, v.ckpt + ((int64_t)seg * v.ck_stride + v.ck_off[t]) * LANES + lane, false);
-    for (int k = 0; k < nsteps; ++k) {
-        double *tp = nullptr;
-        if (mode == 0) {
-            if (k % K == 0)
-                adj_checkpoint(a, v.ckpt + ((int64_t)(k / K) * v.ck_stride + v.ck_off[t]) * LANES + lane, true);
-        } else {
-            tp = v.tape + ((int64_t)k * v.tp_stride + v.tp_off[t]) * LANES + lane;
-        }
-        if (!adj_forward_step(a, Dc, Rc, tp)) {
-            if (v.status) atomicOr(v.status, ST_BAD_OP);
-            return;
-        }
-    }
-    if (mode == 0 && nsteps % K == 0)
-        adj_checkpoint(a, v.ckpt + ((int64_t)(nsteps / K) * v.ck_stride + v.ck_off[t]) * LANES + lane, true);
-}
-
-// Reverse of tape steps nk-1 .. 0 of one segment; step0 = global index of its
-// first step (row of the trace).
-__global__ void __launch_bounds__(32)
-k_adj_reverse(AdjView v, int tile0, int tile1, int smax, int nk, int step0)
-{
-    extern __shared__ double sm[];
-    const int lane = threadIdx.x & 31;
-    const int t = tile0 + blockIdx.x;
-    if (t >= tile1) return;
-    const Tile tl = v.tiles[t];
-    const AdjLane a = adj_lane(v, tl, lane);
-    const int S = a.S;
-    const int ncols = a.tg.ncols;
-    double *Vb = v.Vbar + tl.vm * LANES + lane;
-    double *Xb = v.Xbar + tl.fld * LANES + lane;
-    double *Gf = v.Gf + tl.fld * LANES + lane;
-    double *GA = v.GA + tl.topo * LANES + lane;
-    double *GB = v.GB + tl.topo * LANES + lane;
-    double *GC = v.GC + tl.topo * LANES + lane;
+    const TileType ty = v.types[tl.type];
+    const AdjType at = v.atypes[tl.type];
+    const int S = at.nslots;
+    const bool crank = ty.crank != 0;
+    const AdjRows R = adj_rows(S, at.ngates, at.nchans);
+    const double *P = v.P + tl.fld * LANES + lane;
+    const int *par = v.parent + tl.topo * LANES + lane;
+    const double *Bw = v.B + tl.topo * LANES + lane;
+    const double *Cw = v.Cb + tl.topo * LANES + lane;
     const int *tgt = v.tgt + tl.topo * LANES + lane;
-    double *Db = sm + lane;                    // adjoint of D' (final), then of the initial diag
-    double *Rb = Db + (size_t)smax * LANES;    // adjoint of x, then of R
+    const AdjSlot *slots = v.slot_plan + at.slot_off;
+    const AdjChan *chans = v.chan_plan + at.chan_off;
+    double *Vb = v.Vbar + tl.vm * LANES + lane;
+    double *Xb = v.Xbar + v.xb_off[t] * LANES + lane;
     double *loss = v.loss + (size_t)t * LANES + lane;
+    double *Db = sm + lane;
+    double *Rb = Db + (size_t)smax * LANES;
 
     for (int k = nk - 1; k >= 0; --k) {
-        const double *tp = v.tape + ((int64_t)k * v.tp_stride + v.tp_off[t]) * LANES + lane;
-        const double *tV = tp, *tD = tp + (size_t)S * LANES, *tR = tp + (size_t)2 * S * LANES,
-                     *tX = tp + (size_t)3 * S * LANES, *tG = tp + (size_t)4 * S * LANES;
+        double *tp = adj_tape(v, k, t, lane);
         const double *trow = v.trace + (size_t)(step0 + k) * v.ntargets;
-        // ---- 1. seed (the loss is summed step by step, descending, so the
-        //      total does not depend on the checkpoint interval) ----
+        // seed (the loss is summed step by step, descending, so the total does
+        // not depend on the checkpoint interval)
         double lstep = 0.0;
         for (int s = 0; s < S; ++s) {
             double vb = Vb[s * LANES];
             const int j = tgt[s * LANES];
             if (j >= 0) {
-                const double x = tX[s * LANES];
-                const double vnext = a.crank ? x + x - tV[s * LANES] : x;
+                const double x = tp[(R.X + s) * LANES];
+                const double vnext = crank ? x + x - tp[(R.V + s) * LANES] : x;
                 const double diff = vnext - trow[j];
                 lstep += diff * diff;
                 vb += 2.0 * diff;
             }
-            Rb[s * LANES] = a.crank ? 2.0 * vb : vb;
-            Vb[s * LANES] = a.crank ? -vb : 0.0;
+            Rb[s * LANES] = crank ? 2.0 * vb : vb;
+            Vb[s * LANES] = crank ? -vb : 0.0;
         }
         *loss += lstep;
-        // ---- 2. back substitution reversed ----
+        // back substitution reversed
         for (int s = 0; s < S; ++s) {
-            const int p = a.par[s * LANES];
-            const double rb = Rb[s * LANES] / tD[s * LANES];
+            const int p = par[s * LANES];
+            const double rb = Rb[s * LANES] * tp[(R.RD + s) * LANES];
             Rb[s * LANES] = rb;
-            if (p >= 0) {
-                Rb[p * LANES] -= a.C[s * LANES] * rb;
-                GC[s * LANES] -= tX[p * LANES] * rb;
-            }
-            Db[s * LANES] = -tX[s * LANES] * rb;
+            tp[(R.RBBS + s) * LANES] = rb;
+            if (p >= 0) Rb[p * LANES] -= Cw[s * LANES] * rb;
+            Db[s * LANES] = -tp[(R.X + s) * LANES] * rb;
         }
-        // ---- 3. forward elimination reversed ----
+        // forward elimination reversed
         for (int s = S - 1; s >= 0; --s) {
-            const int p = a.par[s * LANES];
+            const int p = par[s * LANES];
             if (p < 0) continue;
-            const double d = tD[s * LANES];
-            const double tt = a.A[s * LANES] / d;
+            const double tt = tp[(R.T + s) * LANES];
             const double dbp = Db[p * LANES], rbp = Rb[p * LANES];
-            const double tb = -a.B[s * LANES] * dbp - tR[s * LANES] * rbp;
-            GB[s * LANES] -= tt * dbp;
+            const double tb = -Bw[s * LANES] * dbp - tp[(R.RP + s) * LANES] * rbp;
             Rb[s * LANES] -= tt * rbp;
-            const double tbd = tb / d;
-            GA[s * LANES] += tbd;
-            Db[s * LANES] -= tt * tbd;
+            Db[s * LANES] -= tt * (tb * tp[(R.RD + s) * LANES]);
         }
-        // ---- 4. channel program reversed ----
-        VCursor vc;
-        adj_cursor_reset(vc, ncols);
-        double Ek = 0.0, gmax = 0.0, dfdv = 0.0;
-        int fEk = -1, fG = -1, ng = 0, gi = 0;
-        int gf[ADJ_MAX_GATES], gp[ADJ_MAX_GATES];
-        double gX[ADJ_MAX_GATES], gsX[ADJ_MAX_GATES], gsY[ADJ_MAX_GATES], gst[ADJ_MAX_GATES],
-            gx[ADJ_MAX_GATES];
-        const int *pc = a.prog;
+        // channels reversed: the adjoint of Vm and of the gate states
         for (int s = 0; s < S; ++s) {
-            const double Vm = tV[s * LANES];
+            const AdjSlot sp = slots[s];
             const double rb = Rb[s * LANES], db = Db[s * LANES];
-            const int *q = pc;
-            while (q[0] != M_END) q += adj_op_len(q[0]);
-            const double tbyc = a.P[q[1] * LANES];
+            tp[(R.RBF + s) * LANES] = rb;
+            tp[(R.DBF + s) * LANES] = db;
+            const double tbyc = P[sp.f_tbyc * LANES];
             const double Ibar = rb * tbyc, Sbar = db * tbyc;
             double vbn = Vb[s * LANES] + rb;
-            double sumg = 0.0, ichan = 0.0;
-            for (;;) {
-                const int code = pc[0];
-                if (code == M_BEGIN) {
-                    Gf[pc[1] * LANES] += Ibar;
-                    Gf[pc[2] * LANES] += Ibar;
-                    ichan = a.P[pc[1] * LANES] + a.P[pc[2] * LANES];
-                    pc += 5;
-                } else if (code == M_NEWVOLT) {
-                    if (a.interp) {
-                        dfdv = locate_lin(vc, Vm, a.tg, a.xvals) ? a.tg.invdx : 0.0;
-                    } else {
-                        locate(vc, Vm, a.tg.xmin, a.tg.invdx, a.tg.xdivs, a.xvals, ncols, false);
-                        dfdv = 0.0;
-                    }
-                    pc += 1;
-                } else if (code == M_CHAN || code == M_CHAN_G) {
-                    if (code == M_CHAN) {
-                        fEk = pc[1];
-                        Ek = a.P[pc[1] * LANES];
-                        fG = pc[2];
-                        pc += 3;
-                    } else {
-                        fG = pc[1];
-                        pc += 2;
-                    }
-                    gmax = a.P[fG * LANES];
-                    ng = 0;
-                } else if (code == M_GATE) {
-                    const int b = vc.base + pc[2];
-                    double X, Y, sX = 0.0, sY = 0.0;
-                    if (a.interp) {
-                        const double fr = vc.frac;
-                        X = a.tab[b];
-                        sX = a.tab[b + ncols] - X;
-                        X = X + fr * sX;
-                        Y = a.tab[b + 1];
-                        sY = a.tab[b + 1 + ncols] - Y;
-                        Y = Y + fr * sY;
-                    } else {
-                        X = a.tab[b];
-                        Y = a.tab[b + 1];
-                    }
-                    const int p = pc[3];
-                    const double st = tG[gi * LANES];
-                    ++gi;
-                    if (ng < ADJ_MAX_GATES) {
-                        gf[ng] = pc[4];
-                        gp[ng] = p;
-                        gX[ng] = X;
-                        gsX[ng] = sX * dfdv;
-                        gsY[ng] = sY * dfdv;
-                        gst[ng] = st;
-                        gx[ng] = p > 0 ? (st * (2.0 - X) + Y) / X : Y / X;
-                        ++ng;
-                    } else if (v.status) {
-                        atomicOr(v.status, ST_BAD_OP);
-                    }
-                    pc += 5;
-                } else if (code == M_ADDCURR) {
-                    double prod = 1.0;
-                    for (int g = 0; g < ng; ++g) prod = gpow<double>(prod, gx[g], gp[g] > 0 ? gp[g] : -gp[g]);
-                    const double G = gmax * prod;
-                    sumg += G;
-                    ichan += Ek * G;
-                    const double Gbar = Sbar + Ibar * Ek;
-                    if (fEk >= 0) Gf[fEk * LANES] += Ibar * G;
-                    Gf[fG * LANES] += Gbar * prod;
-                    for (int g = 0; g < ng; ++g) {
-                        const int pw = gp[g] > 0 ? gp[g] : -gp[g];
-                        double others = 1.0;
-                        for (int h = 0; h < ng; ++h)
-                            if (h != g) others = gpow<double>(others, gx[h], gp[h] > 0 ? gp[h] : -gp[h]);
-                        double xpm1 = 1.0;
-                        for (int e = 1; e < pw; ++e) xpm1 *= gx[g];
-                        const double xhat = Xb[gf[g] * LANES] + Gbar * gmax * (double)pw * xpm1 * others;
-                        const double rX = 1.0 / gX[g];
-                        const double Abar = xhat * rX;
-                        double Bbar, xbn;
-                        if (gp[g] > 0) {
-                            Bbar = -xhat * (gx[g] + gst[g]) * rX;
-                            xbn = xhat * (2.0 - gX[g]) * rX;
-                        } else {
-                            Bbar = -xhat * gx[g] * rX;
-                            xbn = 0.0;
-                        }
-                        vbn += Abar * gsY[g] + Bbar * gsX[g];
-                        Xb[gf[g] * LANES] = xbn;
-                    }
-                    ng = 0;
-                    pc += 2;
-                } else if (code == M_END) {
-                    Gf[pc[1] * LANES] += rb * ichan + db * sumg;
-                    Gf[pc[2] * LANES] += db;
-                    pc += 4;
-                    break;
-                } else {
-                    if (v.status) atomicOr(v.status, ST_BAD_OP);
-                    return;
+            for (int c = sp.ch0; c < sp.ch0 + sp.nch; ++c) {
+                const AdjChan ch = chans[c];
+                const double Ek = ch.f_ek >= 0 ? P[ch.f_ek * LANES] : 0.0;
+                const double w = (Sbar + Ibar * Ek) * P[ch.f_gmax * LANES];
+                for (int g = ch.g0; g < ch.g0 + ch.ng; ++g) {
+                    const double xhat = Xb[g * LANES] + w * tp[(R.Q + g) * LANES];
+                    vbn += xhat * tp[(R.DXDV + g) * LANES];
+                    Xb[g * LANES] = xhat * tp[(R.DXDST + g) * LANES];
                 }
             }
             Vb[s * LANES] = vbn;
         }
+    }
+}
+
+// ---------------------------------------------------------------- gradient sums
+// grid (tiles, smax), 32 threads: one (tile, slot) per block, one lane per
+// thread. Sums the segment's steps in descending order onto the totals.
+__global__ void __launch_bounds__(32)
+k_adj_reduce(AdjView v, int nk)
+{
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x;
+    const int s = blockIdx.y;
+    const Tile tl = v.tiles[t];
+    const AdjType at = v.atypes[tl.type];
+    if (s >= at.nslots) return;
+    const AdjRows R = adj_rows(at.nslots, at.ngates, at.nchans);
+    const AdjSlot sp = v.slot_plan[at.slot_off + s];
+    const double *P = v.P + tl.fld * LANES + lane;
+    double *Gf = v.Gf + tl.fld * LANES + lane;
+    const int64_t topo = (tl.topo + s) * LANES + lane;
+    const int p = v.parent[topo];
+    const double tbyc = P[sp.f_tbyc * LANES];
+    double g_i = Gf[sp.f_emrm * LANES];     // Em/Rm and inject share the adjoint of ichan
+    double g_j = Gf[sp.f_inj * LANES];
+    double g_t = Gf[sp.f_tbyc * LANES];
+    double g_d = Gf[sp.f_diag * LANES];
+    double ga = v.GA[topo], gb = v.GB[topo], gc = v.GC[topo];
+    const double B = v.B[topo];
+    for (int k = nk - 1; k >= 0; --k) {
+        const double *tp = adj_tape(v, k, t, lane);
+        const double rb = tp[(R.RBF + s) * LANES], db = tp[(R.DBF + s) * LANES];
+        const double ib = rb * tbyc;
+        g_i += ib;
+        g_j += ib;
+        g_t += rb * tp[(R.ICH + s) * LANES] + db * tp[(R.SG + s) * LANES];
+        g_d += db;
+        if (p >= 0) {
+            gc -= tp[(R.X + p) * LANES] * tp[(R.RBBS + s) * LANES];
+            const double dbp = tp[(R.DBF + p) * LANES], rbp = tp[(R.RBF + p) * LANES];
+            gb -= tp[(R.T + s) * LANES] * dbp;
+            ga += (-B * dbp - tp[(R.RP + s) * LANES] * rbp) * tp[(R.RD + s) * LANES];
+        }
+    }
+    Gf[sp.f_emrm * LANES] = g_i;
+    Gf[sp.f_inj * LANES] = g_j;
+    Gf[sp.f_tbyc * LANES] = g_t;
+    Gf[sp.f_diag * LANES] = g_d;
+    v.GA[topo] = ga;
+    v.GB[topo] = gb;
+    v.GC[topo] = gc;
+    // channels of the slot: Ek and gmax gradients, kept per channel
+    for (int c = sp.ch0; c < sp.ch0 + sp.nch; ++c) {
+        const AdjChan ch = v.chan_plan[at.chan_off + c];
+        const double Ek = ch.f_ek >= 0 ? P[ch.f_ek * LANES] : 0.0;
+        const double gmax = P[ch.f_gmax * LANES];
+        double *gek = v.Gek + (v.ch_off[t] + c) * LANES + lane;
+        double *ggm = v.Ggm + (v.ch_off[t] + c) * LANES + lane;
+        double a = *gek, b = *ggm;
+        for (int k = nk - 1; k >= 0; --k) {
+            const double *tp = adj_tape(v, k, t, lane);
+            const double ib = tp[(R.RBF + s) * LANES] * tbyc, sb = tp[(R.DBF + s) * LANES] * tbyc;
+            const double prod = tp[(R.PROD + c) * LANES];
+            a += ib * gmax * prod;
+            b += (sb + ib * Ek) * prod;
+        }
+        *gek = a;
+        *ggm = b;
     }
 }
 

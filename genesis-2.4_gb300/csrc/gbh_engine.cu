@@ -1185,38 +1185,79 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     if (e->has_network)
         return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: synaptic networks are not differentiated");
     const size_t L = LANES;
-    // ---- supported programs; gate count per tile type ----
-    std::vector<int> ngates(e->types.size(), 0);
-    std::vector<int> prog;
-    {
-        prog.resize(e->d_prog.n);
-        if (!prog.empty()) CK(cudaMemcpy(prog.data(), e->d_prog.p, prog.size() * sizeof(int), cudaMemcpyDeviceToHost));
-    }
+    // ---- per type: supported program, plan tables ----
+    std::vector<int> prog(e->d_prog.n);
+    if (!prog.empty()) CK(cudaMemcpy(prog.data(), e->d_prog.p, prog.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<AdjType> atypes(e->types.size());
+    std::vector<int> snap_field;
+    std::vector<AdjSlot> slot_plan;
+    std::vector<AdjChan> chan_plan;
     for (size_t ti = 0; ti < e->types.size(); ++ti) {
         const TileType &tt = e->types[ti];
         if (tt.npools || tt.nsyn || tt.has_spike)
             return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
                             "gbh_loss_gradient: Ca pools, synchans and spike detectors are not differentiated");
-        int pc = tt.prog_off, s = 0, in_chan = 0;
-        while (s < tt.nslots) {
+        AdjType &at = atypes[ti];
+        at.nslots = tt.nslots;
+        at.snap_off = (int)snap_field.size();
+        at.slot_off = (int)slot_plan.size();
+        at.chan_off = (int)chan_plan.size();
+        int pc = tt.prog_off, ek_field = -1, ngates = 0, nchans = 0;
+        AdjSlot sp{};
+        bool in_chan = false;
+        for (int s = 0; s < tt.nslots;) {
             const int code = prog[pc];
             switch (code) {
-            case M_BEGIN: pc += 5; break;
-            case M_NEWVOLT: pc += 1; break;
-            case M_CHAN: pc += 3; in_chan = 0; break;
-            case M_CHAN_G: pc += 2; in_chan = 0; break;
-            case M_ADDCURR: pc += 2; break;
-            case M_END: pc += 4; ++s; break;
+            case M_BEGIN:
+                sp = AdjSlot{};
+                sp.f_emrm = prog[pc + 1];
+                sp.f_inj = prog[pc + 2];
+                sp.ch0 = nchans;
+                pc += 5;
+                break;
+            case M_NEWVOLT:
+                pc += 1;
+                break;
+            case M_CHAN:
+            case M_CHAN_G: {
+                if (in_chan)
+                    return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: channel without ADD_CURR");
+                AdjChan ch{};
+                if (code == M_CHAN) ek_field = prog[pc + 1];
+                ch.f_ek = ek_field;
+                ch.f_gmax = prog[pc + (code == M_CHAN ? 2 : 1)];
+                ch.g0 = ngates;
+                chan_plan.push_back(ch);
+                ++nchans;
+                ++sp.nch;
+                in_chan = true;
+                pc += code == M_CHAN ? 3 : 2;
+                break;
+            }
             case M_GATE:
-                if (prog[pc + 1] != GK_1V || prog[pc + 3] == 0)
+                if (!in_chan || prog[pc + 1] != GK_1V || prog[pc + 3] == 0)
                     return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
                                     "gbh_loss_gradient: only voltage-table gates with a nonzero power are "
                                     "differentiated (kind %d, power %d)", prog[pc + 1], prog[pc + 3]);
-                if (++in_chan > ADJ_MAX_GATES)
+                if (++chan_plan.back().ng > ADJ_MAX_GATES)
                     return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: more than %d gates in a channel",
                                     ADJ_MAX_GATES);
-                ngates[ti]++;
+                snap_field.push_back(prog[pc + 4]);
+                ++ngates;
                 pc += 5;
+                break;
+            case M_ADDCURR:
+                in_chan = false;
+                pc += 2;
+                break;
+            case M_END:
+                if (in_chan)
+                    return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: channel without ADD_CURR");
+                sp.f_tbyc = prog[pc + 1];
+                sp.f_diag = prog[pc + 2];
+                slot_plan.push_back(sp);
+                pc += 4;
+                ++s;
                 break;
             default:
                 return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
@@ -1224,6 +1265,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
                                 "not differentiated", code);
             }
         }
+        at.ngates = ngates;
+        at.nchans = nchans;
+        at.rows = adj_rows(tt.nslots, ngates, nchans).total;
     }
     if (nsteps == 0) {
         if (loss) *loss = 0.0;
@@ -1232,7 +1276,7 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         if (dvm0) memset(dvm0, 0, e->vm_start.back() * sizeof(double));
         return GBH_OK;
     }
-    const int K = std::max(1, std::min(checkpoint_every > 0 ? checkpoint_every : 100, nsteps));
+    const int K = std::max(1, std::min({checkpoint_every > 0 ? checkpoint_every : 100, nsteps, 65535}));
     const int nseg = (nsteps + K - 1) / K;
     // ---- target rows ----
     std::vector<int> tgt(e->rows_topo * L, -1);
@@ -1254,40 +1298,54 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
             cell = j;
         }
     }
-    // ---- checkpoint and tape layout ----
-    std::vector<int64_t> ck_off(e->tiles.size()), tp_off(e->tiles.size());
-    int64_t ck_stride = 0, tp_stride = 0;
-    int smax = 1;
-    for (size_t t = 0; t < e->tiles.size(); ++t) {
-        const TileType &tt = e->types[e->tiles[t].type];
+    // ---- checkpoint, tape and per-tile layouts ----
+    const int ntiles = (int)e->tiles.size();
+    std::vector<int64_t> ck_off(ntiles), tp_off(ntiles), xb_off(ntiles), ch_off(ntiles);
+    int64_t ck_stride = 0, tp_stride = 0, xb_rows = 0, ch_rows = 0;
+    int smax = 1, maxcopy = 1;
+    for (int t = 0; t < ntiles; ++t) {
+        const AdjType &at = atypes[e->tiles[t].type];
         ck_off[t] = ck_stride;
         tp_off[t] = tp_stride;
-        ck_stride += tt.nslots + ngates[e->tiles[t].type];
-        tp_stride += 4 * tt.nslots + ngates[e->tiles[t].type];
-        smax = std::max(smax, tt.nslots);
+        xb_off[t] = xb_rows;
+        ch_off[t] = ch_rows;
+        ck_stride += at.nslots + at.ngates;
+        tp_stride += at.rows;
+        xb_rows += at.ngates;
+        ch_rows += at.nchans;
+        smax = std::max(smax, at.nslots);
+        maxcopy = std::max(maxcopy, at.nslots + at.ngates);
     }
     if ((size_t)2 * smax * L * sizeof(double) > 227 * 1024)
         return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: %d compartments per neuron exceed shared memory",
                         smax);
     // ---- device buffers (released on every return path) ----
     struct Bufs {
-        DBuf<double> P, V, ck, tape, Vb, Xb, Gf, GA, GB, GC, trace, loss;
-        DBuf<int> tgt;
-        DBuf<int64_t> ck_off, tp_off;
+        DBuf<double> P, V, ck, tape, Vb, Xb, Gf, Gek, Ggm, GA, GB, GC, trace, loss;
+        DBuf<int> tgt, snap;
+        DBuf<int64_t> ck_off, tp_off, xb_off, ch_off;
+        DBuf<AdjType> atypes;
+        DBuf<AdjSlot> slots;
+        DBuf<AdjChan> chans;
         ~Bufs()
         {
             P.release(); V.release(); ck.release(); tape.release(); Vb.release(); Xb.release(); Gf.release();
-            GA.release(); GB.release(); GC.release(); trace.release(); loss.release(); tgt.release();
-            ck_off.release(); tp_off.release();
+            Gek.release(); Ggm.release(); GA.release(); GB.release(); GC.release(); trace.release();
+            loss.release(); tgt.release(); snap.release(); ck_off.release(); tp_off.release(); xb_off.release();
+            ch_off.release(); atypes.release(); slots.release(); chans.release();
         }
     } b;
     const int64_t nfld = e->rows_fld * L, nvm = e->rows_vm * L, ntopo = e->rows_topo * L;
     if (b.P.alloc(nfld) || b.V.alloc(nvm) || b.ck.alloc((size_t)nseg * ck_stride * L) ||
-        b.tape.alloc((size_t)K * tp_stride * L) || b.Vb.alloc(nvm) || b.Xb.alloc(nfld) || b.Gf.alloc(nfld) ||
-        b.GA.alloc(ntopo) || b.GB.alloc(ntopo) || b.GC.alloc(ntopo) || b.loss.alloc(e->tiles.size() * L) ||
+        b.tape.alloc((size_t)K * tp_stride * L) || b.Vb.alloc(nvm) || b.Xb.alloc(xb_rows * L) ||
+        b.Gf.alloc(nfld) || b.Gek.alloc(ch_rows * L) || b.Ggm.alloc(ch_rows * L) || b.GA.alloc(ntopo) ||
+        b.GB.alloc(ntopo) || b.GC.alloc(ntopo) || b.loss.alloc((size_t)ntiles * L) ||
         b.trace.alloc(std::max<size_t>(1, (size_t)nsteps * spec->ntargets)))
         return GBH_ERR_CUDA;
-    if (b.tgt.upload(tgt) || b.ck_off.upload(ck_off) || b.tp_off.upload(tp_off)) return GBH_ERR_CUDA;
+    if (b.tgt.upload(tgt) || b.snap.upload(snap_field) || b.ck_off.upload(ck_off) || b.tp_off.upload(tp_off) ||
+        b.xb_off.upload(xb_off) || b.ch_off.upload(ch_off) || b.atypes.upload(atypes) ||
+        b.slots.upload(slot_plan) || b.chans.upload(chan_plan))
+        return GBH_ERR_CUDA;
     cudaStream_t st = e->stream;
     CK(cudaStreamSynchronize(st));
     if (spec->ntargets)
@@ -1296,12 +1354,14 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     CK(cudaMemcpyAsync(b.P.p, e->d_P.p, nfld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(b.V.p, e->d_V.p, nvm * sizeof(double), cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(b.Vb.p, 0, nvm * sizeof(double), st));
-    CK(cudaMemsetAsync(b.Xb.p, 0, nfld * sizeof(double), st));
+    CK(cudaMemsetAsync(b.Xb.p, 0, std::max<int64_t>(1, xb_rows * L) * sizeof(double), st));
     CK(cudaMemsetAsync(b.Gf.p, 0, nfld * sizeof(double), st));
+    CK(cudaMemsetAsync(b.Gek.p, 0, std::max<int64_t>(1, ch_rows * L) * sizeof(double), st));
+    CK(cudaMemsetAsync(b.Ggm.p, 0, std::max<int64_t>(1, ch_rows * L) * sizeof(double), st));
     CK(cudaMemsetAsync(b.GA.p, 0, ntopo * sizeof(double), st));
     CK(cudaMemsetAsync(b.GB.p, 0, ntopo * sizeof(double), st));
     CK(cudaMemsetAsync(b.GC.p, 0, ntopo * sizeof(double), st));
-    CK(cudaMemsetAsync(b.loss.p, 0, e->tiles.size() * L * sizeof(double), st));
+    CK(cudaMemsetAsync(b.loss.p, 0, (size_t)ntiles * L * sizeof(double), st));
     AdjView v{};
     v.tiles = e->d_tiles.p;
     v.types = e->d_types.p;
@@ -1313,6 +1373,10 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     v.A = e->d_A.p;
     v.B = e->d_B.p;
     v.Cb = e->d_Cb.p;
+    v.atypes = b.atypes.p;
+    v.snap_field = b.snap.p;
+    v.slot_plan = b.slots.p;
+    v.chan_plan = b.chans.p;
     v.P = b.P.p;
     v.V = b.V.p;
     v.ckpt = b.ck.p;
@@ -1323,7 +1387,11 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     v.tp_stride = tp_stride;
     v.Vbar = b.Vb.p;
     v.Xbar = b.Xb.p;
+    v.xb_off = b.xb_off.p;
     v.Gf = b.Gf.p;
+    v.Gek = b.Gek.p;
+    v.Ggm = b.Ggm.p;
+    v.ch_off = b.ch_off.p;
     v.GA = b.GA.p;
     v.GB = b.GB.p;
     v.GC = b.GC.p;
@@ -1332,7 +1400,10 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     v.ntargets = spec->ntargets;
     v.loss = b.loss.p;
     v.status = e->d_status.p;
-    const int ntiles = (int)e->tiles.size();
+    // the engine's own FP64 step kernels advance the work copies
+    DevView fv = view_of(e);
+    fv.P = b.P.p;
+    fv.V = b.V.p;
     auto ck_launch = [&](cudaError_t ce) {
         if (ce != cudaSuccess) {
             set_last("adjoint kernel launch failed: %s", cudaGetErrorString(ce));
@@ -1340,19 +1411,40 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         }
         return GBH_OK;
     };
+    auto forward = [&](int n) {
+        for (int done = 0; done < n;) {
+            const int k = std::min(e->steps_per_launch, n - done);
+            for (const Launch &Lc : e->launches) {
+                const int rc = launch_one(e, fv, Lc, k, 0, false, false, st);
+                if (rc) return rc;
+            }
+            done += k;
+        }
+        return GBH_OK;
+    };
     // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed)
     CK(cudaEventRecord(e->ev0, st));
-    if (ck_launch(launch_adj_forward(v, 0, ntiles, smax, (nseg - 1) * K, K, 0, 0, st))) return GBH_ERR_CUDA;
+    for (int seg = 0; seg < nseg; ++seg) {
+        if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, seg, 0, false, st))) return GBH_ERR_CUDA;
+        if (seg + 1 < nseg && forward(K)) return GBH_ERR_CUDA;
+    }
     CK(cudaEventRecord(e->ev1, st));
     CK(cudaEventSynchronize(e->ev1));
     float ms_fwd = 0.f;
     CK(cudaEventElapsedTime(&ms_fwd, e->ev0, e->ev1));
-    // reverse pass, segment by segment
+    // reverse pass, segment by segment: recompute with snapshots, linearise,
+    // sweep back, sum the gradients
     CK(cudaEventRecord(e->ev0, st));
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int nk = std::min(K, nsteps - seg * K);
-        if (ck_launch(launch_adj_forward(v, 0, ntiles, smax, nk, K, 1, seg, st))) return GBH_ERR_CUDA;
-        if (ck_launch(launch_adj_reverse(v, 0, ntiles, smax, nk, seg * K, st))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, seg, 1, false, st))) return GBH_ERR_CUDA;
+        for (int k = 0; k < nk; ++k) {
+            if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, k, 0, true, st))) return GBH_ERR_CUDA;
+            if (k + 1 < nk && forward(1)) return GBH_ERR_CUDA;
+        }
+        if (ck_launch(launch_adj_linearize(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reverse(v, ntiles, smax, nk, seg * K, st))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reduce(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
     }
     CK(cudaEventRecord(e->ev1, st));
     CK(cudaEventSynchronize(e->ev1));
@@ -1360,7 +1452,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     CK(cudaEventElapsedTime(&ms_rev, e->ev0, e->ev1));
     e->stats.grad_forward_ms = ms_fwd;
     e->stats.grad_reverse_ms = ms_rev;
-    e->stats.launches += 1 + 2 * nseg;
+    // forward step launches are counted by launch_one; add the copies
+    // (checkpoint saves and restores, snapshots) and three kernels per segment
+    e->stats.launches += 2 * (int64_t)nseg + nsteps + 3 * (int64_t)nseg;
     int status = 0;
     CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {
@@ -1368,18 +1462,20 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         return GBH_ERR_DEVICE;
     }
     // ---- gather ----
-    std::vector<double> Vb(nvm), Xb(nfld), Gf(nfld), GA(ntopo), GB(ntopo), GC(ntopo), ls(e->tiles.size() * L);
-    CK(cudaMemcpy(Vb.data(), b.Vb.p, nvm * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(Xb.data(), b.Xb.p, nfld * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(Gf.data(), b.Gf.p, nfld * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(GA.data(), b.GA.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(GB.data(), b.GB.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(GC.data(), b.GC.p, ntopo * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ls.data(), b.loss.p, ls.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double> Vb(nvm), Xb(xb_rows * L), Gf(nfld), Gek(ch_rows * L), Ggm(ch_rows * L), GA(ntopo),
+        GB(ntopo), GC(ntopo), ls((size_t)ntiles * L);
+    auto down = [&](std::vector<double> &h, const DBuf<double> &d) {
+        if (h.empty()) return GBH_OK;
+        CK(cudaMemcpy(h.data(), d.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        return GBH_OK;
+    };
+    if (down(Vb, b.Vb) || down(Xb, b.Xb) || down(Gf, b.Gf) || down(Gek, b.Gek) || down(Ggm, b.Ggm) ||
+        down(GA, b.GA) || down(GB, b.GB) || down(GC, b.GC) || down(ls, b.loss))
+        return GBH_ERR_CUDA;
     if (loss) {
         double sum = 0.0;
-        for (size_t t = 0; t < e->tiles.size(); ++t)
-            for (int l = 0; l < e->tiles[t].nlanes; ++l) sum += ls[t * L + l];
+        for (int t = 0; t < ntiles; ++t)
+            for (int l = 0; l < e->tiles[t].nlanes; ++l) sum += ls[(size_t)t * L + l];
         *loss = sum;
     }
     if (dchip) memset(dchip, 0, e->chip_start.back() * sizeof(double));
@@ -1387,15 +1483,25 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     if (dvm0) memset(dvm0, 0, e->vm_start.back() * sizeof(double));
     for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
         const Neuron &N = e->dec.neurons[i];
-        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int ti = e->neuron_tile[i];
+        const Tile &t = e->tiles[ti];
+        const AdjType &at = atypes[t.type];
         const int l = e->neuron_lane[i];
         if (dvm0)
             for (int s = 0; s < N.nrows; ++s) dvm0[e->vm_start[N.solver] + N.row0 + s] = Vb[(t.vm + s) * L + l];
-        if (dchip)
+        if (dchip) {
+            // field gradients: per-slot fields, per-channel Ek and gmax, initial gate states
+            std::vector<double> gfield(N.fsrc.size(), 0.0);
+            for (size_t f = 0; f < N.fsrc.size(); ++f) gfield[f] = Gf[(t.fld + f) * L + l];
+            for (int c = 0; c < at.nchans; ++c) {
+                const AdjChan &ch = chan_plan[at.chan_off + c];
+                if (ch.f_ek >= 0) gfield[ch.f_ek] += Gek[(ch_off[ti] + c) * L + l];
+                gfield[ch.f_gmax] += Ggm[(ch_off[ti] + c) * L + l];
+            }
+            for (int g = 0; g < at.ngates; ++g) gfield[snap_field[at.snap_off + g]] += Xb[(xb_off[ti] + g) * L + l];
             for (size_t f = 0; f < N.fsrc.size(); ++f)
-                if (N.fsrc[f].kind == FS_CHIP)
-                    dchip[e->chip_start[N.solver] + N.fsrc[f].idx] +=
-                        Gf[(t.fld + f) * L + l] + Xb[(t.fld + f) * L + l];
+                if (N.fsrc[f].kind == FS_CHIP) dchip[e->chip_start[N.solver] + N.fsrc[f].idx] += gfield[f];
+        }
         if (dravals)
             for (int s = 0; s < N.nrows; ++s) {
                 const double g[3] = {GA[(t.topo + s) * L + l], GB[(t.topo + s) * L + l], GC[(t.topo + s) * L + l]};
