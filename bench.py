@@ -239,8 +239,9 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
             "steps": nsteps, "checkpoint_every": GRAD_K, "dtype": "f64",
             "forward_ms": fwd_ms, "gradient_ms": grad_ms, "checkpoint_pass_ms": st.grad_forward_ms,
             "reverse_pass_ms": st.grad_reverse_ms, "gradient_wall_s": wall,
-            "ratio_gradient_over_forward": grad_ms / fwd_ms, "loss": loss, "gradients_finite": finite,
-            "launches": 1 + 2 * ((nsteps + GRAD_K - 1) // GRAD_K)}
+            "ratio_gradient_over_forward": grad_ms / fwd_ms,
+            "ratio_backward_over_forward": st.grad_reverse_ms / fwd_ms, "loss": loss, "gradients_finite": finite,
+            "launches": int(st.launches)}
 
 
 def run_reference(args, ws, rank, dist):

@@ -32,13 +32,19 @@ cudaError_t launch_adj_linearize(const AdjView &v, int ntiles, int smax, int nk,
     return cudaGetLastError();
 }
 
-cudaError_t launch_adj_reverse(const AdjView &v, int ntiles, int smax, int nk, int step0, cudaStream_t st)
+size_t adj_reverse_smem(int smax, int hmax)
+{
+    return ((size_t)2 * smax * LANES + (size_t)ADJ_REV_WARPS * LANES) * sizeof(double) + (size_t)smax * sizeof(AdjSlot) +
+           (size_t)hmax * sizeof(AdjChan);
+}
+
+cudaError_t launch_adj_reverse(const AdjView &v, int ntiles, int smax, int hmax, int nk, int step0, cudaStream_t st)
 {
     if (ntiles <= 0 || nk <= 0) return cudaSuccess;
-    const size_t smem = (size_t)2 * smax * LANES * sizeof(double);
+    const size_t smem = adj_reverse_smem(smax, hmax);
     cudaError_t ce = smem_attr((const void *)k_adj_reverse, smem);
     if (ce != cudaSuccess) return ce;
-    k_adj_reverse<<<ntiles, LANES, smem, st>>>(v, smax, nk, step0);
+    k_adj_reverse<<<ntiles, ADJ_REV_WARPS * LANES, smem, st>>>(v, smax, hmax, nk, step0);
     return cudaGetLastError();
 }
 

@@ -22,8 +22,9 @@
 //             of every channel, and per gate d prod/dx, dx'/dVm (table slope,
 //             zero where the lookup clamps or without interpolation) and
 //             dx'/dx (the trapezoid factor (2-B')/B', zero for instant gates);
-//   k_adj_reverse   (sequential over steps, one lane per neuron) the adjoint
-//             recurrence of Vm and the gate states:
+//   k_adj_reverse   (sequential over steps, one lane per neuron; the tree
+//             walk on one warp, the channel phase spread over four) the
+//             adjoint recurrence of Vm and the gate states:
 //               seed      Vm-bar += 2 (Vm after - target) at target rows
 //                         (Crank-Nicolson: Vm after = 2x - Vm before);
 //               back substitution reversed, rows ascending:
@@ -256,12 +257,21 @@ k_adj_linearize(AdjView v, int smax)
 }
 
 // ---------------------------------------------------------------- reverse
-// grid (tiles), 32 threads. Shared memory: 2 * smax * 32 doubles.
-__global__ void __launch_bounds__(32)
-k_adj_reverse(AdjView v, int smax, int nk, int step0)
+// grid (tiles), ADJ_REV_WARPS warps per tile. Warp 0 runs the elimination's
+// reverse (a chain along the tree); the channel phase and the seeds of the
+// next step are split over the warps by slot (slot s to warp s mod W), so
+// the block keeps every FP64 unit of its SM busy. Shared memory: the D and R
+// adjoint columns (2 * smax * 32 doubles), per-warp loss partials
+// (W * 32 doubles) and the tile type's slot and channel plans.
+constexpr int ADJ_REV_WARPS = 4;
+
+__global__ void __launch_bounds__(ADJ_REV_WARPS * 32)
+k_adj_reverse(AdjView v, int smax, int hmax, int nk, int step0)
 {
     extern __shared__ double sm[];
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
     const int t = blockIdx.x;
     const Tile tl = v.tiles[t];
     const TileType ty = v.types[tl.type];
@@ -274,74 +284,95 @@ k_adj_reverse(AdjView v, int smax, int nk, int step0)
     const double *Bw = v.B + tl.topo * LANES + lane;
     const double *Cw = v.Cb + tl.topo * LANES + lane;
     const int *tgt = v.tgt + tl.topo * LANES + lane;
-    const AdjSlot *slots = v.slot_plan + at.slot_off;
-    const AdjChan *chans = v.chan_plan + at.chan_off;
     double *Vb = v.Vbar + tl.vm * LANES + lane;
     double *Xb = v.Xbar + v.xb_off[t] * LANES + lane;
     double *loss = v.loss + (size_t)t * LANES + lane;
     double *Db = sm + lane;
     double *Rb = Db + (size_t)smax * LANES;
+    double *lpart = sm + (size_t)2 * smax * LANES;       // [warp][lane]
+    AdjSlot *slots = reinterpret_cast<AdjSlot *>(lpart + nw * LANES);
+    AdjChan *chans = reinterpret_cast<AdjChan *>(slots + smax);
+    for (int i = threadIdx.x; i < S; i += blockDim.x) slots[i] = v.slot_plan[at.slot_off + i];
+    for (int i = threadIdx.x; i < at.nchans && i < hmax; i += blockDim.x) chans[i] = v.chan_plan[at.chan_off + i];
 
+    // seed of step k at slot s: vb is the adjoint of Vm after step k
+    auto seed = [&](int k, int s, double vb) {
+        double l = 0.0;
+        const int j = tgt[s * LANES];
+        if (j >= 0) {
+            const double *tp = adj_tape(v, k, t, lane);
+            const double x = __ldg(tp + (R.X + s) * LANES);
+            const double vnext = crank ? x + x - __ldg(tp + (R.V + s) * LANES) : x;
+            const double diff = vnext - __ldg(v.trace + (size_t)(step0 + k) * v.ntargets + j);
+            l = diff * diff;
+            vb += 2.0 * diff;
+        }
+        Rb[s * LANES] = crank ? 2.0 * vb : vb;
+        Vb[s * LANES] = crank ? -vb : 0.0;
+        return l;
+    };
+
+    double lw = 0.0;
+    for (int s = warp; s < S; s += nw) lw += seed(nk - 1, s, Vb[s * LANES]);
+    lpart[warp * LANES + lane] = lw;
+    __syncthreads();
     for (int k = nk - 1; k >= 0; --k) {
         double *tp = adj_tape(v, k, t, lane);
-        const double *trow = v.trace + (size_t)(step0 + k) * v.ntargets;
-        // seed (the loss is summed step by step, descending, so the total does
-        // not depend on the checkpoint interval)
-        double lstep = 0.0;
-        for (int s = 0; s < S; ++s) {
-            double vb = Vb[s * LANES];
-            const int j = tgt[s * LANES];
-            if (j >= 0) {
-                const double x = tp[(R.X + s) * LANES];
-                const double vnext = crank ? x + x - tp[(R.V + s) * LANES] : x;
-                const double diff = vnext - trow[j];
-                lstep += diff * diff;
-                vb += 2.0 * diff;
+        if (warp == 0) {
+            // loss of step k, summed in warp order, steps descending
+            double l = 0.0;
+            for (int w = 0; w < nw; ++w) l += lpart[w * LANES + lane];
+            *loss += l;
+            // back substitution reversed
+#pragma unroll 4
+            for (int s = 0; s < S; ++s) {
+                const int p = __ldg(par + s * LANES);
+                const double rb = Rb[s * LANES] * __ldg(tp + (R.RD + s) * LANES);
+                Rb[s * LANES] = rb;
+                tp[(R.RBBS + s) * LANES] = rb;
+                if (p >= 0) Rb[p * LANES] -= __ldg(Cw + s * LANES) * rb;
+                Db[s * LANES] = -__ldg(tp + (R.X + s) * LANES) * rb;
             }
-            Rb[s * LANES] = crank ? 2.0 * vb : vb;
-            Vb[s * LANES] = crank ? -vb : 0.0;
+            // forward elimination reversed
+#pragma unroll 4
+            for (int s = S - 1; s >= 0; --s) {
+                const int p = __ldg(par + s * LANES);
+                if (p < 0) continue;
+                const double tt = __ldg(tp + (R.T + s) * LANES);
+                const double rd = __ldg(tp + (R.RD + s) * LANES);
+                const double tb = -__ldg(Bw + s * LANES) * Db[p * LANES] - __ldg(tp + (R.RP + s) * LANES) * Rb[p * LANES];
+                Rb[s * LANES] -= tt * Rb[p * LANES];
+                Db[s * LANES] -= tt * (tb * rd);
+            }
         }
-        *loss += lstep;
-        // back substitution reversed
-        for (int s = 0; s < S; ++s) {
-            const int p = par[s * LANES];
-            const double rb = Rb[s * LANES] * tp[(R.RD + s) * LANES];
-            Rb[s * LANES] = rb;
-            tp[(R.RBBS + s) * LANES] = rb;
-            if (p >= 0) Rb[p * LANES] -= Cw[s * LANES] * rb;
-            Db[s * LANES] = -tp[(R.X + s) * LANES] * rb;
-        }
-        // forward elimination reversed
-        for (int s = S - 1; s >= 0; --s) {
-            const int p = par[s * LANES];
-            if (p < 0) continue;
-            const double tt = tp[(R.T + s) * LANES];
-            const double dbp = Db[p * LANES], rbp = Rb[p * LANES];
-            const double tb = -Bw[s * LANES] * dbp - tp[(R.RP + s) * LANES] * rbp;
-            Rb[s * LANES] -= tt * rbp;
-            Db[s * LANES] -= tt * (tb * tp[(R.RD + s) * LANES]);
-        }
-        // channels reversed: the adjoint of Vm and of the gate states
-        for (int s = 0; s < S; ++s) {
+        __syncthreads();
+        // channels reversed (adjoint of Vm and of the gate states), then the
+        // seed of step k-1
+        lw = 0.0;
+        for (int s = warp; s < S; s += nw) {
             const AdjSlot sp = slots[s];
             const double rb = Rb[s * LANES], db = Db[s * LANES];
             tp[(R.RBF + s) * LANES] = rb;
             tp[(R.DBF + s) * LANES] = db;
-            const double tbyc = P[sp.f_tbyc * LANES];
+            const double tbyc = __ldg(P + sp.f_tbyc * LANES);
             const double Ibar = rb * tbyc, Sbar = db * tbyc;
             double vbn = Vb[s * LANES] + rb;
             for (int c = sp.ch0; c < sp.ch0 + sp.nch; ++c) {
-                const AdjChan ch = chans[c];
-                const double Ek = ch.f_ek >= 0 ? P[ch.f_ek * LANES] : 0.0;
-                const double w = (Sbar + Ibar * Ek) * P[ch.f_gmax * LANES];
+                const AdjChan ch = c < hmax ? chans[c] : v.chan_plan[at.chan_off + c];
+                const double Ek = ch.f_ek >= 0 ? __ldg(P + ch.f_ek * LANES) : 0.0;
+                const double w = (Sbar + Ibar * Ek) * __ldg(P + ch.f_gmax * LANES);
+#pragma unroll 2
                 for (int g = ch.g0; g < ch.g0 + ch.ng; ++g) {
-                    const double xhat = Xb[g * LANES] + w * tp[(R.Q + g) * LANES];
-                    vbn += xhat * tp[(R.DXDV + g) * LANES];
-                    Xb[g * LANES] = xhat * tp[(R.DXDST + g) * LANES];
+                    const double xhat = Xb[g * LANES] + w * __ldg(tp + (R.Q + g) * LANES);
+                    vbn += xhat * __ldg(tp + (R.DXDV + g) * LANES);
+                    Xb[g * LANES] = xhat * __ldg(tp + (R.DXDST + g) * LANES);
                 }
             }
-            Vb[s * LANES] = vbn;
+            if (k > 0) lw += seed(k - 1, s, vbn);
+            else Vb[s * LANES] = vbn;
         }
+        lpart[warp * LANES + lane] = lw;
+        __syncthreads();
     }
 }
 

@@ -118,8 +118,10 @@ cudaError_t launch_adj_copy(const AdjView &v, int ntiles, int maxrows, int c, in
 // Per-step linearisation of tape steps [0, nk): recomputes each step from
 // its snapshot (parallel over steps and tiles) and fills the tape rows.
 cudaError_t launch_adj_linearize(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st);
-// Reverse sweep over tape steps nk-1 .. 0 (step0: trace row of step 0).
-cudaError_t launch_adj_reverse(const AdjView &v, int ntiles, int smax, int nk, int step0, cudaStream_t st);
+// Reverse sweep over tape steps nk-1 .. 0 (step0: trace row of step 0);
+// hmax: channels per neuron whose plan is cached in shared memory.
+size_t adj_reverse_smem(int smax, int hmax);
+cudaError_t launch_adj_reverse(const AdjView &v, int ntiles, int smax, int hmax, int nk, int step0, cudaStream_t st);
 // Gradient sums of one segment's nk steps (parallel over tiles and slots).
 cudaError_t launch_adj_reduce(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st);
 

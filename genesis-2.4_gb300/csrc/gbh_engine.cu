@@ -1316,9 +1316,12 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         smax = std::max(smax, at.nslots);
         maxcopy = std::max(maxcopy, at.nslots + at.ngates);
     }
-    if ((size_t)2 * smax * L * sizeof(double) > 227 * 1024)
+    if ((size_t)2 * smax * L * sizeof(double) > 200 * 1024)
         return fail_err(nullptr, GBH_ERR_UNSUPPORTED, "gbh_loss_gradient: %d compartments per neuron exceed shared memory",
                         smax);
+    int hmax = 0;   // channel plans cached in shared memory by the reverse kernel
+    for (const AdjType &at : atypes) hmax = std::max(hmax, at.nchans);
+    while (hmax > 0 && adj_reverse_smem(smax, hmax) > 227 * 1024) hmax /= 2;
     // ---- device buffers (released on every return path) ----
     struct Bufs {
         DBuf<double> P, V, ck, tape, Vb, Xb, Gf, Gek, Ggm, GA, GB, GC, trace, loss;
@@ -1443,7 +1446,7 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
             if (k + 1 < nk && forward(1)) return GBH_ERR_CUDA;
         }
         if (ck_launch(launch_adj_linearize(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
-        if (ck_launch(launch_adj_reverse(v, ntiles, smax, nk, seg * K, st))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reverse(v, ntiles, smax, hmax, nk, seg * K, st))) return GBH_ERR_CUDA;
         if (ck_launch(launch_adj_reduce(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
     }
     CK(cudaEventRecord(e->ev1, st));
