@@ -225,6 +225,7 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
     eng.run(nsteps)
     fwd_ms = eng.stats().device_ms - ms0
     eng.set_state(vm=st0["vm"], chip=st0["chip"])
+    launches0 = eng.stats().launches
     t1 = time.time()
     loss, dchip, drav, dvm = eng.loss_gradient(nsteps, solver, soma, tr, GRAD_K)
     wall = time.time() - t1
@@ -234,14 +235,14 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
     finite = bool(np.all(np.isfinite(dchip)) and np.all(np.isfinite(drav)) and np.all(np.isfinite(dvm)))
     log("gradient: forward %.1f ms, gradient %.1f ms (checkpoint pass %.1f, reverse %.1f), ratio %.2f, "
         "loss %.6g" % (fwd_ms, grad_ms, st.grad_forward_ms, st.grad_reverse_ms, grad_ms / fwd_ms, loss))
-    return {"workload": "grad-trees-4096x64: %d random binary trees x %d compartments, Na/K/leak on every "
-                        "compartment, dt 25 us, backward Euler, somatic-trace loss" % (n_neurons, GRAD_NCOMP),
+    return {"workload": "grad-trees-%dx%d: %d random binary trees x %d compartments, Na/K/leak on every "
+                        "compartment, dt 25 us, backward Euler, somatic-trace loss" % (n_neurons, GRAD_NCOMP, n_neurons, GRAD_NCOMP),
             "steps": nsteps, "checkpoint_every": GRAD_K, "dtype": "f64",
             "forward_ms": fwd_ms, "gradient_ms": grad_ms, "checkpoint_pass_ms": st.grad_forward_ms,
             "reverse_pass_ms": st.grad_reverse_ms, "gradient_wall_s": wall,
             "ratio_gradient_over_forward": grad_ms / fwd_ms,
             "ratio_backward_over_forward": st.grad_reverse_ms / fwd_ms, "loss": loss, "gradients_finite": finite,
-            "launches": int(st.launches)}
+            "launches": int(st.launches - launches0)}
 
 
 def run_reference(args, ws, rank, dist):
@@ -295,6 +296,10 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--profile-form", choices=["fp64", "mixed"],
+                    help="time only this form's step loop (for profiler launch lists and captures)")
+    ap.add_argument("--profile-adjoint", type=int, nargs=2, metavar=("NEURONS", "STEPS"),
+                    help="run only the gradient workload at this size")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local, dist = dist_setup()
@@ -305,7 +310,18 @@ def main():
     torch.cuda.set_device(local)
     from gbhsolve import engine
 
+    if args.profile_adjoint:
+        print(json.dumps(adjoint_measure(local, *args.profile_adjoint)), flush=True)
+        return 0
     hs, injects = build_workload(args.neurons)
+    if args.profile_form:
+        prec = engine.PREC_MIXED if args.profile_form == "mixed" else engine.PREC_FP64
+        eng = engine.Engine(hs, precision=prec, steps_per_launch=args.steps_per_launch, device=local)
+        ms, launches, st = time_engine(eng, args.steps, args.warmup)
+        log("%s: %.3f ms for %d steps, %d launches, %d steps/launch" % (args.profile_form, ms, args.steps, launches,
+                                                                    st.steps_per_launch))
+        eng.close()
+        return 0
     M = args.neurons * NCOMP
     results = {}
     for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
