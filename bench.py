@@ -136,8 +136,19 @@ def time_engine(eng, steps, warmup):
     return st1.device_ms - ms0, st1.launches - l0, st1
 
 
-def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE, chunk=500):
-    """max|dVm| of the engine against the FP64 oracle over nsteps steps."""
+def _crossings(v, dt, thresh=0.0):
+    """Upward threshold crossings of a trace, linearly interpolated (s)."""
+    out = []
+    for n in range(1, len(v)):
+        if v[n - 1] < thresh <= v[n]:
+            out.append((n - 1 + (thresh - v[n - 1]) / (v[n] - v[n - 1])) * dt)
+    return out
+
+
+def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE):
+    """max|dVm| of the engine against the FP64 oracle over nsteps steps on a
+    sample of neurons, and the deviation of somatic spike times (upward 0 V
+    crossings, interpolated between steps)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
     from gbhsolve import engine
@@ -145,19 +156,29 @@ def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE, chunk=5
     sample = [hs[i] for i in idx]
     eng = engine.Engine(sample, precision=precision)
     orc = [pyoracle.Solver(h) for h in sample]
+    soma = np.cumsum([h.ncompts for h in sample]) - 1      # the root is each solver's last row
+    trace_e = np.empty((nsteps, len(sample)))
+    trace_o = np.empty((nsteps, len(sample)))
     worst = 0.0
-    done = 0
-    while done < nsteps:
-        k = min(chunk, nsteps - done)
-        eng.run(k)
+    for n in range(nsteps):
+        eng.run(1)
         for s in orc:
-            s.run(k)
+            s.run(1)
         vm = eng.vm()
         ref = np.concatenate([s.vm for s in orc])
         worst = max(worst, float(np.max(np.abs(vm - ref))))
-        done += k
+        trace_e[n] = vm[soma]
+        trace_o[n] = ref[soma]
     eng.close()
-    return worst
+    dt = float(sample[0].dt)
+    dev, nspk, mismatch = 0.0, 0, 0
+    for j in range(len(sample)):
+        te, to = _crossings(trace_e[:, j], dt), _crossings(trace_o[:, j], dt)
+        mismatch += abs(len(te) - len(to))
+        for a, b in zip(te, to):
+            dev = max(dev, abs(a - b))
+            nspk += 1
+    return worst, dev, nspk, mismatch
 
 
 def cpu_sample_rate(hs, seconds=12.0):
@@ -381,10 +402,12 @@ def main():
     eng.close()
 
     # accuracy of the mixed form against the FP64 oracle
-    acc = None
+    acc = spk_dev = None
+    nspk = spk_mismatch = None
     if rank == 0 and not args.skip_accuracy:
-        acc = accuracy_sample(hs, engine.PREC_MIXED)
-        log("mixed max|dVm| over %d steps: %.3e V" % (ACC_STEPS, acc))
+        acc, spk_dev, nspk, spk_mismatch = accuracy_sample(hs, engine.PREC_MIXED)
+        log("mixed max|dVm| over %d steps: %.3e V; spike times: %d spikes, max deviation %.3e s, count "
+            "mismatches %d" % (ACC_STEPS, acc, nspk, spk_dev, spk_mismatch))
 
     adj = None
     if rank == 0 and not args.skip_adjoint:
@@ -422,6 +445,8 @@ def main():
                                "dtype": "f64"},
                       "mixed": {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
                                 "max_abs_dvm_vs_fp64_oracle_V": acc, "accuracy_steps": ACC_STEPS,
+                                "spike_time_max_dev_s": spk_dev, "spikes_compared": nspk,
+                                "spike_count_mismatches": spk_mismatch,
                                 "accuracy_sample_neurons": ACC_SAMPLE}},
             "speedup_mixed_over_fp64": r["value"] / results["fp64"]["value"],
             "e2e": {"value": e2e_val, "unit": "compartment-steps/s", "h2d_bytes_per_step": nh * 8,
