@@ -36,6 +36,9 @@ struct DevView {
     const double *stablist;        // synchan constants (shared by the batch)
     int *status;
     double dt;
+    // Absolute step of launch-relative step 0, read on the device (kernels
+    // replayed from a CUDA graph); null: the step0 argument is absolute.
+    const long long *step_dev;
 };
 
 // ---------------------------------------------------------------- helpers

@@ -125,6 +125,17 @@ struct gbh_engine {
     int jit_choice = 0;
     int jit_compiled = 0;
     std::string jit_log;
+    // CUDA graphs of whole runs (opt.use_graph): one per (steps, steps per
+    // launch, kernel variant); the step number lives on the device
+    struct Graph {
+        int nsteps, spl, variant;
+        cudaGraphExec_t exec;
+        int64_t kernels;
+    };
+    std::vector<Graph> graphs;
+    cudaStream_t cap_stream = nullptr;
+    DBuf<long long> d_step;
+    bool dstep_valid = false;
     // per-step I/O (h_in_msgs / h_out_msgs)
     int n_in = 0, n_out = 0;
     DBuf<double> d_in_vals, d_out_vals;
@@ -657,8 +668,79 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
     return GBH_OK;
 }
 
+__global__ void k_set_step(long long *s, long long v) { *s = v; }
+__global__ void k_add_step(long long *s, long long n) { *s += n; }
+
+void drop_graphs(gbh_engine *e)
+{
+    for (auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
+    e->graphs.clear();
+}
+
+// The launch sequence of nsteps steps captured once as a CUDA graph and
+// replayed: kernels take their step number from the device counter d_step,
+// which the graph's last node advances, so one graph serves every start step.
+int run_graph(gbh_engine *e, int nsteps, cudaStream_t st)
+{
+    gbh_engine::Graph *g = nullptr;
+    for (auto &x : e->graphs)
+        if (x.nsteps == nsteps && x.spl == e->steps_per_launch && x.variant == e->jit_choice) g = &x;
+    if (!g) {
+        if (!e->cap_stream) CK(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking));
+        DevView v = view_of(e);
+        v.step_dev = e->d_step.p;
+        const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+        const int64_t launches0 = e->stats.launches;
+        CK(cudaStreamBeginCapture(e->cap_stream, cudaStreamCaptureModeRelaxed));
+        int64_t kernels = 0;
+        int rc = GBH_OK;
+        for (int done = 0; done < nsteps && rc == GBH_OK;) {
+            const int k = std::min(e->steps_per_launch, nsteps - done);
+            for (const Launch &L : e->launches) {
+                rc = launch_one(e, v, L, k, done, mixed, false, e->cap_stream);
+                if (rc) break;
+                ++kernels;
+            }
+            done += k;
+        }
+        k_add_step<<<1, 1, 0, e->cap_stream>>>(e->d_step.p, nsteps);
+        ++kernels;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(e->cap_stream, &graph);
+        e->stats.launches = launches0;
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) {
+            set_last("graph capture failed: %s", cudaGetErrorString(ce));
+            return GBH_ERR_CUDA;
+        }
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            set_last("graph instantiation failed: %s", cudaGetErrorString(ie));
+            return GBH_ERR_CUDA;
+        }
+        e->graphs.push_back({nsteps, e->steps_per_launch, e->jit_choice, exec, kernels});
+        g = &e->graphs.back();
+    }
+    if (!e->dstep_valid) {
+        k_set_step<<<1, 1, 0, st>>>(e->d_step.p, e->step);
+        CK(cudaGetLastError());
+        e->dstep_valid = true;
+    }
+    CK(cudaGraphLaunch(g->exec, st));
+    e->step += nsteps;
+    e->stats.launches += g->kernels;
+    return GBH_OK;
+}
+
 int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 {
+    if (e->opt.use_graph && !e->givals_enabled) return run_graph(e, nsteps, st);
+    e->dstep_valid = false;   // the launches below carry absolute step numbers
     const DevView v = view_of(e);
     const bool mixed = e->opt.precision == GBH_PREC_MIXED;
     int done = 0;
@@ -681,10 +763,23 @@ int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 
 }  // namespace
 
+int autotune_trials(gbh_engine *e);
+
 // Autotuner: times trial steps for every (kernel variant, steps per launch)
 // candidate on the live engine, saving the mutable state first and restoring
 // it after each trial, and keeps the fastest pair. Results are unaffected.
 int autotune(gbh_engine *e)
+{
+    const int use_graph = e->opt.use_graph;
+    e->opt.use_graph = 0;   // trials time plain launches; graphs are captured afterwards
+    const int rc_t = autotune_trials(e);
+    e->opt.use_graph = use_graph;
+    drop_graphs(e);
+    e->dstep_valid = false;
+    return rc_t;
+}
+
+int autotune_trials(gbh_engine *e)
 {
     std::vector<int> spls;
     if (e->has_network) spls = {1};
@@ -750,6 +845,7 @@ int gbh_internal_device(const gbh_engine *e) { return e->opt.device; }
 
 int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, double *flux)
 {
+    e->dstep_valid = false;
     DevView v = view_of(e);
     v.F = flux;
     const bool mixed = e->opt.precision == GBH_PREC_MIXED;
@@ -996,6 +1092,11 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->ops_orig.assign(desc->ops, desc->ops + desc->ops_start[ns]);
     rc = build_layout(e, desc, syn, err);
     if (rc) {
+        gbh_destroy(e);
+        return nullptr;
+    }
+    if (e->d_step.alloc(1)) {
+        fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
         gbh_destroy(e);
         return nullptr;
     }
@@ -1529,6 +1630,9 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_out_vals.release(); e->d_out_addr.release();
+    drop_graphs(e);
+    if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
+    e->d_step.release();
     for (auto &vars : e->jit_var)
         for (JitKernel &k : vars) jit_release(k);
     if (e->ev0) cudaEventDestroy(e->ev0);

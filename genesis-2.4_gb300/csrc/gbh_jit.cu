@@ -435,6 +435,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     o << "  extern __shared__ double sm[];\n"
       << "  const int lane = threadIdx.x & 31; const int wib = threadIdx.x >> 5;\n"
       << "  const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib; if (t >= tile1) return;\n"
+      << "  const long long sbase = v.step_dev ? *v.step_dev : 0;\n"
       << "  const Tile tl = v.tiles[t];\n"
       << "  const bool active = lane < tl.nlanes; (void)active;\n"
       << "  const bool c5 = " << (tt.chanmode5 ? "true" : "false") << "; (void)c5;\n"
@@ -459,7 +460,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
           << "  double *Dc = sm + (size_t)wib * " << 2 * S * LANES << " + lane; double *Rc = Dc + " << S * LANES << ";\n";
     o << "  const double *Aw = v.A + tl.topo * 32 + lane; const double *Bw = v.B + tl.topo * 32 + lane; const double *Cbw = v.Cb + tl.topo * 32 + lane;\n";
     o << "  for (int it = 0; it < nsteps; ++it) {\n"
-      << "    const long long step = step0 + it; (void)step;\n";
+      << "    const long long step = sbase + step0 + it; (void)step;\n";
     if (mixed) {
         o << "    DCursor vc, cc, c1; vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f); cc = vc; c1 = vc;\n"
           << "    df Ek = df_make(0.f, 0.f), Gk = Ek, gmax = Ek; (void)gmax;\n";

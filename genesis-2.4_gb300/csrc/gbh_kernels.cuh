@@ -34,6 +34,7 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
     const int wib = threadIdx.x >> 5;
     const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib;
     if (t >= tile1) return;
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
     const Tile tl = v.tiles[t];
     const TileType ty = v.types[tl.type];
     const TableGeom tg = v.tgeom[ty.table_set];
@@ -61,7 +62,7 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
     double *Fw = v.F + tl.pools * LANES + lane;
 
     for (int it = 0; it < nsteps; ++it) {
-        const long long step = step0 + it;
+        const long long step = sbase + step0 + it;
         VCursor vc, cc;
         if (tg.ncols) { vc.lo = vc.hi = 0.0; } else { vc.lo = -1e20; vc.hi = 1e20; }
         vc.row = vc.base = 0; vc.frac = 0.0;

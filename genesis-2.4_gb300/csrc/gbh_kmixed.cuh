@@ -27,6 +27,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
     const int wib = threadIdx.x >> 5;
     const int t = tile0 + blockIdx.x * (blockDim.x >> 5) + wib;
     if (t >= tile1) return;
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
     const Tile tl = v.tiles[t];
     const TileType ty = v.types[tl.type];
     const TableGeom tg = v.tgeom[ty.table_set];
@@ -53,7 +54,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
     const int64_t neuron = tl.first_neuron + lane;
 
     for (int it = 0; it < nsteps; ++it) {
-        const long long step = step0 + it;
+        const long long step = sbase + step0 + it;
         DCursor vc, cc, c1;
         vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f);
         cc = vc;

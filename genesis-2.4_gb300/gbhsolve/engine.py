@@ -270,10 +270,12 @@ class Engine:
     """A device engine over a batch of hsolve elements."""
 
     def __init__(self, solvers: Sequence, synapses: Optional[dict] = None, precision: int = PREC_FP64,
-                 steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0, jit: bool = True):
+                 steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0, jit: bool = True,
+                 use_graph: bool = False):
         self.lib = load()
         self.batch = Batch(solvers, synapses)
-        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 0, device, 0 if jit else -1)
+        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device,
+                         0 if jit else -1)
         err = GbhError()
         h = self.lib.gbh_create(C.byref(self.batch.desc),
                                 C.byref(self.batch.syn) if self.batch.syn is not None else None,
