@@ -266,6 +266,61 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
             "launches": int(st.launches - launches0)}
 
 
+def other_configs(device, n_trees=10_000):
+    """Throughput of the other workloads (parity-test cases; not the headline):
+    cables-1k-x16 (1,000 x 16-compartment cables, FP64, 200 steps), the
+    4,000-cell spiking network (2 % connectivity, dt 0.1 ms, FP64, seeded
+    tonic drive U(0.05, 0.3) nA so that it spikes) with and without
+    CUDA-graph replay, and random trees 8-256 compartments with Ca
+    pools (a 10,000-neuron sample of the 50,000, FP64 and mixed, graph replay)."""
+    from gbhsolve import configs, engine, model
+    out = {}
+
+    def rate(eng, steps, warm):
+        eng.run(warm)
+        ms0 = eng.stats().device_ms
+        eng.run(steps)
+        return eng.stats().device_ms - ms0
+
+    hs0 = [model.build(m) for m in configs.cables(1000, per_neuron_solvers=True)]
+    eng = engine.Engine(hs0, precision=engine.PREC_FP64, device=device)
+    ms = rate(eng, 200, 20)
+    out["cables-1k-x16"] = {"compartments": 16_000, "steps": 200, "ms": ms, "value": 16_000 * 200 / (ms / 1e3),
+                            "dtype": "f64"}
+    eng.close()
+
+    ms1, syn = configs.hh_network(4000)
+    drive = np.random.default_rng(1).uniform(0.05e-9, 0.3e-9, size=len(ms1))   # tonic drive, recorded choice
+    for m, x in zip(ms1, drive):
+        m.compartments[0].inject = float(x)
+    hs1 = [model.build(m) for m in ms1]
+    esyn, _ = configs.network_synapses(hs1, syn)
+    net = {"cells": 4000, "synapses": int(len(esyn["target_solver"])), "steps": 5000, "dtype": "f64",
+           "drive": "inject U(0.05, 0.3) nA, seed 1"}
+    for graph in (False, True):
+        eng = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_FP64, device=device, use_graph=graph)
+        ms = rate(eng, 5000, 100)
+        key = "graph" if graph else "launches"
+        net[key] = {"ms": ms, "steps_per_s": 5000 / (ms / 1e3), "value": 4000 * 5000 / (ms / 1e3),
+                    "spikes": int(eng.spike_counts().sum())}
+        eng.close()
+    out["hh-network-4000"] = net
+
+    hs2 = [model.build(m) for m in configs.random_trees(n_trees, seed=2)]
+    M2 = sum(h.ncompts for h in hs2)
+    trees = {"neurons": n_trees, "compartments": M2, "steps": 1000}
+    for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
+        eng = engine.Engine(hs2, precision=prec, device=device, use_graph=True)
+        st = eng.stats()
+        ms = rate(eng, 1000, 20)
+        trees[form] = {"ms": ms, "value": M2 * 1000 / (ms / 1e3), "tiles": int(st.tiles),
+                       "specialised_kernels": int(st.jit_kernels), "steps_per_launch": int(st.steps_per_launch)}
+        eng.close()
+    out["random-trees-ca"] = trees
+    log("other configs: %s" % json.dumps(out))
+    return out
+
+
 def run_reference(args, ws, rank, dist):
     """CPU restatement of the reference solver on every host core."""
     if rank != 0:
@@ -317,6 +372,7 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-adjoint", action="store_true")
+    ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--profile-form", choices=["fp64", "mixed"],
                     help="time only this form's step loop (for profiler launch lists and captures)")
     ap.add_argument("--profile-adjoint", type=int, nargs=2, metavar=("NEURONS", "STEPS"),
@@ -412,6 +468,9 @@ def main():
     adj = None
     if rank == 0 and not args.skip_adjoint:
         adj = adjoint_measure(local)
+    other = None
+    if rank == 0 and not args.skip_configs:
+        other = other_configs(local)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -457,6 +516,7 @@ def main():
                          "alg_bytes_per_compartment_step": ALG_BYTES["mixed"]},
             "cpu_baseline": cpu,
             "adjoint": adj,
+            "other_configs": other,
             "gpu_launches": int(r["launches"]),
             "clocks": r["clocks"],
         }

@@ -134,6 +134,10 @@ struct gbh_engine {
     };
     std::vector<Graph> graphs;
     cudaStream_t cap_stream = nullptr;
+    // side streams: launch groups (tile types) run concurrently
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev_join;
+    cudaEvent_t ev_fork = nullptr;
     DBuf<long long> d_step;
     bool dstep_valid = false;
     // per-step I/O (h_in_msgs / h_out_msgs)
@@ -668,6 +672,62 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
     return GBH_OK;
 }
 
+// Issues nsteps steps of every launch group, numbered from step0 (absolute,
+// or relative to *v.step_dev). With several groups each runs on a side
+// stream: groups share no data within a step and, without synapses, none
+// across steps, so each group runs its whole span alone; with synapses the
+// side streams are joined back into st after every step (events cross
+// tiles). giv_last: the last step alone, recording givals.
+int issue_steps(gbh_engine *e, const DevView &v, int nsteps, long long step0, bool giv_last, cudaStream_t st,
+                int64_t *kernels)
+{
+    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+    const int nl = (int)e->launches.size();
+    const int ns = (int)e->side.size();
+    const int plain = giv_last ? nsteps - 1 : nsteps;
+    if (nl <= 1 || ns == 0) {
+        for (int done = 0; done < plain;) {
+            const int k = std::min(e->steps_per_launch, plain - done);
+            for (const Launch &L : e->launches) {
+                const int rc = launch_one(e, v, L, k, step0 + done, mixed, false, st);
+                if (rc) return rc;
+                if (kernels) ++*kernels;
+            }
+            done += k;
+        }
+    } else {
+        const int span = e->has_network ? 1 : std::max(plain, 1);
+        for (int done = 0; done < plain; done += span) {
+            const int n = std::min(span, plain - done);
+            CK(cudaEventRecord(e->ev_fork, st));
+            for (int i = 0; i < ns; ++i) CK(cudaStreamWaitEvent(e->side[i], e->ev_fork, 0));
+            for (int li = 0; li < nl; ++li) {
+                const Launch &L = e->launches[li];
+                cudaStream_t s = e->side[li % ns];
+                for (int d = 0; d < n;) {
+                    const int k = std::min(e->steps_per_launch, n - d);
+                    const int rc = launch_one(e, v, L, k, step0 + done + d, mixed, false, s);
+                    if (rc) return rc;
+                    if (kernels) ++*kernels;
+                    d += k;
+                }
+            }
+            for (int i = 0; i < ns; ++i) {
+                CK(cudaEventRecord(e->ev_join[i], e->side[i]));
+                CK(cudaStreamWaitEvent(st, e->ev_join[i], 0));
+            }
+        }
+    }
+    if (giv_last && nsteps > 0) {
+        for (const Launch &L : e->launches) {
+            const int rc = launch_one(e, v, L, 1, step0 + nsteps - 1, mixed, true, st);
+            if (rc) return rc;
+            if (kernels) ++*kernels;
+        }
+    }
+    return GBH_OK;
+}
+
 __global__ void k_set_step(long long *s, long long v) { *s = v; }
 __global__ void k_add_step(long long *s, long long n) { *s += n; }
 
@@ -689,20 +749,10 @@ int run_graph(gbh_engine *e, int nsteps, cudaStream_t st)
         if (!e->cap_stream) CK(cudaStreamCreateWithFlags(&e->cap_stream, cudaStreamNonBlocking));
         DevView v = view_of(e);
         v.step_dev = e->d_step.p;
-        const bool mixed = e->opt.precision == GBH_PREC_MIXED;
         const int64_t launches0 = e->stats.launches;
         CK(cudaStreamBeginCapture(e->cap_stream, cudaStreamCaptureModeRelaxed));
         int64_t kernels = 0;
-        int rc = GBH_OK;
-        for (int done = 0; done < nsteps && rc == GBH_OK;) {
-            const int k = std::min(e->steps_per_launch, nsteps - done);
-            for (const Launch &L : e->launches) {
-                rc = launch_one(e, v, L, k, done, mixed, false, e->cap_stream);
-                if (rc) break;
-                ++kernels;
-            }
-            done += k;
-        }
+        const int rc = issue_steps(e, v, nsteps, 0, false, e->cap_stream, &kernels);
         k_add_step<<<1, 1, 0, e->cap_stream>>>(e->d_step.p, nsteps);
         ++kernels;
         cudaGraph_t graph = nullptr;
@@ -742,21 +792,9 @@ int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
     if (e->opt.use_graph && !e->givals_enabled) return run_graph(e, nsteps, st);
     e->dstep_valid = false;   // the launches below carry absolute step numbers
     const DevView v = view_of(e);
-    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
-    int done = 0;
-    while (done < nsteps) {
-        int k = std::min(e->steps_per_launch, nsteps - done);
-        const bool last = done + k == nsteps;
-        const bool giv = e->givals_enabled && last;
-        if (giv && k > 1) k -= 1;  // the recorded step runs on its own
-        const bool giv_now = giv && done + k == nsteps;
-        for (const Launch &L : e->launches) {
-            const int rc = launch_one(e, v, L, k, e->step, mixed, giv_now, st);
-            if (rc) return rc;
-        }
-        e->step += k;
-        done += k;
-    }
+    const int rc = issue_steps(e, v, nsteps, e->step, e->givals_enabled, st, nullptr);
+    if (rc) return rc;
+    e->step += nsteps;
     if (e->givals_enabled) e->givals_valid = true;
     return GBH_OK;
 }
@@ -848,21 +886,9 @@ int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, doubl
     e->dstep_valid = false;
     DevView v = view_of(e);
     v.F = flux;
-    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
-    int done = 0;
-    while (done < nsteps) {
-        int k = std::min(e->steps_per_launch, nsteps - done);
-        const bool last = done + k == nsteps;
-        const bool giv = e->givals_enabled && last;
-        if (giv && k > 1) k -= 1;
-        const bool giv_now = giv && done + k == nsteps;
-        for (const Launch &L : e->launches) {
-            const int rc = launch_one(e, v, L, k, e->step, mixed, giv_now, st);
-            if (rc) return rc;
-        }
-        e->step += k;
-        done += k;
-    }
+    const int rc = issue_steps(e, v, nsteps, e->step, e->givals_enabled, st, nullptr);
+    if (rc) return rc;
+    e->step += nsteps;
     if (e->givals_enabled) e->givals_valid = true;
     return GBH_OK;
 }
@@ -1094,6 +1120,16 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     if (rc) {
         gbh_destroy(e);
         return nullptr;
+    }
+    if (e->launches.size() > 1) {
+        const int ns = (int)std::min<size_t>(e->launches.size(), 8);
+        e->side.resize(ns);
+        e->ev_join.resize(ns);
+        for (int i = 0; i < ns; ++i) {
+            cudaStreamCreateWithFlags(&e->side[i], cudaStreamNonBlocking);
+            cudaEventCreateWithFlags(&e->ev_join[i], cudaEventDisableTiming);
+        }
+        cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming);
     }
     if (e->d_step.alloc(1)) {
         fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
@@ -1515,17 +1551,7 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         }
         return GBH_OK;
     };
-    auto forward = [&](int n) {
-        for (int done = 0; done < n;) {
-            const int k = std::min(e->steps_per_launch, n - done);
-            for (const Launch &Lc : e->launches) {
-                const int rc = launch_one(e, fv, Lc, k, 0, false, false, st);
-                if (rc) return rc;
-            }
-            done += k;
-        }
-        return GBH_OK;
-    };
+    auto forward = [&](int n) { return issue_steps(e, fv, n, 0, false, st, nullptr); };
     // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed)
     CK(cudaEventRecord(e->ev0, st));
     for (int seg = 0; seg < nseg; ++seg) {
@@ -1632,6 +1658,9 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);
     if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
+    for (cudaStream_t x : e->side) cudaStreamDestroy(x);
+    for (cudaEvent_t x : e->ev_join) cudaEventDestroy(x);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     e->d_step.release();
     for (auto &vars : e->jit_var)
         for (JitKernel &k : vars) jit_release(k);
