@@ -1461,7 +1461,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     while (hmax > 0 && adj_reverse_smem(smax, hmax) > 227 * 1024) hmax /= 2;
     // ---- device buffers (released on every return path) ----
     struct Bufs {
-        DBuf<double> P, V, ck, tape, Vb, Xb, Gf, Gek, Ggm, GA, GB, GC, trace, loss;
+        DBuf<double> P, V, ck, tape, tape2, Vb, Xb, Gf, Gek, Ggm, GA, GB, GC, trace, loss;
+        cudaStream_t ast = nullptr;
+        cudaEvent_t ev_tape[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
         DBuf<int> tgt, snap;
         DBuf<int64_t> ck_off, tp_off, xb_off, ch_off;
         DBuf<AdjType> atypes;
@@ -1469,7 +1471,14 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         DBuf<AdjChan> chans;
         ~Bufs()
         {
-            P.release(); V.release(); ck.release(); tape.release(); Vb.release(); Xb.release(); Gf.release();
+            if (ast) cudaStreamSynchronize(ast);
+            for (int i = 0; i < 2; ++i) {
+                if (ev_tape[i]) cudaEventDestroy(ev_tape[i]);
+                if (ev_done[i]) cudaEventDestroy(ev_done[i]);
+            }
+            if (ast) cudaStreamDestroy(ast);
+            P.release(); V.release(); ck.release(); tape.release(); tape2.release(); Vb.release(); Xb.release();
+            Gf.release();
             Gek.release(); Ggm.release(); GA.release(); GB.release(); GC.release(); trace.release();
             loss.release(); tgt.release(); snap.release(); ck_off.release(); tp_off.release(); xb_off.release();
             ch_off.release(); atypes.release(); slots.release(); chans.release();
@@ -1562,20 +1571,42 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     CK(cudaEventSynchronize(e->ev1));
     float ms_fwd = 0.f;
     CK(cudaEventElapsedTime(&ms_fwd, e->ev0, e->ev1));
-    // reverse pass, segment by segment: recompute with snapshots, linearise,
-    // sweep back, sum the gradients
+    // reverse pass, segment by segment, last first: recompute with snapshots
+    // (engine stream), then linearise, sweep back and sum the gradients (a
+    // second stream). With two tape buffers the recomputation of the next
+    // segment overlaps the adjoint kernels of this one; they share only the
+    // constant fields of the work copy.
+    const bool overlap = b.tape2.alloc((size_t)K * tp_stride * L) == GBH_OK;
+    if (!overlap) cudaGetLastError();
+    AdjView vb[2] = {v, v};
+    if (overlap) vb[1].tape = b.tape2.p;
+    CK(cudaStreamCreateWithFlags(&b.ast, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        CK(cudaEventCreateWithFlags(&b.ev_tape[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&b.ev_done[i], cudaEventDisableTiming));
+    }
     CK(cudaEventRecord(e->ev0, st));
-    for (int seg = nseg - 1; seg >= 0; --seg) {
+    for (int idx = 0; idx < nseg; ++idx) {
+        const int seg = nseg - 1 - idx;
+        const int buf = overlap ? idx % 2 : 0;
+        const AdjView &w = vb[buf];
         const int nk = std::min(K, nsteps - seg * K);
-        if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, seg, 1, false, st))) return GBH_ERR_CUDA;
+        // the buffer's previous segment must be through the adjoint kernels
+        if (idx >= (overlap ? 2 : 1)) CK(cudaStreamWaitEvent(st, b.ev_done[buf], 0));
+        if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, seg, 1, false, st))) return GBH_ERR_CUDA;
         for (int k = 0; k < nk; ++k) {
-            if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, k, 0, true, st))) return GBH_ERR_CUDA;
+            if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, k, 0, true, st))) return GBH_ERR_CUDA;
             if (k + 1 < nk && forward(1)) return GBH_ERR_CUDA;
         }
-        if (ck_launch(launch_adj_linearize(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
-        if (ck_launch(launch_adj_reverse(v, ntiles, smax, hmax, nk, seg * K, st))) return GBH_ERR_CUDA;
-        if (ck_launch(launch_adj_reduce(v, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
+        CK(cudaEventRecord(b.ev_tape[buf], st));
+        CK(cudaStreamWaitEvent(b.ast, b.ev_tape[buf], 0));
+        if (ck_launch(launch_adj_linearize(w, ntiles, smax, nk, b.ast))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reverse(w, ntiles, smax, hmax, nk, seg * K, b.ast))) return GBH_ERR_CUDA;
+        if (ck_launch(launch_adj_reduce(w, ntiles, smax, nk, b.ast))) return GBH_ERR_CUDA;
+        CK(cudaEventRecord(b.ev_done[buf], b.ast));
     }
+    CK(cudaEventRecord(b.ev_done[0], b.ast));
+    CK(cudaStreamWaitEvent(st, b.ev_done[0], 0));
     CK(cudaEventRecord(e->ev1, st));
     CK(cudaEventSynchronize(e->ev1));
     float ms_rev = 0.f;
