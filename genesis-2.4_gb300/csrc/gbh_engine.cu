@@ -73,7 +73,7 @@ struct DBuf {
 struct Launch {
     int tile0, tile1, smax, warps;
     int jit = -1;        // index of a specialised kernel, or -1 to interpret
-    size_t jit_smem = 0;
+    bool uniform = false; // every neuron of the type has the same tree
 };
 
 }  // namespace
@@ -122,6 +122,7 @@ struct gbh_engine {
     std::vector<JitKernel> jits;                 // active kernel of each specialised type
     std::vector<std::vector<JitKernel>> jit_var;  // compiled variants per specialised type
     std::vector<int> jit_minb;                    // residency target of each variant
+    std::vector<char> jit_compact;                // variant is the compact (looped) form
     int jit_choice = 0;
     int jit_compiled = 0;
     std::string jit_log;
@@ -533,10 +534,17 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         const int max_jit = 24;
         if ((int)cand.size() > max_jit) cand.resize(max_jit);
         // residency targets (resident blocks of 4 warps per SM) tried by the autotuner
+        // variants: (resident 4-warp blocks per SM, compact form)
         e->jit_minb.clear();
-        if (const char *mb = getenv("GBH_JIT_MINB")) e->jit_minb.push_back(atoi(mb));
-        else if (e->opt.steps_per_launch > 0) e->jit_minb.push_back(6);
-        else e->jit_minb = {4, 6};
+        e->jit_compact.clear();
+        const int form = e->opt.jit;   // 0 autotuned, 1 unrolled only, 2 compact only
+        if (e->opt.steps_per_launch > 0 || form > 0) {
+            e->jit_minb.push_back(6);
+            e->jit_compact.push_back(form == 2);
+        } else {
+            e->jit_minb = {4, 6, 6, 8};
+            e->jit_compact = {0, 0, 1, 1};
+        }
         const int nvar = (int)e->jit_minb.size();
         std::vector<std::string> srcs(cand.size() * nvar);
         std::vector<std::vector<int>> upar(cand.size());
@@ -553,7 +561,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             if (uni && !ref.empty()) upar[c] = ref;
             for (int vi = 0; vi < nvar; ++vi)
                 srcs[c * nvar + vi] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
-                                                 upar[c].empty() ? nullptr : &upar[c], e->jit_minb[vi]);
+                                                 upar[c].empty() ? nullptr : &upar[c], e->jit_minb[vi],
+                                                 e->jit_compact[vi] != 0);
         }
         int dev = e->opt.device, major = 10, minor = 3;
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -595,7 +604,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             const int S = e->types[ty0].nslots;
             Launch L{(int)t0, type_t1[ty0], S, 4};
             L.jit = type_jit[ty0];
-            L.jit_smem = type_uniform[ty0] ? 0 : (size_t)L.warps * 2 * S * LANES * sizeof(double);
+            L.uniform = type_uniform[ty0] != 0;
             e->launches.push_back(L);
             t0 = type_t1[ty0];
             continue;
@@ -654,7 +663,9 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
                bool giv, cudaStream_t st)
 {
     if (L.jit >= 0 && !giv) {
-        const cudaError_t je = jit_launch(e->jits[L.jit], v, L.tile0, L.tile1, L.smax, L.warps, k, step, L.jit_smem, st);
+        const bool cols = !L.uniform || e->jit_compact[e->jit_choice];   // rows in shared-memory columns
+        const size_t smem = cols ? (size_t)L.warps * 2 * L.smax * LANES * sizeof(double) : 0;
+        const cudaError_t je = jit_launch(e->jits[L.jit], v, L.tile0, L.tile1, L.smax, L.warps, k, step, smem, st);
         if (je != cudaSuccess) {
             set_last("specialised kernel launch failed: %s", cudaGetErrorString(je));
             return GBH_ERR_CUDA;
@@ -852,6 +863,7 @@ int autotune_trials(gbh_engine *e)
     int best_v = 0, best_s = spls[0];
     for (int vi = 0; vi < nvar; ++vi) {
         for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][vi];
+        e->jit_choice = vi;   // launch_one sizes the shared memory of the variant in use
         for (int spl : spls) {
             e->steps_per_launch = spl;
             const int steps = e->has_network ? 32 : std::max(2 * spl, 128);
@@ -1010,7 +1022,8 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
     return GBH_OK;
 }
 
-int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, char *buf, int64_t buflen)
+int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, int compact, char *buf,
+                       int64_t buflen)
 {
     gbh_error err{};
     Decoded dec;
@@ -1054,7 +1067,7 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
     build_tables(desc, tg, tab64, xy);
     const std::string src = jit_source(types[type_index], prog_pool, tg[types[type_index].table_set],
                                        precision == GBH_PREC_MIXED, false,
-                                       uniform[type_index] ? &parents[type_index] : nullptr);
+                                       uniform[type_index] ? &parents[type_index] : nullptr, 6, compact != 0);
     if (buf && buflen > 0) {
         const int64_t n = std::min<int64_t>(buflen - 1, (int64_t)src.size());
         memcpy(buf, src.data(), (size_t)n);
@@ -1155,6 +1168,7 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
     e->stats.jit_kernels = e->jit_compiled;
     e->stats.jit_min_blocks = e->jit_minb.empty() ? 0 : e->jit_minb[e->jit_choice];
+    e->stats.jit_compact = e->jit_compact.empty() ? 0 : e->jit_compact[e->jit_choice];
     if (getenv("GBH_VERBOSE") && !e->jit_log.empty())
         fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
                 e->jit_log.c_str());
@@ -1184,7 +1198,10 @@ int gbh_run(gbh_engine *e, int nsteps)
     int status = 0;
     CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {
-        set_last("device status word 0x%x (unimplemented micro-op reached)", status);
+        set_last("device status word 0x%x (%s)", status,
+                 (status & ST_SMEM) ? "kernel launched with too little shared memory"
+                                    : (status & ST_EVENT_OVERFLOW) ? "synaptic event ring overflow"
+                                                                   : "unimplemented micro-op reached");
         return GBH_ERR_DEVICE;
     }
     return GBH_OK;

@@ -94,6 +94,6 @@ struct Tile {
 };
 
 // Device status word bits
-enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2 };
+enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2, ST_SMEM = 4 /* launched with too little shared memory */ };
 
 }  // namespace gbh

@@ -21,6 +21,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <sstream>
 
@@ -115,12 +116,23 @@ std::string litf(float x)
 struct Emit {
     std::ostringstream o;
     bool mixed, giv;
-    std::string P(int f) const { return "Pw[" + std::to_string(f * LANES) + "]"; }
+    // inside a loop over a run of slots: the slot index variable and, per
+    // field row of the run's first slot, its row as an expression of the loop
+    std::string sidx;
+    std::map<int, std::string> fx;
+    std::string frow(int f) const
+    {
+        auto it = fx.find(f);
+        return it == fx.end() ? std::to_string(f * LANES) : "(" + it->second + ") * 32";
+    }
+    std::string P(int f) const { return "Pw[" + frow(f) + "]"; }
     std::string I(int r) const { return "Iw[" + std::to_string(r * LANES) + "]"; }
     std::string C(int p) const { return "Cw[" + std::to_string(p * LANES) + "]"; }
     std::string F(int p) const { return "Fw[" + std::to_string(p * LANES) + "]"; }
     std::string G(int g) const { return "Gw[" + std::to_string(g * LANES) + "]"; }
-    std::string pP(int f) const { return "&Pw[" + std::to_string(f * LANES) + "]"; }
+    std::string pP(int f) const { return "&Pw[" + frow(f) + "]"; }
+    std::string S(int s) const { return sidx.empty() ? std::to_string(s) : sidx; }
+    std::string Vrow(int s) const { return sidx.empty() ? std::to_string(s * LANES) : sidx + " * 32"; }
 };
 
 int nops_of(int code)
@@ -144,8 +156,8 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
     std::ostringstream &o = E.o;
     const bool mx = E.mixed, giv = E.giv;
     const int ncols = tg.ncols;
-    o << "    { // slot " << s << "\n";
-    o << "      const double Vm = Vw[" << s * LANES << "];\n";
+    o << "    { // slot " << E.S(s) << "\n";
+    o << "      const double Vm = Vw[" << E.Vrow(s) << "];\n";
     if (mx) o << "      const df vmd = d2df(Vm);\n      df sumg = df_make(0.f, 0.f), ichan = sumg;\n";
     else o << "      double sumg = 0.0, ichan = 0.0;\n";
     o << "      double Im = 0.0; (void)Im;\n";
@@ -231,10 +243,10 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
         case M_END:
             if (mx) {
                 o << "      { const df tbyc = ld_df(" << E.pP(a[0]) << "); const df dv = df_mul(ichan, tbyc);\n"
-                  << "        R[" << s << "] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);\n"
-                  << "        D[" << s << "] = df2d(df_add(df_mul(sumg, tbyc), ld_df(" << E.pP(a[1]) << "))); }\n";
+                  << "        R[" << E.S(s) << "] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);\n"
+                  << "        D[" << E.S(s) << "] = df2d(df_add(df_mul(sumg, tbyc), ld_df(" << E.pP(a[1]) << "))); }\n";
             } else {
-                o << "      { const double tbyc = " << E.P(a[0]) << "; R[" << s << "] = Vm + ichan * tbyc; D[" << s
+                o << "      { const double tbyc = " << E.P(a[0]) << "; R[" << E.S(s) << "] = Vm + ichan * tbyc; D[" << E.S(s)
                   << "] = sumg * tbyc + " << E.P(a[1]) << "; }\n";
             }
             if (giv) o << "      " << E.G(a[2]) << " = Im;\n";
@@ -419,11 +431,77 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
     }
 }
 
+// Operand roles of the micro-ops a loop over slots may hold: positions of
+// field rows (may vary with the slot), of literals (must be equal), and of
+// givals rows (unused without givals). False for any other op.
+bool loop_roles(int code, std::vector<int> &fpos, std::vector<int> &fixed)
+{
+    fpos.clear();
+    fixed.clear();
+    switch (code) {
+    case M_BEGIN: fpos = {0, 1, 2}; return true;
+    case M_NEWVOLT: return true;
+    case M_CHAN: fpos = {0, 1}; return true;
+    case M_CHAN_G: fpos = {0}; return true;
+    case M_GATE: fixed = {0, 1, 2}; fpos = {3}; return true;
+    case M_ADDCURR: return true;
+    case M_END: fpos = {0, 1}; return true;
+    default: return false;
+    }
+}
+
+// Number of consecutive slots from s0 whose programs equal slot s0's op for
+// op, literals equal and every field row affine in the slot index; fills
+// the first slot's field rows with their strides.
+int loop_run(const std::vector<int> &prog, const std::vector<int> &sstart, int s0, int S,
+             std::map<int, int> &stride_of)
+{
+    stride_of.clear();
+    const int len = sstart[s0 + 1] - sstart[s0];
+    if (s0 + 1 >= S || sstart[s0 + 2] - sstart[s0 + 1] != len) return 1;
+    const int *a = prog.data() + sstart[s0];
+    const int *b = prog.data() + sstart[s0 + 1];
+    std::vector<int> fpos, fixed;
+    std::vector<std::pair<int, int>> fr;   // (offset in the slot program, stride)
+    for (int o = 0; o < len;) {
+        const int code = a[o];
+        if (b[o] != code || !loop_roles(code, fpos, fixed)) return 1;
+        if (code == M_GATE && a[o + 1] != GK_1V) return 1;
+        for (int k : fixed)
+            if (a[o + 1 + k] != b[o + 1 + k]) return 1;
+        for (int k : fpos) fr.push_back({o + 1 + k, b[o + 1 + k] - a[o + 1 + k]});
+        o += 1 + nops_of(code);
+    }
+    for (auto &x : fr) {
+        auto it = stride_of.find(a[x.first]);
+        if (it != stride_of.end() && it->second != x.second) return 1;
+        stride_of[a[x.first]] = x.second;
+    }
+    int run = 2;
+    for (int j = s0 + 2; j < S; ++j) {
+        if (sstart[j + 1] - sstart[j] != len) break;
+        const int *c = prog.data() + sstart[j];
+        bool same = true;
+        for (int o = 0; o < len && same;) {
+            const int code = a[o];
+            if (c[o] != code) { same = false; break; }
+            loop_roles(code, fpos, fixed);
+            for (int k : fixed) same = same && c[o + 1 + k] == a[o + 1 + k];
+            o += 1 + nops_of(code);
+        }
+        for (auto &x : fr) same = same && c[x.first] == a[x.first] + (j - s0) * x.second;
+        if (!same) break;
+        ++run;
+    }
+    return run;
+}
+
 }  // namespace
 
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent, int min_blocks)
+                       const std::vector<int> *uniform_parent, int min_blocks, bool compact)
 {
+    if (compact) uniform_parent = nullptr;   // rows in shared-memory columns, looped elimination
     Emit E;
     E.mixed = mixed;
     E.giv = giv;
@@ -456,7 +534,9 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
           << "  const double *yvals = v.xyvals + " << (tg.yv_off >= 0 ? tg.yv_off : tg.xv_off) << "; (void)yvals;\n";
     }
     if (!uniform_parent)
-        o << "  const int *par = v.parent + tl.topo * 32 + lane;\n"
+        o << "  { unsigned dsz; asm(\"mov.u32 %0, %%dynamic_smem_size;\" : \"=r\"(dsz));\n"
+          << "    if (dsz < (blockDim.x >> 5) * " << 2 * S * LANES * 8 << "u) { if (v.status) atomicOr(v.status, 4); return; } }\n"
+          << "  const int *par = v.parent + tl.topo * 32 + lane;\n"
           << "  double *Dc = sm + (size_t)wib * " << 2 * S * LANES << " + lane; double *Rc = Dc + " << S * LANES << ";\n";
     o << "  const double *Aw = v.A + tl.topo * 32 + lane; const double *Bw = v.B + tl.topo * 32 + lane; const double *Cbw = v.Cb + tl.topo * 32 + lane;\n";
     o << "  for (int it = 0; it < nsteps; ++it) {\n"
@@ -476,10 +556,43 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     if (uniform_parent) o << "    double D[" << S << "], R[" << S << "];\n";
     else o << "    double *D = nullptr, *R = nullptr; (void)D; (void)R;\n";
     std::ostringstream save;
-    const int *pc = prog.data() + tt.prog_off;
-    // in the non-uniform case rows live in shared memory columns
-    for (int s = 0; s < S; ++s) {
-        if (!emit_slot(E, s, pc, tg)) return std::string();
+    // slot extents in the program
+    std::vector<int> sstart(S + 1);
+    {
+        int off = tt.prog_off;
+        for (int s = 0; s < S; ++s) {
+            sstart[s] = off;
+            for (;;) {
+                const int c = prog[off];
+                const int n = nops_of(c);
+                if (n < 0) return std::string();
+                off += 1 + n;
+                if (c == M_END) break;
+            }
+        }
+        sstart[S] = off;
+    }
+    // compact form: runs of four or more identical slot programs become one
+    // loop (keeps the kernel inside the instruction cache)
+    for (int s = 0; s < S;) {
+        std::map<int, int> stride_of;
+        const int run = (compact && !giv) ? loop_run(prog, sstart, s, S, stride_of) : 1;
+        const int *pc = prog.data() + sstart[s];
+        if (run >= 4) {
+            E.sidx = "s";
+            for (auto &x : stride_of)
+                E.fx[x.first] = std::to_string(x.first) + " + " + std::to_string(x.second) + " * (s - " +
+                                std::to_string(s) + ")";
+            o << "    for (int s = " << s << "; s < " << s + run << "; ++s) {\n";
+            if (!emit_slot(E, s, pc, tg)) return std::string();
+            o << "    }\n";
+            E.sidx.clear();
+            E.fx.clear();
+            s += run;
+        } else {
+            if (!emit_slot(E, s, pc, tg)) return std::string();
+            ++s;
+        }
     }
     std::string body = o.str();
     if (!uniform_parent) {

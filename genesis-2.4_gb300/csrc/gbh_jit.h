@@ -17,9 +17,11 @@ struct JitKernel {
 // CUDA source of the step kernel specialised to one tile type; empty if the
 // program holds an op the generator does not emit. uniform_parent: the tree
 // shared by every neuron of the type (elimination unrolled in registers), or
-// null (per-neuron trees, shared-memory columns).
+// null (per-neuron trees, shared-memory columns). compact: runs of identical
+// compartment programs become loops and the rows stay in shared memory
+// (smaller code; the autotuner decides which form runs).
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent, int min_blocks = 4);
+                       const std::vector<int> *uniform_parent, int min_blocks = 4, bool compact = false);
 
 bool jit_available(std::string *why);
 int jit_compile(const std::string &src, bool fp64_exact, int device_major, int device_minor, JitKernel *out,

@@ -73,7 +73,7 @@ class GbhStats(C.Structure):
                 ("tiles", C.c_int64), ("launches", C.c_int64), ("bytes_per_step", C.c_double),
                 ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int),
                 ("jit_kernels", C.c_int), ("jit_min_blocks", C.c_int),
-                ("grad_forward_ms", C.c_double), ("grad_reverse_ms", C.c_double)]
+                ("grad_forward_ms", C.c_double), ("grad_reverse_ms", C.c_double), ("jit_compact", C.c_int)]
 
 
 EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
@@ -102,7 +102,7 @@ def load(build_if_missing: bool = True):
     lib.gbh_create.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhSynapses), C.POINTER(GbhOptions),
                                C.POINTER(GbhError)]
     lib.gbh_jit_source.restype = C.c_int64
-    lib.gbh_jit_source.argtypes = [C.POINTER(GbhBatchDesc), C.c_int, C.c_int, C.c_char_p, C.c_int64]
+    lib.gbh_jit_source.argtypes = [C.POINTER(GbhBatchDesc), C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_int64]
     lib.gbh_validate.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhError), _lp, _lp]
     lib.gbh_run.argtypes = [C.c_void_p, C.c_int]
     lib.gbh_run_async.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
@@ -254,15 +254,15 @@ def validate(solvers: Sequence):
     return nn.value, nt.value
 
 
-def jit_source(solvers: Sequence, precision: int = PREC_FP64, type_index: int = 0) -> str:
+def jit_source(solvers: Sequence, precision: int = PREC_FP64, type_index: int = 0, compact: bool = False) -> str:
     """CUDA source generated for one tile type (host only, no GPU)."""
     lib = load()
     b = Batch(solvers)
-    n = lib.gbh_jit_source(C.byref(b.desc), precision, type_index, None, 0)
+    n = lib.gbh_jit_source(C.byref(b.desc), precision, type_index, int(compact), None, 0)
     if n < 0:
         raise RuntimeError("gbh_jit_source failed: %s" % lib.gbh_last_error().decode())
     buf = C.create_string_buffer(int(n) + 1)
-    lib.gbh_jit_source(C.byref(b.desc), precision, type_index, buf, int(n) + 1)
+    lib.gbh_jit_source(C.byref(b.desc), precision, type_index, int(compact), buf, int(n) + 1)
     return buf.value.decode()
 
 
@@ -274,8 +274,9 @@ class Engine:
                  use_graph: bool = False):
         self.lib = load()
         self.batch = Batch(solvers, synapses)
-        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device,
-                         0 if jit else -1)
+        # jit: True (autotuned forms), False (interpreter), or the ABI value
+        jit_v = (0 if jit else -1) if isinstance(jit, bool) else int(jit)
+        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device, jit_v)
         err = GbhError()
         h = self.lib.gbh_create(C.byref(self.batch.desc),
                                 C.byref(self.batch.syn) if self.batch.syn is not None else None,

@@ -117,8 +117,11 @@ typedef struct gbh_options {
     int warps_per_block; /* 0 = autotune                                      */
     int use_graph;       /* capture multi-launch runs in a CUDA graph         */
     int device;          /* CUDA device ordinal                                */
-    int jit;             /* 0 = specialise each neuron program at setup (NVRTC)
-                            when available, -1 = interpret the programs only   */
+    int jit;             /* 0 = specialise each tile type's program at setup
+                            (NVRTC) in both forms -- unrolled straight-line and
+                            compact (runs of identical compartments looped) --
+                            and let the autotuner pick; 1 = unrolled form only;
+                            2 = compact form only; -1 = interpret the programs */
 } gbh_options;
 
 typedef struct gbh_stats {
@@ -138,6 +141,8 @@ typedef struct gbh_stats {
                                   pass (device time, CUDA events)             */
     double grad_reverse_ms;    /* last gbh_loss_gradient: segment recomputation
                                   + adjoint steps (device time)               */
+    int jit_compact;           /* the chosen specialised variant is the compact
+                                  (looped) form                               */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
@@ -160,7 +165,8 @@ int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons,
  * truncated to buflen). Returns the full source length, or a negative error.
  * Needs no GPU.
  */
-int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, char *buf, int64_t buflen);
+int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, int compact, char *buf,
+                       int64_t buflen);
 
 /* Advances every solver by nsteps PROCESS steps. Returns GBH_OK or an error. */
 int gbh_run(gbh_engine *e, int nsteps);

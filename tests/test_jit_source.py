@@ -49,10 +49,23 @@ def _models():
     yield "network", [model.build(m) for m in ms]
 
 
+@pytest.mark.parametrize("compact", [False, True])
 @pytest.mark.parametrize("prec", [engine.PREC_FP64, engine.PREC_MIXED])
 @pytest.mark.parametrize("name,hs", list(_models()))
-def test_generated_kernel_compiles(name, hs, prec):
-    src = engine.jit_source(hs, precision=prec, type_index=0)
+def test_generated_kernel_compiles(name, hs, prec, compact):
+    src = engine.jit_source(hs, precision=prec, type_index=0, compact=compact)
     assert "gbh_jit" in src
     rc, log = compile_sm103a(src, prec == engine.PREC_FP64)
     assert rc == 0, log[:4000]
+
+
+def test_compact_form_loops_identical_compartments():
+    """The identical dendrites of a cable (all but the first, which holds the
+    K channel's Ek) become one loop in the compact form; the unrolled form
+    has none."""
+    hs = configs.cables_replicated(4, gk_dend=36.0)[0]
+    loop = engine.jit_source(hs, precision=engine.PREC_MIXED, compact=True)
+    flat = engine.jit_source(hs, precision=engine.PREC_MIXED, compact=False)
+    assert "for (int s = 1; s < 15; ++s)" in loop
+    assert "for (int s = " not in flat
+    assert len(loop) < len(flat) / 3
