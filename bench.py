@@ -480,7 +480,7 @@ def main():
     peak, peak_kind = peaks()
     r = results["mixed"]
     launch_ms = r["ms"] / max(r["launches"], 1)
-    units = M * r["spl"]
+    units = M * args.steps / max(r["launches"], 1)     # compartment-steps one launch processes
     achieved = ALG_BYTES["mixed"] * units / (launch_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(REPO, "profiles", "k_steps_traffic.json")

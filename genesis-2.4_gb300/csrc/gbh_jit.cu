@@ -553,7 +553,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
           << "    double Ek = 0.0, Gk = 0.0, gmax = 0.0; (void)gmax;\n";
     }
     o << "    double GHK = 0.0, Ik = 0.0; int doGHK = 0, sel = 0; (void)GHK; (void)doGHK; (void)sel; (void)Ik;\n";
-    if (uniform_parent) o << "    double D[" << S << "], R[" << S << "];\n";
+    if (uniform_parent) o << "    double D[" << S << "], R[" << S << "], T[" << S << "]; (void)T;\n";
     else o << "    double *D = nullptr, *R = nullptr; (void)D; (void)R;\n";
     std::ostringstream save;
     // slot extents in the program
@@ -591,6 +591,31 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
             s += run;
         } else {
             if (!emit_slot(E, s, pc, tg)) return std::string();
+            if (uniform_parent) {
+                // forward elimination fused into the channel phase: row s pulls
+                // its children (ascending, the order the separate sweep pushes
+                // them in, so the arithmetic is unchanged) and prepares its own
+                // factor for its parent; its FP64 work overlaps the next
+                // compartment's channel arithmetic
+                const std::vector<int> &par = *uniform_parent;
+                o << "    {";
+                for (int c = 0; c < s; ++c) {
+                    if (par[c] != s) continue;
+                    if (mixed)
+                        o << " D[" << s << "] = fma(-Bw[" << c * LANES << "], T[" << c << "], D[" << s << "]); R[" << s
+                          << "] = fma(-R[" << c << "], T[" << c << "], R[" << s << "]);";
+                    else
+                        o << " D[" << s << "] -= Bw[" << c * LANES << "] * T[" << c << "]; R[" << s << "] -= R[" << c
+                          << "] * T[" << c << "];";
+                }
+                if (mixed) {
+                    o << " const double ri = rcp_newton(D[" << s << "]); D[" << s << "] = ri;";
+                    if (par[s] >= 0) o << " T[" << s << "] = Aw[" << s * LANES << "] * ri;";
+                } else if (par[s] >= 0) {
+                    o << " T[" << s << "] = Aw[" << s * LANES << "] / D[" << s << "];";
+                }
+                o << " }\n";
+            }
             ++s;
         }
     }
@@ -630,20 +655,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     auto Dx = [&](int s) { return uniform_parent ? "D[" + std::to_string(s) + "]" : "Dc[" + std::to_string(s * LANES) + "]"; };
     auto Rx = [&](int s) { return uniform_parent ? "R[" + std::to_string(s) + "]" : "Rc[" + std::to_string(s * LANES) + "]"; };
     if (uniform_parent) {
-        const std::vector<int> &par = *uniform_parent;
-        for (int s = 0; s < S; ++s) {
-            const int p = par[s];
-            if (mixed) {
-                t << "    { const double ri = rcp_newton(" << Dx(s) << "); " << Dx(s) << " = ri;";
-                if (p >= 0)
-                    t << " const double temp = Aw[" << s * LANES << "] * ri; " << Dx(p) << " = fma(-Bw[" << s * LANES
-                      << "], temp, " << Dx(p) << "); " << Rx(p) << " = fma(-" << Rx(s) << ", temp, " << Rx(p) << ");";
-                t << " }\n";
-            } else if (p >= 0) {
-                t << "    { const double temp = Aw[" << s * LANES << "] / " << Dx(s) << "; " << Dx(p) << " -= Bw["
-                  << s * LANES << "] * temp; " << Rx(p) << " -= " << Rx(s) << " * temp; }\n";
-            }
-        }
+        const std::vector<int> &par = *uniform_parent;   // forward sweep already fused above
         for (int s = S - 1; s >= 0; --s) {
             const int p = par[s];
             t << "    { double r = " << Rx(s) << ";";
