@@ -119,13 +119,25 @@ __device__ __forceinline__ float d2f_trunc_bits(double d)
     return __uint_as_float(bits);
 }
 
-// double -> df with one FP64 add: hi = d truncated to 24 bits, lo = the rest
+// double -> df on the integer pipe: hi = d truncated to 24 significant bits,
+// lo = the next 24 bits of the significand, truncated (|d - hi - lo| <
+// 2^-47 |d|); no FP64 instruction. Values whose hi or lo falls outside the
+// float normal range lose that part (flush to signed zero).
 __device__ __forceinline__ df d2df(double d)
 {
     const uint32_t h = (uint32_t)__double2hiint(d);
-    const uint32_t l = (uint32_t)__double2loint(d) & 0xe0000000u;
-    const double dh = __hiloint2double((int)h, (int)l);
-    return df_make(d2f_trunc_bits(dh), d2f_trunc_bits(d - dh));
+    const uint32_t l = (uint32_t)__double2loint(d);
+    const float fh = d2f_trunc_bits(d);
+    const uint32_t r = l & 0x1fffffffu;
+    const int e = (int)((h >> 20) & 0x7ffu);
+    const int p = 31 - __clz((int)r);
+    const int fe = p + e - 948;
+    uint32_t lo = 0u;
+    if (r != 0u && fe > 0 && e - 896 > 0 && e - 896 < 255) {
+        const uint32_t m = p >= 23 ? (r >> (p - 23)) : (r << (23 - p));
+        lo = (h & 0x80000000u) | ((uint32_t)fe << 23) | (m & 0x7fffffu);
+    }
+    return df_make(fh, __uint_as_float(lo));
 }
 
 // df -> double: exact conversions, one FP64 add
@@ -145,5 +157,6 @@ __device__ __forceinline__ double rcp_newton(double d)
     const double err = fma(-d, r, 1.0);
     return fma(r, err, r);
 }
+
 
 }  // namespace gbh

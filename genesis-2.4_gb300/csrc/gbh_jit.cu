@@ -243,7 +243,7 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
         case M_END:
             if (mx) {
                 o << "      { const df tbyc = ld_df(" << E.pP(a[0]) << "); const df dv = df_mul(ichan, tbyc);\n"
-                  << "        R[" << E.S(s) << "] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);\n"
+                  << "        R[" << E.S(s) << "] = df2d(df_add(vmd, dv));\n"
                   << "        D[" << E.S(s) << "] = df2d(df_add(df_mul(sumg, tbyc), ld_df(" << E.pP(a[1]) << "))); }\n";
             } else {
                 o << "      { const double tbyc = " << E.P(a[0]) << "; R[" << E.S(s) << "] = Vm + ichan * tbyc; D[" << E.S(s)

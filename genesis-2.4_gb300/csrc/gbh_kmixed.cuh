@@ -131,7 +131,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
                 } else if (code == M_END) {
                     const df tbyc = ld_df(&Pw[pc[1] * LANES]);
                     const df dv = df_mul(ichan, tbyc);
-                    Rcol[s * LANES] = (Vm + f2d_bits(dv.hi)) + f2d_bits(dv.lo);
+                    Rcol[s * LANES] = df2d(df_add(vmd, dv));
                     Dcol[s * LANES] = df2d(df_add(df_mul(sumg, tbyc), ld_df(&Pw[pc[2] * LANES])));
                     if (GIV) Gw[pc[3] * LANES] = Im;
                     pc += 4;
