@@ -33,6 +33,7 @@ struct DevView {
     const int64_t *syn_out_base;   // ring base of the target synchan (lane folded in)
     const int *syn_out_delay;      // effective delay in steps
     unsigned long long *spikes;    // per-neuron spike counter
+    unsigned *spiked;              // per-neuron bit: spiked since the host last read it
     const double *stablist;        // synchan constants (shared by the batch)
     int *status;
     double dt;

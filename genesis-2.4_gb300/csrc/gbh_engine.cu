@@ -106,6 +106,12 @@ struct gbh_engine {
     DBuf<int64_t> d_out_start, d_out_base;
     DBuf<int> d_out_delay;
     DBuf<unsigned long long> d_spikes;
+    // partitioned networks: spikes recorded per neuron, remote-source synapses
+    DBuf<unsigned> d_spiked;
+    int nremote = 0;
+    DBuf<int64_t> d_rstart, d_rbase;
+    DBuf<int> d_rdelay;
+    DBuf<unsigned char> d_rbits;
     DBuf<int> d_status;
     int ring_len = 2;
     int64_t rows_fld = 0, rows_int = 0, rows_pool = 0, rows_giv = 0, rows_vm = 0, rows_topo = 0,
@@ -270,7 +276,8 @@ void build_tables(const gbh_batch_desc *d, std::vector<TableGeom> &tg, std::vect
     }
 }
 
-int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn, gbh_error *err)
+int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn, const gbh_remote_synapses *remote,
+                 gbh_error *err)
 {
     Decoded &dec = e->dec;
     const int nneu = (int)dec.neurons.size();
@@ -306,15 +313,23 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         members[it->second].push_back(i);
     }
     // ---- event ring length from the synapse delays ----
-    e->has_network = syn && syn->nsynapses > 0;
+    const bool local_syn = syn && syn->nsynapses > 0;
+    const int64_t nrsyn = (remote && remote->nsources > 0) ? remote->src_start[remote->nsources] : 0;
+    e->has_network = local_syn || nrsyn > 0 || (remote && remote->nsources > 0);
     int maxd = 1;
-    if (e->has_network) {
+    if (local_syn) {
         for (int64_t s = 0; s < syn->nsynapses; ++s) {
             if (syn->delay_steps[s] < 1)
                 return fail_err(err, GBH_ERR_UNSUPPORTED, "synapse %lld has a delay below one step",
                                 (long long)s);
             maxd = std::max(maxd, syn->delay_steps[s] + 1);
         }
+    }
+    for (int64_t k = 0; k < nrsyn; ++k) {
+        if (remote->delay_steps[k] < 1)
+            return fail_err(err, GBH_ERR_UNSUPPORTED, "remote synapse %lld has a delay below one step",
+                            (long long)k);
+        maxd = std::max(maxd, remote->delay_steps[k]);
     }
     e->ring_len = maxd + 1;
     // ---- tiles: types ordered by slot count (descending) ----
@@ -408,7 +423,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             if (dec.neurons[i].spike_op >= 0) src_neuron[dec.neurons[i].solver] = i;
         std::vector<std::vector<std::pair<int64_t, int>>> per(gneuron);
         std::unordered_map<int64_t, double> wset;
-        for (int s = 0; s < e->nsolvers; ++s) {
+        for (int s = 0; s < e->nsolvers && local_syn; ++s) {
             for (int64_t k = syn->src_start[s]; k < syn->src_start[s + 1]; ++k) {
                 if (src_neuron[s] < 0)
                     return fail_err(err, GBH_ERR_ARG, "synapse %lld leaves solver %d, which has no spikegen",
@@ -448,6 +463,38 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 out_base.push_back(pr.first);
                 out_delay.push_back(pr.second);
             }
+        }
+        // synapses from remote sources: ring bases and effective delays, the
+        // same uniform-weight rule per target synchan
+        if (remote && remote->nsources > 0) {
+            e->nremote = remote->nsources;
+            std::vector<int64_t> rbase;
+            std::vector<int> rdelay;
+            for (int64_t k = 0; k < nrsyn; ++k) {
+                const int ts = remote->target_solver[k];
+                if (ts < 0 || ts >= e->nsolvers)
+                    return fail_err(err, GBH_ERR_ARG, "remote synapse %lld targets solver %d", (long long)k, ts);
+                auto it = syn_at.find((int64_t)ts * (1LL << 32) + remote->target_op[k]);
+                if (it == syn_at.end())
+                    return fail_err(err, GBH_ERR_ARG, "remote synapse %lld: ops[%d] of solver %d is not a SYN2/SYN3 op",
+                                    (long long)k, remote->target_op[k], ts);
+                const int tn = it->second.first, srow = it->second.second;
+                const double w = remote->weight[k] / e->dt;
+                const int64_t wkey = (int64_t)tn * 4096 + srow;
+                auto wi = wset.find(wkey);
+                if (wi == wset.end()) wset[wkey] = w;
+                else if (wi->second != w)
+                    return fail_err(err, GBH_ERR_UNSUPPORTED,
+                                    "synapses into one synchan (solver %d, ops[%d]) carry different weights", ts,
+                                    remote->target_op[k]);
+                const Tile &tt = e->tiles[e->neuron_tile[tn]];
+                rbase.push_back((tt.syn + (int64_t)srow * e->ring_len) * LANES + e->neuron_lane[tn]);
+                rdelay.push_back(remote->delay_steps[k]);
+            }
+            std::vector<int64_t> rstart(remote->src_start, remote->src_start + remote->nsources + 1);
+            if (e->d_rstart.upload(rstart) || e->d_rbase.upload(rbase) || e->d_rdelay.upload(rdelay) ||
+                e->d_rbits.alloc(((size_t)remote->nsources + 7) / 8))
+                return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
         }
         for (auto &kv : wset) {
             const int tn = (int)(kv.first / 4096), srow = (int)(kv.first % 4096);
@@ -508,6 +555,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_out_base.upload(out_base);
     rc |= e->d_out_delay.upload(out_delay);
     rc |= e->d_spikes.upload(std::vector<unsigned long long>(gneuron + 1, 0ULL));
+    if (e->has_network) rc |= e->d_spiked.upload(std::vector<unsigned>((gneuron + 31) / 32 + 1, 0u));
     rc |= e->d_status.upload(std::vector<int>(1, 0));
     if (rc) return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
 
@@ -653,6 +701,7 @@ DevView view_of(gbh_engine *e)
     v.syn_out_base = e->d_out_base.p;
     v.syn_out_delay = e->d_out_delay.p;
     v.spikes = e->d_spikes.p;
+    v.spiked = e->has_network ? e->d_spiked.p : nullptr;
     v.stablist = e->d_stab.p;
     v.status = e->d_status.p;
     v.dt = e->dt;
@@ -880,6 +929,7 @@ int autotune_trials(gbh_engine *e)
         }
     }
     for (Save &s : saves) cudaFree(s.dst);
+    if (e->d_spiked.p) CK(cudaMemset(e->d_spiked.p, 0, e->d_spiked.n * sizeof(unsigned)));   // trial spikes
     for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
     e->jit_choice = best_v;
     e->steps_per_launch = best_s;
@@ -922,6 +972,20 @@ __global__ void k_scatter_inputs(const double *vals, const int64_t *start, const
         } else {
             P[a] = v;
         }
+    }
+}
+
+// Events of remote spikes: source i spiked during step `step`; each of its
+// synapses adds one event to its target synchan's ring slot for the step
+// the spike acts in.
+__global__ void k_deliver_remote(const unsigned char *bits, int n, const int64_t *start, const int64_t *base,
+                                 const int *delay, unsigned *ring, int ring_len, long long step)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !(bits[i >> 3] & (1u << (i & 7)))) return;
+    for (int64_t k = start[i]; k < start[i + 1]; ++k) {
+        const int slot = (int)((step + delay[k]) % ring_len);
+        atomicAdd(&ring[base[k] + (int64_t)slot * LANES], 1u);
     }
 }
 
@@ -1097,6 +1161,12 @@ int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons,
 gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_options *opt,
                        gbh_error *err)
 {
+    return gbh_create_dist(desc, syn, nullptr, opt, err);
+}
+
+gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
+                            const gbh_options *opt, gbh_error *err)
+{
     gbh_error local{};
     if (!err) err = &local;
     memset(err, 0, sizeof(*err));
@@ -1129,7 +1199,7 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     e->rav_start.assign(desc->ravals_start, desc->ravals_start + ns + 1);
     e->chip_orig.assign(desc->chip, desc->chip + desc->chip_start[ns]);
     e->ops_orig.assign(desc->ops, desc->ops + desc->ops_start[ns]);
-    rc = build_layout(e, desc, syn, err);
+    rc = build_layout(e, desc, syn, remote, err);
     if (rc) {
         gbh_destroy(e);
         return nullptr;
@@ -1302,6 +1372,40 @@ int gbh_get_givals(gbh_engine *e, double *givals)
         for (size_t r = 0; r < N.giv_ref.size(); ++r)
             givals[e->giv_start[N.solver] + N.giv_ref[r]] = Gv[(t.giv + r) * L + l];
     }
+    return GBH_OK;
+}
+
+int gbh_get_spiked(gbh_engine *e, uint8_t *solver_bits)
+{
+    if (!e || !solver_bits) return GBH_ERR_ARG;
+    memset(solver_bits, 0, ((size_t)e->nsolvers + 7) / 8);
+    if (!e->has_network) return GBH_OK;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<unsigned> w(e->d_spiked.n);
+    if (!w.empty()) CK(cudaMemcpy(w.data(), e->d_spiked.p, w.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    CK(cudaMemsetAsync(e->d_spiked.p, 0, e->d_spiked.n * sizeof(unsigned), e->stream));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        if (N.spike_op < 0) continue;
+        const int64_t g = e->tiles[e->neuron_tile[i]].first_neuron + e->neuron_lane[i];
+        if (w[g >> 5] & (1u << (g & 31))) solver_bits[N.solver >> 3] |= (uint8_t)(1u << (N.solver & 7));
+    }
+    return GBH_OK;
+}
+
+int gbh_deliver_remote(gbh_engine *e, const uint8_t *source_bits)
+{
+    if (!e || !source_bits) return GBH_ERR_ARG;
+    if (e->nremote == 0) return GBH_OK;
+    if (e->step < 1) return fail_err(nullptr, GBH_ERR_ARG, "gbh_deliver_remote before the first step");
+    const size_t nb = ((size_t)e->nremote + 7) / 8;
+    CK(cudaMemcpyAsync(e->d_rbits.p, source_bits, nb, cudaMemcpyHostToDevice, e->stream));
+    const int threads = 256, blocks = (e->nremote + threads - 1) / threads;
+    k_deliver_remote<<<blocks, threads, 0, e->stream>>>(e->d_rbits.p, e->nremote, e->d_rstart.p, e->d_rbase.p,
+                                                        e->d_rdelay.p, e->d_ring.p, e->ring_len, e->step - 1);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));   // the host bitmap may be reused on return
+    e->stats.launches++;
     return GBH_OK;
 }
 
@@ -1702,6 +1806,7 @@ void gbh_destroy(gbh_engine *e)
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
+    e->d_spiked.release(); e->d_rstart.release(); e->d_rbase.release(); e->d_rdelay.release(); e->d_rbits.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);

@@ -221,7 +221,8 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
               << "          for (int64_t e = e0; e < e1; ++e) {\n"
               << "            const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);\n"
               << "            atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * 32], 1u); }\n"
-              << "          v.spikes[neuron] += 1ULL; cnt = " << E.I(a[2]) << "; }\n"
+              << "          v.spikes[neuron] += 1ULL; if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));"
+              << " cnt = " << E.I(a[2]) << "; }\n"
               << "        " << E.I(a[1]) << " = cnt; }\n";
             break;
         case M_ELMMPUMP:

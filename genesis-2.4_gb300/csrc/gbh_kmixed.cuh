@@ -106,6 +106,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
                                 atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
                             }
                             v.spikes[neuron] += 1ULL;
+                            if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
                             cnt = Iw[pc[3] * LANES];
                         }
                     }

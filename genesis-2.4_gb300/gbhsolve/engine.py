@@ -58,6 +58,11 @@ class GbhSynapses(C.Structure):
                 ("target_op", _ip), ("weight", _dp), ("delay_steps", _ip)]
 
 
+class GbhRemoteSynapses(C.Structure):
+    _fields_ = [("nsources", C.c_int), ("src_start", _lp), ("target_solver", _ip), ("target_op", _ip),
+                ("weight", _dp), ("delay_steps", _ip)]
+
+
 class GbhOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("steps_per_launch", C.c_int),
                 ("warps_per_block", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
@@ -79,7 +84,8 @@ class GbhStats(C.Structure):
 EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
-            "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient"]
+            "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
+            "gbh_get_spiked", "gbh_deliver_remote"]
 
 _LIB = None
 
@@ -119,6 +125,11 @@ def load(build_if_missing: bool = True):
     lib.gbh_destroy.argtypes = [C.c_void_p]
     lib.gbh_last_error.restype = C.c_char_p
     lib.gbh_run_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.gbh_create_dist.restype = C.c_void_p
+    lib.gbh_create_dist.argtypes = [C.POINTER(GbhBatchDesc), C.POINTER(GbhSynapses), C.POINTER(GbhRemoteSynapses),
+                                    C.POINTER(GbhOptions), C.POINTER(GbhError)]
+    lib.gbh_get_spiked.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
+    lib.gbh_deliver_remote.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
     lib.gbh_loss_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(GbhLossSpec), _dp, _dp, _dp, _dp]
     _LIB = lib
     return lib
@@ -271,16 +282,25 @@ class Engine:
 
     def __init__(self, solvers: Sequence, synapses: Optional[dict] = None, precision: int = PREC_FP64,
                  steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0, jit: bool = True,
-                 use_graph: bool = False):
+                 use_graph: bool = False, remote: Optional[dict] = None):
         self.lib = load()
         self.batch = Batch(solvers, synapses)
         # jit: True (autotuned forms), False (interpreter), or the ABI value
         jit_v = (0 if jit else -1) if isinstance(jit, bool) else int(jit)
         opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device, jit_v)
         err = GbhError()
-        h = self.lib.gbh_create(C.byref(self.batch.desc),
-                                C.byref(self.batch.syn) if self.batch.syn is not None else None,
-                                C.byref(opt), C.byref(err))
+        syn_p = C.byref(self.batch.syn) if self.batch.syn is not None else None
+        if remote is None:
+            h = self.lib.gbh_create(C.byref(self.batch.desc), syn_p, C.byref(opt), C.byref(err))
+        else:
+            self._remote = {k: np.ascontiguousarray(remote[k], dtype=t) for k, t in
+                            (("src_start", np.int64), ("target_solver", np.int32), ("target_op", np.int32),
+                             ("weight", np.float64), ("delay_steps", np.int32))}
+            r = self._remote
+            self.nremote = len(r["src_start"]) - 1
+            rs = GbhRemoteSynapses(self.nremote, _ptr(r["src_start"], _lp), _ptr(r["target_solver"], _ip),
+                                   _ptr(r["target_op"], _ip), _ptr(r["weight"], _dp), _ptr(r["delay_steps"], _ip))
+            h = self.lib.gbh_create_dist(C.byref(self.batch.desc), syn_p, C.byref(rs), C.byref(opt), C.byref(err))
         if not h:
             raise EngineError(err)
         self.h = h
@@ -371,6 +391,19 @@ class Engine:
         self._check(self.lib.gbh_loss_gradient(self.h, int(nsteps), int(checkpoint_every), C.byref(spec),
                                                C.byref(loss), _ptr(dchip, _dp), _ptr(drav, _dp), _ptr(dvm, _dp)))
         return loss.value, dchip, drav, dvm
+
+    def get_spiked(self) -> np.ndarray:
+        """gbh_get_spiked: bool per local solver, spiked since the last call."""
+        n = self.batch.n
+        bits = np.zeros((n + 7) // 8, dtype=np.uint8)
+        self._check(self.lib.gbh_get_spiked(self.h, bits.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return np.unpackbits(bits, bitorder="little")[:n].astype(bool)
+
+    def deliver_remote(self, spiked_sources) -> None:
+        """gbh_deliver_remote: bool per remote source, spiked in the step just run."""
+        bits = np.packbits(np.asarray(spiked_sources, dtype=bool), bitorder="little")
+        bits = np.ascontiguousarray(bits, dtype=np.uint8)
+        self._check(self.lib.gbh_deliver_remote(self.h, bits.ctypes.data_as(C.POINTER(C.c_uint8))))
 
     def spike_counts(self) -> np.ndarray:
         c = np.zeros(self.batch.n, dtype=np.int64)

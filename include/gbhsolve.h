@@ -108,6 +108,25 @@ typedef struct gbh_synapses {
     const int *delay_steps;    /* [nsynapses]  */
 } gbh_synapses;
 
+/*
+ * Synapses from sources outside this engine (cells simulated by other ranks
+ * of a partitioned network). Sources are numbered by the caller (for
+ * example by their global cell index); CSR over sources. Each synapse
+ * targets the SYN2_OP (target_op, ops[] index within target_solver) of a
+ * local solver. delay_steps is the effective delay: a spike of the source
+ * during step s acts in step s + delay_steps (>= 1). With the reference's
+ * sequential solver order this is (int)(delay/dt + 0.9), plus 1 when the
+ * target's solver precedes the source's in the global order.
+ */
+typedef struct gbh_remote_synapses {
+    int nsources;
+    const int64_t *src_start;  /* [nsources+1] */
+    const int *target_solver;  /* local solver */
+    const int *target_op;
+    const double *weight;
+    const int *delay_steps;
+} gbh_remote_synapses;
+
 typedef struct gbh_options {
     int precision;       /* GBH_PREC_FP64 or GBH_PREC_MIXED                  */
     int steps_per_launch;/* 0 = autotune: gbh_create times trial steps on a saved
@@ -150,6 +169,27 @@ typedef struct gbh_engine gbh_engine;
 /* Builds the device engine; returns NULL and fills *err on failure. */
 gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn,
                        const gbh_options *opt, gbh_error *err);
+
+/*
+ * gbh_create with synapses from remote sources (a partitioned network: one
+ * engine per rank). The caller exchanges spikes between steps:
+ *   gbh_run(e, 1);
+ *   gbh_get_spiked(e, mine);          -- local solvers that spiked
+ *   (all-gather the bitmaps across ranks)
+ *   gbh_deliver_remote(e, theirs);    -- remote sources that spiked
+ * No counterpart in the reference (PGENESIS exchanges through messages).
+ */
+gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
+                            const gbh_remote_synapses *remote, const gbh_options *opt, gbh_error *err);
+
+/* Local solvers with a spikegen that spiked since the previous call, one bit
+ * per solver (bit i of byte i/8), ceil(nsolvers/8) bytes; clears the record. */
+int gbh_get_spiked(gbh_engine *e, uint8_t *solver_bits);
+
+/* Remote sources that spiked during the step just run, one bit per source
+ * (ceil(nsources/8) bytes, host memory): their synapses' events are placed
+ * for step (step just run) + delay_steps. Call before the next step. */
+int gbh_deliver_remote(gbh_engine *e, const uint8_t *source_bits);
 
 /*
  * Runs only the host-side decoder (no GPU needed): checks that every opcode

@@ -634,7 +634,7 @@ struct orc_net {
     orc_solver **sv;
     const int *syn_start, *tgt_solver, *tgt_child, *tgt_op, *delay;
     const double *weight;
-    int nsyn;               /* synchan table */
+    int nsyn, cap_syn;      /* synchan table and its capacity */
     orc_synchan *syn;
     int *syn_of_synapse;    /* synapse -> synchan table index */
     long long step;
@@ -648,6 +648,10 @@ static int orc_find_synchan(orc_net *n, int solver, int child, int op)
     int i;
     for (i = 0; i < n->nsyn; i++)
         if (n->syn[i].solver == solver && n->syn[i].child == child) return i;
+    if (n->nsyn == n->cap_syn) {
+        n->cap_syn = 2 * n->cap_syn + 8;
+        n->syn = (orc_synchan *)realloc(n->syn, (size_t)n->cap_syn * sizeof(orc_synchan));
+    }
     n->syn[n->nsyn].solver = solver;
     n->syn[n->nsyn].child = child;
     n->syn[n->nsyn].op = op;
@@ -719,7 +723,8 @@ orc_net *orc_net_create(int nsolvers, orc_solver **solvers, const int *syn_start
     n->weight = syn_weight;
     n->delay = syn_delay_steps;
     n->process = orc_process;
-    n->syn = (orc_synchan *)calloc(nsynapses + 1, sizeof(orc_synchan));
+    n->cap_syn = nsynapses + 1;
+    n->syn = (orc_synchan *)calloc(n->cap_syn, sizeof(orc_synchan));
     n->syn_of_synapse = (int *)calloc(nsynapses + 1, sizeof(int));
     for (e = 0; e < nsynapses; e++)
         n->syn_of_synapse[e] = orc_find_synchan(n, syn_target_solver[e], syn_target_child[e],
@@ -761,5 +766,27 @@ int orc_net_run(orc_net *n, int nsteps, long long *spike_counts)
 }
 
 long long orc_net_step_count(const orc_net *n) { return n->step; }
+
+/* Events from spikes outside the network (other ranks of a partitioned run),
+ * added after a step: event k acts on the synchan (tgt_solver, tgt_child,
+ * op tgt_op) in step fire_step (> the step just run), with weight w. Queue
+ * order and countdown as orc_net_on_spike, counted from the next step. */
+void orc_net_deliver(orc_net *n, int count, const int *tgt_solver, const int *tgt_child, const int *tgt_op,
+                     const double *w, const long long *fire_step)
+{
+    int k;
+    for (k = 0; k < count; k++) {
+        orc_synchan *sc = &n->syn[orc_find_synchan(n, tgt_solver[k], tgt_child[k], tgt_op[k])];
+        orc_solver *t = n->sv[sc->solver];
+        orc_event *ev = (orc_event *)malloc(sizeof(orc_event));
+        orc_event **pp = &sc->head;
+        ev->fire_step = fire_step[k];
+        ev->weight = w[k];
+        while (*pp && (*pp)->fire_step < fire_step[k]) pp = &(*pp)->next;
+        ev->next = *pp;
+        *pp = ev;
+        if (sc->head == ev) t->ops[sc->op + 2] = (int)(fire_step[k] - n->step);
+    }
+}
 
 void orc_net_set_process(orc_net *n, int (*process)(orc_solver *)) { n->process = process; }

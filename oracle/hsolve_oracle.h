@@ -115,6 +115,8 @@ int orc_net_run(orc_net *n, int nsteps, long long *spike_counts);
 void orc_net_set_process(orc_net *n, int (*process)(orc_solver *));
 /* Number of steps executed so far. */
 long long orc_net_step_count(const orc_net *n);
+void orc_net_deliver(orc_net *n, int count, const int *tgt_solver, const int *tgt_child, const int *tgt_op,
+                     const double *w, const long long *fire_step);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,9 @@ def _lib(which: str):
             lib.orc_net_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]
             lib.orc_net_destroy.argtypes = [C.c_void_p]
             lib.orc_net_set_process.argtypes = [C.c_void_p, C.c_void_p]
+            lib.orc_net_deliver.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(C.c_longlong)]
+            lib.orc_net_step_count.restype = C.c_longlong
+            lib.orc_net_step_count.argtypes = [C.c_void_p]
         else:
             lib.ref_process.argtypes = [C.POINTER(OrcSolver)]
             lib.ref_run.argtypes = [C.POINTER(OrcSolver), C.c_int]
@@ -197,6 +200,19 @@ class Network:
                                   self.spikes.ctypes.data_as(C.POINTER(C.c_longlong)))
         if rc != 0:
             raise RuntimeError("network step failed")
+
+    @property
+    def step(self) -> int:
+        return int(self.lib.orc_net_step_count(self.net))
+
+    def deliver(self, tgt_solver, tgt_child, tgt_op, weight, fire_step) -> None:
+        """Events from outside the network (orc_net_deliver)."""
+        a = [np.ascontiguousarray(x, dtype=np.int32) for x in (tgt_solver, tgt_child, tgt_op)]
+        w = np.ascontiguousarray(weight, dtype=np.float64)
+        f = np.ascontiguousarray(fire_step, dtype=np.int64)
+        if len(w):
+            self.lib.orc_net_deliver(self.net, len(w), _p(a[0], _ip), _p(a[1], _ip), _p(a[2], _ip), _p(w, _dp),
+                                     f.ctypes.data_as(C.POINTER(C.c_longlong)))
 
     def __del__(self):
         try:
