@@ -14,7 +14,9 @@ step over all compartments (channel program, elimination, Vm update).
            against the FP64 CPU oracle over 10,000 steps of a neuron sample
   e2e      the same metric through the C ABI with host buffers: every step
            copies the per-neuron inject currents host->device (h_in_msgs) and
-           the somatic Vm of every neuron device->host (h_out_msgs)
+           the somatic Vm of every neuron device->host (h_out_msgs), through
+           gbh_step_io (the copies run on their own stream and overlap the
+           neighbouring steps); `e2e.serial` is the same I/O on one stream
   roofline HBM roofline of the step kernel (algorithmic bytes per
            compartment-step x compartment-steps per launch / launch time)
 
@@ -421,40 +423,59 @@ def main():
         if form == "fp64":
             eng.close()
 
-    # end to end through the C ABI with host buffers (mixed form)
+    # end to end through the C ABI with host buffers (mixed form): every step
+    # copies the inject currents host->device and the somatic Vm of every
+    # neuron device->host. `e2e`: gbh_step_io (copies on their own stream,
+    # overlapping the neighbouring steps); `e2e_serial`: the same I/O with
+    # set_inputs_async / run_async / get_outputs_async on one stream.
     eng = results["mixed"]["eng"]
     nh = len(hs)
     eng.register_inputs(np.arange(nh, dtype=np.int32),
                         np.full(nh, int(hs[0].compchips[NCOMP - 1]) + 1, dtype=np.int64))
     eng.register_outputs(np.arange(nh, dtype=np.int32), np.full(nh, NCOMP - 1, dtype=np.int32))
-    pin_in = torch.empty(nh, dtype=torch.float64, pin_memory=True)
-    pin_out = torch.empty(nh, dtype=torch.float64, pin_memory=True)
-    pin_in.numpy()[:] = np.array([float(np.float32(x)) for x in injects])
+    inj = np.array([float(np.float32(x)) for x in injects])
+    pin_in = [torch.empty(nh, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    pin_out = [torch.empty(nh, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+    for x in pin_in:
+        x[:] = inj
     stream = torch.cuda.Stream()
-    h_in, h_out = pin_in.numpy(), pin_out.numpy()
     sh = stream.cuda_stream
-    for _ in range(args.warmup):
-        eng.set_inputs_async(h_in, sh)
+
+    def timed(loop):
+        for k in range(args.warmup):
+            loop(k)
+        eng.io_sync()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        e0.record(stream)
+        for k in range(args.steps):
+            loop(k)
+        eng.io_sync()
+        e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    def piped(k):
+        eng.step_io(pin_in[k % 3], pin_out[k % 3], 1, sh)
+
+    def serial(k):
+        eng.set_inputs_async(pin_in[0], sh)
         eng.run_async(1, sh)
-        eng.get_outputs_async(h_out, sh)
-    stream.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        eng.set_inputs_async(h_in, sh)
-        eng.run_async(1, sh)
-        eng.get_outputs_async(h_out, sh)
-    e1.record(stream)
-    stream.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+        eng.get_outputs_async(pin_out[0], sh)
+
+    e2e_ms = timed(piped)
+    e2e_serial_ms = timed(serial)
     e2e_val = M * ws * args.steps / (e2e_ms / 1e3)
+    e2e_serial = M * ws * args.steps / (e2e_serial_ms / 1e3)
+    log("e2e: %.3e cs/s pipelined, %.3e serial" % (e2e_val, e2e_serial))
     eng.close()
 
     # accuracy of the mixed form against the FP64 oracle
@@ -509,7 +530,8 @@ def main():
                                 "accuracy_sample_neurons": ACC_SAMPLE}},
             "speedup_mixed_over_fp64": r["value"] / results["fp64"]["value"],
             "e2e": {"value": e2e_val, "unit": "compartment-steps/s", "h2d_bytes_per_step": nh * 8,
-                    "d2h_bytes_per_step": nh * 8},
+                    "d2h_bytes_per_step": nh * 8, "api": "gbh_step_io (copies overlap neighbouring steps)",
+                    "serial": {"value": e2e_serial, "api": "set_inputs_async + run_async + get_outputs_async"}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "gbh_jit (specialised mixed step)", "launch_ms": launch_ms,

@@ -147,6 +147,20 @@ struct gbh_engine {
     cudaEvent_t ev_fork = nullptr;
     DBuf<long long> d_step;
     bool dstep_valid = false;
+    // pipelined per-step I/O (gbh_step_io): host->device and device->host
+    // copies each on their own stream (one FIFO would put a step's input copy
+    // behind the previous step's output copy), double-buffered staging
+    cudaStream_t io_stream = nullptr, io_out_stream = nullptr;
+    DBuf<double> d_io_in[2], d_io_out[2];
+    cudaEvent_t io_in_copied[2] = {nullptr, nullptr}, io_gathered[2] = {nullptr, nullptr},
+                io_out_copied[2] = {nullptr, nullptr};
+    long long io_calls = 0;
+    int io_nin = -1, io_nout = -1;
+    // the previous call's output gather, issued together with the next
+    // call's input scatter (one kernel between two steps)
+    double *io_pend_host = nullptr;
+    int io_pend_buf = 0;
+    cudaStream_t io_pend_stream = nullptr;
     // per-step I/O (h_in_msgs / h_out_msgs)
     int n_in = 0, n_out = 0;
     DBuf<double> d_in_vals, d_out_vals;
@@ -975,6 +989,28 @@ __global__ void k_scatter_inputs(const double *vals, const int64_t *start, const
     }
 }
 
+// Between two steps: the outputs of the step just run (gather, n_out) and
+// the inputs of the next (scatter, n_in) in one launch.
+__global__ void k_io(const double *V, const int64_t *out_addr, int n_out, double *out, const double *in_vals,
+                     const int64_t *in_start, const int64_t *in_addr, int n_in, double *P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_out) out[i] = V[out_addr[i]];
+    if (i < n_in) {
+        const double v = in_vals[i];
+        for (int64_t k = in_start[i]; k < in_start[i + 1]; ++k) {
+            const int64_t a = in_addr[k];
+            if (a & (1LL << 62)) {
+                const float hi = __double2float_rn(v);
+                const float lo = __double2float_rn(v - (double)hi);
+                *reinterpret_cast<float2 *>(&P[a & ~(1LL << 62)]) = make_float2(hi, lo);
+            } else {
+                P[a] = v;
+            }
+        }
+    }
+}
+
 // Events of remote spikes: source i spiked during step `step`; each of its
 // synapses adds one event to its target synchan's ring slot for the step
 // the spike acts in.
@@ -1083,6 +1119,98 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
                                                              e->d_out_vals.p);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(host_values, e->d_out_vals.p, e->n_out * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return GBH_OK;
+}
+
+// Issues the deferred output copy of the previous call together with this
+// call's input scatter (in_buf < 0: no input).
+static int io_between(gbh_engine *e, cudaStream_t st, int in_buf)
+{
+    const bool out = e->io_pend_host != nullptr;
+    const int n_in = in_buf >= 0 ? e->n_in : 0;
+    const int n_out = out ? e->n_out : 0;
+    const int n = std::max(n_in, n_out);
+    if (n == 0) return GBH_OK;
+    k_io<<<(n + 255) / 256, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, n_out, out ? e->d_io_out[e->io_pend_buf].p : nullptr,
+                                          in_buf >= 0 ? e->d_io_in[in_buf].p : nullptr, e->d_in_start.p,
+                                          e->d_in_addr.p, n_in, e->d_P.p);
+    CK(cudaGetLastError());
+    if (out) {
+        const int pb = e->io_pend_buf;
+        CK(cudaEventRecord(e->io_gathered[pb], st));
+        CK(cudaStreamWaitEvent(e->io_out_stream, e->io_gathered[pb], 0));
+        CK(cudaMemcpyAsync(e->io_pend_host, e->d_io_out[pb].p, e->n_out * sizeof(double), cudaMemcpyDeviceToHost,
+                           e->io_out_stream));
+        CK(cudaEventRecord(e->io_out_copied[pb], e->io_out_stream));
+        e->io_pend_host = nullptr;
+    }
+    return GBH_OK;
+}
+
+int gbh_step_io(gbh_engine *e, const double *host_in, double *host_out, int nsteps, void *stream)
+{
+    if (!e || nsteps < 0) return GBH_ERR_ARG;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    if (!e->io_stream || e->io_nin != e->n_in || e->io_nout != e->n_out) {
+        const int rc = gbh_io_sync(e);
+        if (rc) return rc;
+        if (!e->io_stream) {
+            CK(cudaStreamCreateWithFlags(&e->io_stream, cudaStreamNonBlocking));
+            CK(cudaStreamCreateWithFlags(&e->io_out_stream, cudaStreamNonBlocking));
+            for (int b = 0; b < 2; ++b) {
+                CK(cudaEventCreateWithFlags(&e->io_in_copied[b], cudaEventDisableTiming));
+                CK(cudaEventCreateWithFlags(&e->io_gathered[b], cudaEventDisableTiming));
+                CK(cudaEventCreateWithFlags(&e->io_out_copied[b], cudaEventDisableTiming));
+            }
+        }
+        for (int b = 0; b < 2; ++b) {
+            e->d_io_in[b].release();
+            e->d_io_out[b].release();
+            if (e->d_io_in[b].alloc(e->n_in) || e->d_io_out[b].alloc(e->n_out)) return GBH_ERR_CUDA;
+        }
+        e->io_nin = e->n_in;
+        e->io_nout = e->n_out;
+        e->io_calls = 0;
+    }
+    const int b = (int)(e->io_calls & 1);
+    // the buffers of the call before last are free once its output copy is done
+    if (e->io_calls >= 2) CK(cudaEventSynchronize(e->io_out_copied[b]));
+    int in_buf = -1;
+    if (e->n_in && host_in) {
+        CK(cudaMemcpyAsync(e->d_io_in[b].p, host_in, e->n_in * sizeof(double), cudaMemcpyHostToDevice, e->io_stream));
+        CK(cudaEventRecord(e->io_in_copied[b], e->io_stream));
+        CK(cudaStreamWaitEvent(st, e->io_in_copied[b], 0));
+        in_buf = b;
+    }
+    int rc = io_between(e, st, in_buf);
+    if (rc) return rc;
+    if (nsteps > 0) {
+        rc = run_steps(e, nsteps, st);
+        if (rc) return rc;
+    }
+    if (e->n_out && host_out) {
+        e->io_pend_host = host_out;   // gathered before the next call's steps
+        e->io_pend_buf = b;
+        e->io_pend_stream = st;
+    } else {
+        CK(cudaEventRecord(e->io_out_copied[b], st));
+    }
+    e->io_calls++;
+    e->stats.steps += nsteps;
+    return GBH_OK;
+}
+
+int gbh_io_sync(gbh_engine *e)
+{
+    if (!e) return GBH_ERR_ARG;
+    if (e->io_pend_host) {
+        const int rc = io_between(e, e->io_pend_stream, -1);
+        if (rc) return rc;
+    }
+    if (e->io_stream) CK(cudaStreamSynchronize(e->io_stream));
+    if (e->io_out_stream) CK(cudaStreamSynchronize(e->io_out_stream));
+    for (int b = 0; b < 2; ++b)
+        if (e->io_out_copied[b]) CK(cudaEventSynchronize(e->io_out_copied[b]));
     return GBH_OK;
 }
 
@@ -1811,6 +1939,18 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);
     if (e->cap_stream) cudaStreamDestroy(e->cap_stream);
+    for (cudaStream_t x : {e->io_stream, e->io_out_stream})
+        if (x) {
+            cudaStreamSynchronize(x);
+            cudaStreamDestroy(x);
+        }
+    for (int b = 0; b < 2; ++b) {
+        if (e->io_in_copied[b]) cudaEventDestroy(e->io_in_copied[b]);
+        if (e->io_gathered[b]) cudaEventDestroy(e->io_gathered[b]);
+        if (e->io_out_copied[b]) cudaEventDestroy(e->io_out_copied[b]);
+        e->d_io_in[b].release();
+        e->d_io_out[b].release();
+    }
     for (cudaStream_t x : e->side) cudaStreamDestroy(x);
     for (cudaEvent_t x : e->ev_join) cudaEventDestroy(x);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);

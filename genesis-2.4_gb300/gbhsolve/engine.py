@@ -85,7 +85,7 @@ EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
-            "gbh_get_spiked", "gbh_deliver_remote"]
+            "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync"]
 
 _LIB = None
 
@@ -130,6 +130,8 @@ def load(build_if_missing: bool = True):
                                     C.POINTER(GbhOptions), C.POINTER(GbhError)]
     lib.gbh_get_spiked.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
     lib.gbh_deliver_remote.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
+    lib.gbh_step_io.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_void_p]
+    lib.gbh_io_sync.argtypes = [C.c_void_p]
     lib.gbh_loss_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(GbhLossSpec), _dp, _dp, _dp, _dp]
     _LIB = lib
     return lib
@@ -371,6 +373,16 @@ class Engine:
         self._out_r = np.ascontiguousarray(row, dtype=np.int32)
         self._check(self.lib.gbh_register_outputs(self.h, len(self._out_s), _ptr(self._out_s, _ip),
                                                   _ptr(self._out_r, _ip)))
+
+    def step_io(self, host_in, host_out, nsteps: int = 1, stream_handle: int = 0):
+        """gbh_step_io: inputs, nsteps steps and outputs, copies pipelined
+        (host_out complete after the second following call or io_sync)."""
+        pin = _ptr(host_in, _dp) if host_in is not None else None
+        pout = _ptr(host_out, _dp) if host_out is not None else None
+        self._check(self.lib.gbh_step_io(self.h, pin, pout, int(nsteps), C.c_void_p(stream_handle)))
+
+    def io_sync(self):
+        self._check(self.lib.gbh_io_sync(self.h))
 
     def get_outputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
         self._check(self.lib.gbh_get_outputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))

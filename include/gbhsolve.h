@@ -253,6 +253,22 @@ int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream)
 int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row);
 int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream);
 
+/*
+ * gbh_step_io -- one call per simulation step with host inputs and outputs,
+ * pipelined: the registered inputs (host_in, n_in doubles, pinned memory
+ * for overlap) are copied to the device on the engine's copy stream while
+ * earlier work runs, scattered and stepped (nsteps steps) on `stream` (NULL
+ * = the engine's stream), and the registered outputs are gathered and copied
+ * to host_out on the copy stream while the next call's step runs. Device
+ * staging is double-buffered: the buffers passed to a call may be reused,
+ * and its host_out is complete, once the second following call has
+ * returned, or after gbh_io_sync. Either pointer may be NULL. Results equal
+ * gbh_set_inputs_async + gbh_run_async + gbh_get_outputs_async. No
+ * counterpart in the reference (h_in_msgs / h_out_msgs run on the host).
+ */
+int gbh_step_io(gbh_engine *e, const double *host_in, double *host_out, int nsteps, void *stream);
+int gbh_io_sync(gbh_engine *e);
+
 /* Per-solver spike counts since creation (int64[nsolvers]). */
 int gbh_get_spike_counts(gbh_engine *e, int64_t *counts);
 
