@@ -40,7 +40,46 @@ struct DevView {
     // Absolute step of launch-relative step 0, read on the device (kernels
     // replayed from a CUDA graph); null: the step0 argument is absolute.
     const long long *step_dev;
+    // Grid barrier {arrivals, generation, abort} of a cooperative multi-step
+    // launch (spikes cross tiles every step); null: no barrier.
+    unsigned *gbar;
 };
+
+// Barrier over all blocks of a cooperative launch: the last block to arrive
+// resets the count and advances the generation; the others wait for the
+// generation to change, for at most ~2^22 polls (then they record
+// ST_BARRIER, raise the abort word and leave, and so does every later
+// barrier). Returns false once aborted.
+__device__ __forceinline__ bool grid_sync(unsigned *bar, unsigned nblocks, int *status)
+{
+    __shared__ int ok_s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        volatile unsigned *abort_w = bar + 2;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == nblocks - 1) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned polls = 0;
+            while (*gen == g && !*abort_w) {
+                if (++polls > (1u << 22)) {
+                    atomicExch(bar + 2, 1u);
+                    if (status) atomicOr(status, ST_BARRIER);
+                    break;
+                }
+                if (polls > 4096) __nanosleep(64);   // spin first: steps are microseconds apart
+            }
+        }
+        __threadfence();
+        ok_s = *abort_w ? 0 : 1;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
 
 // ---------------------------------------------------------------- helpers
 struct VCursor {

@@ -106,6 +106,10 @@ struct gbh_engine {
     DBuf<int64_t> d_out_start, d_out_base;
     DBuf<int> d_out_delay;
     DBuf<unsigned long long> d_spikes;
+    // networks: cooperative multi-step launches (grid barrier every step)
+    DBuf<unsigned> d_gbar;
+    bool net_coop = false;
+    int net_spl = 1;
     // partitioned networks: spikes recorded per neuron, remote-source synapses
     DBuf<unsigned> d_spiked;
     int nremote = 0;
@@ -861,8 +865,37 @@ int run_graph(gbh_engine *e, int nsteps, cudaStream_t st)
     return GBH_OK;
 }
 
+// Networks: K steps per cooperative launch of the interpreting kernel over
+// every tile, a grid barrier between steps (events cross tiles).
+int run_coop(gbh_engine *e, int nsteps, cudaStream_t st)
+{
+    DevView v = view_of(e);
+    v.gbar = e->d_gbar.p;
+    const bool mixed = e->opt.precision == GBH_PREC_MIXED;
+    int smax = 1;
+    for (const TileType &tt : e->types) smax = std::max(smax, tt.nslots);
+    for (int done = 0; done < nsteps;) {
+        const int k = std::min(e->net_spl, nsteps - done);
+        CK(cudaMemsetAsync(e->d_gbar.p, 0, 3 * sizeof(unsigned), st));
+        const cudaError_t ce = mixed ? launch_mixed_coop(v, (int)e->tiles.size(), smax, k, e->step, st)
+                                     : launch_fp64_coop(v, (int)e->tiles.size(), smax, k, e->step, st);
+        if (ce != cudaSuccess) {
+            set_last("cooperative launch failed: %s", cudaGetErrorString(ce));
+            return GBH_ERR_CUDA;
+        }
+        e->stats.launches++;
+        e->step += k;
+        done += k;
+    }
+    return GBH_OK;
+}
+
 int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 {
+    if (e->net_coop && !e->givals_enabled && e->nremote == 0) {
+        e->dstep_valid = false;
+        return run_coop(e, nsteps, st);
+    }
     if (e->opt.use_graph && !e->givals_enabled) return run_graph(e, nsteps, st);
     e->dstep_valid = false;   // the launches below carry absolute step numbers
     const DevView v = view_of(e);
@@ -929,7 +962,7 @@ int autotune_trials(gbh_engine *e)
         e->jit_choice = vi;   // launch_one sizes the shared memory of the variant in use
         for (int spl : spls) {
             e->steps_per_launch = spl;
-            const int steps = e->has_network ? 32 : std::max(2 * spl, 128);
+            const int steps = std::max(2 * spl, 128);
             run_steps(e, 8, e->stream);          // warm caches and clocks
             CK(cudaEventRecord(e->ev0, e->stream));
             run_steps(e, steps, e->stream);
@@ -940,6 +973,45 @@ int autotune_trials(gbh_engine *e)
             const double per = ms / steps;
             if (per < best) { best = per; best_v = vi; best_s = spl; }
             for (Save &s : saves) CK(cudaMemcpy((void *)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice));
+        }
+    }
+    // networks: the cooperative multi-step launch against the best per-step plan
+    if (e->has_network && e->nremote == 0 && e->d_gbar.p) {
+        for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
+        e->jit_choice = best_v;
+        e->steps_per_launch = best_s;
+        int coop_k = 0;
+        for (int K : {16, 64}) {
+            e->net_coop = true;
+            e->net_spl = K;
+            const int steps = std::max(2 * K, 128);   // the same length as the per-step trials
+            int rc_c = run_steps(e, 8, e->stream);
+            if (rc_c == GBH_OK) {
+                CK(cudaEventRecord(e->ev0, e->stream));
+                rc_c = run_steps(e, steps, e->stream);
+                CK(cudaEventRecord(e->ev1, e->stream));
+            }
+            const cudaError_t se = cudaEventSynchronize(e->ev1);
+            float ms = 0.f;
+            if (rc_c == GBH_OK && se == cudaSuccess && cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess) {
+                const double per = ms / steps;
+                if (per < best) { best = per; coop_k = K; }
+            } else {
+                cudaGetLastError();   // e.g. too many tiles to be resident at once: keep per-step launches
+            }
+            e->net_coop = false;
+            for (Save &s : saves) CK(cudaMemcpy((void *)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice));
+        }
+        int status = 0;
+        CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (status & ST_BARRIER) {   // a barrier ran out: keep per-step launches
+            coop_k = 0;
+            status &= ~ST_BARRIER;
+            CK(cudaMemcpy(e->d_status.p, &status, sizeof(int), cudaMemcpyHostToDevice));
+        }
+        if (coop_k) {
+            e->net_coop = true;
+            e->net_spl = coop_k;
         }
     }
     for (Save &s : saves) cudaFree(s.dst);
@@ -1342,17 +1414,21 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
         }
         cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming);
     }
-    if (e->d_step.alloc(1)) {
+    if (e->d_step.alloc(1) || (e->has_network && e->d_gbar.upload(std::vector<unsigned>(3, 0u)))) {
         fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
         gbh_destroy(e);
         return nullptr;
     }
     e->steps_per_launch = e->opt.steps_per_launch > 0 ? e->opt.steps_per_launch : 64;
+    if (e->opt.steps_per_launch < 0 && e->has_network && e->nremote == 0) {   // forced cooperative plan
+        e->net_coop = true;
+        e->net_spl = -e->opt.steps_per_launch;
+    }
     if (e->has_network) e->steps_per_launch = 1;  // spikes cross tiles every step
     cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
     cudaEventCreate(&e->ev0);
     cudaEventCreate(&e->ev1);
-    if (e->opt.steps_per_launch <= 0 && autotune(e) != GBH_OK) {
+    if (e->opt.steps_per_launch == 0 && autotune(e) != GBH_OK) {
         fail_err(err, GBH_ERR_CUDA, "autotuner: %s", g_last_error);
         gbh_destroy(e);
         return nullptr;
@@ -1362,7 +1438,8 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
     e->stats.compartments = comps;
     e->stats.tiles = (int64_t)e->tiles.size();
     e->stats.precision = e->opt.precision;
-    e->stats.steps_per_launch = e->steps_per_launch;
+    e->stats.steps_per_launch = e->net_coop ? e->net_spl : e->steps_per_launch;
+    e->stats.cooperative = e->net_coop ? 1 : 0;
     e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
     e->stats.jit_kernels = e->jit_compiled;
     e->stats.jit_min_blocks = e->jit_minb.empty() ? 0 : e->jit_minb[e->jit_choice];
@@ -1934,7 +2011,7 @@ void gbh_destroy(gbh_engine *e)
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
-    e->d_spiked.release(); e->d_rstart.release(); e->d_rbase.release(); e->d_rdelay.release(); e->d_rbits.release();
+    e->d_gbar.release(); e->d_spiked.release(); e->d_rstart.release(); e->d_rbase.release(); e->d_rdelay.release(); e->d_rbits.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);

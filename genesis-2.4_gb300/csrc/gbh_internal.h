@@ -94,6 +94,7 @@ struct Tile {
 };
 
 // Device status word bits
-enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2, ST_SMEM = 4 /* launched with too little shared memory */ };
+enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2, ST_SMEM = 4 /* launched with too little shared memory */,
+              ST_BARRIER = 8 /* a grid barrier wait ran out */ };
 
 }  // namespace gbh

@@ -373,6 +373,9 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
                 Vw[s * LANES] = r;
             }
         }
+        // cooperative multi-step launch: every tile's events of this step
+        // are in the rings before any tile starts the next step
+        if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
     }
 }
 
@@ -382,6 +385,32 @@ cudaError_t launch_fp64(const DevView &v, int tile0, int tile1, int smax, int wa
                         long long step, bool giv, cudaStream_t st);
 cudaError_t launch_mixed(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
                          long long step, bool giv, cudaStream_t st);
+
+// Cooperative multi-step launch over tiles [0, ntiles), one warp per block,
+// with a grid barrier after every step (v.gbar set): every block must be
+// resident at once, otherwise cudaErrorCooperativeLaunchTooLarge.
+cudaError_t launch_fp64_coop(const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st);
+cudaError_t launch_mixed_coop(const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st);
+
+template <typename Fn>
+cudaError_t coop_launch(Fn fn, const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st)
+{
+    const size_t smem = (size_t)2 * smax * LANES * sizeof(double);
+    cudaError_t ce;
+    if (smem > 48 * 1024) {
+        ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ce != cudaSuccess) return ce;
+    }
+    int dev = 0, nsm = 0, per_sm = 0;
+    if ((ce = cudaGetDevice(&dev)) != cudaSuccess) return ce;
+    if ((ce = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return ce;
+    if ((ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LANES, smem)) != cudaSuccess) return ce;
+    if ((long long)per_sm * nsm < ntiles) return cudaErrorCooperativeLaunchTooLarge;
+    DevView vv = v;
+    int t0 = 0, t1 = ntiles;
+    void *args[] = {&vv, &t0, &t1, &smax, &nsteps, &step};
+    return cudaLaunchCooperativeKernel((const void *)fn, dim3(ntiles), dim3(LANES), args, smem, st);
+}
 
 template <typename G>
 cudaError_t launch_impl(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,

@@ -340,6 +340,9 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
                 Vw[s * LANES] = r;
             }
         }
+        // cooperative multi-step launch: every tile's events of this step
+        // are in the rings before any tile starts the next step
+        if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
     }
 }
 

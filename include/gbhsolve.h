@@ -131,8 +131,11 @@ typedef struct gbh_options {
     int precision;       /* GBH_PREC_FP64 or GBH_PREC_MIXED                  */
     int steps_per_launch;/* 0 = autotune: gbh_create times trial steps on a saved
                             copy of the state for each candidate kernel variant
-                            and steps-per-launch, restores the state and keeps
-                            the fastest; otherwise steps fused per launch     */
+                            and steps-per-launch (networks: also cooperative
+                            launches of K steps with a grid barrier per step),
+                            restores the state and keeps the fastest; > 0 =
+                            steps fused per launch; < 0 (networks) = -K steps
+                            per cooperative launch                            */
     int warps_per_block; /* 0 = autotune                                      */
     int use_graph;       /* capture multi-launch runs in a CUDA graph         */
     int device;          /* CUDA device ordinal                                */
@@ -162,6 +165,8 @@ typedef struct gbh_stats {
                                   + adjoint steps (device time)               */
     int jit_compact;           /* the chosen specialised variant is the compact
                                   (looped) form                               */
+    int cooperative;           /* network steps run K per cooperative launch
+                                  with a grid barrier between steps           */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;

@@ -53,3 +53,38 @@ def test_network_longer_delays(oracle, gpu_engine):
     solvers, ref_spikes = _oracle_net(oracle, hs, esyn, child, 2500)
     np.testing.assert_array_equal(eng.spike_counts(), ref_spikes)
     np.testing.assert_array_equal(eng.vm(), np.concatenate([s.vm for s in solvers]))
+
+
+@pytest.mark.parametrize("K", [1, 16, 50])
+def test_network_cooperative_launches(oracle, gpu_engine, K):
+    """K steps per cooperative launch with a grid barrier between steps equal
+    the oracle bit for bit (calls of odd lengths split the K-step chunks)."""
+    rng = np.random.default_rng(8)
+    n = 150
+    hs, esyn, child = _network(n, 0.07, seed=9, inject=rng.uniform(0.0, 0.3e-9, size=n))
+    eng = gpu_engine.Engine(hs, synapses=esyn, steps_per_launch=-K)
+    assert eng.stats().cooperative == 1
+    for m in (700, 333, 967):
+        eng.run(m)
+    solvers, ref_spikes = _oracle_net(oracle, hs, esyn, child, 2000)
+    assert ref_spikes.sum() > n
+    np.testing.assert_array_equal(eng.spike_counts(), ref_spikes)
+    np.testing.assert_array_equal(eng.vm(), np.concatenate([s.vm for s in solvers]))
+    eng.close()
+
+
+def test_network_cooperative_mixed_matches_launches(gpu_engine):
+    """Mixed form: the cooperative plan equals per-step launches of the same
+    interpreting kernel bit for bit."""
+    rng = np.random.default_rng(10)
+    n = 120
+    hs, esyn, _ = _network(n, 0.08, seed=10, inject=rng.uniform(0.0, 0.3e-9, size=n))
+    a = gpu_engine.Engine(hs, synapses=esyn, precision=gpu_engine.PREC_MIXED, jit=False, steps_per_launch=1)
+    b = gpu_engine.Engine(hs, synapses=esyn, precision=gpu_engine.PREC_MIXED, jit=False, steps_per_launch=-32)
+    a.run(1500)
+    b.run(1500)
+    np.testing.assert_array_equal(a.spike_counts(), b.spike_counts())
+    np.testing.assert_array_equal(a.vm(), b.vm())
+    assert a.spike_counts().sum() > n
+    a.close()
+    b.close()
