@@ -418,9 +418,10 @@ def main():
             ms = float(t.item())
         results[form] = dict(ms=ms, launches=launches, spl=st.steps_per_launch,
                              value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng)
-        log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels (min blocks %d), %d steps/launch"
-            " -> %.3e cs/s" % (form, ms, args.steps, launches, st.jit_kernels, st.jit_min_blocks,
-                               st.steps_per_launch, results[form]["value"]))
+        log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels (min blocks %d, %s form),"
+            " %d steps/launch -> %.3e cs/s" % (form, ms, args.steps, launches, st.jit_kernels, st.jit_min_blocks,
+                                               ["unrolled", "compact", "unrolled/shared-rows"][st.jit_compact],
+                                               st.steps_per_launch, results[form]["value"]))
         if form == "fp64":
             eng.close()
 

@@ -187,6 +187,23 @@ __device__ __forceinline__ df ld_df(const double *p)
     return df_make(v.x, v.y);
 }
 
+// a row the kernel never writes during the launch (coefficients, gmax, Ek,
+// tbyc, ...): read through the non-coherent path so the compiler may move the
+// load ahead of the stores that precede it
+__device__ __forceinline__ df ld_df_ro(const double *p)
+{
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return df_make(v.x, v.y);
+}
+
+// read-only view of a neuron-interleaved row array: r[i] loads through the
+// non-coherent path
+template <typename T>
+struct RoRow {
+    const T *p;
+    __device__ __forceinline__ T operator[](int i) const { return __ldg(p + i); }
+};
+
 __device__ __forceinline__ void st_df(double *p, df x)
 {
     *reinterpret_cast<float2 *>(p) = make_float2(x.hi, x.lo);
@@ -195,13 +212,13 @@ __device__ __forceinline__ void st_df(double *p, df x)
 // interpolated value of table entry e at fraction fr: value + fr*difference
 __device__ __forceinline__ df interp_df(const float4 *tab, int e, df fr)
 {
-    const float4 t = tab[e];
+    const float4 t = __ldg(tab + e);
     return df_add(df_make(t.x, t.y), df_mul(df_make(t.z, t.w), fr));
 }
 
 __device__ __forceinline__ df val_df(const float4 *tab, int e)
 {
-    const float4 t = tab[e];
+    const float4 t = __ldg(tab + e);
     return df_make(t.x, t.y);
 }
 

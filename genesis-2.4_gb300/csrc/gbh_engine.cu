@@ -133,6 +133,8 @@ struct gbh_engine {
     std::vector<std::vector<JitKernel>> jit_var;  // compiled variants per specialised type
     std::vector<int> jit_minb;                    // residency target of each variant
     std::vector<char> jit_compact;                // variant is the compact (looped) form
+    std::vector<char> jit_smemrows;               // variant keeps the unrolled form's rows in shared memory
+    std::vector<int> jit_warps;                   // warps per block of each variant
     int jit_choice = 0;
     int jit_compiled = 0;
     std::string jit_log;
@@ -601,15 +603,27 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         if ((int)cand.size() > max_jit) cand.resize(max_jit);
         // residency targets (resident blocks of 4 warps per SM) tried by the autotuner
         // variants: (resident 4-warp blocks per SM, compact form)
+        // variants: (warps per block, resident blocks per SM, compact form,
+        // unrolled form with its rows in shared memory). Blocks of one or two
+        // warps spread the tiles evenly over the SMs (782 4-warp blocks put 6
+        // on 22 SMs and 5 on the rest); the shared-rows form is only forced
+        // (jit 3): it shrinks the L1 the table gathers hit in
         e->jit_minb.clear();
         e->jit_compact.clear();
-        const int form = e->opt.jit;   // 0 autotuned, 1 unrolled only, 2 compact only
+        e->jit_smemrows.clear();
+        e->jit_warps.clear();
+        const int form = e->opt.jit;   // 0 autotuned, 1 unrolled, 2 compact, 3 unrolled with shared rows
         if (e->opt.steps_per_launch > 0 || form > 0) {
-            e->jit_minb.push_back(6);
+            const bool unrolled = form == 0 || form == 1;
+            e->jit_minb.push_back(unrolled ? 24 : 6);
             e->jit_compact.push_back(form == 2);
+            e->jit_smemrows.push_back(form == 3);
+            e->jit_warps.push_back(unrolled ? 1 : 4);
         } else {
-            e->jit_minb = {4, 6, 6, 8};
-            e->jit_compact = {0, 0, 1, 1};
+            e->jit_minb = {4, 6, 6, 8, 24, 12, 32};
+            e->jit_compact = {0, 0, 1, 1, 0, 0, 1};
+            e->jit_smemrows = {0, 0, 0, 0, 0, 0, 0};
+            e->jit_warps = {4, 4, 4, 4, 1, 2, 1};
         }
         const int nvar = (int)e->jit_minb.size();
         std::vector<std::string> srcs(cand.size() * nvar);
@@ -628,7 +642,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             for (int vi = 0; vi < nvar; ++vi)
                 srcs[c * nvar + vi] = jit_source(e->types[ti], prog_pool, tg[e->types[ti].table_set], mixed, false,
                                                  upar[c].empty() ? nullptr : &upar[c], e->jit_minb[vi],
-                                                 e->jit_compact[vi] != 0);
+                                                 e->jit_compact[vi] != 0, e->jit_smemrows[vi] != 0,
+                                                 e->jit_warps[vi]);
         }
         int dev = e->opt.device, major = 10, minor = 3;
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
@@ -730,9 +745,11 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
                bool giv, cudaStream_t st)
 {
     if (L.jit >= 0 && !giv) {
-        const bool cols = !L.uniform || e->jit_compact[e->jit_choice];   // rows in shared-memory columns
-        const size_t smem = cols ? (size_t)L.warps * 2 * L.smax * LANES * sizeof(double) : 0;
-        const cudaError_t je = jit_launch(e->jits[L.jit], v, L.tile0, L.tile1, L.smax, L.warps, k, step, smem, st);
+        // rows in shared-memory columns
+        const bool cols = !L.uniform || e->jit_compact[e->jit_choice] || e->jit_smemrows[e->jit_choice];
+        const int warps = e->jit_warps[e->jit_choice];
+        const size_t smem = cols ? (size_t)warps * 2 * L.smax * LANES * sizeof(double) : 0;
+        const cudaError_t je = jit_launch(e->jits[L.jit], v, L.tile0, L.tile1, L.smax, warps, k, step, smem, st);
         if (je != cudaSuccess) {
             set_last("specialised kernel launch failed: %s", cudaGetErrorString(je));
             return GBH_ERR_CUDA;
@@ -971,6 +988,10 @@ int autotune_trials(gbh_engine *e)
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
             const double per = ms / steps;
+            if (getenv("GBH_VERBOSE") && !e->jit_minb.empty())
+                fprintf(stderr, "gbhsolve: trial %d warps x min blocks %d, form %d, %d steps/launch: %.2f us/step\n",
+                        e->jit_warps[vi], e->jit_minb[vi], e->jit_compact[vi] ? 1 : e->jit_smemrows[vi] ? 2 : 0, spl,
+                        per * 1e3);
             if (per < best) { best = per; best_v = vi; best_s = spl; }
             for (Save &s : saves) CK(cudaMemcpy((void *)s.src, s.dst, s.bytes, cudaMemcpyDeviceToDevice));
         }
@@ -1331,7 +1352,8 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
     build_tables(desc, tg, tab64, xy);
     const std::string src = jit_source(types[type_index], prog_pool, tg[types[type_index].table_set],
                                        precision == GBH_PREC_MIXED, false,
-                                       uniform[type_index] ? &parents[type_index] : nullptr, 6, compact != 0);
+                                       uniform[type_index] ? &parents[type_index] : nullptr, 6, compact == 1,
+                                       compact == 2);
     if (buf && buflen > 0) {
         const int64_t n = std::min<int64_t>(buflen - 1, (int64_t)src.size());
         memcpy(buf, src.data(), (size_t)n);
@@ -1441,9 +1463,13 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
     e->stats.steps_per_launch = e->net_coop ? e->net_spl : e->steps_per_launch;
     e->stats.cooperative = e->net_coop ? 1 : 0;
     e->stats.warps_per_block = e->launches.empty() ? 0 : e->launches[0].warps;
+    if (!e->launches.empty() && e->launches[0].jit >= 0 && !e->jit_warps.empty())
+        e->stats.warps_per_block = e->jit_warps[e->jit_choice];
     e->stats.jit_kernels = e->jit_compiled;
     e->stats.jit_min_blocks = e->jit_minb.empty() ? 0 : e->jit_minb[e->jit_choice];
-    e->stats.jit_compact = e->jit_compact.empty() ? 0 : e->jit_compact[e->jit_choice];
+    e->stats.jit_compact = e->jit_compact.empty() ? 0
+                           : e->jit_compact[e->jit_choice] ? 1
+                           : e->jit_smemrows[e->jit_choice] ? 2 : 0;
     if (getenv("GBH_VERBOSE") && !e->jit_log.empty())
         fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
                 e->jit_log.c_str());

@@ -131,6 +131,10 @@ struct Emit {
     std::string F(int p) const { return "Fw[" + std::to_string(p * LANES) + "]"; }
     std::string G(int g) const { return "Gw[" + std::to_string(g * LANES) + "]"; }
     std::string pP(int f) const { return "&Pw[" + frow(f) + "]"; }
+    // rows no op of the kernel writes (chip constants: Em/Rm, inject, tbyc,
+    // diagterm, Ek, gmax): non-coherent loads
+    std::string Pr(int f) const { return "__ldg(&Pw[" + frow(f) + "])"; }
+    std::string ldr(int f) const { return "ld_df_ro(&Pw[" + frow(f) + "])"; }
     std::string S(int s) const { return sidx.empty() ? std::to_string(s) : sidx; }
     std::string Vrow(int s) const { return sidx.empty() ? std::to_string(s * LANES) : sidx + " * 32"; }
 };
@@ -170,12 +174,11 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
         switch (code) {
         case M_BEGIN:
             if (mx) {
-                o << "      { const df emrm = ld_df(" << E.pP(a[0]) << "); ichan = df_add(emrm, ld_df(" << E.pP(a[1])
-                  << "));";
+                o << "      { const df emrm = " << E.ldr(a[0]) << "; ichan = df_add(emrm, " << E.ldr(a[1]) << ");";
                 if (giv) o << " Im = df2d(emrm) - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
                 o << " }\n";
             } else {
-                o << "      { const double emrm = " << E.P(a[0]) << "; ichan = emrm + " << E.P(a[1]) << ";";
+                o << "      { const double emrm = " << E.Pr(a[0]) << "; ichan = emrm + " << E.Pr(a[1]) << ";";
                 if (giv) o << " Im = emrm - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
                 o << " }\n";
             }
@@ -243,12 +246,12 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
             break;
         case M_END:
             if (mx) {
-                o << "      { const df tbyc = ld_df(" << E.pP(a[0]) << "); const df dv = df_mul(ichan, tbyc);\n"
+                o << "      { const df tbyc = " << E.ldr(a[0]) << "; const df dv = df_mul(ichan, tbyc);\n"
                   << "        R[" << E.S(s) << "] = df2d(df_add(vmd, dv));\n"
-                  << "        D[" << E.S(s) << "] = df2d(df_add(df_mul(sumg, tbyc), ld_df(" << E.pP(a[1]) << "))); }\n";
+                  << "        D[" << E.S(s) << "] = df2d(df_add(df_mul(sumg, tbyc), " << E.ldr(a[1]) << ")); }\n";
             } else {
-                o << "      { const double tbyc = " << E.P(a[0]) << "; R[" << E.S(s) << "] = Vm + ichan * tbyc; D[" << E.S(s)
-                  << "] = sumg * tbyc + " << E.P(a[1]) << "; }\n";
+                o << "      { const double tbyc = " << E.Pr(a[0]) << "; R[" << E.S(s) << "] = Vm + ichan * tbyc; D[" << E.S(s)
+                  << "] = sumg * tbyc + " << E.Pr(a[1]) << "; }\n";
             }
             if (giv) o << "      " << E.G(a[2]) << " = Im;\n";
             pc += 1 + n;
@@ -281,11 +284,11 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
                     o << "      Ek = log(Cw[(sel + 1) * 32] / Cw[sel * 32]) * " << E.P(a[0]) << "; gmax = Gk = "
                       << E.P(a[1]) << ";\n";
             } else if (code == M_CHAN) {
-                if (mx) o << "      Ek = ld_df(" << E.pP(a[0]) << "); gmax = Gk = ld_df(" << E.pP(a[1]) << ");\n";
-                else o << "      Ek = " << E.P(a[0]) << "; gmax = Gk = " << E.P(a[1]) << ";\n";
+                if (mx) o << "      Ek = " << E.ldr(a[0]) << "; gmax = Gk = " << E.ldr(a[1]) << ";\n";
+                else o << "      Ek = " << E.Pr(a[0]) << "; gmax = Gk = " << E.Pr(a[1]) << ";\n";
             } else if (code == M_CHAN_G) {
-                if (mx) o << "      gmax = Gk = ld_df(" << E.pP(a[0]) << ");\n";
-                else o << "      gmax = Gk = " << E.P(a[0]) << ";\n";
+                if (mx) o << "      gmax = Gk = " << E.ldr(a[0]) << ";\n";
+                else o << "      gmax = Gk = " << E.Pr(a[0]) << ";\n";
             } else {
                 return false;
             }
@@ -500,16 +503,18 @@ int loop_run(const std::vector<int> &prog, const std::vector<int> &sstart, int s
 }  // namespace
 
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent, int min_blocks, bool compact)
+                       const std::vector<int> *uniform_parent, int min_blocks, bool compact, bool smem_rows,
+                       int warps)
 {
     if (compact) uniform_parent = nullptr;   // rows in shared-memory columns, looped elimination
+    const bool cols = !uniform_parent || smem_rows;   // D/R rows in shared-memory columns
     Emit E;
     E.mixed = mixed;
     E.giv = giv;
     std::ostringstream &o = E.o;
     const int S = tt.nslots;
     o << "#include \"gbh_devfn.cuh\"\nusing namespace gbh;\n";
-    o << "extern \"C\" __global__ void __launch_bounds__(128, " << min_blocks
+    o << "extern \"C\" __global__ void __launch_bounds__(" << warps * LANES << ", " << min_blocks
       << ") gbh_jit(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)\n{\n";
     o << "  extern __shared__ double sm[];\n"
       << "  const int lane = threadIdx.x & 31; const int wib = threadIdx.x >> 5;\n"
@@ -534,12 +539,12 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
           << "  const double *xvals = v.xyvals + " << tg.xv_off << "; (void)xvals;\n"
           << "  const double *yvals = v.xyvals + " << (tg.yv_off >= 0 ? tg.yv_off : tg.xv_off) << "; (void)yvals;\n";
     }
-    if (!uniform_parent)
+    if (cols)
         o << "  { unsigned dsz; asm(\"mov.u32 %0, %%dynamic_smem_size;\" : \"=r\"(dsz));\n"
           << "    if (dsz < (blockDim.x >> 5) * " << 2 * S * LANES * 8 << "u) { if (v.status) atomicOr(v.status, 4); return; } }\n"
-          << "  const int *par = v.parent + tl.topo * 32 + lane;\n"
           << "  double *Dc = sm + (size_t)wib * " << 2 * S * LANES << " + lane; double *Rc = Dc + " << S * LANES << ";\n";
-    o << "  const double *Aw = v.A + tl.topo * 32 + lane; const double *Bw = v.B + tl.topo * 32 + lane; const double *Cbw = v.Cb + tl.topo * 32 + lane;\n";
+    if (!uniform_parent) o << "  const RoRow<int> par{v.parent + tl.topo * 32 + lane};\n";
+    o << "  const RoRow<double> Aw{v.A + tl.topo * 32 + lane}, Bw{v.B + tl.topo * 32 + lane}, Cbw{v.Cb + tl.topo * 32 + lane};\n";
     o << "  for (int it = 0; it < nsteps; ++it) {\n"
       << "    const long long step = sbase + step0 + it; (void)step;\n";
     if (mixed) {
@@ -554,7 +559,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
           << "    double Ek = 0.0, Gk = 0.0, gmax = 0.0; (void)gmax;\n";
     }
     o << "    double GHK = 0.0, Ik = 0.0; int doGHK = 0, sel = 0; (void)GHK; (void)doGHK; (void)sel; (void)Ik;\n";
-    if (uniform_parent) o << "    double D[" << S << "], R[" << S << "], T[" << S << "]; (void)T;\n";
+    if (!cols) o << "    double D[" << S << "], R[" << S << "], T[" << S << "]; (void)T;\n";
+    else if (uniform_parent) o << "    double T[" << S << "]; (void)T;\n";
     else o << "    double *D = nullptr, *R = nullptr; (void)D; (void)R;\n";
     std::ostringstream save;
     // slot extents in the program
@@ -621,7 +627,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
     }
     std::string body = o.str();
-    if (!uniform_parent) {
+    if (cols) {
         // rewrite D[s]/R[s] into the shared columns
         std::string out;
         out.reserve(body.size());
@@ -651,10 +657,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         pp += 5;
     }
     // elimination
-    const char *dv = uniform_parent ? "D[%d]" : "Dc[%d]";
-    (void)dv;
-    auto Dx = [&](int s) { return uniform_parent ? "D[" + std::to_string(s) + "]" : "Dc[" + std::to_string(s * LANES) + "]"; };
-    auto Rx = [&](int s) { return uniform_parent ? "R[" + std::to_string(s) + "]" : "Rc[" + std::to_string(s * LANES) + "]"; };
+    auto Dx = [&](int s) { return !cols ? "D[" + std::to_string(s) + "]" : "Dc[" + std::to_string(s * LANES) + "]"; };
+    auto Rx = [&](int s) { return !cols ? "R[" + std::to_string(s) + "]" : "Rc[" + std::to_string(s * LANES) + "]"; };
     if (uniform_parent) {
         const std::vector<int> &par = *uniform_parent;   // forward sweep already fused above
         for (int s = S - 1; s >= 0; --s) {

@@ -19,9 +19,13 @@ struct JitKernel {
 // shared by every neuron of the type (elimination unrolled in registers), or
 // null (per-neuron trees, shared-memory columns). compact: runs of identical
 // compartment programs become loops and the rows stay in shared memory
-// (smaller code; the autotuner decides which form runs).
+// (smaller code; the autotuner decides which form runs). smem_rows: the
+// unrolled form of a uniform tree keeps the eliminated rows (D, R) in
+// shared-memory columns instead of registers, which frees ~4 registers a
+// compartment for loads in flight.
 std::string jit_source(const TileType &tt, const std::vector<int> &prog, const TableGeom &tg, bool mixed, bool giv,
-                       const std::vector<int> *uniform_parent, int min_blocks = 4, bool compact = false);
+                       const std::vector<int> *uniform_parent, int min_blocks = 4, bool compact = false,
+                       bool smem_rows = false, int warps = 4);
 
 bool jit_available(std::string *why);
 int jit_compile(const std::string &src, bool fp64_exact, int device_major, int device_minor, JitKernel *out,

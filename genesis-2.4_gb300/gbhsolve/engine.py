@@ -268,8 +268,11 @@ def validate(solvers: Sequence):
     return nn.value, nt.value
 
 
-def jit_source(solvers: Sequence, precision: int = PREC_FP64, type_index: int = 0, compact: bool = False) -> str:
-    """CUDA source generated for one tile type (host only, no GPU)."""
+def jit_source(solvers: Sequence, precision: int = PREC_FP64, type_index: int = 0, compact: int = 0) -> str:
+    """CUDA source generated for one tile type (host only, no GPU).
+
+    compact: 0 (or False) unrolled form, 1 (or True) compact looped form,
+    2 unrolled form with the eliminated rows in shared memory."""
     lib = load()
     b = Batch(solvers)
     n = lib.gbh_jit_source(C.byref(b.desc), precision, type_index, int(compact), None, 0)

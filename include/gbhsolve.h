@@ -140,10 +140,13 @@ typedef struct gbh_options {
     int use_graph;       /* capture multi-launch runs in a CUDA graph         */
     int device;          /* CUDA device ordinal                                */
     int jit;             /* 0 = specialise each tile type's program at setup
-                            (NVRTC) in both forms -- unrolled straight-line and
-                            compact (runs of identical compartments looped) --
-                            and let the autotuner pick; 1 = unrolled form only;
-                            2 = compact form only; -1 = interpret the programs */
+                            (NVRTC) in three forms -- unrolled straight-line,
+                            unrolled with the eliminated rows in shared memory,
+                            and compact (runs of identical compartments looped)
+                            -- and let the autotuner pick; 1 = unrolled form
+                            only; 2 = compact form only; 3 = unrolled form with
+                            shared-memory rows only; -1 = interpret the
+                            programs                                          */
 } gbh_options;
 
 typedef struct gbh_stats {
@@ -163,8 +166,9 @@ typedef struct gbh_stats {
                                   pass (device time, CUDA events)             */
     double grad_reverse_ms;    /* last gbh_loss_gradient: segment recomputation
                                   + adjoint steps (device time)               */
-    int jit_compact;           /* the chosen specialised variant is the compact
-                                  (looped) form                               */
+    int jit_compact;           /* form of the chosen specialised variant:
+                                  0 unrolled, 1 compact (looped), 2 unrolled
+                                  with its rows in shared memory              */
     int cooperative;           /* network steps run K per cooperative launch
                                   with a grid barrier between steps           */
 } gbh_stats;
@@ -208,7 +212,8 @@ int gbh_validate(const gbh_batch_desc *desc, gbh_error *err, int64_t *n_neurons,
  * Diagnostics: writes the CUDA source the engine generates for tile type
  * type_index (neurons sharing one program) into buf (NUL-terminated,
  * truncated to buflen). Returns the full source length, or a negative error.
- * Needs no GPU.
+ * compact: 0 unrolled form, 1 compact (looped) form, 2 unrolled form with its
+ * rows in shared memory. Needs no GPU.
  */
 int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index, int compact, char *buf,
                        int64_t buflen);

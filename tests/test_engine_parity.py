@@ -58,7 +58,7 @@ def test_random_trees_with_ca_bitwise(oracle, gpu_engine):
         np.testing.assert_array_equal(st["conc"][i], ref.conc[:len(hs[i].conc)])
 
 
-@pytest.mark.parametrize("jit", [True, False, 2])
+@pytest.mark.parametrize("jit", [True, False, 2, 3])
 def test_jit_and_interpreter_agree_bitwise(oracle, gpu_engine, jit):
     """Both execution paths -- programs specialised at setup and the
     interpreting kernel -- reproduce the oracle exactly."""

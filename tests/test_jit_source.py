@@ -49,7 +49,7 @@ def _models():
     yield "network", [model.build(m) for m in ms]
 
 
-@pytest.mark.parametrize("compact", [False, True])
+@pytest.mark.parametrize("compact", [0, 1, 2])
 @pytest.mark.parametrize("prec", [engine.PREC_FP64, engine.PREC_MIXED])
 @pytest.mark.parametrize("name,hs", list(_models()))
 def test_generated_kernel_compiles(name, hs, prec, compact):
@@ -69,3 +69,15 @@ def test_compact_form_loops_identical_compartments():
     assert "for (int s = 1; s < 15; ++s)" in loop
     assert "for (int s = " not in flat
     assert len(loop) < len(flat) / 3
+
+
+def test_shared_rows_form_keeps_rows_out_of_registers():
+    """The unrolled form with shared-memory rows declares no D/R register
+    arrays; its fused elimination and back-substitution address the columns."""
+    hs = configs.cables_replicated(4, gk_dend=36.0)[0]
+    regs = engine.jit_source(hs, precision=engine.PREC_MIXED, compact=0)
+    cols = engine.jit_source(hs, precision=engine.PREC_MIXED, compact=2)
+    assert "double D[16], R[16], T[16]" in regs
+    assert "double D[16]" not in cols and "double T[16]" in cols
+    assert "Dc[(15) * 32]" in cols and "Rc[480]" in cols
+    assert "dynamic_smem_size" in cols and "dynamic_smem_size" not in regs

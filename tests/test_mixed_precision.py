@@ -27,7 +27,7 @@ def _max_dev(oracle, gpu_engine, hs, nsteps, chunk=500, **kw):
     return worst
 
 
-@pytest.mark.parametrize("jit", [True, False, 2])
+@pytest.mark.parametrize("jit", [True, False, 2, 3])
 def test_mixed_cables_10k_steps(oracle, gpu_engine, jit):
     hs, _ = configs.cables_replicated(32, gk_dend=36.0, seed=3)
     dev = _max_dev(oracle, gpu_engine, hs, 10000, jit=jit)

@@ -27,7 +27,7 @@ def _oracle_net(oracle, hs, esyn, child, nsteps):
     return solvers, net.spikes
 
 
-@pytest.mark.parametrize("jit", [True, False, 2])
+@pytest.mark.parametrize("jit", [True, False, 2, 3])
 def test_network_spikes_and_vm_bitwise(oracle, gpu_engine, jit):
     rng = np.random.default_rng(3)
     n = 120

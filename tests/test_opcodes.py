@@ -140,7 +140,7 @@ def _compare(a, b, libm):
         np.testing.assert_array_equal(a, b)
 
 
-@pytest.mark.parametrize("jit", [True, False, 2])
+@pytest.mark.parametrize("jit", [True, False, 2, 3])
 @pytest.mark.parametrize("name", sorted(PROGRAMS))
 def test_program_fp64(oracle, gpu_engine, name, jit):
     for chanmode, calcmode, crank in ((4, 1, False), (5, 1, True), (4, 0, False)):
