@@ -21,6 +21,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -530,6 +531,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
       << "  const int64_t neuron = tl.first_neuron + lane; (void)neuron;\n";
     if (mixed) {
         o << "  const float4 *tab = v.tabdf + " << tg.tab_off << "; (void)tab;\n"
+
           << "  const df xnmin = df_make(" << litf(-tg.xmin_hi) << ", " << litf(-tg.xmin_lo) << "), xinv = df_make("
           << litf(tg.invdx_hi) << ", " << litf(tg.invdx_lo) << "); (void)xnmin; (void)xinv;\n"
           << "  const df ynmin = df_make(" << litf(-tg.ymin_hi) << ", " << litf(-tg.ymin_lo) << "), yinv = df_make("
@@ -579,6 +581,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
         sstart[S] = off;
     }
+    std::deque<std::string> pending;   // fused elimination blocks not yet emitted
+    const int elim_lag = 1;   // measured: 1 beats 0, 2 and 3 on the 16-compartment cable
     // compact form: runs of four or more identical slot programs become one
     // loop (keeps the kernel inside the instruction cache)
     for (int s = 0; s < S;) {
@@ -602,30 +606,38 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 // forward elimination fused into the channel phase: row s pulls
                 // its children (ascending, the order the separate sweep pushes
                 // them in, so the arithmetic is unchanged) and prepares its own
-                // factor for its parent; its FP64 work overlaps the next
-                // compartment's channel arithmetic
+                // factor for its parent. It is emitted after the channel code
+                // of the next `lag` compartments, so that its chain of FP64
+                // operations overlaps their loads and FP32 arithmetic
                 const std::vector<int> &par = *uniform_parent;
-                o << "    {";
+                std::ostringstream el;
+                el << "    {";
                 for (int c = 0; c < s; ++c) {
                     if (par[c] != s) continue;
                     if (mixed)
-                        o << " D[" << s << "] = fma(-Bw[" << c * LANES << "], T[" << c << "], D[" << s << "]); R[" << s
-                          << "] = fma(-R[" << c << "], T[" << c << "], R[" << s << "]);";
+                        el << " D[" << s << "] = fma(-Bw[" << c * LANES << "], T[" << c << "], D[" << s << "]); R[" << s
+                           << "] = fma(-R[" << c << "], T[" << c << "], R[" << s << "]);";
                     else
-                        o << " D[" << s << "] -= Bw[" << c * LANES << "] * T[" << c << "]; R[" << s << "] -= R[" << c
-                          << "] * T[" << c << "];";
+                        el << " D[" << s << "] -= Bw[" << c * LANES << "] * T[" << c << "]; R[" << s << "] -= R[" << c
+                           << "] * T[" << c << "];";
                 }
                 if (mixed) {
-                    o << " const double ri = rcp_newton(D[" << s << "]); D[" << s << "] = ri;";
-                    if (par[s] >= 0) o << " T[" << s << "] = Aw[" << s * LANES << "] * ri;";
+                    el << " const double ri = rcp_newton(D[" << s << "]); D[" << s << "] = ri;";
+                    if (par[s] >= 0) el << " T[" << s << "] = Aw[" << s * LANES << "] * ri;";
                 } else if (par[s] >= 0) {
-                    o << " T[" << s << "] = Aw[" << s * LANES << "] / D[" << s << "];";
+                    el << " T[" << s << "] = Aw[" << s * LANES << "] / D[" << s << "];";
                 }
-                o << " }\n";
+                el << " }\n";
+                pending.push_back(el.str());
+                if ((int)pending.size() > elim_lag) {
+                    o << pending.front();
+                    pending.pop_front();
+                }
             }
             ++s;
         }
     }
+    for (const std::string &x : pending) o << x;
     std::string body = o.str();
     if (cols) {
         // rewrite D[s]/R[s] into the shared columns
