@@ -162,6 +162,12 @@ struct gbh_engine {
                 io_out_copied[2] = {nullptr, nullptr};
     long long io_calls = 0;
     int io_nin = -1, io_nout = -1;
+    // block-streamed I/O (gbh_run_io): staging for `blk_cap` steps of inputs
+    // and outputs, double-buffered
+    DBuf<double> d_blk_in[2], d_blk_out[2];
+    cudaEvent_t blk_in_copied[2] = {nullptr, nullptr}, blk_done[2] = {nullptr, nullptr},
+                blk_out_copied[2] = {nullptr, nullptr};
+    int blk_cap = 0, blk_nin = -1, blk_nout = -1;
     // the previous call's output gather, issued together with the next
     // call's input scatter (one kernel between two steps)
     double *io_pend_host = nullptr;
@@ -1293,6 +1299,88 @@ int gbh_step_io(gbh_engine *e, const double *host_in, double *host_out, int nste
     return GBH_OK;
 }
 
+int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nsteps, int block, void *stream)
+{
+    if (!e || nsteps < 0 || block < 0) return GBH_ERR_ARG;
+    if (nsteps == 0) return GBH_OK;
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    int rc = gbh_io_sync(e);   // pipelined gbh_step_io calls complete first
+    if (rc) return rc;
+    const int n_in = host_in ? (int)e->n_in : 0, n_out = host_out ? (int)e->n_out : 0;
+    const int B = std::min(block > 0 ? block : 16, nsteps);
+    if (!e->io_stream) {
+        CK(cudaStreamCreateWithFlags(&e->io_stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&e->io_out_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            CK(cudaEventCreateWithFlags(&e->io_in_copied[b], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->io_gathered[b], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->io_out_copied[b], cudaEventDisableTiming));
+        }
+    }
+    if (!e->blk_done[0])
+        for (int b = 0; b < 2; ++b) {
+            CK(cudaEventCreateWithFlags(&e->blk_in_copied[b], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->blk_done[b], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&e->blk_out_copied[b], cudaEventDisableTiming));
+        }
+    if (B > e->blk_cap || n_in != e->blk_nin || n_out != e->blk_nout) {
+        for (int b = 0; b < 2; ++b) {
+            CK(cudaEventSynchronize(e->blk_done[b]));
+            CK(cudaEventSynchronize(e->blk_out_copied[b]));
+            e->d_blk_in[b].release();
+            e->d_blk_out[b].release();
+            if (e->d_blk_in[b].alloc((size_t)B * n_in) || e->d_blk_out[b].alloc((size_t)B * n_out))
+                return GBH_ERR_CUDA;
+        }
+        e->blk_cap = B;
+        e->blk_nin = n_in;
+        e->blk_nout = n_out;
+    }
+    const int nio = std::max(n_in, n_out);
+    const unsigned grid = (unsigned)((nio + 255) / 256);
+    int last = 0;
+    for (int s0 = 0, j = 0; s0 < nsteps; s0 += B, ++j) {
+        const int nb = std::min(B, nsteps - s0), b = j & 1;
+        double *din = e->d_blk_in[b].p, *dout = e->d_blk_out[b].p;
+        if (n_in) {
+            // staging b is free once the block that used it two blocks ago has stepped
+            CK(cudaStreamWaitEvent(e->io_stream, e->blk_done[b], 0));
+            CK(cudaMemcpyAsync(din, host_in + (int64_t)s0 * n_in, (size_t)nb * n_in * sizeof(double),
+                               cudaMemcpyHostToDevice, e->io_stream));
+            CK(cudaEventRecord(e->blk_in_copied[b], e->io_stream));
+            CK(cudaStreamWaitEvent(st, e->blk_in_copied[b], 0));
+            k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, 0, nullptr, din, e->d_in_start.p, e->d_in_addr.p,
+                                       n_in, e->d_P.p);
+            CK(cudaGetLastError());
+        }
+        if (n_out) CK(cudaStreamWaitEvent(st, e->blk_out_copied[b], 0));   // its outputs were copied out
+        for (int k = 0; k < nb; ++k) {
+            rc = run_steps(e, 1, st);
+            if (rc) return rc;
+            // this step's outputs and the next step's inputs, one launch
+            const int go = n_out, si = k + 1 < nb ? n_in : 0;
+            if (go || si) {
+                k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, go, dout + (int64_t)k * n_out,
+                                           din + (int64_t)(k + 1) * n_in, e->d_in_start.p, e->d_in_addr.p, si,
+                                           e->d_P.p);
+                CK(cudaGetLastError());
+            }
+        }
+        CK(cudaEventRecord(e->blk_done[b], st));
+        if (n_out) {
+            CK(cudaStreamWaitEvent(e->io_out_stream, e->blk_done[b], 0));
+            CK(cudaMemcpyAsync(host_out + (int64_t)s0 * n_out, dout, (size_t)nb * n_out * sizeof(double),
+                               cudaMemcpyDeviceToHost, e->io_out_stream));
+            CK(cudaEventRecord(e->blk_out_copied[b], e->io_out_stream));
+        }
+        last = b;
+    }
+    CK(cudaEventSynchronize(e->blk_done[last]));
+    if (n_out) CK(cudaEventSynchronize(e->blk_out_copied[last]));
+    e->stats.steps += nsteps;
+    return GBH_OK;
+}
+
 int gbh_io_sync(gbh_engine *e)
 {
     if (!e) return GBH_ERR_ARG;
@@ -2053,6 +2141,11 @@ void gbh_destroy(gbh_engine *e)
         if (e->io_out_copied[b]) cudaEventDestroy(e->io_out_copied[b]);
         e->d_io_in[b].release();
         e->d_io_out[b].release();
+        if (e->blk_in_copied[b]) cudaEventDestroy(e->blk_in_copied[b]);
+        if (e->blk_done[b]) cudaEventDestroy(e->blk_done[b]);
+        if (e->blk_out_copied[b]) cudaEventDestroy(e->blk_out_copied[b]);
+        e->d_blk_in[b].release();
+        e->d_blk_out[b].release();
     }
     for (cudaStream_t x : e->side) cudaStreamDestroy(x);
     for (cudaEvent_t x : e->ev_join) cudaEventDestroy(x);

@@ -86,7 +86,7 @@ EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
-            "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync"]
+            "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync", "gbh_run_io"]
 
 _LIB = None
 
@@ -133,6 +133,7 @@ def load(build_if_missing: bool = True):
     lib.gbh_deliver_remote.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
     lib.gbh_step_io.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_void_p]
     lib.gbh_io_sync.argtypes = [C.c_void_p]
+    lib.gbh_run_io.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_void_p]
     lib.gbh_loss_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(GbhLossSpec), _dp, _dp, _dp, _dp]
     _LIB = lib
     return lib
@@ -387,6 +388,18 @@ class Engine:
 
     def io_sync(self):
         self._check(self.lib.gbh_io_sync(self.h))
+
+    def run_io(self, host_in, host_out, nsteps: int, block: int = 0, stream_handle: int = 0):
+        """gbh_run_io: nsteps steps, row k of host_in (nsteps x n_in) applied
+        before step k, row k of host_out (nsteps x n_out) read after it; the
+        copies stream in blocks of `block` steps. Returns when host_out is
+        complete."""
+        for a, n in ((host_in, len(getattr(self, "_in_s", ()))), (host_out, len(getattr(self, "_out_s", ())))):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.size < nsteps * n):
+                raise ValueError("run_io: arrays must be C-contiguous float64 with nsteps rows")
+        pin = _ptr(host_in, _dp) if host_in is not None else None
+        pout = _ptr(host_out, _dp) if host_out is not None else None
+        self._check(self.lib.gbh_run_io(self.h, pin, pout, int(nsteps), int(block), C.c_void_p(stream_handle)))
 
     def get_outputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
         self._check(self.lib.gbh_get_outputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))

@@ -279,6 +279,24 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream);
 int gbh_step_io(gbh_engine *e, const double *host_in, double *host_out, int nsteps, void *stream);
 int gbh_io_sync(gbh_engine *e);
 
+/*
+ * gbh_run_io -- nsteps steps with per-step host inputs and outputs streamed
+ * in blocks: host_in holds nsteps rows of the registered inputs (row k is
+ * applied before step k, as gbh_set_inputs_async), host_out receives nsteps
+ * rows of the registered outputs (row k after step k). Each block of `block`
+ * steps (0 = 16) is copied host->device in one transfer on a copy stream
+ * while the previous block steps, and its outputs device->host in one
+ * transfer while the next block steps; between two steps one kernel gathers
+ * the outputs and scatters the next inputs. Staging is double-buffered on
+ * the device (2 x block x (n_in + n_out) doubles). Either pointer may be
+ * NULL. Returns when host_out is complete. Results equal nsteps rounds of
+ * gbh_set_inputs_async + gbh_run_async(1) + gbh_get_outputs_async. Host
+ * buffers should be pinned for the copies to overlap. Serves h_in_msgs /
+ * h_out_msgs-style stimulus and recording for a whole run (the reference
+ * runs both on the host every step, hines_msgs.c:351-486).
+ */
+int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nsteps, int block, void *stream);
+
 /* Per-solver spike counts since creation (int64[nsolvers]). */
 int gbh_get_spike_counts(gbh_engine *e, int64_t *counts);
 
