@@ -38,7 +38,7 @@ typedef struct gbh_hstate {
     int nin;
     int *in_chip;        /* chip[] index of every ininfo target */
     double *in_vals;
-    int64_t starts[12][2];
+    int64_t starts[14][2];
 } gbh_hstate;
 
 static Hsolve *gbh_registry[GBH_MAX_SOLVERS];
@@ -86,6 +86,24 @@ static int gbh_fill_desc(Hsolve *h, gbh_batch_desc *d, gbh_tables *t, int *scala
     st[6][1] = (int64_t)h->sntab * SYNSIZE;
     d->stab_start = st[6];
     d->stablist = h->stablist;
+    if (h->ndiffs) {   /* difshell systems (h_init_conc_solve / h_setup_conc_solve) */
+        st[10][0] = 0;
+        st[10][1] = h->ndiffs;
+        d->diff_start = st[10];
+        d->dconc = h->dconc;
+        d->nshells = h->nshells;
+        d->nshrows = h->nshrows;
+        d->nshfix = h->nshfix;
+        d->fbufval = h->fbufval;
+        st[11][0] = 0;
+        st[11][1] = h->fcoval[h->ndiffs];
+        d->covals0_start = st[11];
+        d->covals0 = h->covals0;
+        st[12][0] = 0;
+        st[12][1] = h->fbufval[h->ndiffs];
+        d->bufvals_start = st[12];
+        d->bufvals = h->bufvals;
+    }
     return 0;
 }
 
@@ -103,8 +121,8 @@ int gbh_init(Hsolve *h)
     int64_t *idx;
 
     if (h->accel_state) return 0;
-    if (h->spikegen || h->ndiffs) {
-        fprintf(stderr, "gbh_init %s: spike events and diffusion shells need the batch API\n", h->name);
+    if (h->spikegen) {
+        fprintf(stderr, "gbh_init %s: spike events need the batch API\n", h->name);
         return -1;
     }
     s = (gbh_hstate *)calloc(1, sizeof(*s));

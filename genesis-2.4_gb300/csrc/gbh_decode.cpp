@@ -561,37 +561,244 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         }
         if (row != n) return fail(c, GBH_ERR_OPCODE, row, 0, o, "ops[] has %d compartments for %d rows", row, n);
 
-        // ---- concops (hines_conc_chip.c:79-219) ----
+        // ---- concops (hines_conc_chip.c:59-221) and diffusion systems
+        //      (hines_conc.c:39-396) ----
         {
             const int *cops = d->concops + d->concops_start[si];
             const int64_t ncops = d->concops_start[si + 1] - d->concops_start[si];
             const int64_t ccbase = d->concchip_start[si];
-            int64_t co = 0, cc = 0;
-            std::vector<int> pool_owner(d->conc_start[si + 1] - d->conc_start[si], -1);
+            const int64_t ncchip = d->concchip_start[si + 1] - ccbase;
+            const int nconc = (int)(d->conc_start[si + 1] - d->conc_start[si]);
+            const int64_t ds0 = d->diff_start ? d->diff_start[si] : 0;
+            const int64_t ds1 = d->diff_start ? d->diff_start[si + 1] : 0;
+            // Every conc belongs to one neuron: the one whose compartment program
+            // reads it, or the one of a conc it is tied to (same diffusion system,
+            // the shell a Hill pump draws from, the buffer of a pool).
+            std::vector<int> uf(nconc), owner(nconc, -1);
+            for (int k = 0; k < nconc; ++k) uf[k] = k;
+            auto find = [&](int x) {
+                while (uf[x] != x) x = uf[x] = uf[uf[x]];
+                return x;
+            };
+            auto unite = [&](int a2, int b2) { uf[find(a2)] = find(b2); };
+            auto claim = [&](int k, int nrn) -> bool {
+                const int r = find(k);
+                if (owner[r] >= 0 && owner[r] != nrn) return false;
+                owner[r] = nrn;
+                return true;
+            };
+            auto cidx = [&](int64_t at, int k) -> int {
+                if (k < 0 || k >= nconc) {
+                    fail(c, GBH_ERR_ARG, -1, cops[at], at, "conc index %d out of range", k);
+                    return -1;
+                }
+                return k;
+            };
+            for (int64_t i = ds0; i < ds1; ++i) {
+                const int c0 = d->dconc[i], ms = d->nshells[i], w = d->nshrows[i];
+                if (ms < 2 || w < 1 || d->nshfix[i] < 0 || d->nshfix[i] > w - 1 || c0 < 0 ||
+                    (int64_t)c0 + (int64_t)ms * w > nconc)
+                    return fail(c, GBH_ERR_ARG, -1, 0, i - ds0,
+                                "diffusion system %lld: %d shells x %d rows at conc %d do not fit",
+                                (long long)(i - ds0), ms, w, c0);
+                for (int j = 1; j < ms * w; ++j) unite(c0, c0 + j);
+            }
+            // first pass: ties between concs and the current group conc
+            {
+                int64_t co = 0;
+                int ix = 0;
+                while (co < ncops) {
+                    const int op = cops[co++];
+                    if (op == R_LCONC || op == R_LCACONC) break;
+                    auto need2 = [&](int k) { return co + k <= ncops; };
+                    if (op == R_CONC || op == R_FCONC || op == R_CACONC) {
+                        if (!need2(1)) return fail(c, GBH_ERR_OPCODE, -1, op, co, "truncated concops");
+                        const int k = cidx(co, cops[co]);
+                        if (k < 0) return GBH_ERR_ARG;
+                        if (op != R_CACONC) ix = k;
+                        co++;
+                    } else if (op == R_TAUPUMP) {
+                        if (!need2(1)) return fail(c, GBH_ERR_OPCODE, -1, op, co, "truncated TAUPUMP_OP");
+                        const int vr = cops[co++];
+                        if (vr < 0 || vr >= n) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "vm index %d out of range", vr);
+                        if (!claim(ix, tree_neuron[tree[vr]] - nbase))
+                            return fail(c, GBH_ERR_UNSUPPORTED, vr, op, co - 1, "pump reads the Vm of another neuron");
+                    } else if (op == R_HILLPUMP) {
+                        co++;
+                    } else if (op == R_PHILLPUMP) {
+                        if (!need2(2)) return fail(c, GBH_ERR_OPCODE, -1, op, co, "truncated PHILLPUMP_OP");
+                        const int k = cidx(co + 1, cops[co + 1]);
+                        if (k < 0) return GBH_ERR_ARG;
+                        unite(ix, k);
+                        co += 2;
+                    } else if (op == R_BUFFER) {
+                        if (!need2(1)) return fail(c, GBH_ERR_OPCODE, -1, op, co, "truncated BUFFER_OP");
+                        const int k = cidx(co, cops[co]);
+                        if (k < 0) return GBH_ERR_ARG;
+                        unite(ix, k);
+                        co++;
+                    } else if (op != R_FLUXCONC && op != R_CTAUPUMP && op != R_MMPUMP && op != R_POOL) {
+                        return fail(c, GBH_ERR_OPCODE, -1, op, co - 1, "concops opcode %d is not implemented", op);
+                    }
+                }
+            }
             for (int k = 0; k < ntrees; ++k)
-                for (int pc : nbs[k].n->pool_conc) pool_owner[pc] = k;
+                for (int pc : nbs[k].n->pool_conc)
+                    if (!claim(pc, k))
+                        return fail(c, GBH_ERR_UNSUPPORTED, -1, 0, pc,
+                                    "conc %d is tied to concentrations of two neurons", pc);
+            auto owner_of = [&](int k) -> int {
+                const int r = find(k);
+                if (owner[r] < 0 && ntrees == 1) owner[r] = 0;
+                return owner[r];
+            };
+            // second pass: micro-ops into the owning neuron's pool program
+            int64_t co = 0, cc = 0;
+            int ix = 0, grp = -1;   // current group conc and its owner
+            auto chipf = [&](NB &nb, int64_t k) { return nb.fld(FS_CCHIP, k, d->concchip[ccbase + k]); };
+            auto need_chips = [&](int k) { return cc + k <= ncchip; };
+            auto open_group = [&](int k) -> int {
+                const int o2 = owner_of(k);
+                if (o2 < 0) return -1;
+                NB &nb = nbs[o2];
+                nb.n->pool_prog.push_back(PO_GRP);
+                nb.n->pool_prog.push_back(nb.pool(k));
+                nb.n->has_cd = true;
+                return o2;
+            };
+            auto close_group = [&](bool store) {
+                if (grp >= 0 && store) nbs[grp].n->pool_prog.push_back(PO_STORE);
+            };
+            bool opened = false;
             while (co < ncops) {
                 const int op = cops[co++];
                 if (op == R_LCACONC) break;
+                if (op == R_LCONC) {
+                    if (!opened) grp = open_group(ix), opened = true;
+                    close_group(true);
+                    break;
+                }
                 if (op == R_CACONC) {
                     const int k = cops[co++];
-                    if (k < 0 || k >= (int)pool_owner.size())
-                        return fail(c, GBH_ERR_ARG, -1, op, co - 1, "conc index %d out of range", k);
-                    if (pool_owner[k] < 0)
+                    const int o2 = owner_of(k);
+                    if (o2 < 0)
                         return fail(c, GBH_ERR_UNSUPPORTED, -1, op, co - 1,
                                     "Ca pool %d is not used by any compartment program", k);
-                    NB &nb = nbs[pool_owner[k]];
+                    if (!need_chips(3)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    NB &nb = nbs[o2];
                     std::vector<int> &PP = nb.n->pool_prog;
                     PP.push_back(PO_CACONC);
                     PP.push_back(nb.pool(k));
-                    PP.push_back(nb.fld(FS_CCHIP, cc, d->concchip[ccbase + cc]));
-                    PP.push_back(nb.fld(FS_CCHIP, cc + 1, d->concchip[ccbase + cc + 1]));
-                    PP.push_back(nb.fld(FS_CCHIP, cc + 2, d->concchip[ccbase + cc + 2]));
+                    PP.push_back(chipf(nb, cc));
+                    PP.push_back(chipf(nb, cc + 1));
+                    PP.push_back(chipf(nb, cc + 2));
                     cc += 3;
-                } else {
-                    return fail(c, GBH_ERR_OPCODE, -1, op, co - 1,
-                                "concops opcode %d (diffusion shells, pumps, buffers) is not implemented", op);
+                    continue;
                 }
+                if (op == R_CONC || op == R_FCONC) {
+                    if (opened) close_group(op == R_CONC);
+                    ix = cops[co++];
+                    grp = open_group(ix);
+                    opened = true;
+                    if (grp < 0)
+                        return fail(c, GBH_ERR_UNSUPPORTED, -1, op, co - 1,
+                                    "conc %d is not tied to a neuron of a multi-neuron solver", ix);
+                    continue;
+                }
+                if (!opened) {   // ops before the first FCONC act on conc 0
+                    grp = open_group(ix);
+                    opened = true;
+                    if (grp < 0) return fail(c, GBH_ERR_UNSUPPORTED, -1, op, co - 1, "conc 0 has no neuron");
+                }
+                NB &nb = nbs[grp];
+                std::vector<int> &PP = nb.n->pool_prog;
+                switch (op) {
+                case R_FLUXCONC:
+                    if (!need_chips(2)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_FLUXCONC, chipf(nb, cc), chipf(nb, cc + 1)});
+                    cc += 2;
+                    break;
+                case R_CTAUPUMP:
+                    if (!need_chips(2)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_CTAU, chipf(nb, cc), chipf(nb, cc + 1)});
+                    cc += 2;
+                    break;
+                case R_TAUPUMP: {
+                    const int vr = cops[co++];
+                    if (!need_chips(5)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_TAU, vr - nb.n->row0, chipf(nb, cc), chipf(nb, cc + 1), chipf(nb, cc + 2),
+                                         chipf(nb, cc + 3), chipf(nb, cc + 4)});
+                    cc += 5;
+                    break;
+                }
+                case R_MMPUMP:
+                    if (!need_chips(2)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_MM, chipf(nb, cc), chipf(nb, cc + 1)});
+                    cc += 2;
+                    break;
+                case R_HILLPUMP: {
+                    const int h = cops[co++];
+                    if (!need_chips(2)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_HILL, h, chipf(nb, cc), chipf(nb, cc + 1)});
+                    cc += 2;
+                    break;
+                }
+                case R_PHILLPUMP: {
+                    const int h = cops[co], k = cops[co + 1];
+                    co += 2;
+                    if (!need_chips(3)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_PHILL, h, nb.pool(k), chipf(nb, cc), chipf(nb, cc + 1), chipf(nb, cc + 2)});
+                    cc += 3;
+                    break;
+                }
+                case R_BUFFER: {
+                    const int k = cops[co++];
+                    if (!need_chips(3)) return fail(c, GBH_ERR_ARG, -1, op, co - 1, "concchip[] too short");
+                    PP.insert(PP.end(), {PO_BUFFER, nb.pool(k), chipf(nb, cc), chipf(nb, cc + 1), chipf(nb, cc + 2)});
+                    cc += 3;
+                    break;
+                }
+                case R_POOL:
+                    PP.push_back(PO_POOL);
+                    break;
+                default:
+                    return fail(c, GBH_ERR_OPCODE, -1, op, co - 1, "concops opcode %d is not implemented", op);
+                }
+            }
+            // diffusion systems, in the order the reference solves them
+            int64_t q0 = d->covals0_start ? d->covals0_start[si] : 0;
+            const int64_t q1 = d->covals0_start ? d->covals0_start[si + 1] : 0;
+            const int64_t b0 = d->bufvals_start ? d->bufvals_start[si] : 0;
+            const int64_t nbufv = d->bufvals_start ? d->bufvals_start[si + 1] - b0 : 0;
+            for (int64_t i = ds0; i < ds1; ++i) {
+                const int c0 = d->dconc[i], ms = d->nshells[i], w = d->nshrows[i], nfix = d->nshfix[i];
+                const int o2 = owner_of(c0);
+                if (o2 < 0)
+                    return fail(c, GBH_ERR_UNSUPPORTED, -1, 0, i - ds0,
+                                "diffusion system %lld is not tied to a neuron", (long long)(i - ds0));
+                // covals0 entries it consumes: one per fixed buffer, one or two
+                // (inner shells) per diffusible buffer and per shell row
+                int64_t nq = 0;
+                for (int m = 0; m < ms; ++m) nq += nfix + (int64_t)(w - nfix) * ((m == 0 || m == ms - 1) ? 1 : 2);
+                const int nb3 = 3 * (w - 1);
+                if (q0 + nq > q1 || (w > 1 && (d->fbufval[i] < 0 || d->fbufval[i] + nb3 > nbufv)))
+                    return fail(c, GBH_ERR_ARG, -1, 0, i - ds0, "covals0[]/bufvals[] too short for diffusion system %lld",
+                                (long long)(i - ds0));
+                NB &nb = nbs[o2];
+                Neuron &N = *nb.n;
+                N.has_cd = true;
+                const int nfac = w > 1 ? ms * w * w : ms + 1, npart = ms * w;
+                std::vector<int> &PP = N.pool_prog;
+                PP.insert(PP.end(), {PO_DIFF, ms, w, nfix, N.crank, N.nscratch, (int)nq, w > 1 ? nb3 : 0});
+                for (int j = 0; j < ms * w; ++j) PP.push_back(nb.pool(c0 + j));
+                for (int64_t q = 0; q < nq; ++q) PP.push_back(nb.fld(FS_COV0, q0 + q, d->covals0[q0 + q]));
+                if (w > 1)
+                    for (int j = 0; j < nb3; ++j) {
+                        const int64_t bi = b0 + d->fbufval[i] + j;
+                        PP.push_back(nb.fld(FS_BUFV, bi, d->bufvals[bi]));
+                    }
+                N.nscratch += nfac + npart;
+                q0 += nq;
             }
         }
         for (int k = 0; k < ntrees; ++k) {
@@ -603,6 +810,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             put(N.nrows); put(N.table_set); put(N.crank); put(N.c5); put(N.interp);
             put((int)N.fsrc.size()); put((int)N.iops.size()); put((int)N.pool_conc.size());
             put((int)N.giv_ref.size()); put((int)N.syn_op.size()); put(N.spike_op >= 0);
+            put(N.has_cd); put(N.nscratch);
             put((int)N.prog.size());
             for (int v : N.prog) put(v);
             for (int v : N.pool_prog) put(v);

@@ -9,7 +9,7 @@
 
 namespace gbh {
 
-enum FieldKind { FS_CHIP = 0, FS_GIV = 1, FS_CONST = 2, FS_CCHIP = 3, FS_WDT = 4 };
+enum FieldKind { FS_CHIP = 0, FS_GIV = 1, FS_CONST = 2, FS_CCHIP = 3, FS_WDT = 4, FS_COV0 = 5, FS_BUFV = 6 };
 
 struct FieldSrc {
     int kind;
@@ -35,6 +35,8 @@ struct Neuron {
     std::vector<double> A, B, C;  // per slot
     std::vector<int> ridx;        // per slot: ravals index of A, B, C (-1: none)
     int spike_op = -1;
+    bool has_cd = false;          // diffusion systems: codiag/coresult rows in use
+    int nscratch = 0;             // scratch rows of its diffusion solves
     std::string key;              // grouping signature
 };
 

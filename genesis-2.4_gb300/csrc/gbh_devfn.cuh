@@ -43,6 +43,9 @@ struct DevView {
     // Grid barrier {arrivals, generation, abort} of a cooperative multi-step
     // launch (spikes cross tiles every step); null: no barrier.
     unsigned *gbar;
+    // concentration rows beside C: coresult and codiag of each pool row
+    // (diffusion systems), and per-lane scratch rows of the diffusion solves
+    double *CR, *CD, *S;
 };
 
 // Barrier over all blocks of a cooperative launch: the last block to arrive
@@ -235,4 +238,307 @@ __device__ __forceinline__ df dpow(df g, df x, int p)
 }
 
 
+
+// ---- concentration pool phase (FP64 in every form) ------------------------
+// Row views of one lane: conc C, flux F, coresult CR, codiag CD, fields P,
+// vm V, scratch S (all neuron-interleaved, stride 32).
+struct PoolLane {
+    double *C, *F, *CR, *CD, *S;
+    const double *P, *V;
+    double dt;
+    int crank;
+};
+
+__device__ __forceinline__ double hill_factor(int h, double X)
+{
+    return h == 2 ? X : h == 3 ? X * X : h == 4 ? X * X * X : 1.0;
+}
+
+// Shells without buffers, tridiagonal in the shell index (hines_conc.c:337-395).
+// R: pool row of each shell, K: field row of each coupling term in the order
+// consumed, fac/part: scratch rows.
+__device__ __forceinline__ void diff_shells_dev(const PoolLane &L, int ms, const int *R, const int *K, int fac,
+                                                int part)
+{
+    constexpr int W = 32;
+#define GBH_C(j) L.C[R[j] * W]
+#define GBH_CD(j) L.CD[R[j] * W]
+#define GBH_CR(j) L.CR[R[j] * W]
+#define GBH_K(q) L.P[K[q] * W]
+    int q = 0, m;
+    double up = GBH_K(q), dn, dd, f, x;
+    q++;
+    dd = up + GBH_CD(0);
+    GBH_CD(0) = 1.0;
+    L.S[part * W] = (GBH_C(0) + GBH_CR(0)) / dd;
+    for (m = 1; m < ms - 1; m++) {
+        f = -up / dd;
+        L.S[(fac + m) * W] = f;
+        dn = GBH_K(q);
+        up = GBH_K(q + 1);
+        q += 2;
+        dd = GBH_CD(m) + dn * (1.0 + f) + up;
+        GBH_CD(m) = 1.0;
+        L.S[(part + m) * W] = (GBH_C(m) + GBH_CR(m) + dn * L.S[(part + m - 1) * W]) / dd;
+    }
+    f = -up / dd;
+    L.S[(fac + m) * W] = f;
+    dn = GBH_K(q);
+    dd = GBH_CD(m) + dn * (1.0 + f);
+    GBH_CD(m) = 1.0;
+    x = (GBH_C(m) + GBH_CR(m) + dn * L.S[(part + m - 1) * W]) / dd;
+    if (L.crank) {
+        GBH_C(m) = x + x - GBH_C(m);
+        for (m--; m >= 0; m--) {
+            x = L.S[(part + m) * W] - L.S[(fac + m + 1) * W] * x;
+            GBH_C(m) = x + x - GBH_C(m);
+        }
+    } else {
+        GBH_C(m) = x;
+        for (m--; m >= 0; m--) {
+            x = L.S[(part + m) * W] - L.S[(fac + m + 1) * W] * x;
+            GBH_C(m) = x;
+        }
+    }
+}
+
+// Shells with fixed and diffusible buffers (hines_conc.c:123-335): rows of a
+// shell (nfix fixed buffers, diffusible buffers, the shell) eliminated as
+// they are filled; BV: field rows of the buffer rates (3 per buffer).
+// Scratch: fac[(shell*w + row)*w + column], part[shell*w + row].
+__device__ __forceinline__ void diff_buffered_dev(const PoolLane &L, int ms, int w, int nfix, const int *R,
+                                                  const int *K, const int *BV, int fac, int part)
+{
+    constexpr int W = 32;
+#define GBH_F(i) L.S[(fac + (i)) * W]
+#define GBH_PT(i) L.S[(part + (i)) * W]
+#define GBH_B(i) L.P[BV[i] * W]
+    const int w1 = w - 1, sq = w * w, last = ms - 1;
+    int q = 0, m, n, nb, nc = 0, pr = 0, prev = -1, row = 0, srow = sq - w, sprev = srow - sq, cs = w1;
+    double co = GBH_C(cs), dsh, rsh, dd, t, t2, h;
+    for (m = 0; m < ms; m++) {
+        dsh = GBH_CD(cs);
+        GBH_CD(cs) = 1.0;
+        rsh = GBH_CR(cs);
+        for (n = 0, nb = 0; n < nfix; n++, nb += 3) {
+            GBH_F(srow + n) = dd = GBH_B(nb) * co + GBH_B(nb + 1);
+            dsh += t = GBH_B(nb) * GBH_C(nc);
+            dd = 1.0 / (1.0 + dd);
+            GBH_F(row) = t * dd;
+            rsh += t2 = -GBH_B(nb + 1) * GBH_C(nc) + GBH_K(q);
+            q++;
+            GBH_PT(pr) = (GBH_C(nc) + t2) * dd;
+            pr++;
+            nc++;
+            row += w;
+        }
+        for (; n < w1; n++, nb += 3) {
+            GBH_F(srow + n) = dd = GBH_B(nb) * co + GBH_B(nb + 1);
+            dsh += t = GBH_B(nb) * GBH_C(nc);
+            rsh += t2 = -GBH_B(nb + 1) * GBH_C(nc) + GBH_B(nb + 2);
+            if (m) {
+                h = GBH_K(q) * GBH_F(row - sq);
+                if (m < last) {
+                    dd += 1.0 + GBH_K(q + 1) + GBH_K(q) * (1.0 + GBH_F(row - sq + 1)) - h * GBH_F(sprev + n);
+                    GBH_F(row + 1) = -GBH_K(q + 1) / dd;
+                    t2 += GBH_K(q) * GBH_C(nc - w) + (1.0 - GBH_K(q) - GBH_K(q + 1)) * GBH_C(nc) +
+                          GBH_K(q + 1) * GBH_C(nc + w);
+                } else {
+                    dd += 1.0 + GBH_K(q) * (1.0 + GBH_F(row - sq + 1)) - h * GBH_F(sprev + n);
+                    t2 += GBH_K(q) * GBH_C(nc - w) + (1.0 - GBH_K(q)) * GBH_C(nc);
+                }
+                GBH_PT(pr) = (t2 + GBH_K(q) * GBH_PT(pr - w) - h * GBH_PT(prev)) / dd;
+                q += m < last ? 2 : 1;
+            } else {
+                dd += 1.0 + GBH_K(q);
+                GBH_F(row + 1) = -GBH_K(q) / dd;
+                GBH_PT(pr) = (t2 + (1.0 - GBH_K(q)) * GBH_C(nc) + GBH_K(q) * GBH_C(nc + w)) / dd;
+                q++;
+            }
+            GBH_F(row) = t / dd;
+            pr++;
+            nc++;
+            row += w;
+        }
+        if (m) {
+            if (m < last) {
+                dsh += GBH_K(q + 1) + GBH_K(q) * (1.0 + GBH_F(sprev + w1));
+                rsh += GBH_K(q) * (GBH_C(nc - w) + GBH_PT(prev)) + (1.0 - GBH_K(q) - GBH_K(q + 1)) * co;
+                cs += w;
+                co = GBH_C(cs);
+                rsh += GBH_K(q + 1) * co;
+            } else {
+                dsh += GBH_K(q) * (1.0 + GBH_F(sprev + w1));
+                rsh += GBH_K(q) * (GBH_C(nc - w) + GBH_PT(prev)) + (1.0 - GBH_K(q)) * co;
+            }
+        } else {
+            dsh += GBH_K(q);
+            rsh += (1.0 - GBH_K(q)) * co;
+            cs += w;
+            co = GBH_C(cs);
+            rsh += GBH_K(q) * co;
+        }
+        for (n = 0, nb = sprev; n < nfix; n++) {
+            nb += w;
+            prev++;
+            dsh -= GBH_F(row + n) * GBH_F(nb);
+            rsh -= GBH_F(row + n) * GBH_PT(prev);
+        }
+        for (; n < w1; n++) {
+            nb += w;
+            prev++;
+            const double e = m ? GBH_F(row + n) + GBH_K(q) * GBH_F(sprev + n) : GBH_F(row + n);
+            dsh -= e * GBH_F(nb);
+            rsh -= e * GBH_PT(prev);
+            if (m < last) GBH_F(row + n) *= -GBH_F(nb + 1);
+        }
+        if (m < last) {
+            for (n = nfix; n < w1; n++) GBH_F(row + n) /= dsh;
+            if (m) {
+                GBH_F(row + w1) = -GBH_K(q + 1) / dsh;
+                q += 2;
+            } else {
+                GBH_F(row + w1) = -GBH_K(q) / dsh;
+                q++;
+            }
+            GBH_PT(pr) = rsh / dsh;
+            prev = pr++;
+            nc++;
+            sprev = row;
+            srow += sq;
+            row += w;
+        } else {
+            co = GBH_C(nc) = rsh / dsh;
+            nc--;
+            q++;
+        }
+    }
+    for (m = last; m >= 0; m--) {
+        if (m < last) {
+            row -= w;
+            co = GBH_PT(--pr) - GBH_F(row + w1) * GBH_C(nc + w);
+            for (n = nfix; n < w1; n++) co -= GBH_F(row + n) * GBH_C(nc + n + 1);
+            GBH_C(nc) = co;
+            nc--;
+            for (n = w1; n > nfix; n--) {
+                row -= w;
+                GBH_C(nc) = GBH_PT(--pr) - GBH_F(row) * co - GBH_F(row + 1) * GBH_C(nc + w);
+                nc--;
+            }
+        } else {
+            for (n = w1; n > nfix; n--) {
+                row -= w;
+                GBH_C(nc) = GBH_PT(--pr) - GBH_F(row) * co;
+                nc--;
+            }
+        }
+        for (; n > 0; n--) {
+            row -= w;
+            GBH_C(nc) = GBH_PT(--pr) - GBH_F(row) * co;
+            nc--;
+        }
+    }
+#undef GBH_F
+#undef GBH_PT
+#undef GBH_B
+#undef GBH_C
+#undef GBH_CD
+#undef GBH_CR
+#undef GBH_K
+}
+
+// The pool program of one lane (Ca_concen pools, concops groups, diffusion
+// solves). Returns false on an unknown micro-op.
+__device__ __forceinline__ bool pool_phase(const int *pp, const PoolLane &L)
+{
+    constexpr int W = 32;
+    int ix = 0;
+    double res = 0.0;
+    while (pp[0] != 0) {
+        switch (pp[0]) {
+        case PO_CACONC: {
+            double *cx = &L.C[pp[1] * W];
+            const double base = L.P[pp[2] * W];
+            const double itau = L.P[pp[3] * W];
+            *cx = base + ((*cx - base) * (2.0 - itau) + (L.F[pp[1] * W] * L.P[pp[4] * W])) / itau;
+            pp += 5;
+            break;
+        }
+        case PO_GRP:
+            ix = pp[1];
+            res = 0.0;
+            pp += 2;
+            break;
+        case PO_STORE:
+            L.CR[ix * W] = res;
+            pp += 1;
+            break;
+        case PO_FLUXCONC:
+            res += L.P[pp[1] * W] + L.F[ix * W] * L.P[pp[2] * W];
+            pp += 3;
+            break;
+        case PO_CTAU:
+            res += L.P[pp[1] * W];
+            L.CD[ix * W] += L.P[pp[2] * W];
+            pp += 3;
+            break;
+        case PO_TAU: {
+            const double itau = L.dt / (L.P[pp[2] * W] + L.P[pp[3] * W] *
+                                        (exp((L.V[pp[1] * W] - L.P[pp[4] * W]) * L.P[pp[5] * W])));
+            res += L.P[pp[6] * W] * itau;
+            L.CD[ix * W] += itau;
+            pp += 7;
+            break;
+        }
+        case PO_MM:
+            L.CD[ix * W] += L.P[pp[1] * W] / (L.C[ix * W] + L.P[pp[2] * W]);
+            pp += 3;
+            break;
+        case PO_HILL: {
+            const double X = L.C[ix * W];
+            double c = hill_factor(pp[1], X);
+            c = c / (c * X + L.P[pp[2] * W]);
+            L.CD[ix * W] += L.P[pp[3] * W] * c;
+            pp += 4;
+            break;
+        }
+        case PO_PHILL: {
+            const double X = L.C[pp[2] * W];
+            double c = hill_factor(pp[1], X);
+            c = c / (c * X + L.P[pp[3] * W]);
+            L.CD[pp[2] * W] += L.P[pp[4] * W] * c;
+            res += L.P[pp[5] * W] * c * X;
+            pp += 6;
+            break;
+        }
+        case PO_BUFFER: {
+            double *bf = &L.C[pp[1] * W];
+            const double X = L.P[pp[2] * W];
+            const double c = ((1.0 - X) * *bf + L.P[pp[3] * W]) / (1.0 + X + L.P[pp[4] * W] * L.C[ix * W]);
+            res += c - *bf;
+            *bf = c;
+            pp += 5;
+            break;
+        }
+        case PO_POOL:
+            L.C[ix * W] += res;
+            pp += 1;
+            break;
+        case PO_DIFF: {
+            const int ms = pp[1], w = pp[2], nfix = pp[3], sbase = pp[5], nq = pp[6], nb = pp[7];
+            const int *R = pp + 8, *K = R + ms * w, *BV = K + nq;
+            PoolLane L2 = L;
+            L2.crank = pp[4];
+            const int nfac = w > 1 ? ms * w * w : ms + 1;
+            if (w > 1) diff_buffered_dev(L2, ms, w, nfix, R, K, BV, sbase, sbase + nfac);
+            else diff_shells_dev(L2, ms, R, K, sbase, sbase + nfac);
+            pp += 8 + ms * w + nq + nb;
+            break;
+        }
+        default:
+            return false;
+        }
+    }
+    return true;
+}
 }  // namespace gbh

@@ -101,6 +101,7 @@ struct gbh_engine {
     DBuf<float4> d_tabdf;
     std::vector<std::vector<char>> type_df;     // mixed: field rows stored as packed double-float
     DBuf<double> d_P, d_V, d_C, d_F, d_A, d_B, d_Cb, d_giv, d_stab;
+    DBuf<double> d_CR, d_CD, d_S;   // coresult / codiag rows, diffusion scratch
     DBuf<int> d_I, d_par;
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
@@ -119,7 +120,7 @@ struct gbh_engine {
     DBuf<int> d_status;
     int ring_len = 2;
     int64_t rows_fld = 0, rows_int = 0, rows_pool = 0, rows_giv = 0, rows_vm = 0, rows_topo = 0,
-            rows_syn = 0;
+            rows_syn = 0, rows_scr = 0;
     std::vector<Launch> launches;
     int steps_per_launch = 1;
     bool has_network = false;
@@ -331,6 +332,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             tt.interp = N.interp;
             tt.has_spike = N.spike_op >= 0;
             tt.nsyn = (int)N.syn_op.size();
+            tt.has_cd = N.has_cd;
+            tt.nscratch = N.nscratch;
             type_of_key[N.key] = (int)e->types.size();
             e->types.push_back(tt);
             members.emplace_back();
@@ -380,6 +383,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             t.vm = e->rows_vm; e->rows_vm += tt.nslots;
             t.topo = e->rows_topo; e->rows_topo += tt.nslots;
             t.syn = e->rows_syn; e->rows_syn += (int64_t)tt.nsyn * e->ring_len;
+            t.scr = e->rows_scr; e->rows_scr += tt.nscratch;
             t.first_neuron = gneuron;
             gneuron += LANES;
             for (int l = 0; l < t.nlanes; ++l) {
@@ -569,6 +573,13 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_V.upload(V);
     rc |= e->d_C.upload(C);
     rc |= e->d_F.upload(std::vector<double>(C.size(), 0.0));
+    bool any_cd = false;
+    for (const TileType &tt : e->types) any_cd = any_cd || tt.has_cd;
+    if (any_cd) {   // coresult 0, codiag 1 (hines_conc_init.c:121-126), solve scratch
+        rc |= e->d_CR.upload(std::vector<double>(C.size(), 0.0));
+        rc |= e->d_CD.upload(std::vector<double>(C.size(), 1.0));
+        rc |= e->d_S.upload(std::vector<double>(std::max<int64_t>(e->rows_scr, 1) * L, 0.0));
+    }
     rc |= e->d_A.upload(A);
     rc |= e->d_B.upload(B);
     rc |= e->d_Cb.upload(Cb);
@@ -729,6 +740,9 @@ DevView view_of(gbh_engine *e)
     v.V = e->d_V.p;
     v.C = e->d_C.p;
     v.F = e->d_F.p;
+    v.CR = e->d_CR.p;
+    v.CD = e->d_CD.p;
+    v.S = e->d_S.p;
     v.parent = e->d_par.p;
     v.A = e->d_A.p;
     v.B = e->d_B.p;
@@ -970,6 +984,8 @@ int autotune_trials(gbh_engine *e)
     rc |= keep(e->d_P.p, e->d_P.n * sizeof(double));
     rc |= keep(e->d_V.p, e->d_V.n * sizeof(double));
     rc |= keep(e->d_C.p, e->d_C.n * sizeof(double));
+    rc |= keep(e->d_CR.p, e->d_CR.n * sizeof(double));
+    rc |= keep(e->d_CD.p, e->d_CD.n * sizeof(double));
     rc |= keep(e->d_I.p, e->d_I.n * sizeof(int));
     rc |= keep(e->d_ring.p, e->d_ring.n * sizeof(unsigned));
     rc |= keep(e->d_spikes.p, e->d_spikes.n * sizeof(unsigned long long));
@@ -1426,6 +1442,8 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
             tt.crank = N.crank;
             tt.chanmode5 = N.c5;
             tt.interp = N.interp;
+            tt.has_cd = N.has_cd;
+            tt.nscratch = N.nscratch;
             keys[N.key] = (int)types.size();
             types.push_back(tt);
             parents.push_back(N.parent);
@@ -2121,7 +2139,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_A.release(); e->d_B.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_A.release(); e->d_B.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

@@ -15,7 +15,8 @@ enum RefOp {
     R_SYN3 = 4101, R_MGBLOCK = 4200, R_NEWVOLT = 5100, R_NEWCONC1 = 5110,
     R_NEWCONC2 = 5111, R_DOMAIN = 5112,
     R_CONC = 10100, R_FCONC = 10101, R_LCONC = 10102, R_FLUXCONC = 10103,
-    R_CACONC = 10200, R_LCACONC = 10202
+    R_CACONC = 10200, R_LCACONC = 10202, R_TAUPUMP = 11000, R_CTAUPUMP = 11001, R_MMPUMP = 11010,
+    R_HILLPUMP = 11011, R_PHILLPUMP = 11012, R_BUFFER = 12000, R_POOL = 12100
 };
 enum RefFunc { F_ELIM = 0, F_SET_DIAG = 1, F_SKIP_DIAG = 2, F_FASTSIB = 3, F_COPY = 4,
                F_SIB = 5, F_CALC = 6, F_FINISH = 7 };
@@ -48,7 +49,24 @@ enum MicroOp {
     M_END            // fTbyc fDiag gIm
 };
 enum GateKind { GK_1V = 0, GK_1C = 1, GK_2V = 2, GK_2C = 3 };
-enum PoolOp { PO_CACONC = 1 };   // pConc fBase fItau fDtB
+// Pool-phase micro-ops (do_h4_conc_chip_update, hines_conc_chip.c:59-221, and
+// do_h_conc_solve, hines_conc.c:39-396). Operands: p* pool (conc) rows,
+// f* field rows, s a compartment slot; `ix` is the current conc of a group
+// and `res` its running result.
+enum PoolOp {
+    PO_CACONC = 1,    // p fBase fItau fDtB              Ca_concen
+    PO_GRP = 2,       // p                               ix = p, res = 0 (FCONC/CONC)
+    PO_STORE = 3,     //                                 coresult[ix] = res
+    PO_FLUXCONC = 4,  // f0 f1                           res += f0 + flux[ix] f1
+    PO_CTAU = 5,      // f0 f1                           res += f0, codiag[ix] += f1
+    PO_TAU = 6,       // s f0 f1 f2 f3 f4                voltage-dependent tau pump
+    PO_MM = 7,        // f0 f1                           codiag[ix] += f0 / (c[ix] + f1)
+    PO_HILL = 8,      // h f0 f1                         Hill pump on ix
+    PO_PHILL = 9,     // h p f0 f1 f2                    Hill pump from shell p into ix
+    PO_BUFFER = 10,   // p f0 f1 f2                      pool buffer p of ix
+    PO_POOL = 11,     //                                 c[ix] += res
+    PO_DIFF = 12      // ms w nfix crank sbase nq nb, ms*w rows p, nq rows f, nb rows f
+};
 
 // Lanes per tile: one neuron per lane of a warp.
 constexpr int LANES = 32;
@@ -78,6 +96,8 @@ struct TileType {
     int interp;      // calcmode
     int has_spike;
     int nsyn;        // synchan rows
+    int has_cd;      // keeps codiag rows (diffusion systems): ELMMPUMP adds to them
+    int nscratch;    // per-lane scratch rows of the diffusion solves
 };
 
 struct Tile {
@@ -90,6 +110,7 @@ struct Tile {
     int64_t giv;
     int64_t vm;      // nslots rows
     int64_t syn;     // event-ring rows (nsyn * ring_len)
+    int64_t scr;     // diffusion scratch rows (nscratch)
     int64_t first_neuron; // global neuron index of lane 0
 };
 

@@ -135,6 +135,7 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
                     ichan += Ik = vmax * cx * X;
                     if (GIV) Gw[pc[4] * LANES] = c5 ? Ik / vmax : Ik;
                     Im += Ik;
+                    if (ty.has_cd) v.CD[(tl.pools + sel) * LANES + lane] += Pw[pc[3] * LANES] * X;   // hines_chip.c:301
                     pc += 5;
                 } else if (code == M_FLUX) {
                     Fw[sel * LANES] += Ik;
@@ -333,20 +334,19 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
 
         // ---------------- pool phase ----------------
         {
-            const int *pp = v.prog + ty.pool_off;
-            const double dtl = v.dt;
-            (void)dtl;
-            while (pp[0] != 0) {
-                if (pp[0] == PO_CACONC) {
-                    double *cx = &Cw[pp[1] * LANES];
-                    const double base = Pw[pp[2] * LANES];
-                    const double itau = Pw[pp[3] * LANES];
-                    *cx = base + ((*cx - base) * (2.0 - itau) + (Fw[pp[1] * LANES] * Pw[pp[4] * LANES])) / itau;
-                    pp += 5;
-                } else {
-                    if (v.status) atomicOr(v.status, ST_BAD_OP);
-                    return;
-                }
+            PoolLane PL;
+            PL.C = Cw;
+            PL.F = Fw;
+            PL.CR = v.CR ? v.CR + tl.pools * LANES + lane : nullptr;
+            PL.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+            PL.S = v.S ? v.S + tl.scr * LANES + lane : nullptr;
+            PL.P = Pw;
+            PL.V = Vw;
+            PL.dt = v.dt;
+            PL.crank = ty.crank;
+            if (!pool_phase(v.prog + ty.pool_off, PL)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
             }
         }
 

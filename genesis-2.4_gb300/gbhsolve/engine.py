@@ -22,7 +22,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_int64)
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 PREC_FP64, PREC_MIXED = 0, 1
 
 
@@ -50,7 +50,10 @@ class GbhBatchDesc(C.Structure):
                 ("stab_start", _lp), ("stablist", _dp),
                 ("conc_start", _lp), ("conc", _dp),
                 ("concops_start", _lp), ("concops", _ip),
-                ("concchip_start", _lp), ("concchip", _dp)]
+                ("concchip_start", _lp), ("concchip", _dp),
+                ("diff_start", _lp), ("dconc", _ip), ("nshells", _ip), ("nshrows", _ip), ("nshfix", _ip),
+                ("fbufval", _ip), ("covals0_start", _lp), ("covals0", _dp), ("bufvals_start", _lp),
+                ("bufvals", _dp)]
 
 
 class GbhSynapses(C.Structure):
@@ -233,6 +236,21 @@ class Batch:
             start = "stab_start" if name == "stablist" else name + "_start"
             setattr(d, start, _ptr(getattr(self, start), _lp))
             setattr(d, name, _ptr(getattr(self, name), t))
+        # diffusion systems (optional `diff` dict on a solver)
+        diffs = [getattr(s, "diff", None) for s in self.solvers]
+        if any(x is not None and len(x["nshells"]) for x in diffs):
+            empty = dict(dconc=[], nshells=[], nshrows=[], nshfix=[], fbufval=[], covals0=[], bufvals=[])
+            diffs = [x if x is not None else empty for x in diffs]
+            self.diff_start, self.dconc = _cat([x["dconc"] for x in diffs], np.int32)
+            for k in ("nshells", "nshrows", "nshfix", "fbufval"):
+                setattr(self, k, _cat([x[k] for x in diffs], np.int32)[1])
+            self.covals0_start, self.covals0 = _cat([x["covals0"] for x in diffs], np.float64)
+            self.bufvals_start, self.bufvals = _cat([x["bufvals"] for x in diffs], np.float64)
+            d.diff_start = _ptr(self.diff_start, _lp)
+            for k in ("dconc", "nshells", "nshrows", "nshfix", "fbufval"):
+                setattr(d, k, _ptr(getattr(self, k), _ip))
+            d.covals0_start, d.covals0 = _ptr(self.covals0_start, _lp), _ptr(self.covals0, _dp)
+            d.bufvals_start, d.bufvals = _ptr(self.bufvals_start, _lp), _ptr(self.bufvals, _dp)
         self.desc = d
         self.syn = None
         if synapses is not None:

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define GBH_ABI_VERSION 1
+#define GBH_ABI_VERSION 2
 
 /* precision of gate/table arithmetic (elimination, Vm and Ca are always FP64) */
 #define GBH_PREC_FP64 0
@@ -88,6 +88,16 @@ typedef struct gbh_batch_desc {
     const int64_t *conc_start;   const double *conc;
     const int64_t *concops_start;  const int *concops;
     const int64_t *concchip_start; const double *concchip;
+    /* Concentration diffusion systems (difshells with buffers), solved by
+     * do_h_conc_solve (hines_conc.c:39-396); diff_start NULL = none. Per
+     * system: first conc (solver-local), shells, rows per shell (buffers +
+     * the shell), fixed buffers among them, first bufvals entry
+     * (hsolve->dconc, nshells, nshrows, nshfix, fbufval). covals0 and
+     * bufvals as the reference's setup fills them (h_setup_conc_solve). */
+    const int64_t *diff_start;   /* [nsolvers+1] */
+    const int *dconc, *nshells, *nshrows, *nshfix, *fbufval;
+    const int64_t *covals0_start; const double *covals0;
+    const int64_t *bufvals_start; const double *bufvals;
 } gbh_batch_desc;
 
 /*

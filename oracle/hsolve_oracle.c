@@ -493,6 +493,215 @@ int orc_conc_update(orc_solver *s)
 }
 
 /*
+ * Concentration diffusion (difshell systems), do_h_conc_solve
+ * (hines_conc.c:39-396). Each system i holds nshells[i] shells of
+ * nshrows[i] rows: nshfix[i] fixed buffers, then diffusible buffers, then the
+ * shell's free concentration, at conc[dconc[i] + shell*rows + row]. covals0
+ * is consumed in order across the systems; codiag/coresult carry what the
+ * pumps and fluxes of the concops program added this step, and codiag is
+ * reset to 1 once used. Crank-Nicolson systems without buffers return
+ * 2x - c (hines_conc.c:380-387); the buffered form is written for either
+ * method (setup scales its terms by dt or dt/2).
+ */
+
+/* Shells only: tridiagonal in the shell index (hines_conc.c:337-395). */
+static void diff_shells(orc_solver *s, int c0, int ms, int *cursor)
+{
+    double *conc = s->conc, *cd = s->codiag, *cr = s->coresult;
+    double *fac = s->covals, *part = s->cores;
+    const double *k = s->covals0;
+    int q = *cursor, m, c = c0;
+    double up = k[q++], dn, d, f, x;
+    d = up + cd[c];
+    cd[c] = 1.0;
+    part[0] = (conc[c] + cr[c]) / d;
+    for (m = 1; m < ms - 1; m++) {
+        f = fac[m] = -up / d;
+        dn = k[q];
+        up = k[q + 1];
+        q += 2;
+        c++;
+        d = cd[c] + dn * (1.0 + f) + up;
+        cd[c] = 1.0;
+        part[m] = (conc[c] + cr[c] + dn * part[m - 1]) / d;
+    }
+    f = fac[m] = -up / d;
+    dn = k[q++];
+    c++;
+    d = cd[c] + dn * (1.0 + f);
+    cd[c] = 1.0;
+    x = (conc[c] + cr[c] + dn * part[m - 1]) / d;
+    if (s->crank) {
+        conc[c] = x + x - conc[c];
+        for (m--, c--; m >= 0; m--, c--) {
+            x = part[m] - fac[m + 1] * x;
+            conc[c] = x + x - conc[c];
+        }
+    } else {
+        conc[c] = x;
+        for (m--, c--; m >= 0; m--, c--) {
+            x = part[m] - fac[m + 1] * x;
+            conc[c] = x;
+        }
+    }
+    *cursor = q;
+}
+
+/* Shells with buffers: banded system, rows of a shell eliminated as they are
+ * filled (hines_conc.c:123-335). Scratch layout: fac[(shell*rows + row)*rows
+ * + column], part[shell*rows + row]. */
+static void diff_buffered(orc_solver *s, int c0, int ms, int w, int nfix, int b0, int *cursor)
+{
+    double *conc = s->conc, *cd = s->codiag, *cr = s->coresult;
+    double *fac = s->covals, *part = s->cores;
+    const double *k = s->covals0, *bv = s->bufvals;
+    const int w1 = w - 1, sq = w * w, last = ms - 1;
+    int q = *cursor, m, n, nb, nc = c0, pr = 0, prev_shell = -1;
+    int row = 0, srow = sq - w, srow_prev = srow - sq, cs = c0 + w1;
+    double co = conc[cs], dsh, rsh, d, t, t2, h;
+
+    for (m = 0; m < ms; m++) {
+        dsh = cd[cs];
+        cd[cs] = 1.0;
+        rsh = cr[cs];
+        /* fixed buffers: no coupling to other shells */
+        for (n = 0, nb = b0; n < nfix; n++, nb += 3) {
+            fac[srow + n] = d = bv[nb] * co + bv[nb + 1];
+            dsh += t = bv[nb] * conc[nc];
+            d = 1.0 / (1.0 + d);
+            fac[row] = t * d;
+            rsh += t2 = -bv[nb + 1] * conc[nc] + k[q++];
+            part[pr++] = (conc[nc] + t2) * d;
+            nc++;
+            row += w;
+        }
+        /* diffusible buffers: coupled to the same buffer in the neighbours */
+        for (; n < w1; n++, nb += 3) {
+            fac[srow + n] = d = bv[nb] * co + bv[nb + 1];
+            dsh += t = bv[nb] * conc[nc];
+            rsh += t2 = -bv[nb + 1] * conc[nc] + bv[nb + 2];
+            if (m) {
+                h = k[q] * fac[row - sq];
+                if (m < last) {
+                    d += 1.0 + k[q + 1] + k[q] * (1.0 + fac[row - sq + 1]) - h * fac[srow_prev + n];
+                    fac[row + 1] = -k[q + 1] / d;
+                    t2 += k[q] * conc[nc - w] + (1.0 - k[q] - k[q + 1]) * conc[nc] + k[q + 1] * conc[nc + w];
+                } else {
+                    d += 1.0 + k[q] * (1.0 + fac[row - sq + 1]) - h * fac[srow_prev + n];
+                    t2 += k[q] * conc[nc - w] + (1.0 - k[q]) * conc[nc];
+                }
+                /* (the reference stores (t - h*fac[srow_prev + w1]) / d here
+                 * and overwrites it with t / d below) */
+                part[pr] = (t2 + k[q] * part[pr - w] - h * part[prev_shell]) / d;
+                q += m < last ? 2 : 1;
+            } else {
+                d += 1.0 + k[q];
+                fac[row + 1] = -k[q] / d;
+                part[pr] = (t2 + (1.0 - k[q]) * conc[nc] + k[q] * conc[nc + w]) / d;
+                q++;
+            }
+            fac[row] = t / d;
+            pr++;
+            nc++;
+            row += w;
+        }
+        /* the shell row */
+        if (m) {
+            if (m < last) {
+                dsh += k[q + 1] + k[q] * (1.0 + fac[srow_prev + w1]);
+                rsh += k[q] * (conc[nc - w] + part[prev_shell]) + (1.0 - k[q] - k[q + 1]) * co;
+                cs += w;
+                co = conc[cs];
+                rsh += k[q + 1] * co;
+            } else {
+                dsh += k[q] * (1.0 + fac[srow_prev + w1]);
+                rsh += k[q] * (conc[nc - w] + part[prev_shell]) + (1.0 - k[q]) * co;
+            }
+        } else {
+            dsh += k[q];
+            rsh += (1.0 - k[q]) * co;
+            cs += w;
+            co = conc[cs];
+            rsh += k[q] * co;
+        }
+        /* eliminate the buffer terms of the shell row */
+        for (n = 0, nb = srow_prev; n < nfix; n++) {
+            nb += w;
+            prev_shell++;
+            dsh -= fac[row + n] * fac[nb];
+            rsh -= fac[row + n] * part[prev_shell];
+        }
+        for (; n < w1; n++) {
+            double e;
+            nb += w;
+            prev_shell++;
+            e = m ? fac[row + n] + k[q] * fac[srow_prev + n] : fac[row + n];
+            dsh -= e * fac[nb];
+            rsh -= e * part[prev_shell];
+            if (m < last) fac[row + n] *= -fac[nb + 1];
+        }
+        if (m < last) {
+            for (n = nfix; n < w1; n++) fac[row + n] /= dsh;
+            if (m) {
+                fac[row + w1] = -k[q + 1] / dsh;
+                q += 2;
+            } else {
+                fac[row + w1] = -k[q] / dsh;
+                q++;
+            }
+            part[pr] = rsh / dsh;
+            prev_shell = pr++;
+            nc++;
+            srow_prev = row;
+            srow += sq;
+            row += w;
+        } else {
+            co = conc[nc] = rsh / dsh;
+            nc--;
+            q++;
+        }
+    }
+    /* back substitution, outermost shell first */
+    for (m = last; m >= 0; m--) {
+        if (m < last) {
+            row -= w;
+            co = part[--pr] - fac[row + w1] * conc[nc + w];
+            for (n = nfix; n < w1; n++) co -= fac[row + n] * conc[nc + n + 1];
+            conc[nc] = co;
+            nc--;
+            for (n = w1; n > nfix; n--) {
+                row -= w;
+                conc[nc] = part[--pr] - fac[row] * co - fac[row + 1] * conc[nc + w];
+                nc--;
+            }
+        } else {
+            for (n = w1; n > nfix; n--) {
+                row -= w;
+                conc[nc] = part[--pr] - fac[row] * co;
+                nc--;
+            }
+        }
+        for (; n > 0; n--) {
+            row -= w;
+            conc[nc] = part[--pr] - fac[row] * co;
+            nc--;
+        }
+    }
+    *cursor = q;
+}
+
+void orc_conc_solve(orc_solver *s)
+{
+    int i, cursor = 0;
+    for (i = 0; i < s->ndiffs; i++) {
+        if (s->nshrows[i] > 1)
+            diff_buffered(s, s->dconc[i], s->nshells[i], s->nshrows[i], s->nshfix[i], s->fbufval[i], &cursor);
+        else
+            diff_shells(s, s->dconc[i], s->nshells[i], &cursor);
+    }
+}
+
+/*
  * Hines elimination over funcs[] (hines_solve.c:140-296). resultval/diaval
  * are the running row accumulators; 'cur' is the row-pair cursor into
  * results[]. crank: vm = 2x - vm, otherwise vm = x.
@@ -578,6 +787,7 @@ int orc_process(orc_solver *s)
     if (s->nconcchips_used) {
         if (orc_conc_update(s)) return -1;
     }
+    if (s->ndiffs) orc_conc_solve(s);
     orc_solve(s);
     return 0;
 }

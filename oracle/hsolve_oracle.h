@@ -12,6 +12,7 @@
  *                        (genesis/src/hines/hines_chip.c:78-602, instantiated
  *                        by hines_4chip.c:7-11 and hines_4nichip.c)
  *   orc_conc_update   <- do_h4_conc_chip_update (hines_conc_chip.c:59-221)
+ *   orc_conc_solve    <- do_h_conc_solve (hines_conc.c:39-396)
  *   orc_solve         <- do_euler_hsolve / do_crank_hsolve (hines_solve.c:140-296)
  *   orc_process       <- HinesSolver PROCESS, chanmode 4/5 (hines.c:222-270)
  * Spike and synaptic-event hooks (h_dospike_event / h_dosynchan,
@@ -68,6 +69,13 @@ struct orc_solver {
     int *concops;
     double *concchip;
     double *ovals;     /* givals cursor used by TAUPUMP_OP (may be NULL)     */
+    /* diffusion systems (difshells and their buffers, do_h_conc_solve) */
+    int ndiffs;
+    int *dconc, *nshells, *nshrows, *nshfix, *fbufval;   /* [ndiffs] */
+    double *covals0;   /* coupling / buffer-total terms, consumed in order  */
+    double *bufvals;   /* 3 per buffer type: dt2*kBf, dt2*kBb, dt*kBb*Btot  */
+    double *covals;    /* scratch: nshells*nshrows^2 of the largest system  */
+    double *cores;     /* scratch: nshells*nshrows                          */
     int nconcchips_used;
     double *itotal;    /* [nelm_names] or NULL                               */
     int nelm_names;
@@ -85,6 +93,7 @@ struct orc_solver {
 /* Returns 0 on success, -1 on an unknown opcode (err_op is set). */
 int orc_chip_update(orc_solver *s);
 int orc_conc_update(orc_solver *s);
+void orc_conc_solve(orc_solver *s);
 void orc_solve(orc_solver *s);
 /* One PROCESS step (chip update, conc update, elimination). */
 int orc_process(orc_solver *s);

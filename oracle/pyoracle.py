@@ -39,6 +39,8 @@ class OrcSolver(C.Structure):
         ("conc", _dp), ("flux", _dp), ("codiag", _dp), ("coresult", _dp),
         ("nconcchips", C.c_int), ("nconcops", C.c_int),
         ("concops", _ip), ("concchip", _dp), ("ovals", _dp),
+        ("ndiffs", C.c_int), ("dconc", _ip), ("nshells", _ip), ("nshrows", _ip), ("nshfix", _ip),
+        ("fbufval", _ip), ("covals0", _dp), ("bufvals", _dp), ("covals", _dp), ("cores", _dp),
         ("nconcchips_used", C.c_int),
         ("itotal", _dp), ("nelm_names", C.c_int),
         ("childops", _ip), ("childchips", _ip),
@@ -144,7 +146,26 @@ class Solver:
         s.nconcchips = len(self.concchip)
         s.nconcops = len(self.concops)
         s.concops, s.concchip = _p(self.concops, _ip), _p(self.concchip, _dp)
-        s.ovals = C.cast(0, _dp)
+        # TAUPUMP_OP writes its 1/tau into ovals[] (hines_conc_chip.c:118-121)
+        self.ovals = np.zeros(max(1, int(np.count_nonzero(self.concops == 11000))), dtype=np.float64)
+        s.ovals = _p(self.ovals, _dp)
+        diff = getattr(h, "diff", None)
+        if diff is not None and len(diff["nshells"]):
+            self.dconc, self.nshells, self.nshrows, self.nshfix, self.fbufval = (
+                np.array(diff[k], dtype=np.int32, copy=True) for k in ("dconc", "nshells", "nshrows", "nshfix",
+                                                                         "fbufval"))
+            self.covals0 = np.array(diff["covals0"], dtype=np.float64, copy=True)
+            self.bufvals = np.array(diff["bufvals"], dtype=np.float64, copy=True)
+            w = self.nshells * self.nshrows
+            self.covals = np.zeros(int(np.max(w * self.nshrows + self.nshrows)) + 1)
+            self.cores = np.zeros(int(np.max(w)) + 1)
+            s.ndiffs = len(self.nshells)
+            s.dconc, s.nshells, s.nshrows = _p(self.dconc, _ip), _p(self.nshells, _ip), _p(self.nshrows, _ip)
+            s.nshfix, s.fbufval = _p(self.nshfix, _ip), _p(self.fbufval, _ip)
+            s.covals0, s.bufvals = _p(self.covals0, _dp), _p(self.bufvals, _dp)
+            s.covals, s.cores = _p(self.covals, _dp), _p(self.cores, _dp)
+        else:
+            s.ndiffs = 0
         s.nconcchips_used = 1 if len(self.concchip) else 0
         s.itotal = C.cast(0, _dp)
         s.nelm_names = 0

@@ -3,15 +3,16 @@
  * oracle's flat-array solver struct.
  *
  * TEST INFRASTRUCTURE ONLY. Compiled together with the reference sources
- * genesis/src/hines/{hines_4chip,hines_4nichip,hines_conc_4chip,hines_solve}.c
+ * genesis/src/hines/{hines_4chip,hines_4nichip,hines_conc_4chip,hines_conc,hines_solve}.c
  * (never copied into this repository) into oracle/_ref/libhsolve_ref.so by
  * oracle/Makefile, and used to pin the oracle restatement bit for bit.
  *
- * It supplies the four symbols those files need from the rest of GENESIS:
+ * It supplies the symbols those files need from the rest of GENESIS:
  *   Error()            -- message banner (sim/)
  *   G_RNG()            -- SPRNG uniform deviate used by SYN3_OP
  *   h_dospike_event()  -- hines_conn.c:44-58, routed to the solver's hook
  *   h_dosynchan()      -- hines_conn.c:62-89, routed to the solver's hook
+ *   BaseObject()       -- the element's object, for its integration method
  * and builds a transient Hsolve around the oracle struct's arrays for each call.
  */
 #include <stdlib.h>
@@ -24,8 +25,18 @@ extern int do_chip_hh4ni_update(Hsolve *);
 extern int do_h4_conc_chip_update(Hsolve *);
 extern void do_euler_hsolve(Hsolve *);
 extern void do_crank_hsolve(Hsolve *);
+extern void do_h_conc_solve(Hsolve *);
 
 void Error(void) {}
+
+/* do_h_conc_solve reads the integration method from the element's object
+ * (sim/sim_func_ext.h:258); one static object carries the current solver's */
+static GenesisObject ref_object;
+GenesisObject *BaseObject(Element *e)
+{
+    (void)e;
+    return &ref_object;
+}
 
 static unsigned long long ref_rng_state = 0x9E3779B97F4A7C15ULL;
 float G_RNG()
@@ -97,6 +108,16 @@ static void ref_fill(Hsolve *h, orc_solver *s)
     h->concops = s->concops;
     h->itotal = s->itotal;
     h->nelm_names = s->nelm_names;
+    h->ndiffs = s->ndiffs;
+    h->dconc = s->dconc;
+    h->nshells = s->nshells;
+    h->nshrows = s->nshrows;
+    h->nshfix = s->nshfix;
+    h->fbufval = s->fbufval;
+    h->covals0 = s->covals0;
+    h->bufvals = s->bufvals;
+    h->covals = s->covals;
+    h->cores = s->cores;
     h->childops = s->childops;
     h->childchips = s->childchips;
     h->dt = s->dt;
@@ -113,6 +134,10 @@ int ref_process(orc_solver *s)
     if (rc) return -1;
     if (h.nconcchips) {
         if (do_h4_conc_chip_update(&h)) return -1;
+    }
+    if (h.ndiffs) {
+        ref_object.method = s->crank ? CRANK_INT : BEULER_INT;
+        do_h_conc_solve(&h);
     }
     if (s->crank)
         do_crank_hsolve(&h);

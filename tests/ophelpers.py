@@ -16,6 +16,9 @@ import numpy as np
                                 3300, 3301, 3501, 4001, 4002, 4003, 4004, 4100, 4101, 4200, 5100, 5110,
                                 5111, 5112)
 CACONC, LCACONC = 10200, 10202
+# concops (hines_defs.h:210-222)
+CONC, FCONC, LCONC, FLUXCONC = 10100, 10101, 10102, 10103
+TAUPUMP, CTAUPUMP, MMPUMP, HILLPUMP, PHILLPUMP, BUFFER, POOL = 11000, 11001, 11010, 11011, 11012, 12000, 12100
 
 
 class Compt:
@@ -65,9 +68,11 @@ def tables(ncols, xdivs, xmin=-0.1, xmax=0.05, seed=0, ydivs=0, ymin=0.0, ymax=1
 
 
 def solver(compts, tabs, dt=2e-5, conc=(), stablist=(), concops=(), concchip=(), chanmode=4, calcmode=1,
-           crank=False, parents=None):
+           crank=False, parents=None, diff=None):
     """Arrays of one hsolve. parents: Hines-order parent rows (None = every
-    compartment its own root), used to emit funcs[]/ravals[]."""
+    compartment its own root), used to emit funcs[]/ravals[]. diff: the
+    diffusion-system arrays (dconc, nshells, nshrows, nshfix, fbufval,
+    covals0, bufvals) of do_h_conc_solve, or None."""
     n = len(compts)
     ops, chip, giv, vm = [], [], [0.0], []
     for i, c in enumerate(compts):
@@ -85,7 +90,7 @@ def solver(compts, tabs, dt=2e-5, conc=(), stablist=(), concops=(), concchip=(),
         conc=np.array(conc, np.float64), concops=np.array(concops, np.int32),
         concchip=np.array(concchip, np.float64), childops=np.zeros(1, np.int32),
         childchips=np.zeros(1, np.int32), dt=dt, method=11 if crank else 10, crank=1 if crank else 0,
-        chanmode=chanmode, calcmode=calcmode, **tabs)
+        chanmode=chanmode, calcmode=calcmode, diff=diff, **tabs)
 
 
 def _funcs(n, parents):
@@ -119,3 +124,49 @@ def _funcs(n, parents):
         funcs.append(6)
     funcs.append(7)
     return funcs, ravals
+
+
+def diffusion_system(rng, nshells, nfix=0, ndif=0, dt=2e-5, crank=True):
+    """covals0 / bufvals of one difshell system with nfix fixed and ndif
+    diffusible buffers per shell, in the order h_setup_conc_solve
+    (genesis/src/hines/hines_conc_init.c:313-475) emits them: per shell, per
+    row (fixed buffers, diffusible buffers, the shell): fixed buffer
+    dt*kBb*Btot; diffusible rows the down- and up-coupling
+    2*dt2*D*surf/(vol*(thick+thick')) (one of them at the first and last
+    shell). Shell geometry and rate constants are drawn from plausible
+    ranges (thickness 0.1-0.5 um, D 2e-10 m^2/s for Ca, kBf 1e5-1e6
+    /(mM s), kBb 50-500 /s, Btot 0.01-0.2 mM)."""
+    dt2 = dt / 2.0 if crank else dt
+    w = nfix + ndif + 1
+    thick = rng.uniform(0.1e-6, 0.5e-6, nshells)
+    vol = rng.uniform(0.5, 2.0, nshells) * thick * 1e-10
+    surf = rng.uniform(0.8, 1.2, nshells + 1) * 1e-10
+    Dca, Dbuf = 2e-10, rng.uniform(2e-11, 8e-11, ndif)
+    kf, kb, btot = (rng.uniform(1e5, 1e6, nfix + ndif), rng.uniform(50, 500, nfix + ndif),
+                    rng.uniform(0.01, 0.2, nfix + ndif))
+    bufvals = []
+    for b in range(nfix + ndif):
+        bufvals += [dt2 * kf[b], dt2 * kb[b], dt * kb[b] * btot[b]]
+    cov0 = []
+    for m in range(nshells):
+        for r in range(w):
+            if r < nfix:
+                cov0.append(dt * kb[r] * btot[r] * rng.uniform(0.9, 1.1))
+                continue
+            D = Dbuf[r - nfix] if r < w - 1 else Dca
+            diffc = 2.0 * dt2 * D / vol[m]
+            t0 = 2 * thick[0] if m == 1 else thick[m - 1] if m else 0.0
+            if m < nshells - 1:
+                if m:
+                    cov0.append(diffc * surf[m] / (t0 + thick[m]))
+                    cov0.append(diffc * surf[m + 1] / (thick[m] + thick[m + 1]))
+                else:
+                    cov0.append(diffc * surf[1] / (2 * thick[0] + thick[1]))
+            else:
+                cov0.append(diffc * surf[m] / (thick[m - 1] + thick[m]))
+    # equilibrium-ish initial concentrations: free buffer, then Ca 50-100 nM
+    conc = []
+    for m in range(nshells):
+        ca = rng.uniform(5e-5, 1e-4)
+        conc += [btot[b] * kb[b] / (kb[b] + kf[b] * ca) for b in range(nfix + ndif)] + [ca]
+    return np.array(cov0), np.array(bufvals), conc
