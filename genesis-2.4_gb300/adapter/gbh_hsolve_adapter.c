@@ -36,7 +36,7 @@
 typedef struct gbh_hstate {
     gbh_engine *e;
     int nin;
-    int *in_chip;        /* chip[] index of every ininfo target */
+    Iinfo **in_msg;      /* the ininfo entry of every registered input */
     double *in_vals;
     int64_t starts[14][2];
 } gbh_hstate;
@@ -135,27 +135,49 @@ int gbh_init(Hsolve *h)
         free(s);
         return -1;   /* hard SETUP error: there is no CPU fallback */
     }
-    /* per-step inputs written by h_in_msgs into chip[] (hines_msgs.c:367-372) */
+    /* h_in_msgs inputs (hines_msgs.c:351-405): INJECT/BASE/THRESH set a chip,
+       SYN2 adds to a synchan's X, FLUX sets a concentration's flux. The engine
+       applies them itself from the message values, in ininfo order. */
     n = 0;
     for (ii = h->ininfo; ii; ii = ii->next)
-        if (ii->type == INJECT_OP || ii->type == BASE_OP || ii->type == THRESH_OP) n++;
+        if (ii->type == INJECT_OP || ii->type == BASE_OP || ii->type == THRESH_OP || ii->type == SYN2_OP ||
+            ii->type == FLUX_OP)
+            n++;
     if (n) {
+        int *kind = (int *)calloc(n, sizeof(int));
+        double *sa = (double *)calloc(n, sizeof(double));
+        double *sb = (double *)calloc(n, sizeof(double));
         s->nin = n;
-        s->in_chip = (int *)calloc(n, sizeof(int));
+        s->in_msg = (Iinfo **)calloc(n, sizeof(Iinfo *));
         s->in_vals = (double *)calloc(n, sizeof(double));
         solver = (int *)calloc(n, sizeof(int));
         idx = (int64_t *)calloc(n, sizeof(int64_t));
         i = 0;
-        for (ii = h->ininfo; ii; ii = ii->next)
+        for (ii = h->ininfo; ii; ii = ii->next) {
             if (ii->type == INJECT_OP || ii->type == BASE_OP || ii->type == THRESH_OP) {
-                s->in_chip[i] = ii->nchip;
-                idx[i] = ii->nchip;
-                i++;
+                kind[i] = GBH_IN_SET;
+                sa[i] = sb[i] = 1.0;
+            } else if (ii->type == SYN2_OP) {
+                kind[i] = GBH_IN_ADD;
+                sa[i] = h->stablist[ii->nop + 3];
+                sb[i] = (ii->msgin->type == ACTIVATION && ii->sChildType == SYNCHANC_T) ? h->dt : 1.0;
+            } else if (ii->type == FLUX_OP) {
+                kind[i] = GBH_IN_FLUX;
+                sa[i] = sb[i] = 1.0;
+            } else {
+                continue;
             }
-        if (gbh_register_inputs(s->e, n, solver, idx) != GBH_OK)
+            s->in_msg[i] = ii;
+            idx[i] = ii->nchip;
+            i++;
+        }
+        if (gbh_register_inputs_typed(s->e, n, solver, kind, idx, sa, sb) != GBH_OK)
             fprintf(stderr, "gbh_init %s: %s\n", h->name, gbh_last_error());
         free(solver);
         free(idx);
+        free(kind);
+        free(sa);
+        free(sb);
     }
     h->accel_state = s;
     if (gbh_nreg < GBH_MAX_SOLVERS) gbh_registry[gbh_nreg++] = h;
@@ -169,7 +191,7 @@ int gbh_chip_update(Hsolve *h)
     if (!h->accel_state && gbh_init(h)) return -1;
     s = (gbh_hstate *)h->accel_state;
     if (s->nin) {
-        for (i = 0; i < s->nin; i++) s->in_vals[i] = h->chip[s->in_chip[i]];
+        for (i = 0; i < s->nin; i++) s->in_vals[i] = MSGVALUE(s->in_msg[i]->msgin, 0);
         if (gbh_set_inputs_async(s->e, s->in_vals, NULL) != GBH_OK) return -1;
     }
     if (gbh_run(s->e, 1) != GBH_OK) {
@@ -194,7 +216,7 @@ void gbh_cleanup(void)
         gbh_hstate *s = (gbh_hstate *)h->accel_state;
         if (!s) continue;
         gbh_destroy(s->e);
-        free(s->in_chip);
+        free(s->in_msg);
         free(s->in_vals);
         free(s);
         h->accel_state = NULL;

@@ -175,9 +175,10 @@ struct gbh_engine {
     int io_pend_buf = 0;
     cudaStream_t io_pend_stream = nullptr;
     // per-step I/O (h_in_msgs / h_out_msgs)
-    int n_in = 0, n_out = 0;
-    DBuf<double> d_in_vals, d_out_vals;
+    int n_in = 0, n_out = 0, n_tgt = 0;   // input values, distinct input targets, outputs
+    DBuf<double> d_in_vals, d_out_vals, d_in_sa, d_in_sb;
     DBuf<int64_t> d_in_start, d_in_addr, d_out_addr;
+    DBuf<int> d_in_item;
 };
 
 namespace {
@@ -1084,46 +1085,68 @@ int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, doubl
     return GBH_OK;
 }
 
-constexpr int64_t kPackedFlag = 1LL << 62;   // input address holds a packed double-float
+constexpr int64_t kPackedFlag = 1LL << 62;   // input target holds a packed double-float
+constexpr int64_t kFluxFlag = 1LL << 61;     // input target is a flux row (F), not a field (P)
+constexpr int64_t kAddFlag = 1LL << 60;      // input adds v*sa*sb when v > VTINY (SYN2 messages)
+constexpr int64_t kAddrMask = (1LL << 60) - 1;
 
-__global__ void k_scatter_inputs(const double *vals, const int64_t *start, const int64_t *addr, int n,
-                                 double *P)
+// Registered inputs grouped by target: each thread applies the inputs of one
+// target in registration order, as h_in_msgs walks its list
+// (hines_msgs.c:351-405): INJECT/BASE/THRESH set a chip value, SYN2 adds
+// X*stablist[nop+3] (*dt for ACTIVATION messages) when X > VTINY, FLUX sets
+// the flux of a concentration.
+struct InPlan {
+    const int64_t *start;   // [ntgt+1] items of each target
+    const int *item;        // input index of each item
+    const double *sa, *sb;  // factors of an adding item
+    const int64_t *addr;    // target address and flags
+    int ntgt;
+};
+
+__device__ __forceinline__ void apply_inputs(const InPlan &pl, int t, const double *vals, double *P, double *F)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double v = vals[i];
-    for (int64_t k = start[i]; k < start[i + 1]; ++k) {
-        const int64_t a = addr[k];
-        if (a & kPackedFlag) {
-            const float hi = __double2float_rn(v);
-            const float lo = __double2float_rn(v - (double)hi);
-            *reinterpret_cast<float2 *>(&P[a & ~kPackedFlag]) = make_float2(hi, lo);
+    const int64_t a = pl.addr[t];
+    double *dst = (a & kFluxFlag) ? &F[a & kAddrMask] : &P[a & kAddrMask];
+    const bool packed = (a & kPackedFlag) != 0;
+    double x;
+    if (packed) {
+        const float2 f = *reinterpret_cast<const float2 *>(dst);
+        x = (double)f.x + (double)f.y;
+    } else {
+        x = *dst;
+    }
+    for (int64_t k = pl.start[t]; k < pl.start[t + 1]; ++k) {
+        const double v = vals[pl.item[k]];
+        if (a & kAddFlag) {
+            // explicit roundings: no multiply-add contraction, as the host does it
+            if (v > 1.0e-10) x = __dadd_rn(x, __dmul_rn(__dmul_rn(v, pl.sa[k]), pl.sb[k]));
         } else {
-            P[a] = v;
+            x = v;
         }
+    }
+    if (packed) {
+        const float hi = __double2float_rn(x);
+        const float lo = __double2float_rn(x - (double)hi);
+        *reinterpret_cast<float2 *>(dst) = make_float2(hi, lo);
+    } else {
+        *dst = x;
     }
 }
 
+__global__ void k_scatter_inputs(const double *vals, InPlan pl, double *P, double *F)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < pl.ntgt) apply_inputs(pl, t, vals, P, F);
+}
+
 // Between two steps: the outputs of the step just run (gather, n_out) and
-// the inputs of the next (scatter, n_in) in one launch.
+// the inputs of the next (one thread per input target) in one launch.
 __global__ void k_io(const double *V, const int64_t *out_addr, int n_out, double *out, const double *in_vals,
-                     const int64_t *in_start, const int64_t *in_addr, int n_in, double *P)
+                     InPlan pl, double *P, double *F)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_out) out[i] = V[out_addr[i]];
-    if (i < n_in) {
-        const double v = in_vals[i];
-        for (int64_t k = in_start[i]; k < in_start[i + 1]; ++k) {
-            const int64_t a = in_addr[k];
-            if (a & (1LL << 62)) {
-                const float hi = __double2float_rn(v);
-                const float lo = __double2float_rn(v - (double)hi);
-                *reinterpret_cast<float2 *>(&P[a & ~(1LL << 62)]) = make_float2(hi, lo);
-            } else {
-                P[a] = v;
-            }
-        }
-    }
+    if (in_vals && i < pl.ntgt) apply_inputs(pl, i, in_vals, P, F);
 }
 
 // Events of remote spikes: source i spiked during step `step`; each of its
@@ -1150,43 +1173,101 @@ extern "C" {
 
 const char *gbh_last_error(void) { return g_last_error; }
 
-int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index)
+InPlan in_plan(const gbh_engine *e)
 {
-    if (!e || n < 0 || (n && (!solver || !chip_index))) return GBH_ERR_ARG;
-    // chip index -> every field row that copies it
+    InPlan pl;
+    pl.start = e->d_in_start.p;
+    pl.item = e->d_in_item.p;
+    pl.sa = e->d_in_sa.p;
+    pl.sb = e->d_in_sb.p;
+    pl.addr = e->d_in_addr.p;
+    pl.ntgt = e->n_tgt;
+    return pl;
+}
+
+int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int *kind, const int64_t *index,
+                              const double *sa, const double *sb)
+{
+    if (!e || n < 0 || (n && (!solver || !index))) return GBH_ERR_ARG;
+    // target address (with flags) of every input; inputs sharing a target are
+    // applied in registration order by one thread
     std::vector<std::vector<int64_t>> addrs(n);
-    std::unordered_map<int64_t, int> want;
+    std::unordered_map<int64_t, std::vector<int>> want_chip, want_conc;
     for (int i = 0; i < n; ++i) {
         if (solver[i] < 0 || solver[i] >= e->nsolvers) return GBH_ERR_ARG;
-        want[e->chip_start[solver[i]] + chip_index[i]] = i;
-    }
-    for (size_t k = 0; k < e->dec.neurons.size(); ++k) {
-        const Neuron &N = e->dec.neurons[k];
-        const Tile &t = e->tiles[e->neuron_tile[k]];
-        const int l = e->neuron_lane[k];
-        for (size_t f = 0; f < N.fsrc.size(); ++f) {
-            if (N.fsrc[f].kind != FS_CHIP) continue;
-            auto it = want.find(e->chip_start[N.solver] + N.fsrc[f].idx);
-            if (it != want.end()) {
-                const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
-                addrs[it->second].push_back(((t.fld + (int64_t)f) * LANES + l) | (packed ? kPackedFlag : 0));
-            }
-        }
-    }
-    std::vector<int64_t> start(n + 1, 0), flat;
-    for (int i = 0; i < n; ++i) {
-        if (addrs[i].empty()) {
-            set_last("input %d (solver %d, chip[%lld]) is not read by any compartment program", i, solver[i],
-                     (long long)chip_index[i]);
+        const int k = kind ? kind[i] : GBH_IN_SET;
+        if (k != GBH_IN_SET && k != GBH_IN_ADD && k != GBH_IN_FLUX) {
+            set_last("input %d: unknown kind %d", i, k);
             return GBH_ERR_ARG;
         }
-        start[i + 1] = start[i] + (int64_t)addrs[i].size();
-        flat.insert(flat.end(), addrs[i].begin(), addrs[i].end());
+        if (k == GBH_IN_FLUX) want_conc[e->conc_start[solver[i]] + index[i]].push_back(i);
+        else want_chip[e->chip_start[solver[i]] + index[i]].push_back(i);
+    }
+    for (size_t q = 0; q < e->dec.neurons.size(); ++q) {
+        const Neuron &N = e->dec.neurons[q];
+        const Tile &t = e->tiles[e->neuron_tile[q]];
+        const int l = e->neuron_lane[q];
+        for (size_t f = 0; f < N.fsrc.size(); ++f) {
+            if (N.fsrc[f].kind != FS_CHIP) continue;
+            auto it = want_chip.find(e->chip_start[N.solver] + N.fsrc[f].idx);
+            if (it == want_chip.end()) continue;
+            const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
+            for (int i : it->second) {
+                const bool add = kind && kind[i] == GBH_IN_ADD;
+                addrs[i].push_back(((t.fld + (int64_t)f) * LANES + l) | (packed ? kPackedFlag : 0) |
+                                   (add ? kAddFlag : 0));
+            }
+        }
+        for (size_t p = 0; p < N.pool_conc.size(); ++p) {
+            auto it = want_conc.find(e->conc_start[N.solver] + N.pool_conc[p]);
+            if (it == want_conc.end()) continue;
+            for (int i : it->second) addrs[i].push_back(((t.pools + (int64_t)p) * LANES + l) | kFluxFlag);
+        }
+    }
+    std::map<int64_t, std::vector<int>> by_target;   // keyed by address without the add flag
+    std::map<int64_t, int64_t> flags;
+    for (int i = 0; i < n; ++i) {
+        if (addrs[i].empty()) {
+            set_last("input %d (solver %d, index %lld) is not read by any compartment program", i, solver[i],
+                     (long long)index[i]);
+            return GBH_ERR_ARG;
+        }
+        for (int64_t a : addrs[i]) {
+            const int64_t key = a & ~kAddFlag;
+            auto f = flags.find(key);
+            if (f != flags.end() && (f->second & kAddFlag) != (a & kAddFlag)) {
+                set_last("input %d: a target both set and added to", i);
+                return GBH_ERR_ARG;
+            }
+            flags[key] = a;
+            by_target[key].push_back(i);
+        }
+    }
+    std::vector<int64_t> start(1, 0), taddr;
+    std::vector<int> item;
+    std::vector<double> fa, fb;
+    for (auto &kv : by_target) {
+        taddr.push_back(flags[kv.first]);
+        for (int i : kv.second) {
+            item.push_back(i);
+            fa.push_back(sa ? sa[i] : 1.0);
+            fb.push_back(sb ? sb[i] : 1.0);
+        }
+        start.push_back((int64_t)item.size());
     }
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
-    if (e->d_in_vals.alloc(n) || e->d_in_start.upload(start) || e->d_in_addr.upload(flat)) return GBH_ERR_CUDA;
+    e->d_in_item.release(); e->d_in_sa.release(); e->d_in_sb.release();
+    if (e->d_in_vals.alloc(n) || e->d_in_start.upload(start) || e->d_in_addr.upload(taddr) ||
+        e->d_in_item.upload(item) || e->d_in_sa.upload(fa) || e->d_in_sb.upload(fb))
+        return GBH_ERR_CUDA;
     e->n_in = n;
+    e->n_tgt = (int)taddr.size();
     return GBH_OK;
+}
+
+int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index)
+{
+    return gbh_register_inputs_typed(e, n, solver, nullptr, chip_index, nullptr, nullptr);
 }
 
 int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream)
@@ -1195,8 +1276,7 @@ int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream)
     if (e->n_in == 0) return GBH_OK;
     cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
     CK(cudaMemcpyAsync(e->d_in_vals.p, host_values, e->n_in * sizeof(double), cudaMemcpyHostToDevice, st));
-    k_scatter_inputs<<<(e->n_in + 255) / 256, 256, 0, st>>>(e->d_in_vals.p, e->d_in_start.p, e->d_in_addr.p,
-                                                           e->n_in, e->d_P.p);
+    k_scatter_inputs<<<(e->n_tgt + 255) / 256, 256, 0, st>>>(e->d_in_vals.p, in_plan(e), e->d_P.p, e->d_F.p);
     CK(cudaGetLastError());
     return GBH_OK;
 }
@@ -1242,13 +1322,13 @@ int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream)
 static int io_between(gbh_engine *e, cudaStream_t st, int in_buf)
 {
     const bool out = e->io_pend_host != nullptr;
-    const int n_in = in_buf >= 0 ? e->n_in : 0;
+    const int n_tg = in_buf >= 0 ? e->n_tgt : 0;
     const int n_out = out ? e->n_out : 0;
-    const int n = std::max(n_in, n_out);
+    const int n = std::max(n_tg, n_out);
     if (n == 0) return GBH_OK;
     k_io<<<(n + 255) / 256, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, n_out, out ? e->d_io_out[e->io_pend_buf].p : nullptr,
-                                          in_buf >= 0 ? e->d_io_in[in_buf].p : nullptr, e->d_in_start.p,
-                                          e->d_in_addr.p, n_in, e->d_P.p);
+                                          in_buf >= 0 ? e->d_io_in[in_buf].p : nullptr, in_plan(e), e->d_P.p,
+                                          e->d_F.p);
     CK(cudaGetLastError());
     if (out) {
         const int pb = e->io_pend_buf;
@@ -1352,7 +1432,8 @@ int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nstep
         e->blk_nin = n_in;
         e->blk_nout = n_out;
     }
-    const int nio = std::max(n_in, n_out);
+    const int nio = std::max(n_in ? e->n_tgt : 0, n_out);
+    const InPlan plan = in_plan(e);
     const unsigned grid = (unsigned)((nio + 255) / 256);
     int last = 0;
     for (int s0 = 0, j = 0; s0 < nsteps; s0 += B, ++j) {
@@ -1365,8 +1446,7 @@ int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nstep
                                cudaMemcpyHostToDevice, e->io_stream));
             CK(cudaEventRecord(e->blk_in_copied[b], e->io_stream));
             CK(cudaStreamWaitEvent(st, e->blk_in_copied[b], 0));
-            k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, 0, nullptr, din, e->d_in_start.p, e->d_in_addr.p,
-                                       n_in, e->d_P.p);
+            k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, 0, nullptr, din, plan, e->d_P.p, e->d_F.p);
             CK(cudaGetLastError());
         }
         if (n_out) CK(cudaStreamWaitEvent(st, e->blk_out_copied[b], 0));   // its outputs were copied out
@@ -1377,8 +1457,7 @@ int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nstep
             const int go = n_out, si = k + 1 < nb ? n_in : 0;
             if (go || si) {
                 k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, go, dout + (int64_t)k * n_out,
-                                           din + (int64_t)(k + 1) * n_in, e->d_in_start.p, e->d_in_addr.p, si,
-                                           e->d_P.p);
+                                           si ? din + (int64_t)(k + 1) * n_in : nullptr, plan, e->d_P.p, e->d_F.p);
                 CK(cudaGetLastError());
             }
         }
@@ -1635,11 +1714,15 @@ int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *op
             for (int s = 0; s < N.nrows; ++s) vm[e->vm_start[N.solver] + N.row0 + s] = V[(t.vm + s) * L + l];
         const std::vector<char> &dfm = e->type_df[t.type];
         if (chip)
-            for (size_t f = 0; f < N.fsrc.size(); ++f)
-                if (N.fsrc[f].state && N.fsrc[f].kind == FS_CHIP) {
-                    const double raw = P[(t.fld + f) * L + l];
-                    chip[e->chip_start[N.solver] + N.fsrc[f].idx] = (!dfm.empty() && dfm[f]) ? unpack_df(raw) : raw;
-                }
+            for (size_t f = 0; f < N.fsrc.size(); ++f) {
+                if (N.fsrc[f].kind != FS_CHIP) continue;
+                const bool packed = !dfm.empty() && dfm[f];
+                const double raw = P[(t.fld + f) * L + l];
+                // constants are reported as given; state and input-written
+                // entries (the device copy changed) from the device
+                if (!N.fsrc[f].state && raw == (packed ? pack_df(N.fval[f]) : N.fval[f])) continue;
+                chip[e->chip_start[N.solver] + N.fsrc[f].idx] = packed ? unpack_df(raw) : raw;
+            }
         if (conc)
             for (size_t p = 0; p < N.pool_conc.size(); ++p)
                 conc[e->conc_start[N.solver] + N.pool_conc[p]] = C[(t.pools + p) * L + l];
@@ -2145,6 +2228,7 @@ void gbh_destroy(gbh_engine *e)
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();
     e->d_gbar.release(); e->d_spiked.release(); e->d_rstart.release(); e->d_rbase.release(); e->d_rdelay.release(); e->d_rbits.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
+    e->d_in_item.release(); e->d_in_sa.release(); e->d_in_sb.release();
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);
     if (e->cap_stream) cudaStreamDestroy(e->cap_stream);

@@ -24,6 +24,7 @@ _lp = C.POINTER(C.c_int64)
 
 ABI_VERSION = 2
 PREC_FP64, PREC_MIXED = 0, 1
+IN_SET, IN_ADD, IN_FLUX = 0, 1, 2     # gbh_register_inputs_typed kinds
 
 
 class GbhError(C.Structure):
@@ -89,7 +90,8 @@ EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_
             "gbh_enable_givals", "gbh_get_givals", "gbh_register_inputs", "gbh_set_inputs_async",
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
-            "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync", "gbh_run_io"]
+            "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync", "gbh_run_io",
+            "gbh_register_inputs_typed"]
 
 _LIB = None
 
@@ -137,6 +139,7 @@ def load(build_if_missing: bool = True):
     lib.gbh_step_io.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_void_p]
     lib.gbh_io_sync.argtypes = [C.c_void_p]
     lib.gbh_run_io.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_int, C.c_void_p]
+    lib.gbh_register_inputs_typed.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _lp, _dp, _dp]
     lib.gbh_loss_gradient.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(GbhLossSpec), _dp, _dp, _dp, _dp]
     _LIB = lib
     return lib
@@ -382,11 +385,23 @@ class Engine:
         self._check(self.lib.gbh_get_givals(self.h, _ptr(g, _dp)))
         return b.split(g, b.givals_start)
 
-    def register_inputs(self, solver, chip_index):
+    def register_inputs(self, solver, chip_index, kind=None, sa=None, sb=None):
+        """Inputs of h_in_msgs: kind IN_SET (chip[index] = v, the default),
+        IN_ADD (chip[index] += v*sa*sb when v > 1e-10: SYN2 messages) or
+        IN_FLUX (flux[index] = v, index a conc index)."""
         self._in_s = np.ascontiguousarray(solver, dtype=np.int32)
         self._in_c = np.ascontiguousarray(chip_index, dtype=np.int64)
-        self._check(self.lib.gbh_register_inputs(self.h, len(self._in_s), _ptr(self._in_s, _ip),
-                                                 _ptr(self._in_c, _lp)))
+        if kind is None and sa is None and sb is None:
+            self._check(self.lib.gbh_register_inputs(self.h, len(self._in_s), _ptr(self._in_s, _ip),
+                                                     _ptr(self._in_c, _lp)))
+            return
+        n = len(self._in_s)
+        self._in_k = np.ascontiguousarray(kind if kind is not None else np.zeros(n), dtype=np.int32)
+        self._in_a = np.ascontiguousarray(sa if sa is not None else np.ones(n), dtype=np.float64)
+        self._in_b = np.ascontiguousarray(sb if sb is not None else np.ones(n), dtype=np.float64)
+        self._check(self.lib.gbh_register_inputs_typed(self.h, n, _ptr(self._in_s, _ip), _ptr(self._in_k, _ip),
+                                                       _ptr(self._in_c, _lp), _ptr(self._in_a, _dp),
+                                                       _ptr(self._in_b, _dp)))
 
     def set_inputs_async(self, host_values: np.ndarray, stream_handle: int = 0):
         self._check(self.lib.gbh_set_inputs_async(self.h, _ptr(host_values, _dp), C.c_void_p(stream_handle)))

@@ -269,6 +269,20 @@ int gbh_get_givals(gbh_engine *e, double *givals);
  * two, stream NULL means the engine's own stream.
  */
 int gbh_register_inputs(gbh_engine *e, int n, const int *solver, const int64_t *chip_index);
+
+/*
+ * The general form of h_in_msgs (hines_msgs.c:351-405): input i of kind
+ *   GBH_IN_SET  (INJECT/BASE/THRESH)  chip[index] = v
+ *   GBH_IN_ADD  (SYN2 messages)       chip[index] += v * sa * sb  when v > 1e-10
+ *                                     (sa = stablist[nop+3]; sb = hsolve->dt for
+ *                                     ACTIVATION messages into a synchan, else 1)
+ *   GBH_IN_FLUX (FLUX messages)       flux[index] = v  (index: conc index)
+ * Inputs with the same target are applied in registration order, as the
+ * reference walks its ininfo list. kind, sa, sb may be NULL (all SET, 1, 1).
+ */
+enum { GBH_IN_SET = 0, GBH_IN_ADD = 1, GBH_IN_FLUX = 2 };
+int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int *kind, const int64_t *index,
+                              const double *sa, const double *sb);
 int gbh_set_inputs_async(gbh_engine *e, const double *host_values, void *stream);
 int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row);
 int gbh_get_outputs_async(gbh_engine *e, double *host_values, void *stream);
