@@ -1655,6 +1655,10 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
     e->stats.jit_compact = e->jit_compact.empty() ? 0
                            : e->jit_compact[e->jit_choice] ? 1
                            : e->jit_smemrows[e->jit_choice] ? 2 : 0;
+    if (getenv("GBH_VERBOSE"))
+        for (const Launch &L : e->launches)
+            fprintf(stderr, "gbhsolve: launch group tiles [%d, %d) smax %d %s\n", L.tile0, L.tile1, L.smax,
+                    L.jit >= 0 ? "specialised" : "interpreted");
     if (getenv("GBH_VERBOSE") && !e->jit_log.empty())
         fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
                 e->jit_log.c_str());

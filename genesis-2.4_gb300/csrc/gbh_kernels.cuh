@@ -23,6 +23,335 @@
 
 namespace gbh {
 
+
+// Per-type constants of the compartment interpreter.
+template <typename G>
+struct ChanEnv {
+    const G *tab;
+    const double *xvals, *yvals;
+    TableGeom tg;
+    int ncols;
+    bool interp, c5, has_cd;
+};
+
+// State the reference carries from one compartment to the next within a
+// step (table cursors and their bases, the selected conc, the last channel's
+// Ek/Gk/Ik, GHK): reset at the start of every step.
+struct ChanState {
+    VCursor vc, cc;
+    double save_frac;
+    int tab_base, ctab_base, sel;
+    double Ek, Gk, gmax, Ik, GHK;
+    int doGHK;
+};
+
+__device__ __forceinline__ void chan_state_reset(ChanState &cs, int ncols)
+{
+    if (ncols) { cs.vc.lo = cs.vc.hi = 0.0; } else { cs.vc.lo = -1e20; cs.vc.hi = 1e20; }
+    cs.vc.row = cs.vc.base = 0;
+    cs.vc.frac = 0.0;
+    cs.cc.lo = cs.cc.hi = 0.0;
+    cs.cc.row = cs.cc.base = 0;
+    cs.cc.frac = 0.0;
+    cs.save_frac = 0.0;
+    cs.tab_base = cs.ctab_base = cs.sel = 0;
+    cs.Ek = cs.Gk = cs.gmax = cs.Ik = cs.GHK = 0.0;
+    cs.doGHK = 0;
+}
+
+// One neuron's rows: parameter fields P, integer state I, conc C, flux F,
+// givals G, codiag CD at stride STR (32: lane-interleaved tile, 1: wide
+// tile); ring: its synchan event rows (lane-interleaved in both layouts).
+struct ChanRows {
+    double *P;
+    int *I;
+    double *C, *F, *G, *CD;
+    unsigned *ring;
+    int64_t neuron;
+    bool active;
+};
+
+// One compartment's program (do_chip_hh4_update's body for one compartment,
+// genesis/src/hines/hines_chip.c:157-600): leaves its row's right-hand side
+// R and diagonal D. pc advances past the compartment. Returns false on an
+// unknown micro-op.
+template <typename G, bool GIV, int STR>
+__device__ __forceinline__ bool chan_compartment(const DevView &v, const ChanEnv<G> &E, ChanState &cs,
+                                                 const ChanRows &N, const int *&pc, double Vm, long long step,
+                                                 double &R, double &D)
+{
+    VCursor &vc = cs.vc, &cc = cs.cc;
+    double &save_frac = cs.save_frac;
+    int &tab_base = cs.tab_base, &ctab_base = cs.ctab_base, &sel = cs.sel;
+    double &Ek = cs.Ek, &Gk = cs.Gk, &gmax = cs.gmax, &Ik = cs.Ik, &GHK = cs.GHK;
+    int &doGHK = cs.doGHK;
+    const G *tab = E.tab;
+    const TableGeom &tg = E.tg;
+    const double *xvals = E.xvals, *yvals = E.yvals;
+    const int ncols = E.ncols;
+    const bool interp = E.interp, c5 = E.c5;
+    const int64_t neuron = N.neuron;
+    const bool active = N.active;
+    (void)neuron;
+    (void)active;
+    double sumg = 0.0, ichan = 0.0, Im = 0.0;
+    for (;;) {
+
+        const int code = pc[0];
+        if (code == M_BEGIN) {
+            const double emrm = N.P[(pc[1]) * STR];
+            ichan = emrm + N.P[(pc[2]) * STR];
+            if (GIV) {
+                Im = emrm - Vm / N.P[(pc[3]) * STR];
+                N.G[(pc[4]) * STR] = Im;
+            }
+            pc += 5;
+        } else if (code == M_NEWVOLT) {
+            locate(vc, Vm, tg.xmin, tg.invdx, tg.xdivs, xvals, ncols, interp);
+            pc += 1;
+        } else if (code == M_CONCVAL) {
+            sel = pc[1];
+            N.F[(sel) * STR] = 0.0;
+            pc += 2;
+        } else if (code == M_DOMAIN) {
+            const double concen = N.P[(pc[1]) * STR] * Ik;
+            locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
+            ctab_base = cc.base;
+            pc += 2;
+        } else if (code == M_NEWCONC2) {
+            const double concen = N.C[(pc[1]) * STR];
+            tab_base = ctab_base;
+            save_frac = cc.frac;
+            locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
+            ctab_base = cc.base;
+            pc += 2;
+        } else if (code == M_NEWCONC1) {
+            const double concen = N.C[(sel) * STR];
+            locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
+            ctab_base = cc.base;
+            pc += 1;
+        } else if (code == M_SPIKE) {
+            int cnt = N.I[(pc[2]) * STR] - 1;
+            if (Vm > N.P[(pc[1]) * STR]) {
+                if (cnt <= 0 && active) {
+                    // h_dospike_event: deliver to every target synchan
+                    const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
+                    for (int64_t e = e0; e < e1; ++e) {
+                        const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
+                        atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
+                    }
+                    v.spikes[neuron] += 1ULL;
+                    if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
+                    cnt = N.I[(pc[3]) * STR];
+                }
+            }
+            N.I[(pc[2]) * STR] = cnt;
+            pc += 4;
+        } else if (code == M_ELMMPUMP) {
+            const double cx = N.C[(sel) * STR];
+            const double X = 1.0 / (cx + N.P[(pc[1]) * STR]);
+            const double vmax = N.P[(pc[2]) * STR];
+            ichan += Ik = vmax * cx * X;
+            if (GIV) N.G[(pc[4]) * STR] = c5 ? Ik / vmax : Ik;
+            Im += Ik;
+            if (E.has_cd) N.CD[sel * STR] += N.P[(pc[3]) * STR] * X;   // hines_chip.c:301
+            pc += 5;
+        } else if (code == M_FLUX) {
+            N.F[(sel) * STR] += Ik;
+            pc += 1;
+        } else if (code == M_SCALE_FLUX) {
+            N.F[(sel) * STR] += N.P[(pc[1]) * STR] * Ik;
+            pc += 2;
+        } else if (code == M_STORE) {
+            pc += 3;  // itotal accumulation is host-visible only; rejected at setup
+        } else if (code == M_END) {
+            const double tbyc = N.P[(pc[1]) * STR];
+            R = Vm + ichan * tbyc;
+            D = sumg * tbyc + N.P[(pc[2]) * STR];
+            if (GIV) N.G[(pc[3]) * STR] = Im;
+            pc += 4;
+            break;
+        } else {
+            // current-producing ops, then the conductance sub-program
+            bool current = true;
+            if (code == M_GHK) {
+                const double cin = N.C[(sel) * STR], cout = N.C[((sel + 1)) * STR];
+                GHK = N.P[(pc[1]) * STR];
+                double X = Vm * GHK;
+                double Y = exp(-X);
+                Ek = N.P[(pc[2]) * STR];
+                Ik = Ek * (cin - (Y * cout));
+                if (fabs(X) < 1.0e-6) {
+                    Gk = 1.0 - 0.5 * X;
+                    GHK = 0.5 * GHK * Ek * (cin + cout);
+                    Ik = -Ik / Gk;
+                } else {
+                    Gk = 1.0 - Y;
+                    GHK = GHK * (Ik / Gk - Ek * GHK * (cin - cout) * Vm * Y / (Gk * Gk));
+                    Ik = -X * Ik / Gk;
+                }
+                Ek = (Ik + GHK * Vm) / GHK;
+                gmax = N.P[(pc[3]) * STR];
+                Gk = gmax * GHK;
+                pc += 4;
+            } else if (code == M_SAME_GHK) {
+                gmax = N.P[(pc[1]) * STR];
+                Gk = gmax * GHK;
+                pc += 2;
+            } else if (code == M_DO_TABGHK) {
+                doGHK = 1;
+                pc += 1;
+            } else if (code == M_NERNST) {
+                Ek = log(N.C[((sel + 1)) * STR] / N.C[(sel) * STR]) * N.P[(pc[1]) * STR];
+                gmax = Gk = N.P[(pc[2]) * STR];
+                pc += 3;
+            } else if (code == M_CHAN) {
+                Ek = N.P[(pc[1]) * STR];
+                gmax = Gk = N.P[(pc[2]) * STR];
+                pc += 3;
+            } else if (code == M_CHAN_G) {
+                gmax = Gk = N.P[(pc[1]) * STR];
+                pc += 2;
+            } else {
+                current = false;
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return false;
+            }
+            if (!current) continue;
+            for (;;) {
+                const int k = pc[0];
+                if (k == M_GATE) {
+                    const int kind = pc[1];
+                    int b;
+                    G X, Y;
+                    if (kind == GK_1V || kind == GK_1C) {
+                        const VCursor &cu = (kind == GK_1V) ? vc : cc;
+                        b = ((kind == GK_1V) ? vc.base : ctab_base) + pc[2];
+                        if (interp) {
+                            const G fr = (G)cu.frac;
+                            X = tab[b];
+                            X = X + fr * (tab[b + ncols] - X);
+                            Y = tab[b + 1];
+                            Y = Y + fr * (tab[b + 1 + ncols] - Y);
+                        } else {
+                            X = tab[b];
+                            Y = tab[b + 1];
+                        }
+                    } else {
+                        const G rf = (G)((kind == GK_2V) ? vc.frac : save_frac);
+                        const G cf = (G)cc.frac;
+                        b = ((kind == GK_2V) ? vc.base : tab_base) + cc.row + cc.row + pc[2];
+                        if (interp) {
+                            const int n = b + ncols;
+                            X = ((G)1.0 - rf) * (((G)1.0 - cf) * tab[b] + cf * tab[b + 2]) +
+                                rf * (((G)1.0 - cf) * tab[n] + cf * tab[n + 2]);
+                            Y = ((G)1.0 - rf) * (((G)1.0 - cf) * tab[b + 1] + cf * tab[b + 3]) +
+                                rf * (((G)1.0 - cf) * tab[n + 1] + cf * tab[n + 3]);
+                        } else {
+                            X = tab[b];
+                            Y = tab[b + 1];
+                        }
+                    }
+                    tab_base = b + 1;
+                    const int p = pc[3];
+                    if (p == 0) {
+                        Ek = (double)Y;
+                        pc += 5;
+                        if (doGHK) {
+                            GHK = (double)X;
+                            doGHK = 0;
+                            break;
+                        }
+                        Gk *= (double)X;   // tabcurrent; M_ADDCURR follows
+                        continue;
+                    } else {
+                        double *st = &N.P[(pc[4]) * STR];
+                        G x;
+                        int pw = p;
+                        if (p > 0) {
+                            x = ((G)(*st) * ((G)2.0 - X) + Y) / X;
+                        } else {
+                            x = Y / X;
+                            pw = -p;
+                        }
+                        *st = (double)x;
+                        Gk = (double)gpow<G>((G)Gk, x, pw);
+                        pc += 5;
+                        continue;
+                    }
+                } else if (k == M_SYN) {
+                    // SYN2_OP / SYN3_OP (hines_chip.c:511-531): decay X, add the
+                    // events due now (h_dosynchan, hines_conn.c:62-89), update Y.
+                    const double *sl = v.stablist + pc[2];
+                    double *px = &N.P[(pc[4]) * STR];
+                    double *py = &N.P[(pc[5]) * STR];
+                    if (pc[1] >= 0) {
+                        const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^
+                                             (uint64_t)pc[4];
+                        if (syn3_uniform(key) <= N.P[(pc[1]) * STR]) *px += sl[3];
+                    }
+                    double X = *px * sl[0];
+                    unsigned *cell = N.ring + ((int64_t)pc[3] * v.ring_len +
+                                               (int64_t)(step % v.ring_len)) * LANES;
+                    const unsigned n = *cell;
+                    if (n) {
+                        const double wdt = N.P[(pc[6]) * STR];
+                        double act = 0.0;
+                        for (unsigned q = 0; q < n; ++q) act += wdt;
+                        X += v.dt * act * sl[3];
+                        *cell = 0u;
+                    }
+                    *px = X;
+                    const double Y = X * sl[1] + *py * sl[2];
+                    *py = Y;
+                    Gk *= Y;
+                    pc += 7;
+                    continue;
+                } else if (k == M_MGBLOCK) {
+                    if (GIV) {
+                        const int g = pc[4];
+                        if (c5) {
+                            N.G[(g) * STR] = Gk / gmax;
+                            N.G[((g + 1)) * STR] = Gk * (Ek - Vm) / gmax;
+                        } else {
+                            N.G[(g) * STR] = Gk;
+                            N.G[((g + 1)) * STR] = Gk * (Ek - Vm);
+                        }
+                        N.G[((g + 2)) * STR] = Ek;
+                    }
+                    const double X = N.P[(pc[1]) * STR] * exp(Vm * N.P[(pc[2]) * STR]);
+                    Gk *= X / (X + N.P[(pc[3]) * STR]);
+                    pc += 5;
+                    continue;
+                } else if (k == M_ADDCURR) {
+                    // DOADDCURR (hines_chip.c:551-567)
+                    const int g = pc[1];
+                    sumg += Gk;
+                    ichan += Ek * Gk;
+                    Ik = Gk * (Ek - Vm);
+                    if (GIV) {
+                        if (c5) {
+                            N.G[(g) * STR] = Gk / gmax;
+                            N.G[((g + 1)) * STR] = Ik / gmax;
+                        } else {
+                            N.G[(g) * STR] = Gk;
+                            N.G[((g + 1)) * STR] = Ik;
+                        }
+                        N.G[((g + 2)) * STR] = Ek;
+                    }
+                    pc += 2;
+                } else {
+                    if (v.status) atomicOr(v.status, ST_BAD_OP);
+                    return false;
+                }
+                Im += Ik;
+                break;
+            }
+        }
+    }
+    return true;
+}
+
 // ---------------------------------------------------------------- kernel
 // Shared memory per warp: 2 * nslots_max * 32 doubles (diag and rhs columns).
 template <typename G, bool GIV>
@@ -61,275 +390,40 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
     const int64_t neuron = tl.first_neuron + lane;
     double *Fw = v.F + tl.pools * LANES + lane;
 
+    ChanEnv<G> E;
+    E.tab = tab;
+    E.xvals = xvals;
+    E.yvals = yvals;
+    E.tg = tg;
+    E.ncols = ncols;
+    E.interp = interp;
+    E.c5 = c5;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = Pw;
+    NR.I = Iw;
+    NR.C = Cw;
+    NR.F = Fw;
+    NR.G = Gw;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.ring = v.ring + tl.syn * LANES + lane;
+    NR.neuron = neuron;
+    NR.active = active;
+
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
-        VCursor vc, cc;
-        if (tg.ncols) { vc.lo = vc.hi = 0.0; } else { vc.lo = -1e20; vc.hi = 1e20; }
-        vc.row = vc.base = 0; vc.frac = 0.0;
-        cc.lo = cc.hi = 0.0; cc.row = cc.base = 0; cc.frac = 0.0;
-        double save_frac = 0.0;
-        int tab_base = 0, ctab_base = 0, sel = 0;
-        double Ek = 0.0, Gk = 0.0, gmax = 0.0, Ik = 0.0, GHK = 0.0;
-        int doGHK = 0;
-
         // ---------------- channel phase ----------------
+        ChanState cs;
+        chan_state_reset(cs, tg.ncols);
         const int *pc = v.prog + ty.prog_off;
         for (int s = 0; s < S; ++s) {
-            const double Vm = Vw[s * LANES];
-            double sumg = 0.0, ichan = 0.0, Im = 0.0;
-            for (;;) {
-                const int code = pc[0];
-                if (code == M_BEGIN) {
-                    const double emrm = Pw[pc[1] * LANES];
-                    ichan = emrm + Pw[pc[2] * LANES];
-                    if (GIV) {
-                        Im = emrm - Vm / Pw[pc[3] * LANES];
-                        Gw[pc[4] * LANES] = Im;
-                    }
-                    pc += 5;
-                } else if (code == M_NEWVOLT) {
-                    locate(vc, Vm, tg.xmin, tg.invdx, tg.xdivs, xvals, ncols, interp);
-                    pc += 1;
-                } else if (code == M_CONCVAL) {
-                    sel = pc[1];
-                    Fw[sel * LANES] = 0.0;
-                    pc += 2;
-                } else if (code == M_DOMAIN) {
-                    const double concen = Pw[pc[1] * LANES] * Ik;
-                    locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
-                    ctab_base = cc.base;
-                    pc += 2;
-                } else if (code == M_NEWCONC2) {
-                    const double concen = Cw[pc[1] * LANES];
-                    tab_base = ctab_base;
-                    save_frac = cc.frac;
-                    locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
-                    ctab_base = cc.base;
-                    pc += 2;
-                } else if (code == M_NEWCONC1) {
-                    const double concen = Cw[sel * LANES];
-                    locate(cc, concen, tg.ymin, tg.invdy, tg.ydivs, yvals, ncols, interp);
-                    ctab_base = cc.base;
-                    pc += 1;
-                } else if (code == M_SPIKE) {
-                    int cnt = Iw[pc[2] * LANES] - 1;
-                    if (Vm > Pw[pc[1] * LANES]) {
-                        if (cnt <= 0 && active) {
-                            // h_dospike_event: deliver to every target synchan
-                            const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
-                            for (int64_t e = e0; e < e1; ++e) {
-                                const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
-                                atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
-                            }
-                            v.spikes[neuron] += 1ULL;
-                            if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
-                            cnt = Iw[pc[3] * LANES];
-                        }
-                    }
-                    Iw[pc[2] * LANES] = cnt;
-                    pc += 4;
-                } else if (code == M_ELMMPUMP) {
-                    const double cx = Cw[sel * LANES];
-                    const double X = 1.0 / (cx + Pw[pc[1] * LANES]);
-                    const double vmax = Pw[pc[2] * LANES];
-                    ichan += Ik = vmax * cx * X;
-                    if (GIV) Gw[pc[4] * LANES] = c5 ? Ik / vmax : Ik;
-                    Im += Ik;
-                    if (ty.has_cd) v.CD[(tl.pools + sel) * LANES + lane] += Pw[pc[3] * LANES] * X;   // hines_chip.c:301
-                    pc += 5;
-                } else if (code == M_FLUX) {
-                    Fw[sel * LANES] += Ik;
-                    pc += 1;
-                } else if (code == M_SCALE_FLUX) {
-                    Fw[sel * LANES] += Pw[pc[1] * LANES] * Ik;
-                    pc += 2;
-                } else if (code == M_STORE) {
-                    pc += 3;  // itotal accumulation is host-visible only; rejected at setup
-                } else if (code == M_END) {
-                    const double tbyc = Pw[pc[1] * LANES];
-                    Rcol[s * LANES] = Vm + ichan * tbyc;
-                    Dcol[s * LANES] = sumg * tbyc + Pw[pc[2] * LANES];
-                    if (GIV) Gw[pc[3] * LANES] = Im;
-                    pc += 4;
-                    break;
-                } else {
-                    // current-producing ops, then the conductance sub-program
-                    bool current = true;
-                    if (code == M_GHK) {
-                        const double cin = Cw[sel * LANES], cout = Cw[(sel + 1) * LANES];
-                        GHK = Pw[pc[1] * LANES];
-                        double X = Vm * GHK;
-                        double Y = exp(-X);
-                        Ek = Pw[pc[2] * LANES];
-                        Ik = Ek * (cin - (Y * cout));
-                        if (fabs(X) < 1.0e-6) {
-                            Gk = 1.0 - 0.5 * X;
-                            GHK = 0.5 * GHK * Ek * (cin + cout);
-                            Ik = -Ik / Gk;
-                        } else {
-                            Gk = 1.0 - Y;
-                            GHK = GHK * (Ik / Gk - Ek * GHK * (cin - cout) * Vm * Y / (Gk * Gk));
-                            Ik = -X * Ik / Gk;
-                        }
-                        Ek = (Ik + GHK * Vm) / GHK;
-                        gmax = Pw[pc[3] * LANES];
-                        Gk = gmax * GHK;
-                        pc += 4;
-                    } else if (code == M_SAME_GHK) {
-                        gmax = Pw[pc[1] * LANES];
-                        Gk = gmax * GHK;
-                        pc += 2;
-                    } else if (code == M_DO_TABGHK) {
-                        doGHK = 1;
-                        pc += 1;
-                    } else if (code == M_NERNST) {
-                        Ek = log(Cw[(sel + 1) * LANES] / Cw[sel * LANES]) * Pw[pc[1] * LANES];
-                        gmax = Gk = Pw[pc[2] * LANES];
-                        pc += 3;
-                    } else if (code == M_CHAN) {
-                        Ek = Pw[pc[1] * LANES];
-                        gmax = Gk = Pw[pc[2] * LANES];
-                        pc += 3;
-                    } else if (code == M_CHAN_G) {
-                        gmax = Gk = Pw[pc[1] * LANES];
-                        pc += 2;
-                    } else {
-                        current = false;
-                        if (v.status) atomicOr(v.status, ST_BAD_OP);
-                        return;
-                    }
-                    if (!current) continue;
-                    for (;;) {
-                        const int k = pc[0];
-                        if (k == M_GATE) {
-                            const int kind = pc[1];
-                            int b;
-                            G X, Y;
-                            if (kind == GK_1V || kind == GK_1C) {
-                                const VCursor &cu = (kind == GK_1V) ? vc : cc;
-                                b = ((kind == GK_1V) ? vc.base : ctab_base) + pc[2];
-                                if (interp) {
-                                    const G fr = (G)cu.frac;
-                                    X = tab[b];
-                                    X = X + fr * (tab[b + ncols] - X);
-                                    Y = tab[b + 1];
-                                    Y = Y + fr * (tab[b + 1 + ncols] - Y);
-                                } else {
-                                    X = tab[b];
-                                    Y = tab[b + 1];
-                                }
-                            } else {
-                                const G rf = (G)((kind == GK_2V) ? vc.frac : save_frac);
-                                const G cf = (G)cc.frac;
-                                b = ((kind == GK_2V) ? vc.base : tab_base) + cc.row + cc.row + pc[2];
-                                if (interp) {
-                                    const int n = b + ncols;
-                                    X = ((G)1.0 - rf) * (((G)1.0 - cf) * tab[b] + cf * tab[b + 2]) +
-                                        rf * (((G)1.0 - cf) * tab[n] + cf * tab[n + 2]);
-                                    Y = ((G)1.0 - rf) * (((G)1.0 - cf) * tab[b + 1] + cf * tab[b + 3]) +
-                                        rf * (((G)1.0 - cf) * tab[n + 1] + cf * tab[n + 3]);
-                                } else {
-                                    X = tab[b];
-                                    Y = tab[b + 1];
-                                }
-                            }
-                            tab_base = b + 1;
-                            const int p = pc[3];
-                            if (p == 0) {
-                                Ek = (double)Y;
-                                pc += 5;
-                                if (doGHK) {
-                                    GHK = (double)X;
-                                    doGHK = 0;
-                                    break;
-                                }
-                                Gk *= (double)X;   // tabcurrent; M_ADDCURR follows
-                                continue;
-                            } else {
-                                double *st = &Pw[pc[4] * LANES];
-                                G x;
-                                int pw = p;
-                                if (p > 0) {
-                                    x = ((G)(*st) * ((G)2.0 - X) + Y) / X;
-                                } else {
-                                    x = Y / X;
-                                    pw = -p;
-                                }
-                                *st = (double)x;
-                                Gk = (double)gpow<G>((G)Gk, x, pw);
-                                pc += 5;
-                                continue;
-                            }
-                        } else if (k == M_SYN) {
-                            // SYN2_OP / SYN3_OP (hines_chip.c:511-531): decay X, add the
-                            // events due now (h_dosynchan, hines_conn.c:62-89), update Y.
-                            const double *sl = v.stablist + pc[2];
-                            double *px = &Pw[pc[4] * LANES];
-                            double *py = &Pw[pc[5] * LANES];
-                            if (pc[1] >= 0) {
-                                const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^
-                                                     (uint64_t)pc[4];
-                                if (syn3_uniform(key) <= Pw[pc[1] * LANES]) *px += sl[3];
-                            }
-                            double X = *px * sl[0];
-                            unsigned *cell = v.ring + ((tl.syn + (int64_t)pc[3] * v.ring_len +
-                                                        (int64_t)(step % v.ring_len)) * LANES + lane);
-                            const unsigned n = *cell;
-                            if (n) {
-                                const double wdt = Pw[pc[6] * LANES];
-                                double act = 0.0;
-                                for (unsigned q = 0; q < n; ++q) act += wdt;
-                                X += v.dt * act * sl[3];
-                                *cell = 0u;
-                            }
-                            *px = X;
-                            const double Y = X * sl[1] + *py * sl[2];
-                            *py = Y;
-                            Gk *= Y;
-                            pc += 7;
-                            continue;
-                        } else if (k == M_MGBLOCK) {
-                            if (GIV) {
-                                const int g = pc[4];
-                                if (c5) {
-                                    Gw[g * LANES] = Gk / gmax;
-                                    Gw[(g + 1) * LANES] = Gk * (Ek - Vm) / gmax;
-                                } else {
-                                    Gw[g * LANES] = Gk;
-                                    Gw[(g + 1) * LANES] = Gk * (Ek - Vm);
-                                }
-                                Gw[(g + 2) * LANES] = Ek;
-                            }
-                            const double X = Pw[pc[1] * LANES] * exp(Vm * Pw[pc[2] * LANES]);
-                            Gk *= X / (X + Pw[pc[3] * LANES]);
-                            pc += 5;
-                            continue;
-                        } else if (k == M_ADDCURR) {
-                            // DOADDCURR (hines_chip.c:551-567)
-                            const int g = pc[1];
-                            sumg += Gk;
-                            ichan += Ek * Gk;
-                            Ik = Gk * (Ek - Vm);
-                            if (GIV) {
-                                if (c5) {
-                                    Gw[g * LANES] = Gk / gmax;
-                                    Gw[(g + 1) * LANES] = Ik / gmax;
-                                } else {
-                                    Gw[g * LANES] = Gk;
-                                    Gw[(g + 1) * LANES] = Ik;
-                                }
-                                Gw[(g + 2) * LANES] = Ek;
-                            }
-                            pc += 2;
-                        } else {
-                            if (v.status) atomicOr(v.status, ST_BAD_OP);
-                            return;
-                        }
-                        Im += Ik;
-                        break;
-                    }
-                }
+            double R, D;
+            if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
             }
+            Rcol[s * LANES] = R;
+            Dcol[s * LANES] = D;
         }
 
         // ---------------- pool phase ----------------

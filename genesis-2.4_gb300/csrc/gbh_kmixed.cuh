@@ -18,6 +18,293 @@
 
 namespace gbh {
 
+
+// Per-type constants of the mixed compartment interpreter.
+struct ChanEnvDF {
+    const float4 *tab;
+    TableGeom tg;
+    int ncols;
+    df xnmin, xinv, ynmin, yinv;
+    bool c5, has_cd;
+};
+
+// Carried state of the mixed interpreter (reset every step).
+struct ChanStateDF {
+    DCursor vc, cc, c1;
+    int sel;
+    df Ek, Gk, gmax;
+    double GHK, Ik;
+    int doGHK;
+};
+
+__device__ __forceinline__ void chan_state_reset_df(ChanStateDF &cs)
+{
+    cs.vc.row = cs.vc.base = 0;
+    cs.vc.frac = df_make(0.f, 0.f);
+    cs.cc = cs.vc;
+    cs.c1 = cs.vc;
+    cs.sel = 0;
+    cs.Ek = cs.Gk = cs.gmax = df_make(0.f, 0.f);
+    cs.GHK = cs.Ik = 0.0;
+    cs.doGHK = 0;
+}
+
+// One compartment of the mixed form: double-float gates, FP64 row terms.
+template <bool GIV, int STR>
+__device__ __forceinline__ bool chan_compartment_df(const DevView &v, const ChanEnvDF &E, ChanStateDF &cs,
+                                                    const ChanRows &N, const int *&pc, double Vm, long long step,
+                                                    double &R, double &D)
+{
+    DCursor &vc = cs.vc, &cc = cs.cc, &c1 = cs.c1;
+    int &sel = cs.sel;
+    df &Ek = cs.Ek, &Gk = cs.Gk, &gmax = cs.gmax;
+    double &GHK = cs.GHK, &Ik = cs.Ik;
+    int &doGHK = cs.doGHK;
+    const float4 *tab = E.tab;
+    const TableGeom &tg = E.tg;
+    const int ncols = E.ncols;
+    const df xnmin = E.xnmin, xinv = E.xinv, ynmin = E.ynmin, yinv = E.yinv;
+    const bool c5 = E.c5;
+    const int64_t neuron = N.neuron;
+    const bool active = N.active;
+    (void)neuron;
+    (void)active;
+    (void)c1;
+    const df vmd = d2df(Vm);
+    df sumg = df_make(0.f, 0.f), ichan = sumg;
+    double Im = 0.0;
+    for (;;) {
+
+        const int code = pc[0];
+        if (code == M_BEGIN) {
+            const df emrm = ld_df(&N.P[(pc[1]) * STR]);
+            ichan = df_add(emrm, ld_df(&N.P[(pc[2]) * STR]));
+            if (GIV) {
+                Im = df2d(emrm) - Vm / N.P[(pc[3]) * STR];
+                N.G[(pc[4]) * STR] = Im;
+            }
+            pc += 5;
+        } else if (code == M_NEWVOLT) {
+            locate_df(vc, vmd, xnmin, xinv, tg.xdivs, ncols);
+            pc += 1;
+        } else if (code == M_CONCVAL) {
+            sel = pc[1];
+            N.F[(sel) * STR] = 0.0;
+            pc += 2;
+        } else if (code == M_DOMAIN) {
+            locate_df(cc, d2df(N.P[(pc[1]) * STR] * Ik), ynmin, yinv, tg.ydivs, ncols);
+            pc += 2;
+        } else if (code == M_NEWCONC2) {
+            c1 = cc;
+            locate_df(cc, d2df(N.C[(pc[1]) * STR]), ynmin, yinv, tg.ydivs, ncols);
+            pc += 2;
+        } else if (code == M_NEWCONC1) {
+            locate_df(cc, d2df(N.C[(sel) * STR]), ynmin, yinv, tg.ydivs, ncols);
+            pc += 1;
+        } else if (code == M_SPIKE) {
+            int cnt = N.I[(pc[2]) * STR] - 1;
+            if (Vm > N.P[(pc[1]) * STR]) {
+                if (cnt <= 0 && active) {
+                    const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
+                    for (int64_t e = e0; e < e1; ++e) {
+                        const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
+                        atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
+                    }
+                    v.spikes[neuron] += 1ULL;
+                    if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
+                    cnt = N.I[(pc[3]) * STR];
+                }
+            }
+            N.I[(pc[2]) * STR] = cnt;
+            pc += 4;
+        } else if (code == M_ELMMPUMP) {
+            const double cx = N.C[(sel) * STR];
+            const double X = 1.0 / (cx + N.P[(pc[1]) * STR]);
+            const double vmax = N.P[(pc[2]) * STR];
+            Ik = vmax * cx * X;
+            ichan = df_add(ichan, d2df(Ik));
+            if (GIV) N.G[(pc[4]) * STR] = c5 ? Ik / vmax : Ik;
+            Im += Ik;
+            if (E.has_cd) N.CD[sel * STR] += N.P[(pc[3]) * STR] * X;   // hines_chip.c:301
+            pc += 5;
+        } else if (code == M_FLUX) {
+            N.F[(sel) * STR] += Ik;
+            pc += 1;
+        } else if (code == M_SCALE_FLUX) {
+            N.F[(sel) * STR] += N.P[(pc[1]) * STR] * Ik;
+            pc += 2;
+        } else if (code == M_STORE) {
+            pc += 3;
+        } else if (code == M_END) {
+            const df tbyc = ld_df(&N.P[(pc[1]) * STR]);
+            const df dv = df_mul(ichan, tbyc);
+            R = df2d(df_add(vmd, dv));
+            D = df2d(df_add(df_mul(sumg, tbyc), ld_df(&N.P[(pc[2]) * STR])));
+            if (GIV) N.G[(pc[3]) * STR] = Im;
+            pc += 4;
+            break;
+        } else {
+            if (code == M_GHK) {
+                const double cin = N.C[(sel) * STR], cout = N.C[((sel + 1)) * STR];
+                double g = N.P[(pc[1]) * STR];
+                const double X = Vm * g;
+                const double Y = exp(-X);
+                double e = N.P[(pc[2]) * STR];
+                double ik = e * (cin - (Y * cout));
+                double gk;
+                if (fabs(X) < 1.0e-6) {
+                    gk = 1.0 - 0.5 * X;
+                    g = 0.5 * g * e * (cin + cout);
+                    ik = -ik / gk;
+                } else {
+                    gk = 1.0 - Y;
+                    g = g * (ik / gk - e * g * (cin - cout) * Vm * Y / (gk * gk));
+                    ik = -X * ik / gk;
+                }
+                GHK = g;
+                Ek = d2df((ik + g * Vm) / g);
+                gmax = d2df(N.P[(pc[3]) * STR]);
+                Gk = d2df(N.P[(pc[3]) * STR] * GHK);
+                pc += 4;
+            } else if (code == M_SAME_GHK) {
+                gmax = d2df(N.P[(pc[1]) * STR]);
+                Gk = d2df(N.P[(pc[1]) * STR] * GHK);
+                pc += 2;
+            } else if (code == M_DO_TABGHK) {
+                doGHK = 1;
+                pc += 1;
+            } else if (code == M_NERNST) {
+                Ek = d2df(log(N.C[((sel + 1)) * STR] / N.C[(sel) * STR]) * N.P[(pc[1]) * STR]);
+                gmax = Gk = d2df(N.P[(pc[2]) * STR]);
+                pc += 3;
+            } else if (code == M_CHAN) {
+                Ek = ld_df(&N.P[(pc[1]) * STR]);
+                gmax = Gk = ld_df(&N.P[(pc[2]) * STR]);
+                pc += 3;
+            } else if (code == M_CHAN_G) {
+                gmax = Gk = ld_df(&N.P[(pc[1]) * STR]);
+                pc += 2;
+            } else {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return false;
+            }
+            for (;;) {
+                const int k = pc[0];
+                if (k == M_GATE) {
+                    const int kind = pc[1];
+                    df X, Y;
+                    if (kind == GK_1V || kind == GK_1C) {
+                        const DCursor &cu = (kind == GK_1V) ? vc : cc;
+                        const int b = cu.base + pc[2];
+                        X = interp_df(tab, b, cu.frac);
+                        Y = interp_df(tab, b + 1, cu.frac);
+                    } else {
+                        // 2-D tables: rows from the voltage (or first conc) cursor,
+                        // columns from the conc cursor
+                        const DCursor &ru = (kind == GK_2V) ? vc : c1;
+                        const int b = ru.base + cc.row + cc.row + pc[2];
+                        const df cf = cc.frac, rf = ru.frac;
+                        const df one_c = df_add_f(df_neg(cf), 1.0f), one_r = df_add_f(df_neg(rf), 1.0f);
+                        df q[2];
+                        for (int h = 0; h < 2; ++h) {
+                            const df t00 = val_df(tab, b + h), t01 = val_df(tab, b + 2 + h);
+                            const df t10 = interp_df(tab, b + h, df_make(1.f, 0.f));
+                            const df t11 = interp_df(tab, b + 2 + h, df_make(1.f, 0.f));
+                            const df lo = df_add(df_mul(one_c, t00), df_mul(cf, t01));
+                            const df hi = df_add(df_mul(one_c, t10), df_mul(cf, t11));
+                            q[h] = df_add(df_mul(one_r, lo), df_mul(rf, hi));
+                        }
+                        X = q[0];
+                        Y = q[1];
+                    }
+                    const int p = pc[3];
+                    if (p == 0) {
+                        Ek = Y;
+                        pc += 5;
+                        if (doGHK) {
+                            GHK = df2d(X);
+                            doGHK = 0;
+                            break;
+                        }
+                        Gk = df_mul(Gk, X);
+                        continue;
+                    }
+                    double *st = &N.P[(pc[4]) * STR];
+                    df x;
+                    int pw = p;
+                    if (p > 0) {
+                        x = df_div(df_add(df_mul(ld_df(st), df_add_f(df_neg(X), 2.0f)), Y), X);
+                    } else {
+                        x = df_div(Y, X);
+                        pw = -p;
+                    }
+                    st_df(st, x);
+                    Gk = dpow(Gk, x, pw);
+                    pc += 5;
+                    continue;
+                } else if (k == M_SYN) {
+                    const double *sl = v.stablist + pc[2];
+                    double *px = &N.P[(pc[4]) * STR];
+                    double *py = &N.P[(pc[5]) * STR];
+                    if (pc[1] >= 0) {
+                        const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^
+                                             (uint64_t)pc[4];
+                        if (syn3_uniform(key) <= N.P[(pc[1]) * STR]) *px += sl[3];
+                    }
+                    double X = *px * sl[0];
+                    unsigned *cell = N.ring + ((int64_t)pc[3] * v.ring_len + (int64_t)(step % v.ring_len)) * LANES;
+                    const unsigned n = *cell;
+                    if (n) {
+                        const double wdt = N.P[(pc[6]) * STR];
+                        double act = 0.0;
+                        for (unsigned q = 0; q < n; ++q) act += wdt;
+                        X += v.dt * act * sl[3];
+                        *cell = 0u;
+                    }
+                    *px = X;
+                    const double Y = X * sl[1] + *py * sl[2];
+                    *py = Y;
+                    Gk = df_mul(Gk, d2df(Y));
+                    pc += 7;
+                    continue;
+                } else if (k == M_MGBLOCK) {
+                    const double gk = df2d(Gk), ek = df2d(Ek);
+                    if (GIV) {
+                        const int g = pc[4];
+                        const double gm = c5 ? df2d(gmax) : 1.0;
+                        N.G[(g) * STR] = gk / gm;
+                        N.G[((g + 1)) * STR] = gk * (ek - Vm) / gm;
+                        N.G[((g + 2)) * STR] = ek;
+                    }
+                    const double X = N.P[(pc[1]) * STR] * exp(Vm * N.P[(pc[2]) * STR]);
+                    Gk = d2df(gk * (X / (X + N.P[(pc[3]) * STR])));
+                    pc += 5;
+                    continue;
+                } else if (k == M_ADDCURR) {
+                    const int g = pc[1];
+                    sumg = df_add(sumg, Gk);
+                    ichan = df_add(ichan, df_mul(Ek, Gk));
+                    const double gk = df2d(Gk), ek = df2d(Ek);
+                    Ik = gk * (ek - Vm);
+                    if (GIV) {
+                        const double gm = c5 ? df2d(gmax) : 1.0;
+                        N.G[(g) * STR] = gk / gm;
+                        N.G[((g + 1)) * STR] = Ik / gm;
+                        N.G[((g + 2)) * STR] = ek;
+                    }
+                    Im += Ik;
+                    pc += 2;
+                    break;
+                } else {
+                    if (v.status) atomicOr(v.status, ST_BAD_OP);
+                    return false;
+                }
+            }
+        }
+    }
+    return true;
+}
+
 template <bool GIV>
 __global__ void __launch_bounds__(128, 6)
 k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
@@ -53,251 +340,40 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
     const int S = ty.nslots;
     const int64_t neuron = tl.first_neuron + lane;
 
+    ChanEnvDF E;
+    E.tab = tab;
+    E.tg = tg;
+    E.ncols = ncols;
+    E.xnmin = xnmin;
+    E.xinv = xinv;
+    E.ynmin = ynmin;
+    E.yinv = yinv;
+    E.c5 = c5;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = Pw;
+    NR.I = Iw;
+    NR.C = Cw;
+    NR.F = Fw;
+    NR.G = Gw;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.ring = v.ring + tl.syn * LANES + lane;
+    NR.neuron = neuron;
+    NR.active = active;
+
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
-        DCursor vc, cc, c1;
-        vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f);
-        cc = vc;
-        c1 = vc;
-        int sel = 0;
-        df Ek = df_make(0.f, 0.f), Gk = Ek, gmax = Ek;
-        double GHK = 0.0, Ik = 0.0;
-        int doGHK = 0;
+        ChanStateDF cs;
+        chan_state_reset_df(cs);
         const int *pc = v.prog + ty.prog_off;
         for (int s = 0; s < S; ++s) {
-            const double Vm = Vw[s * LANES];
-            const df vmd = d2df(Vm);
-            df sumg = df_make(0.f, 0.f), ichan = sumg;
-            double Im = 0.0;
-            for (;;) {
-                const int code = pc[0];
-                if (code == M_BEGIN) {
-                    const df emrm = ld_df(&Pw[pc[1] * LANES]);
-                    ichan = df_add(emrm, ld_df(&Pw[pc[2] * LANES]));
-                    if (GIV) {
-                        Im = df2d(emrm) - Vm / Pw[pc[3] * LANES];
-                        Gw[pc[4] * LANES] = Im;
-                    }
-                    pc += 5;
-                } else if (code == M_NEWVOLT) {
-                    locate_df(vc, vmd, xnmin, xinv, tg.xdivs, ncols);
-                    pc += 1;
-                } else if (code == M_CONCVAL) {
-                    sel = pc[1];
-                    Fw[sel * LANES] = 0.0;
-                    pc += 2;
-                } else if (code == M_DOMAIN) {
-                    locate_df(cc, d2df(Pw[pc[1] * LANES] * Ik), ynmin, yinv, tg.ydivs, ncols);
-                    pc += 2;
-                } else if (code == M_NEWCONC2) {
-                    c1 = cc;
-                    locate_df(cc, d2df(Cw[pc[1] * LANES]), ynmin, yinv, tg.ydivs, ncols);
-                    pc += 2;
-                } else if (code == M_NEWCONC1) {
-                    locate_df(cc, d2df(Cw[sel * LANES]), ynmin, yinv, tg.ydivs, ncols);
-                    pc += 1;
-                } else if (code == M_SPIKE) {
-                    int cnt = Iw[pc[2] * LANES] - 1;
-                    if (Vm > Pw[pc[1] * LANES]) {
-                        if (cnt <= 0 && active) {
-                            const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
-                            for (int64_t e = e0; e < e1; ++e) {
-                                const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
-                                atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
-                            }
-                            v.spikes[neuron] += 1ULL;
-                            if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
-                            cnt = Iw[pc[3] * LANES];
-                        }
-                    }
-                    Iw[pc[2] * LANES] = cnt;
-                    pc += 4;
-                } else if (code == M_ELMMPUMP) {
-                    const double cx = Cw[sel * LANES];
-                    const double X = 1.0 / (cx + Pw[pc[1] * LANES]);
-                    const double vmax = Pw[pc[2] * LANES];
-                    Ik = vmax * cx * X;
-                    ichan = df_add(ichan, d2df(Ik));
-                    if (GIV) Gw[pc[4] * LANES] = c5 ? Ik / vmax : Ik;
-                    Im += Ik;
-                    if (ty.has_cd) v.CD[(tl.pools + sel) * LANES + lane] += Pw[pc[3] * LANES] * X;   // hines_chip.c:301
-                    pc += 5;
-                } else if (code == M_FLUX) {
-                    Fw[sel * LANES] += Ik;
-                    pc += 1;
-                } else if (code == M_SCALE_FLUX) {
-                    Fw[sel * LANES] += Pw[pc[1] * LANES] * Ik;
-                    pc += 2;
-                } else if (code == M_STORE) {
-                    pc += 3;
-                } else if (code == M_END) {
-                    const df tbyc = ld_df(&Pw[pc[1] * LANES]);
-                    const df dv = df_mul(ichan, tbyc);
-                    Rcol[s * LANES] = df2d(df_add(vmd, dv));
-                    Dcol[s * LANES] = df2d(df_add(df_mul(sumg, tbyc), ld_df(&Pw[pc[2] * LANES])));
-                    if (GIV) Gw[pc[3] * LANES] = Im;
-                    pc += 4;
-                    break;
-                } else {
-                    if (code == M_GHK) {
-                        const double cin = Cw[sel * LANES], cout = Cw[(sel + 1) * LANES];
-                        double g = Pw[pc[1] * LANES];
-                        const double X = Vm * g;
-                        const double Y = exp(-X);
-                        double e = Pw[pc[2] * LANES];
-                        double ik = e * (cin - (Y * cout));
-                        double gk;
-                        if (fabs(X) < 1.0e-6) {
-                            gk = 1.0 - 0.5 * X;
-                            g = 0.5 * g * e * (cin + cout);
-                            ik = -ik / gk;
-                        } else {
-                            gk = 1.0 - Y;
-                            g = g * (ik / gk - e * g * (cin - cout) * Vm * Y / (gk * gk));
-                            ik = -X * ik / gk;
-                        }
-                        GHK = g;
-                        Ek = d2df((ik + g * Vm) / g);
-                        gmax = d2df(Pw[pc[3] * LANES]);
-                        Gk = d2df(Pw[pc[3] * LANES] * GHK);
-                        pc += 4;
-                    } else if (code == M_SAME_GHK) {
-                        gmax = d2df(Pw[pc[1] * LANES]);
-                        Gk = d2df(Pw[pc[1] * LANES] * GHK);
-                        pc += 2;
-                    } else if (code == M_DO_TABGHK) {
-                        doGHK = 1;
-                        pc += 1;
-                    } else if (code == M_NERNST) {
-                        Ek = d2df(log(Cw[(sel + 1) * LANES] / Cw[sel * LANES]) * Pw[pc[1] * LANES]);
-                        gmax = Gk = d2df(Pw[pc[2] * LANES]);
-                        pc += 3;
-                    } else if (code == M_CHAN) {
-                        Ek = ld_df(&Pw[pc[1] * LANES]);
-                        gmax = Gk = ld_df(&Pw[pc[2] * LANES]);
-                        pc += 3;
-                    } else if (code == M_CHAN_G) {
-                        gmax = Gk = ld_df(&Pw[pc[1] * LANES]);
-                        pc += 2;
-                    } else {
-                        if (v.status) atomicOr(v.status, ST_BAD_OP);
-                        return;
-                    }
-                    for (;;) {
-                        const int k = pc[0];
-                        if (k == M_GATE) {
-                            const int kind = pc[1];
-                            df X, Y;
-                            if (kind == GK_1V || kind == GK_1C) {
-                                const DCursor &cu = (kind == GK_1V) ? vc : cc;
-                                const int b = cu.base + pc[2];
-                                X = interp_df(tab, b, cu.frac);
-                                Y = interp_df(tab, b + 1, cu.frac);
-                            } else {
-                                // 2-D tables: rows from the voltage (or first conc) cursor,
-                                // columns from the conc cursor
-                                const DCursor &ru = (kind == GK_2V) ? vc : c1;
-                                const int b = ru.base + cc.row + cc.row + pc[2];
-                                const df cf = cc.frac, rf = ru.frac;
-                                const df one_c = df_add_f(df_neg(cf), 1.0f), one_r = df_add_f(df_neg(rf), 1.0f);
-                                df q[2];
-                                for (int h = 0; h < 2; ++h) {
-                                    const df t00 = val_df(tab, b + h), t01 = val_df(tab, b + 2 + h);
-                                    const df t10 = interp_df(tab, b + h, df_make(1.f, 0.f));
-                                    const df t11 = interp_df(tab, b + 2 + h, df_make(1.f, 0.f));
-                                    const df lo = df_add(df_mul(one_c, t00), df_mul(cf, t01));
-                                    const df hi = df_add(df_mul(one_c, t10), df_mul(cf, t11));
-                                    q[h] = df_add(df_mul(one_r, lo), df_mul(rf, hi));
-                                }
-                                X = q[0];
-                                Y = q[1];
-                            }
-                            const int p = pc[3];
-                            if (p == 0) {
-                                Ek = Y;
-                                pc += 5;
-                                if (doGHK) {
-                                    GHK = df2d(X);
-                                    doGHK = 0;
-                                    break;
-                                }
-                                Gk = df_mul(Gk, X);
-                                continue;
-                            }
-                            double *st = &Pw[pc[4] * LANES];
-                            df x;
-                            int pw = p;
-                            if (p > 0) {
-                                x = df_div(df_add(df_mul(ld_df(st), df_add_f(df_neg(X), 2.0f)), Y), X);
-                            } else {
-                                x = df_div(Y, X);
-                                pw = -p;
-                            }
-                            st_df(st, x);
-                            Gk = dpow(Gk, x, pw);
-                            pc += 5;
-                            continue;
-                        } else if (k == M_SYN) {
-                            const double *sl = v.stablist + pc[2];
-                            double *px = &Pw[pc[4] * LANES];
-                            double *py = &Pw[pc[5] * LANES];
-                            if (pc[1] >= 0) {
-                                const uint64_t key = ((uint64_t)neuron << 24) ^ ((uint64_t)step << 1) ^
-                                                     (uint64_t)pc[4];
-                                if (syn3_uniform(key) <= Pw[pc[1] * LANES]) *px += sl[3];
-                            }
-                            double X = *px * sl[0];
-                            unsigned *cell = v.ring + ((tl.syn + (int64_t)pc[3] * v.ring_len +
-                                                        (int64_t)(step % v.ring_len)) * LANES + lane);
-                            const unsigned n = *cell;
-                            if (n) {
-                                const double wdt = Pw[pc[6] * LANES];
-                                double act = 0.0;
-                                for (unsigned q = 0; q < n; ++q) act += wdt;
-                                X += v.dt * act * sl[3];
-                                *cell = 0u;
-                            }
-                            *px = X;
-                            const double Y = X * sl[1] + *py * sl[2];
-                            *py = Y;
-                            Gk = df_mul(Gk, d2df(Y));
-                            pc += 7;
-                            continue;
-                        } else if (k == M_MGBLOCK) {
-                            const double gk = df2d(Gk), ek = df2d(Ek);
-                            if (GIV) {
-                                const int g = pc[4];
-                                const double gm = c5 ? df2d(gmax) : 1.0;
-                                Gw[g * LANES] = gk / gm;
-                                Gw[(g + 1) * LANES] = gk * (ek - Vm) / gm;
-                                Gw[(g + 2) * LANES] = ek;
-                            }
-                            const double X = Pw[pc[1] * LANES] * exp(Vm * Pw[pc[2] * LANES]);
-                            Gk = d2df(gk * (X / (X + Pw[pc[3] * LANES])));
-                            pc += 5;
-                            continue;
-                        } else if (k == M_ADDCURR) {
-                            const int g = pc[1];
-                            sumg = df_add(sumg, Gk);
-                            ichan = df_add(ichan, df_mul(Ek, Gk));
-                            const double gk = df2d(Gk), ek = df2d(Ek);
-                            Ik = gk * (ek - Vm);
-                            if (GIV) {
-                                const double gm = c5 ? df2d(gmax) : 1.0;
-                                Gw[g * LANES] = gk / gm;
-                                Gw[(g + 1) * LANES] = Ik / gm;
-                                Gw[(g + 2) * LANES] = ek;
-                            }
-                            Im += Ik;
-                            pc += 2;
-                            break;
-                        } else {
-                            if (v.status) atomicOr(v.status, ST_BAD_OP);
-                            return;
-                        }
-                    }
-                }
+            double R, D;
+            if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
             }
+            Rcol[s * LANES] = R;
+            Dcol[s * LANES] = D;
         }
 
         // Ca pools (FP64)
