@@ -246,7 +246,7 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
         et.get_outputs_async(tr[n], stream.cuda_stream)
     stream.synchronize()
     et.close()
-    eng = engine.Engine(hs, precision=engine.PREC_FP64, device=device)
+    eng = engine.Engine(hs, precision=engine.PREC_FP64, device=device, wide_min=-1)   # the adjoint runs lane-mapped
     st0 = eng.get_state()
     ms0 = eng.stats().device_ms
     eng.run(nsteps)

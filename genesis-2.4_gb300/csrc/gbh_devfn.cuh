@@ -46,6 +46,8 @@ struct DevView {
     // concentration rows beside C: coresult and codiag of each pool row
     // (diffusion systems), and per-lane scratch rows of the diffusion solves
     double *CR, *CD, *S;
+    // wide tiles (one neuron per block): per-tile elimination schedules
+    const int *wtop;
 };
 
 // Barrier over all blocks of a cooperative launch: the last block to arrive
@@ -257,10 +259,10 @@ __device__ __forceinline__ double hill_factor(int h, double X)
 // Shells without buffers, tridiagonal in the shell index (hines_conc.c:337-395).
 // R: pool row of each shell, K: field row of each coupling term in the order
 // consumed, fac/part: scratch rows.
+template <int W>
 __device__ __forceinline__ void diff_shells_dev(const PoolLane &L, int ms, const int *R, const int *K, int fac,
                                                 int part)
 {
-    constexpr int W = 32;
 #define GBH_C(j) L.C[R[j] * W]
 #define GBH_CD(j) L.CD[R[j] * W]
 #define GBH_CR(j) L.CR[R[j] * W]
@@ -306,10 +308,10 @@ __device__ __forceinline__ void diff_shells_dev(const PoolLane &L, int ms, const
 // shell (nfix fixed buffers, diffusible buffers, the shell) eliminated as
 // they are filled; BV: field rows of the buffer rates (3 per buffer).
 // Scratch: fac[(shell*w + row)*w + column], part[shell*w + row].
+template <int W>
 __device__ __forceinline__ void diff_buffered_dev(const PoolLane &L, int ms, int w, int nfix, const int *R,
                                                   const int *K, const int *BV, int fac, int part)
 {
-    constexpr int W = 32;
 #define GBH_F(i) L.S[(fac + (i)) * W]
 #define GBH_PT(i) L.S[(part + (i)) * W]
 #define GBH_B(i) L.P[BV[i] * W]
@@ -447,11 +449,12 @@ __device__ __forceinline__ void diff_buffered_dev(const PoolLane &L, int ms, int
 #undef GBH_K
 }
 
-// The pool program of one lane (Ca_concen pools, concops groups, diffusion
-// solves). Returns false on an unknown micro-op.
+// The pool program of one neuron (Ca_concen pools, concops groups, diffusion
+// solves); W: row stride (32 lane-interleaved tiles, 1 wide tiles). Returns
+// false on an unknown micro-op.
+template <int W>
 __device__ __forceinline__ bool pool_phase(const int *pp, const PoolLane &L)
 {
-    constexpr int W = 32;
     int ix = 0;
     double res = 0.0;
     while (pp[0] != 0) {
@@ -530,8 +533,8 @@ __device__ __forceinline__ bool pool_phase(const int *pp, const PoolLane &L)
             PoolLane L2 = L;
             L2.crank = pp[4];
             const int nfac = w > 1 ? ms * w * w : ms + 1;
-            if (w > 1) diff_buffered_dev(L2, ms, w, nfix, R, K, BV, sbase, sbase + nfac);
-            else diff_shells_dev(L2, ms, R, K, sbase, sbase + nfac);
+            if (w > 1) diff_buffered_dev<W>(L2, ms, w, nfix, R, K, BV, sbase, sbase + nfac);
+            else diff_shells_dev<W>(L2, ms, R, K, sbase, sbase + nfac);
             pp += 8 + ms * w + nq + nb;
             break;
         }

@@ -74,7 +74,19 @@ struct Launch {
     int tile0, tile1, smax, warps;
     int jit = -1;        // index of a specialised kernel, or -1 to interpret
     bool uniform = false; // every neuron of the type has the same tree
+    bool wide = false;    // one neuron per block (wide tiles)
 };
+
+// Element idx of a block of rows starting at row `base`: lane-interleaved
+// tiles keep it at (base + idx) * 32 + lane, wide tiles (one neuron)
+// contiguously at base * 32 + idx.
+inline int64_t at(int64_t base, int64_t idx, int lane, bool wide)
+{
+    return wide ? base * LANES + idx : (base + idx) * LANES + lane;
+}
+
+// Rows a block of n elements takes in a tile.
+inline int64_t rows_of(int64_t n, bool wide) { return wide ? (n + LANES - 1) / LANES : n; }
 
 }  // namespace
 
@@ -102,6 +114,7 @@ struct gbh_engine {
     std::vector<std::vector<char>> type_df;     // mixed: field rows stored as packed double-float
     DBuf<double> d_P, d_V, d_C, d_F, d_A, d_B, d_Cb, d_giv, d_stab;
     DBuf<double> d_CR, d_CD, d_S;   // coresult / codiag rows, diffusion scratch
+    DBuf<int> d_wtop;               // elimination schedules of wide tiles
     DBuf<int> d_I, d_par;
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
@@ -304,6 +317,104 @@ void build_tables(const gbh_batch_desc *d, std::vector<TableGeom> &tg, std::vect
     }
 }
 
+// Can a type run wide (its compartments on separate threads)? Each
+// compartment must start from nothing but the table cursors the chain of
+// NEWVOLT / NEWCONC1 lookups leaves (resolved per step in the kernel): no
+// DOMAIN / NEWCONC2 / 2-D tables / TABGHK / SAME_GHK, a CONC_VAL before
+// anything that uses the selected conc, a current before FLUX, a lookup
+// before a gate that reads its cursor, at most one lookup of each kind per
+// compartment. On success meta = [program offset of each slot | previous
+// NEWVOLT slot (-1 none, -2 the slot has none) | same for NEWCONC1 | conc
+// row NEWCONC1 reads].
+bool wide_plan(const std::vector<int> &prog, const TileType &tt, std::vector<int> &meta)
+{
+    const int S = tt.nslots;
+    std::vector<int> sofs(S), vprev(S, -2), cprev(S, -2), cpool(S, 0);
+    size_t pc = tt.prog_off;
+    int lastv = -1, lastc = -1;
+    for (int s = 0; s < S; ++s) {
+        sofs[s] = (int)pc;
+        bool sel = false, ik = false;
+        int nv = 0, nc = 0, selrow = 0;
+        for (;;) {
+            const int code = prog[pc];
+            const int n = micro_operands(code);
+            if (n < 0) return false;
+            const int *o = &prog[pc + 1];
+            switch (code) {
+            case M_DOMAIN: case M_NEWCONC2: case M_SAME_GHK: case M_DO_TABGHK: case M_STORE:
+                return false;
+            case M_CONCVAL: sel = true; selrow = o[0]; break;
+            case M_NEWVOLT: if (++nv > 1) return false; break;
+            case M_NEWCONC1:
+                if (!sel || ++nc > 1) return false;
+                cpool[s] = selrow;
+                break;
+            case M_ELMMPUMP: if (!sel) return false; ik = true; break;
+            case M_GHK: case M_NERNST: if (!sel) return false; break;
+            case M_FLUX: case M_SCALE_FLUX: if (!sel || !ik) return false; break;
+            case M_GATE:
+                if (o[0] == GK_2V || o[0] == GK_2C) return false;
+                if ((o[0] == GK_1V && !nv) || (o[0] == GK_1C && !nc)) return false;
+                break;
+            case M_ADDCURR: ik = true; break;
+            default: break;
+            }
+            pc += 1 + n;
+            if (code == M_END) break;
+        }
+        if (nv) { vprev[s] = lastv; lastv = s; }
+        if (nc) { cprev[s] = lastc; lastc = s; }
+    }
+    meta = sofs;
+    meta.insert(meta.end(), vprev.begin(), vprev.end());
+    meta.insert(meta.end(), cprev.begin(), cprev.end());
+    meta.insert(meta.end(), cpool.begin(), cpool.end());
+    return true;
+}
+
+// Elimination schedule of one wide neuron (see k_wide): forward levels by
+// height (leaves 0), children of each row in ascending order, backward
+// levels by depth (root 0).
+void wide_schedule(const std::vector<int> &parent, std::vector<int> &out)
+{
+    const int S = (int)parent.size();
+    std::vector<int> h(S, 0), dep(S, 0);
+    for (int s = 0; s < S; ++s)   // children have lower rows than their parents
+        if (parent[s] >= 0) h[parent[s]] = std::max(h[parent[s]], h[s] + 1);
+    for (int s = S - 1; s >= 0; --s)
+        if (parent[s] >= 0) dep[s] = dep[parent[s]] + 1;
+    auto levels = [&](const std::vector<int> &lv, std::vector<int> &start, std::vector<int> &rows) {
+        const int nl = S ? *std::max_element(lv.begin(), lv.end()) + 1 : 0;
+        start.assign(nl + 1, 0);
+        for (int s = 0; s < S; ++s) start[lv[s] + 1]++;
+        for (int l = 0; l < nl; ++l) start[l + 1] += start[l];
+        rows.assign(S, 0);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int s = 0; s < S; ++s) rows[fill[lv[s]]++] = s;
+        return nl;
+    };
+    std::vector<int> fs, fr, bs, br;
+    const int nf = levels(h, fs, fr), nb = levels(dep, bs, br);
+    std::vector<int> kst(S + 1, 0), kids;
+    for (int s = 0; s < S; ++s)
+        if (parent[s] >= 0) kst[parent[s] + 1]++;
+    for (int s = 0; s < S; ++s) kst[s + 1] += kst[s];
+    kids.assign(std::max(S - 1, 0), 0);
+    std::vector<int> fill(kst.begin(), kst.end() - 1);
+    for (int s = 0; s < S; ++s)   // ascending: the order the sequential sweep applies them
+        if (parent[s] >= 0) kids[fill[parent[s]]++] = s;
+    out.clear();
+    out.push_back(nf);
+    out.insert(out.end(), fs.begin(), fs.end());
+    out.insert(out.end(), fr.begin(), fr.end());
+    out.insert(out.end(), kst.begin(), kst.end());
+    out.insert(out.end(), kids.begin(), kids.end());
+    out.push_back(nb);
+    out.insert(out.end(), bs.begin(), bs.end());
+    out.insert(out.end(), br.begin(), br.end());
+}
+
 int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn, const gbh_remote_synapses *remote,
                  gbh_error *err)
 {
@@ -342,6 +453,19 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         }
         members[it->second].push_back(i);
     }
+    // ---- wide types: one neuron per tile, its compartments on a block's threads ----
+    if (e->opt.wide_min >= 0) {
+        const int wmin = e->opt.wide_min == 0 ? 32 : e->opt.wide_min;
+        for (size_t ti = 0; ti < e->types.size(); ++ti) {
+            TileType &tt = e->types[ti];
+            std::vector<int> meta;
+            if (tt.nslots >= wmin && wide_plan(prog_pool, tt, meta)) {
+                tt.wide = 1;
+                tt.wide_off = (int)prog_pool.size();
+                prog_pool.insert(prog_pool.end(), meta.begin(), meta.end());
+            }
+        }
+    }
     // ---- event ring length from the synapse delays ----
     const bool local_syn = syn && syn->nsynapses > 0;
     const int64_t nrsyn = (remote && remote->nsources > 0) ? remote->src_start[remote->nsources] : 0;
@@ -370,23 +494,32 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     e->neuron_tile.assign(nneu, -1);
     e->neuron_lane.assign(nneu, -1);
     int64_t gneuron = 0;
+    std::vector<int> wtop;   // elimination schedules of the wide tiles
     for (int ti : torder) {
         const TileType &tt = e->types[ti];
         const std::vector<int> &m = members[ti];
-        for (size_t k = 0; k < m.size(); k += LANES) {
+        const bool w = tt.wide != 0;
+        const size_t per = w ? 1 : LANES;   // neurons per tile
+        for (size_t k = 0; k < m.size(); k += per) {
             Tile t{};
             t.type = ti;
-            t.nlanes = (int)std::min<size_t>(LANES, m.size() - k);
-            t.fld = e->rows_fld; e->rows_fld += tt.nfields;
-            t.ints = e->rows_int; e->rows_int += tt.nints;
-            t.pools = e->rows_pool; e->rows_pool += tt.npools;
-            t.giv = e->rows_giv; e->rows_giv += tt.ngiv;
-            t.vm = e->rows_vm; e->rows_vm += tt.nslots;
-            t.topo = e->rows_topo; e->rows_topo += tt.nslots;
+            t.nlanes = (int)std::min<size_t>(per, m.size() - k);
+            t.fld = e->rows_fld; e->rows_fld += rows_of(tt.nfields, w);
+            t.ints = e->rows_int; e->rows_int += rows_of(tt.nints, w);
+            t.pools = e->rows_pool; e->rows_pool += rows_of(tt.npools, w);
+            t.giv = e->rows_giv; e->rows_giv += rows_of(tt.ngiv, w);
+            t.vm = e->rows_vm; e->rows_vm += rows_of(tt.nslots, w);
+            t.topo = e->rows_topo; e->rows_topo += rows_of(tt.nslots, w);
             t.syn = e->rows_syn; e->rows_syn += (int64_t)tt.nsyn * e->ring_len;
-            t.scr = e->rows_scr; e->rows_scr += tt.nscratch;
+            t.scr = e->rows_scr; e->rows_scr += rows_of(tt.nscratch, w);
             t.first_neuron = gneuron;
             gneuron += LANES;
+            if (w) {
+                std::vector<int> sched;
+                wide_schedule(dec.neurons[m[k]].parent, sched);
+                t.wtop = (int64_t)wtop.size();
+                wtop.insert(wtop.end(), sched.begin(), sched.end());
+            }
             for (int l = 0; l < t.nlanes; ++l) {
                 e->neuron_tile[m[k + l]] = (int)e->tiles.size();
                 e->neuron_lane[m[k + l]] = l;
@@ -402,6 +535,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     // padding lanes: a passive row that solves to zero and never spikes
     for (const Tile &t : e->tiles) {
         const TileType &tt = e->types[t.type];
+        if (tt.wide) continue;
         for (int l = t.nlanes; l < LANES; ++l) {
             for (int f = 0; f < tt.nfields; ++f) P[(t.fld + f) * L + l] = 1.0;
             for (int s = 0; s < tt.nslots; ++s) V[(t.vm + s) * L + l] = 0.0;
@@ -413,18 +547,19 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         const Neuron &N = dec.neurons[i];
         const Tile &t = e->tiles[e->neuron_tile[i]];
         const int l = e->neuron_lane[i];
+        const bool w = e->types[t.type].wide != 0;
         const int64_t vbase = d->vm_start[N.solver] + N.row0;
         for (int s = 0; s < N.nrows; ++s) {
-            V[(t.vm + s) * L + l] = d->vm[vbase + s];
-            par[(t.topo + s) * L + l] = N.parent[s];
-            A[(t.topo + s) * L + l] = N.A[s];
-            B[(t.topo + s) * L + l] = N.B[s];
-            Cb[(t.topo + s) * L + l] = N.C[s];
+            V[at(t.vm, s, l, w)] = d->vm[vbase + s];
+            par[at(t.topo, s, l, w)] = N.parent[s];
+            A[at(t.topo, s, l, w)] = N.A[s];
+            B[at(t.topo, s, l, w)] = N.B[s];
+            Cb[at(t.topo, s, l, w)] = N.C[s];
         }
-        for (size_t f = 0; f < N.fsrc.size(); ++f) P[(t.fld + f) * L + l] = N.fval[f];
-        for (size_t r = 0; r < N.iops.size(); ++r) I[(t.ints + r) * L + l] = N.ival[r];
+        for (size_t f = 0; f < N.fsrc.size(); ++f) P[at(t.fld, f, l, w)] = N.fval[f];
+        for (size_t r = 0; r < N.iops.size(); ++r) I[at(t.ints, r, l, w)] = N.ival[r];
         for (size_t p = 0; p < N.pool_conc.size(); ++p)
-            C[(t.pools + p) * L + l] = d->conc[d->conc_start[N.solver] + N.pool_conc[p]];
+            C[at(t.pools, p, l, w)] = d->conc[d->conc_start[N.solver] + N.pool_conc[p]];
     }
     // ---- mixed precision: double-float packing of the fields read as df ----
     const bool mixed = e->opt.precision == GBH_PREC_MIXED;
@@ -433,9 +568,10 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         for (size_t ti = 0; ti < e->types.size(); ++ti) e->type_df[ti] = df_fields_of(e->types[ti], prog_pool);
         for (const Tile &t : e->tiles) {
             const std::vector<char> &m = e->type_df[t.type];
+            const bool w = e->types[t.type].wide != 0;
             for (int f = 0; f < (int)m.size(); ++f)
                 if (m[f])
-                    for (int l = 0; l < LANES; ++l) P[(t.fld + f) * L + l] = pack_df(P[(t.fld + f) * L + l]);
+                    for (int l = 0; l < (w ? 1 : LANES); ++l) P[at(t.fld, f, l, w)] = pack_df(P[at(t.fld, f, l, w)]);
         }
     }
     // ---- synapses: CSR over global neuron index ----
@@ -533,7 +669,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             const Tile &t = e->tiles[e->neuron_tile[tn]];
             for (size_t f = 0; f < N.fsrc.size(); ++f)
                 if (N.fsrc[f].kind == FS_WDT && N.fsrc[f].idx == srow)
-                    P[(t.fld + f) * L + e->neuron_lane[tn]] = kv.second;
+                    P[at(t.fld, (int64_t)f, e->neuron_lane[tn], e->types[t.type].wide != 0)] = kv.second;
         }
     }
     // ---- tables ----
@@ -574,6 +710,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_V.upload(V);
     rc |= e->d_C.upload(C);
     rc |= e->d_F.upload(std::vector<double>(C.size(), 0.0));
+    rc |= e->d_wtop.upload(wtop.empty() ? std::vector<int>(1, 0) : wtop);
     bool any_cd = false;
     for (const TileType &tt : e->types) any_cd = any_cd || tt.has_cd;
     if (any_cd) {   // coresult 0, codiag 1 (hines_conc_init.c:121-126), solve scratch
@@ -612,8 +749,10 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     if (jit_on) {
         // types in tile order, largest first
         std::vector<int> cand;
+        // the looped forms keep 2 x nslots x 32 rows per warp in shared memory:
+        // 4-warp blocks of more than 96 compartments would not fit
         for (int ti : torder)
-            if (type_t0[ti] >= 0) cand.push_back(ti);
+            if (type_t0[ti] >= 0 && !e->types[ti].wide && e->types[ti].nslots <= 96) cand.push_back(ti);
         std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
             return (type_t1[a] - type_t0[a]) > (type_t1[b] - type_t0[b]);
         });
@@ -710,7 +849,20 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         }
         const int smax = e->types[ty0].nslots;
         size_t t1 = t0;
-        while (t1 < e->tiles.size() && type_jit[e->tiles[t1].type] < 0 &&
+        if (e->types[ty0].wide) {   // one block per neuron
+            while (t1 < e->tiles.size() && e->types[e->tiles[t1].type].wide &&
+                   e->types[e->tiles[t1].type].nslots * 2 > smax)
+                ++t1;
+            if (smax * (2 * sizeof(double) + 4 * sizeof(int)) > 200 * 1024)
+                return fail_err(err, GBH_ERR_UNSUPPORTED, "neuron with %d compartments exceeds the shared memory",
+                                smax);
+            Launch L{(int)t0, (int)t1, smax, 1};
+            L.wide = true;
+            e->launches.push_back(L);
+            t0 = t1;
+            continue;
+        }
+        while (t1 < e->tiles.size() && type_jit[e->tiles[t1].type] < 0 && !e->types[e->tiles[t1].type].wide &&
                e->types[e->tiles[t1].type].nslots * 2 > smax)
             ++t1;
         const int per_warp = 2 * smax * LANES * (int)sizeof(double);
@@ -741,6 +893,7 @@ DevView view_of(gbh_engine *e)
     v.V = e->d_V.p;
     v.C = e->d_C.p;
     v.F = e->d_F.p;
+    v.wtop = e->d_wtop.p;
     v.CR = e->d_CR.p;
     v.CD = e->d_CD.p;
     v.S = e->d_S.p;
@@ -778,8 +931,13 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
         e->stats.launches++;
         return GBH_OK;
     }
-    cudaError_t ce = mixed ? launch_mixed(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st)
-                           : launch_fp64(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st);
+    cudaError_t ce;
+    if (L.wide)
+        ce = mixed ? launch_mixed_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st)
+                   : launch_fp64_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st);
+    else
+        ce = mixed ? launch_mixed(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st)
+                   : launch_fp64(v, L.tile0, L.tile1, L.smax, L.warps, k, step, giv, st);
     if (ce != cudaSuccess) {
         set_last("kernel launch failed: %s", cudaGetErrorString(ce));
         return GBH_ERR_CUDA;
@@ -1003,14 +1161,16 @@ int autotune_trials(gbh_engine *e)
         for (int spl : spls) {
             e->steps_per_launch = spl;
             const int steps = std::max(2 * spl, 128);
-            run_steps(e, 8, e->stream);          // warm caches and clocks
+            int rc_t = run_steps(e, 8, e->stream);   // warm caches and clocks
             CK(cudaEventRecord(e->ev0, e->stream));
-            run_steps(e, steps, e->stream);
+            if (rc_t == GBH_OK) rc_t = run_steps(e, steps, e->stream);
             CK(cudaEventRecord(e->ev1, e->stream));
             CK(cudaEventSynchronize(e->ev1));
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
-            const double per = ms / steps;
+            // a variant that cannot launch here (resources) never wins
+            const double per = rc_t == GBH_OK ? ms / steps : 1e300;
+            if (rc_t != GBH_OK) cudaGetLastError();
             if (getenv("GBH_VERBOSE") && !e->jit_minb.empty())
                 fprintf(stderr, "gbhsolve: trial %d warps x min blocks %d, form %d, %d steps/launch: %.2f us/step\n",
                         e->jit_warps[vi], e->jit_minb[vi], e->jit_compact[vi] ? 1 : e->jit_smemrows[vi] ? 2 : 0, spl,
@@ -1020,7 +1180,9 @@ int autotune_trials(gbh_engine *e)
         }
     }
     // networks: the cooperative multi-step launch against the best per-step plan
-    if (e->has_network && e->nremote == 0 && e->d_gbar.p) {
+    bool any_wide = false;
+    for (const TileType &tt : e->types) any_wide = any_wide || tt.wide;
+    if (e->has_network && e->nremote == 0 && e->d_gbar.p && !any_wide) {
         for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
         e->jit_choice = best_v;
         e->steps_per_launch = best_s;
@@ -1214,14 +1376,15 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
             const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
             for (int i : it->second) {
                 const bool add = kind && kind[i] == GBH_IN_ADD;
-                addrs[i].push_back(((t.fld + (int64_t)f) * LANES + l) | (packed ? kPackedFlag : 0) |
-                                   (add ? kAddFlag : 0));
+                addrs[i].push_back(at(t.fld, (int64_t)f, l, e->types[t.type].wide != 0) |
+                                   (packed ? kPackedFlag : 0) | (add ? kAddFlag : 0));
             }
         }
         for (size_t p = 0; p < N.pool_conc.size(); ++p) {
             auto it = want_conc.find(e->conc_start[N.solver] + N.pool_conc[p]);
             if (it == want_conc.end()) continue;
-            for (int i : it->second) addrs[i].push_back(((t.pools + (int64_t)p) * LANES + l) | kFluxFlag);
+            for (int i : it->second)
+                addrs[i].push_back(at(t.pools, (int64_t)p, l, e->types[t.type].wide != 0) | kFluxFlag);
         }
     }
     std::map<int64_t, std::vector<int>> by_target;   // keyed by address without the add flag
@@ -1297,7 +1460,7 @@ int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row
         if (found < 0) return GBH_ERR_ARG;
         const Neuron &N = e->dec.neurons[found];
         const Tile &t = e->tiles[e->neuron_tile[found]];
-        addr[i] = (t.vm + (row[i] - N.row0)) * LANES + e->neuron_lane[found];
+        addr[i] = at(t.vm, row[i] - N.row0, e->neuron_lane[found], e->types[t.type].wide != 0);
     }
     e->d_out_vals.release(); e->d_out_addr.release();
     if (e->d_out_vals.alloc(n) || e->d_out_addr.upload(addr)) return GBH_ERR_CUDA;
@@ -1627,7 +1790,9 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
         return nullptr;
     }
     e->steps_per_launch = e->opt.steps_per_launch > 0 ? e->opt.steps_per_launch : 64;
-    if (e->opt.steps_per_launch < 0 && e->has_network && e->nremote == 0) {   // forced cooperative plan
+    bool wide_tiles = false;
+    for (const TileType &tt : e->types) wide_tiles = wide_tiles || tt.wide;
+    if (e->opt.steps_per_launch < 0 && e->has_network && e->nremote == 0 && !wide_tiles) {   // forced cooperative plan
         e->net_coop = true;
         e->net_spl = -e->opt.steps_per_launch;
     }
@@ -1714,14 +1879,15 @@ int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *op
         const Neuron &N = e->dec.neurons[i];
         const Tile &t = e->tiles[e->neuron_tile[i]];
         const int l = e->neuron_lane[i];
+        const bool w = e->types[t.type].wide != 0;
         if (vm)
-            for (int s = 0; s < N.nrows; ++s) vm[e->vm_start[N.solver] + N.row0 + s] = V[(t.vm + s) * L + l];
+            for (int s = 0; s < N.nrows; ++s) vm[e->vm_start[N.solver] + N.row0 + s] = V[at(t.vm, s, l, w)];
         const std::vector<char> &dfm = e->type_df[t.type];
         if (chip)
             for (size_t f = 0; f < N.fsrc.size(); ++f) {
                 if (N.fsrc[f].kind != FS_CHIP) continue;
                 const bool packed = !dfm.empty() && dfm[f];
-                const double raw = P[(t.fld + f) * L + l];
+                const double raw = P[at(t.fld, f, l, w)];
                 // constants are reported as given; state and input-written
                 // entries (the device copy changed) from the device
                 if (!N.fsrc[f].state && raw == (packed ? pack_df(N.fval[f]) : N.fval[f])) continue;
@@ -1729,10 +1895,10 @@ int gbh_get_state(gbh_engine *e, double *vm, double *chip, double *conc, int *op
             }
         if (conc)
             for (size_t p = 0; p < N.pool_conc.size(); ++p)
-                conc[e->conc_start[N.solver] + N.pool_conc[p]] = C[(t.pools + p) * L + l];
+                conc[e->conc_start[N.solver] + N.pool_conc[p]] = C[at(t.pools, p, l, w)];
         if (ops)
             for (size_t r = 0; r < N.iops.size(); ++r)
-                ops[e->ops_start[N.solver] + N.iops[r]] = I[(t.ints + r) * L + l];
+                ops[e->ops_start[N.solver] + N.iops[r]] = I[at(t.ints, r, l, w)];
     }
     return GBH_OK;
 }
@@ -1750,18 +1916,19 @@ int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const dou
         const Neuron &N = e->dec.neurons[i];
         const Tile &t = e->tiles[e->neuron_tile[i]];
         const int l = e->neuron_lane[i];
+        const bool w = e->types[t.type].wide != 0;
         if (vm)
-            for (int s = 0; s < N.nrows; ++s) V[(t.vm + s) * L + l] = vm[e->vm_start[N.solver] + N.row0 + s];
+            for (int s = 0; s < N.nrows; ++s) V[at(t.vm, s, l, w)] = vm[e->vm_start[N.solver] + N.row0 + s];
         const std::vector<char> &dfm = e->type_df[t.type];
         if (chip)
             for (size_t f = 0; f < N.fsrc.size(); ++f)
                 if (N.fsrc[f].kind == FS_CHIP) {
                     const double val = chip[e->chip_start[N.solver] + N.fsrc[f].idx];
-                    P[(t.fld + f) * L + l] = (!dfm.empty() && dfm[f]) ? pack_df(val) : val;
+                    P[at(t.fld, f, l, w)] = (!dfm.empty() && dfm[f]) ? pack_df(val) : val;
                 }
         if (conc)
             for (size_t p = 0; p < N.pool_conc.size(); ++p)
-                C[(t.pools + p) * L + l] = conc[e->conc_start[N.solver] + N.pool_conc[p]];
+                C[at(t.pools, p, l, w)] = conc[e->conc_start[N.solver] + N.pool_conc[p]];
     }
     if (chip) e->chip_orig.assign(chip, chip + e->chip_orig.size());
     if (!V.empty()) CK(cudaMemcpy(e->d_V.p, V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -1793,8 +1960,9 @@ int gbh_get_givals(gbh_engine *e, double *givals)
         const Neuron &N = e->dec.neurons[i];
         const Tile &t = e->tiles[e->neuron_tile[i]];
         const int l = e->neuron_lane[i];
+        const bool w = e->types[t.type].wide != 0;
         for (size_t r = 0; r < N.giv_ref.size(); ++r)
-            givals[e->giv_start[N.solver] + N.giv_ref[r]] = Gv[(t.giv + r) * L + l];
+            givals[e->giv_start[N.solver] + N.giv_ref[r]] = Gv[at(t.giv, r, l, w)];
     }
     return GBH_OK;
 }
@@ -1879,6 +2047,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         if (tt.npools || tt.nsyn || tt.has_spike)
             return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
                             "gbh_loss_gradient: Ca pools, synchans and spike detectors are not differentiated");
+        if (tt.wide)
+            return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
+                            "gbh_loss_gradient: create the engine with wide_min < 0 (one neuron per lane)");
         AdjType &at = atypes[ti];
         at.nslots = tt.nslots;
         at.snap_off = (int)snap_field.size();
@@ -2226,7 +2397,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_A.release(); e->d_B.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_A.release(); e->d_B.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

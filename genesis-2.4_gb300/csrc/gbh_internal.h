@@ -98,6 +98,9 @@ struct TileType {
     int nsyn;        // synchan rows
     int has_cd;      // keeps codiag rows (diffusion systems): ELMMPUMP adds to them
     int nscratch;    // per-lane scratch rows of the diffusion solves
+    int wide;        // one neuron per tile, its compartments across a block's threads
+    int wide_off;    // wide: prog-pool offset of [slot program offsets | previous NEWVOLT slot |
+                     //        previous NEWCONC1 slot | NEWCONC1 conc row], nslots each
 };
 
 struct Tile {
@@ -111,6 +114,7 @@ struct Tile {
     int64_t vm;      // nslots rows
     int64_t syn;     // event-ring rows (nsyn * ring_len)
     int64_t scr;     // diffusion scratch rows (nscratch)
+    int64_t wtop;    // wide: offset into DevView::wtop of its elimination schedule
     int64_t first_neuron; // global neuron index of lane 0
 };
 

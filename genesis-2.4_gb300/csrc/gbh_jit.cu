@@ -780,10 +780,13 @@ cudaError_t jit_launch(const JitKernel &k, const DevView &v, int tile0, int tile
     }
     DevView vv = v;
     void *args[] = {&vv, &tile0, &tile1, &smax, &nsteps, &step};
-    if (g_api.launch((CUfunction)k.fn, blocks, 1, 1, warps * LANES, 1, 1, (unsigned)smem, (CUstream)st, args,
-                     nullptr) != CUDA_SUCCESS)
-        return cudaErrorLaunchFailure;
-    return cudaSuccess;
+    const CUresult r = g_api.launch((CUfunction)k.fn, blocks, 1, 1, warps * LANES, 1, 1, (unsigned)smem,
+                                    (CUstream)st, args, nullptr);
+    if (r == CUDA_SUCCESS) return cudaSuccess;
+    // a fault of earlier work stays a launch failure; a launch this device
+    // refuses (resources, shared memory) is a configuration error
+    return r == CUDA_ERROR_LAUNCH_FAILED || r == CUDA_ERROR_ILLEGAL_ADDRESS ? cudaErrorLaunchFailure
+                                                                          : cudaErrorInvalidConfiguration;
 }
 
 void jit_release(JitKernel &k)

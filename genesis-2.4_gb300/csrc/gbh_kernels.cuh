@@ -18,6 +18,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
 #include "gbh_internal.h"
 #include "gbh_devfn.cuh"
 
@@ -438,7 +439,7 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
             PL.V = Vw;
             PL.dt = v.dt;
             PL.crank = ty.crank;
-            if (!pool_phase(v.prog + ty.pool_off, PL)) {
+            if (!pool_phase<LANES>(v.prog + ty.pool_off, PL)) {
                 if (v.status) atomicOr(v.status, ST_BAD_OP);
                 return;
             }
@@ -471,6 +472,224 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
         // are in the rings before any tile starts the next step
         if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
     }
+}
+
+// ------------------------------------------------------------ wide tiles
+// A wide tile holds one neuron; its compartments run on the threads of one
+// block (slot s on thread s mod blockDim), its rows are contiguous (stride
+// 1). Per step: the table cursors each compartment starts from are resolved
+// first (the reference carries the bracket of the last NEWVOLT / NEWCONC1
+// from one compartment to the next, hines_chip.c:174-203), then every
+// compartment's program runs, the pool program runs on thread 0, and the
+// elimination runs level by level: forward, a row pulls its children in
+// ascending row order once they are final (the order the sequential sweep
+// applies them in); backward, top-down from the root.
+//
+// Elimination schedule at DevView::wtop + Tile::wtop:
+//   nf, fwd_start[nf+1], fwd_rows[S], kid_start[S+1], kids[S-1],
+//   nb, bwd_start[nb+1], bwd_rows[S]
+
+// Row of the table bracket a fresh lookup of v lands in (clamped).
+__device__ __forceinline__ int fresh_row(double v, double vmin, double inv, int divs)
+{
+    double f = (v - vmin) * inv;
+    if (f < 0.0) f = 0.0;
+    else if (f > divs) f = divs;
+    return (int)f;
+}
+
+__device__ __forceinline__ bool bracket_hit(const double *vals, int row, double v)
+{
+    return !((vals[row] > v) || (v >= vals[row + 1]));
+}
+
+__device__ __forceinline__ void cursor_at(VCursor &c, int row, const double *vals, int ncols)
+{
+    c.row = row;
+    c.lo = vals[row];
+    c.hi = vals[row + 1];
+    c.base = row * ncols;
+}
+
+// Incoming bracket rows of one cursor chain: slots with prev[s] != -2 look
+// the value val(s) up; prev[s] is the previous such slot (-1: none). Fresh
+// lookups are exact unless a value sits in the previous bracket while its
+// own fresh row differs (a rounding edge): then thread 0 replays the chain.
+template <typename VAL>
+__device__ __forceinline__ void cursor_chain(int S, const int *prev, VAL val, const double *vals, double vmin,
+                                             double inv, int divs, int *fresh, int *in)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int s = tid; s < S; s += nt) fresh[s] = prev[s] != -2 ? fresh_row(val(s), vmin, inv, divs) : -1;
+    __syncthreads();
+    int edge = 0;
+    for (int s = tid; s < S; s += nt) {
+        if (prev[s] == -2) continue;
+        const int r = prev[s] >= 0 ? fresh[prev[s]] : -1;
+        if (r >= 0 && bracket_hit(vals, r, val(s)) && r != fresh[s]) edge = 1;
+    }
+    if (__syncthreads_or(edge)) {
+        if (tid == 0) {
+            int state = -1;
+            for (int s = 0; s < S; ++s) {
+                if (prev[s] == -2) continue;
+                in[s] = state;
+                const double x = val(s);
+                if (state < 0 || !bracket_hit(vals, state, x)) state = fresh_row(x, vmin, inv, divs);
+            }
+        }
+    } else {
+        for (int s = tid; s < S; s += nt)
+            if (prev[s] != -2) in[s] = prev[s] >= 0 ? fresh[prev[s]] : -1;
+    }
+    __syncthreads();
+}
+
+// Shared memory: 2*smax doubles (diagonal, right-hand side) + 4*smax ints.
+template <typename G, bool GIV>
+__global__ void __launch_bounds__(256)
+k_wide(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
+{
+    extern __shared__ double sm[];
+    const int t = tile0 + blockIdx.x;
+    if (t >= tile1) return;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const int S = ty.nslots;
+    double *Ds = sm, *Rs = sm + smax;
+    int *vfresh = reinterpret_cast<int *>(sm + 2 * smax), *vin = vfresh + smax, *cfresh = vin + smax,
+        *cin = cfresh + smax;
+    const int *meta = v.prog + ty.wide_off;
+    const int *sofs = meta, *vprev = meta + S, *cprev = meta + 2 * S, *cpool = meta + 3 * S;
+    const int *wt = v.wtop + tl.wtop;
+    const int nf = wt[0];
+    const int *fst = wt + 1, *frows = fst + nf + 1, *kst = frows + S, *kids = kst + S + 1;
+    const int nb = kids[S - 1];
+    const int *bst = kids + S, *brows = bst + nb + 1;
+
+    double *P = v.P + tl.fld * LANES;
+    double *V = v.V + tl.vm * LANES;
+    double *C = v.C + tl.pools * LANES;
+    const int *par = v.parent + tl.topo * LANES;
+    const double *A = v.A + tl.topo * LANES, *B = v.B + tl.topo * LANES, *Cb = v.Cb + tl.topo * LANES;
+
+    ChanEnv<G> E;
+    E.tab = tab_ptr<G>(v, tg.tab_off);
+    E.xvals = v.xyvals + tg.xv_off;
+    E.yvals = tg.yv_off >= 0 ? v.xyvals + tg.yv_off : E.xvals;
+    E.tg = tg;
+    E.ncols = tg.ncols;
+    E.interp = ty.interp != 0;
+    E.c5 = ty.chanmode5 != 0;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = P;
+    NR.I = v.I + tl.ints * LANES;
+    NR.C = C;
+    NR.F = v.F + tl.pools * LANES;
+    NR.G = v.giv + tl.giv * LANES;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES : nullptr;
+    NR.ring = v.ring + tl.syn * LANES;
+    NR.neuron = tl.first_neuron;
+    NR.active = true;
+
+    for (int it = 0; it < nsteps; ++it) {
+        const long long step = sbase + step0 + it;
+        if (tg.ncols) {
+            cursor_chain(S, vprev, [&](int s) { return V[s]; }, E.xvals, tg.xmin, tg.invdx, tg.xdivs, vfresh, vin);
+            cursor_chain(S, cprev, [&](int s) { return C[cpool[s]]; }, E.yvals, tg.ymin, tg.invdy, tg.ydivs, cfresh,
+                         cin);
+        }
+        // channel phase
+        for (int s = tid; s < S; s += nt) {
+            ChanState cs;
+            chan_state_reset(cs, tg.ncols);
+            if (tg.ncols && vprev[s] != -2 && vin[s] >= 0) cursor_at(cs.vc, vin[s], E.xvals, tg.ncols);
+            if (tg.ncols && cprev[s] != -2 && cin[s] >= 0) {
+                cursor_at(cs.cc, cin[s], E.yvals, tg.ncols);
+                cs.ctab_base = cs.cc.base;
+            }
+            const int *pc = v.prog + sofs[s];
+            double R = 0.0, D = 1.0;
+            if (!chan_compartment<G, GIV, 1>(v, E, cs, NR, pc, V[s], step, R, D) && v.status)
+                atomicOr(v.status, ST_BAD_OP);
+            Rs[s] = R;
+            Ds[s] = D;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            PoolLane PL;
+            PL.C = C;
+            PL.F = NR.F;
+            PL.CR = v.CR ? v.CR + tl.pools * LANES : nullptr;
+            PL.CD = NR.CD;
+            PL.S = v.S ? v.S + tl.scr * LANES : nullptr;
+            PL.P = P;
+            PL.V = V;
+            PL.dt = v.dt;
+            PL.crank = ty.crank;
+            if (!pool_phase<1>(v.prog + ty.pool_off, PL) && v.status) atomicOr(v.status, ST_BAD_OP);
+        }
+        __syncthreads();
+        // forward elimination, leaves first
+        for (int l = 0; l < nf; ++l) {
+            for (int i = fst[l] + tid; i < fst[l + 1]; i += nt) {
+                const int s = frows[i];
+                double d = Ds[s], r = Rs[s];
+                for (int k = kst[s]; k < kst[s + 1]; ++k) {
+                    const int c = kids[k];
+                    const double temp = A[c] / Ds[c];
+                    d -= B[c] * temp;
+                    r -= Rs[c] * temp;
+                }
+                Ds[s] = d;
+                Rs[s] = r;
+            }
+            __syncthreads();
+        }
+        // back substitution, root first
+        for (int l = 0; l < nb; ++l) {
+            for (int i = bst[l] + tid; i < bst[l + 1]; i += nt) {
+                const int s = brows[i];
+                const int p = par[s];
+                double r = Rs[s];
+                if (p >= 0) r -= Cb[s] * Rs[p];
+                r = r / Ds[s];
+                Rs[s] = r;
+                if (ty.crank) {
+                    const double old = V[s];
+                    V[s] = r + r - old;
+                } else {
+                    V[s] = r;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+cudaError_t launch_fp64_wide(const DevView &v, int tile0, int tile1, int smax, int nsteps, long long step, bool giv,
+                             cudaStream_t st);
+cudaError_t launch_mixed_wide(const DevView &v, int tile0, int tile1, int smax, int nsteps, long long step, bool giv,
+                              cudaStream_t st);
+
+inline size_t wide_smem(int smax) { return (size_t)smax * (2 * sizeof(double) + 4 * sizeof(int)); }
+inline int wide_threads(int smax) { return std::min(256, ((smax + 31) / 32) * 32); }
+
+template <typename KF>
+cudaError_t wide_launch(KF fn, const DevView &v, int tile0, int tile1, int smax, int nsteps, long long step,
+                        cudaStream_t st)
+{
+    const size_t smem = wide_smem(smax);
+    if (smem > 48 * 1024) {
+        const cudaError_t ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ce != cudaSuccess) return ce;
+    }
+    fn<<<tile1 - tile0, wide_threads(smax), smem, st>>>(v, tile0, tile1, smax, nsteps, step);
+    return cudaGetLastError();
 }
 
 // Launchers, one per precision translation unit (the FP64 unit is compiled

@@ -388,7 +388,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
             PL.V = Vw;
             PL.dt = v.dt;
             PL.crank = ty.crank;
-            if (!pool_phase(v.prog + ty.pool_off, PL)) {
+            if (!pool_phase<LANES>(v.prog + ty.pool_off, PL)) {
                 if (v.status) atomicOr(v.status, ST_BAD_OP);
                 return;
             }
@@ -421,6 +421,118 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
         // cooperative multi-step launch: every tile's events of this step
         // are in the rings before any tile starts the next step
         if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
+    }
+}
+
+// Wide tiles of the mixed form (see k_wide): the double-float lookups keep
+// no bracket cache, so every compartment starts from a fresh cursor.
+template <bool GIV>
+__global__ void __launch_bounds__(256)
+k_wide_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
+{
+    extern __shared__ double sm[];
+    const int t = tile0 + blockIdx.x;
+    if (t >= tile1) return;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const int S = ty.nslots;
+    double *Ds = sm, *Rs = sm + smax;
+    const int *sofs = v.prog + ty.wide_off;
+    const int *wt = v.wtop + tl.wtop;
+    const int nf = wt[0];
+    const int *fst = wt + 1, *frows = fst + nf + 1, *kst = frows + S, *kids = kst + S + 1;
+    const int nb = kids[S - 1];
+    const int *bst = kids + S, *brows = bst + nb + 1;
+
+    double *P = v.P + tl.fld * LANES;
+    double *V = v.V + tl.vm * LANES;
+    double *C = v.C + tl.pools * LANES;
+    const int *par = v.parent + tl.topo * LANES;
+    const double *A = v.A + tl.topo * LANES, *B = v.B + tl.topo * LANES, *Cb = v.Cb + tl.topo * LANES;
+
+    ChanEnvDF E;
+    E.tab = v.tabdf + tg.tab_off;
+    E.tg = tg;
+    E.ncols = tg.ncols;
+    E.xnmin = df_make(-tg.xmin_hi, -tg.xmin_lo);
+    E.xinv = df_make(tg.invdx_hi, tg.invdx_lo);
+    E.ynmin = df_make(-tg.ymin_hi, -tg.ymin_lo);
+    E.yinv = df_make(tg.invdy_hi, tg.invdy_lo);
+    E.c5 = ty.chanmode5 != 0;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = P;
+    NR.I = v.I + tl.ints * LANES;
+    NR.C = C;
+    NR.F = v.F + tl.pools * LANES;
+    NR.G = v.giv + tl.giv * LANES;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES : nullptr;
+    NR.ring = v.ring + tl.syn * LANES;
+    NR.neuron = tl.first_neuron;
+    NR.active = true;
+
+    for (int it = 0; it < nsteps; ++it) {
+        const long long step = sbase + step0 + it;
+        for (int s = tid; s < S; s += nt) {
+            ChanStateDF cs;
+            chan_state_reset_df(cs);
+            const int *pc = v.prog + sofs[s];
+            double R = 0.0, D = 1.0;
+            if (!chan_compartment_df<GIV, 1>(v, E, cs, NR, pc, V[s], step, R, D) && v.status)
+                atomicOr(v.status, ST_BAD_OP);
+            Rs[s] = R;
+            Ds[s] = D;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            PoolLane PL;
+            PL.C = C;
+            PL.F = NR.F;
+            PL.CR = v.CR ? v.CR + tl.pools * LANES : nullptr;
+            PL.CD = NR.CD;
+            PL.S = v.S ? v.S + tl.scr * LANES : nullptr;
+            PL.P = P;
+            PL.V = V;
+            PL.dt = v.dt;
+            PL.crank = ty.crank;
+            if (!pool_phase<1>(v.prog + ty.pool_off, PL) && v.status) atomicOr(v.status, ST_BAD_OP);
+        }
+        __syncthreads();
+        for (int l = 0; l < nf; ++l) {
+            for (int i = fst[l] + tid; i < fst[l + 1]; i += nt) {
+                const int s = frows[i];
+                double d = Ds[s], r = Rs[s];
+                for (int k = kst[s]; k < kst[s + 1]; ++k) {
+                    const int c = kids[k];
+                    const double temp = A[c] * Ds[c];   // Ds[c] holds the child's reciprocal
+                    d = fma(-B[c], temp, d);
+                    r = fma(-Rs[c], temp, r);
+                }
+                Ds[s] = rcp_newton(d);
+                Rs[s] = r;
+            }
+            __syncthreads();
+        }
+        for (int l = 0; l < nb; ++l) {
+            for (int i = bst[l] + tid; i < bst[l + 1]; i += nt) {
+                const int s = brows[i];
+                const int p = par[s];
+                double r = Rs[s];
+                if (p >= 0) r = fma(-Cb[s], Rs[p], r);
+                r = r * Ds[s];
+                Rs[s] = r;
+                if (ty.crank) {
+                    const double old = V[s];
+                    V[s] = fma(2.0, r, -old);
+                } else {
+                    V[s] = r;
+                }
+            }
+            __syncthreads();
+        }
     }
 }
 

@@ -70,7 +70,7 @@ class GbhRemoteSynapses(C.Structure):
 class GbhOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("steps_per_launch", C.c_int),
                 ("warps_per_block", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
-                ("jit", C.c_int)]
+                ("jit", C.c_int), ("wide_min", C.c_int)]
 
 
 class GbhLossSpec(C.Structure):
@@ -310,12 +310,15 @@ class Engine:
 
     def __init__(self, solvers: Sequence, synapses: Optional[dict] = None, precision: int = PREC_FP64,
                  steps_per_launch: int = 0, warps_per_block: int = 0, device: int = 0, jit: bool = True,
-                 use_graph: bool = False, remote: Optional[dict] = None):
+                 use_graph: bool = False, remote: Optional[dict] = None, wide_min: int = 0):
         self.lib = load()
         self.batch = Batch(solvers, synapses)
         # jit: True (autotuned forms), False (interpreter), or the ABI value
         jit_v = (0 if jit else -1) if isinstance(jit, bool) else int(jit)
-        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device, jit_v)
+        # wide_min: neurons of at least this many compartments run one per
+        # block (0: 32, negative: never)
+        opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device, jit_v,
+                         int(wide_min))
         err = GbhError()
         syn_p = C.byref(self.batch.syn) if self.batch.syn is not None else None
         if remote is None:

@@ -157,6 +157,10 @@ typedef struct gbh_options {
                             only; 2 = compact form only; 3 = unrolled form with
                             shared-memory rows only; -1 = interpret the
                             programs                                          */
+    int wide_min;        /* neurons with at least this many compartments run
+                            one per thread block, compartments across its
+                            threads (0 = 32; < 0 = never; gbh_loss_gradient
+                            needs < 0)                                       */
 } gbh_options;
 
 typedef struct gbh_stats {

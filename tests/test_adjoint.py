@@ -109,7 +109,7 @@ def _engine_vs_reference(oracle, gpu_engine, hs, rows_per_solver, nsteps, checkp
     import adjoint_ref
     rng = np.random.default_rng(11)
     traces = [-0.065 + 0.02 * rng.normal(size=(nsteps, len(r))) for r in rows_per_solver]
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     solver = np.concatenate([np.full(len(r), i) for i, r in enumerate(rows_per_solver)])
     row = np.concatenate(rows_per_solver)
     trace = np.concatenate(traces, axis=1)
@@ -181,7 +181,7 @@ def test_checkpoint_interval_invariance_and_state(oracle, gpu_engine):
     nsteps = 600
     rows = [[h.ncompts - 1] for h in hs]
     traces = _oracle_trace(oracle, _trees(40, 16, seed=26)[2], nsteps, rows)
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     solver = np.arange(len(hs))
     row = np.array([r[0] for r in rows])
     trace = np.concatenate(traces, axis=1)
@@ -207,7 +207,7 @@ def test_checkpoint_interval_invariance_and_state(oracle, gpu_engine):
 @pytest.mark.gpu
 def test_unsupported_programs_rejected(gpu_engine):
     hs = [model.build(m) for m in configs.random_trees(2, size_range=(8, 12), seed=5)]   # Ca pools
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     with pytest.raises(RuntimeError, match="error -6"):
         eng.loss_gradient(10, [0], [hs[0].ncompts - 1], np.zeros(10))
     eng.close()
@@ -216,7 +216,7 @@ def test_unsupported_programs_rejected(gpu_engine):
     with pytest.raises(RuntimeError, match="error -6"):
         eng.loss_gradient(10, [0], [hs[0].ncompts - 1], np.zeros(10))
     eng.close()
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     with pytest.raises(RuntimeError, match="error -1"):     # target row out of range
         eng.loss_gradient(10, [0], [999], np.zeros(10))
     with pytest.raises(RuntimeError, match="error -1"):     # repeated target
@@ -234,7 +234,7 @@ def test_autograd_function_wrapper(oracle, gpu_engine):
     nsteps = 120
     rows = np.array([h.ncompts - 1 for h in hs])
     trace = np.full((nsteps, len(hs)), -0.06)
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     b = eng.batch
 
     class SomaLoss(torch.autograd.Function):
@@ -274,7 +274,7 @@ def test_config4_shape_physical_parameters_vs_fd(oracle, gpu_engine):
     ht = [model.build(t.model(na, k, dt=DT), exact=True) for t in targets]
     rows = [[h.ncompts - 1] for h in hs]
     traces = _oracle_trace(oracle, ht, nsteps, rows)
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_FP64, wide_min=-1)
     b = eng.batch
     L, dchip, drav, dvm = eng.loss_gradient(nsteps, np.arange(n_neurons), np.array([r[0] for r in rows]),
                                             np.concatenate(traces, axis=1), K)
