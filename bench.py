@@ -272,13 +272,14 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
             "launches": int(st.launches - launches0)}
 
 
-def other_configs(device, n_trees=10_000):
+def other_configs(device, n_trees=50_000):
     """Throughput of the other workloads (parity-test cases; not the headline):
     cables-1k-x16 (1,000 x 16-compartment cables, FP64, 200 steps), the
     4,000-cell spiking network (2 % connectivity, dt 0.1 ms, FP64, seeded
     tonic drive U(0.05, 0.3) nA so that it spikes) with and without
     CUDA-graph replay, and random trees 8-256 compartments with Ca
-    pools (a 10,000-neuron sample of the 50,000, FP64 and mixed, graph replay)."""
+    pools (50,000 neurons, 3.6 M compartments, FP64 and mixed, graph replay,
+    500 steps)."""
     from gbhsolve import configs, engine, model
     out = {}
 
@@ -314,12 +315,12 @@ def other_configs(device, n_trees=10_000):
 
     hs2 = [model.build(m) for m in configs.random_trees(n_trees, seed=2)]
     M2 = sum(h.ncompts for h in hs2)
-    trees = {"neurons": n_trees, "compartments": M2, "steps": 1000}
+    trees = {"neurons": n_trees, "compartments": M2, "steps": 500}
     for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
         eng = engine.Engine(hs2, precision=prec, device=device, use_graph=True)
         st = eng.stats()
-        ms = rate(eng, 1000, 20)
-        trees[form] = {"ms": ms, "value": M2 * 1000 / (ms / 1e3), "tiles": int(st.tiles),
+        ms = rate(eng, 500, 20)
+        trees[form] = {"ms": ms, "value": M2 * 500 / (ms / 1e3), "tiles": int(st.tiles),
                        "specialised_kernels": int(st.jit_kernels), "steps_per_launch": int(st.steps_per_launch)}
         eng.close()
     out["random-trees-ca"] = trees

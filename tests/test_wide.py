@@ -24,7 +24,7 @@ def _oracle_run(oracle, h, n):
 @pytest.mark.parametrize("method", [model.BEULER, model.CRANK])
 def test_random_trees_wide_fp64(oracle, gpu_engine, method):
     hs = [model.build(m) for m in configs.random_trees(24, size_range=(32, 200), seed=7, method=method)]
-    eng = gpu_engine.Engine(hs)
+    eng = gpu_engine.Engine(hs, wide_min=32)
     assert eng.stats().tiles == len(hs)          # one neuron per tile: all wide
     eng.run(300)
     st = eng.get_state()
@@ -39,7 +39,7 @@ def test_random_trees_wide_fp64(oracle, gpu_engine, method):
 def test_random_trees_wide_equals_lane(gpu_engine):
     """The same batch with and without wide tiles: bit-identical."""
     hs = [model.build(m) for m in configs.random_trees(40, size_range=(8, 120), seed=8)]
-    a = gpu_engine.Engine(hs)
+    a = gpu_engine.Engine(hs, wide_min=32)
     b = gpu_engine.Engine(hs, wide_min=-1)
     a.run(400)
     b.run(400)
@@ -141,7 +141,7 @@ def test_table_bracket_carried_between_compartments(oracle, gpu_engine):
     vm[30] = x + 0.6 * dx
     vm[31] = x
     h.vm = vm
-    eng = gpu_engine.Engine([h])
+    eng = gpu_engine.Engine([h], wide_min=32)
     assert eng.stats().tiles == 1
     ref = oracle.Solver(h)
     for _ in range(3):
