@@ -385,6 +385,10 @@ def main():
                     help="time only this form's step loop (for profiler launch lists and captures)")
     ap.add_argument("--profile-adjoint", type=int, nargs=2, metavar=("NEURONS", "STEPS"),
                     help="run only the gradient workload at this size")
+    ap.add_argument("--profile-trees", type=int, metavar="NEURONS",
+                    help="run only random trees (8-256 compartments, Ca) of this many neurons, the form of "
+                         "--profile-form (default mixed), steps_per_launch --steps-per-launch (default 64); "
+                         "the timed steps run between cudaProfilerStart/Stop")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local, dist = dist_setup()
@@ -397,6 +401,23 @@ def main():
 
     if args.profile_adjoint:
         print(json.dumps(adjoint_measure(local, *args.profile_adjoint)), flush=True)
+        return 0
+    if args.profile_trees:
+        from gbhsolve import configs, model
+        ht = [model.build(m) for m in configs.random_trees(args.profile_trees, seed=2)]
+        prec = engine.PREC_FP64 if args.profile_form == "fp64" else engine.PREC_MIXED
+        eng = engine.Engine(ht, precision=prec, steps_per_launch=args.steps_per_launch or 64, device=local)
+        eng.run(args.warmup)
+        eng.vm()
+        torch.cuda.profiler.start()
+        t0 = time.time()
+        eng.run(args.steps)
+        eng.vm()
+        dt = time.time() - t0
+        torch.cuda.profiler.stop()
+        log("random trees %d: %d steps in %.1f ms, %d tiles" % (args.profile_trees, args.steps, dt * 1e3,
+                                                              eng.stats().tiles))
+        eng.close()
         return 0
     hs, injects = build_workload(args.neurons)
     if args.profile_form:

@@ -455,11 +455,9 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     }
     // ---- wide types: one neuron per tile, its compartments on a block's threads ----
     if (e->opt.wide_min >= 0) {
-        // default: 32 compartments for the mixed form; the FP64 form is held by
-        // its FP64 units either way and goes wide only from 128 (measured on
-        // 10,000 random trees 8-256: mixed 3.2e9 against 1.2e9 lane-mapped)
-        const int wmin = e->opt.wide_min != 0 ? e->opt.wide_min
-                                               : e->opt.precision == GBH_PREC_MIXED ? 32 : 128;
+        // default 32 compartments (10,000 random trees of 8-256: mixed 3.2e9
+        // against 1.2e9 lane-mapped, FP64 1.4e9 against 0.88e9)
+        const int wmin = e->opt.wide_min != 0 ? e->opt.wide_min : 32;
         for (size_t ti = 0; ti < e->types.size(); ++ti) {
             TileType &tt = e->types[ti];
             std::vector<int> meta;

@@ -546,8 +546,10 @@ __device__ __forceinline__ void cursor_chain(int S, const int *prev, VAL val, co
 }
 
 // Shared memory: 2*smax doubles (diagonal, right-hand side) + 4*smax ints.
+// 128 registers a thread (2 blocks of 256 per SM): the FP64 interpreter
+// spills at less (measured: 513 against 841 us/step on 10,000 random trees).
 template <typename G, bool GIV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_wide(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
 {
     extern __shared__ double sm[];

@@ -159,8 +159,8 @@ typedef struct gbh_options {
                             programs                                          */
     int wide_min;        /* neurons with at least this many compartments run
                             one per thread block, compartments across its
-                            threads (0 = 32 for the mixed form, 128 for FP64;
-                            < 0 = never; gbh_loss_gradient needs < 0)        */
+                            threads (0 = 32; < 0 = never; gbh_loss_gradient
+                            needs < 0)                                       */
 } gbh_options;
 
 typedef struct gbh_stats {
