@@ -546,10 +546,11 @@ __device__ __forceinline__ void cursor_chain(int S, const int *prev, VAL val, co
 }
 
 // Shared memory: 2*smax doubles (diagonal, right-hand side) + 4*smax ints.
-// 128 registers a thread (2 blocks of 256 per SM): the FP64 interpreter
-// spills at less (measured: 513 against 841 us/step on 10,000 random trees).
+// One warp per block (wide_threads); 128 registers a thread: the FP64
+// interpreter spills at 80 (measured with 256-thread blocks: 513 against 841
+// us/step on 10,000 random trees).
 template <typename G, bool GIV>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(32, 16)
 k_wide(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
 {
     extern __shared__ double sm[];
@@ -679,7 +680,11 @@ cudaError_t launch_mixed_wide(const DevView &v, int tile0, int tile1, int smax, 
                               cudaStream_t st);
 
 inline size_t wide_smem(int smax) { return (size_t)smax * (2 * sizeof(double) + 4 * sizeof(int)); }
-inline int wide_threads(int smax) { return std::min(256, ((smax + 31) / 32) * 32); }
+// One warp per neuron: a warp's __syncthreads is cheap, and many small
+// blocks hide each other's waits (10,000 random trees, mixed: 146 us/step
+// with 32 threads, 154 with 64, 199 with 128, 216 with 256; FP64 332 / 348 /
+// 409 / 539).
+inline int wide_threads(int) { return 32; }
 
 template <typename KF>
 cudaError_t wide_launch(KF fn, const DevView &v, int tile0, int tile1, int smax, int nsteps, long long step,

@@ -427,7 +427,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
 // Wide tiles of the mixed form (see k_wide): the double-float lookups keep
 // no bracket cache, so every compartment starts from a fresh cursor.
 template <bool GIV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32, 24)
 k_wide_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
 {
     extern __shared__ double sm[];
