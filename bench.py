@@ -160,7 +160,9 @@ def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE):
     from gbhsolve import engine
     idx = np.linspace(0, len(hs) - 1, nsample).astype(int)
     sample = [hs[i] for i in idx]
-    eng = engine.Engine(sample, precision=precision)
+    # the sample runs the kernels of the full workload: 32 neurons per warp
+    # (a sample this small would otherwise go one neuron per warp)
+    eng = engine.Engine(sample, precision=precision, wide_min=-1)
     orc = [pyoracle.Solver(h) for h in sample]
     soma = np.cumsum([h.ncompts for h in sample]) - 1      # the root is each solver's last row
     trace_e = np.empty((nsteps, len(sample)))

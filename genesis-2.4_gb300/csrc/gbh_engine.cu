@@ -455,13 +455,16 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     }
     // ---- wide types: one neuron per tile, its compartments on a block's threads ----
     if (e->opt.wide_min >= 0) {
-        // default 32 compartments (10,000 random trees of 8-256: mixed 3.2e9
-        // against 1.2e9 lane-mapped, FP64 1.4e9 against 0.88e9)
-        const int wmin = e->opt.wide_min != 0 ? e->opt.wide_min : 32;
+        // Default 32 compartments. Measured (compartment-steps/s, mixed / FP64):
+        // 50,000 random trees of 8-256 compartments, threshold 32: 8.5e9 / 2.9e9;
+        // 16 (for types of fewer than 1,024 neurons): 8.1e9 / 2.6e9; all
+        // lane-mapped (10,000 trees): 1.2e9 / 0.9e9. 1,000 16-compartment
+        // cables ran 20 % slower one per warp than 32 per warp.
         for (size_t ti = 0; ti < e->types.size(); ++ti) {
             TileType &tt = e->types[ti];
+            const bool by_size = tt.nslots >= (e->opt.wide_min > 0 ? e->opt.wide_min : 32);
             std::vector<int> meta;
-            if (tt.nslots >= wmin && wide_plan(prog_pool, tt, meta)) {
+            if (by_size && wide_plan(prog_pool, tt, meta)) {
                 tt.wide = 1;
                 tt.wide_off = (int)prog_pool.size();
                 prog_pool.insert(prog_pool.end(), meta.begin(), meta.end());

@@ -158,9 +158,9 @@ typedef struct gbh_options {
                             shared-memory rows only; -1 = interpret the
                             programs                                          */
     int wide_min;        /* neurons with at least this many compartments run
-                            one per thread block, compartments across its
-                            threads (0 = 32; < 0 = never; gbh_loss_gradient
-                            needs < 0)                                       */
+                            one per warp, compartments across its threads
+                            (0 = 32; < 0 = never; gbh_loss_gradient needs
+                            < 0)                                             */
 } gbh_options;
 
 typedef struct gbh_stats {
