@@ -201,12 +201,42 @@ __device__ __forceinline__ df ld_df_ro(const double *p)
     return df_make(v.x, v.y);
 }
 
+// the same for a row read once per step (the unrolled form): first out of
+// L1, which then keeps the table rows the gates gather from
+__device__ __forceinline__ df ld_df_stream(const double *p)
+{
+    float2 v;
+    asm("ld.global.nc.L1::evict_first.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+    return df_make(v.x, v.y);
+}
+
+__device__ __forceinline__ double ld_ro_stream(const double *p)
+{
+    double v;
+    asm("ld.global.nc.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ int ld_ro_stream(const int *p)
+{
+    int v;
+    asm("ld.global.nc.L1::evict_first.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 // read-only view of a neuron-interleaved row array: r[i] loads through the
 // non-coherent path
 template <typename T>
 struct RoRow {
     const T *p;
     __device__ __forceinline__ T operator[](int i) const { return __ldg(p + i); }
+};
+
+// read-only rows read once per step (the unrolled form): evict-first loads
+template <typename T>
+struct RoStream {
+    const T *p;
+    __device__ __forceinline__ T operator[](int i) const { return ld_ro_stream(p + i); }
 };
 
 __device__ __forceinline__ void st_df(double *p, df x)
