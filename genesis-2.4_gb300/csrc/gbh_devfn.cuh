@@ -48,6 +48,17 @@ struct DevView {
     double *CR, *CD, *S;
     // wide tiles (one neuron per block): per-tile elimination schedules
     const int *wtop;
+    // Per-step host I/O inside a multi-step launch of the specialised kernels
+    // (gbh_run_io): io_in[k * io_nin + i] is input i of step io_step0 + k and
+    // io_out likewise. Per tile, tin_* list (offset in the tile's field block,
+    // bit 30 set when the field is a packed double-float; input index) and
+    // tout_* list (offset in its Vm block; output index). Null: none.
+    const double *io_in;
+    double *io_out;
+    int io_nin, io_nout;
+    long long io_step0;
+    const int *tin_start, *tin_off, *tin_idx;
+    const int *tout_start, *tout_off, *tout_idx;
 };
 
 // Barrier over all blocks of a cooperative launch: the last block to arrive
@@ -198,6 +209,14 @@ __device__ __forceinline__ df ld_df(const double *p)
 __device__ __forceinline__ df ld_df_ro(const double *p)
 {
     const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return df_make(v.x, v.y);
+}
+
+// a row the kernel itself may write between steps (the inject row, fused
+// host I/O): read at L2, past L1, so a lane sees what another lane stored
+__device__ __forceinline__ df ld_df_cg(const double *p)
+{
+    const float2 v = __ldcg(reinterpret_cast<const float2 *>(p));
     return df_make(v.x, v.y);
 }
 

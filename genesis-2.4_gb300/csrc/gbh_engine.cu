@@ -192,6 +192,11 @@ struct gbh_engine {
     DBuf<double> d_in_vals, d_out_vals, d_in_sa, d_in_sb;
     DBuf<int64_t> d_in_start, d_in_addr, d_out_addr;
     DBuf<int> d_in_item;
+    // the same inputs / outputs as per-tile lists for the specialised kernels,
+    // which apply them inside multi-step launches (gbh_run_io); fuse_in: every
+    // input sets a compartment's inject (the row those kernels read coherently)
+    DBuf<int> d_tin_start, d_tin_off, d_tin_idx, d_tout_start, d_tout_off, d_tout_idx;
+    bool fuse_in = false;
 };
 
 namespace {
@@ -1340,6 +1345,28 @@ extern "C" {
 
 const char *gbh_last_error(void) { return g_last_error; }
 
+// Per-tile CSR of (offset within the tile's block, index) pairs.
+int upload_tile_lists(gbh_engine *e, std::vector<std::vector<std::pair<int, int>>> &per_tile, DBuf<int> &start,
+                      DBuf<int> &off, DBuf<int> &idx)
+{
+    std::vector<int> st(per_tile.size() + 1, 0), o, ix;
+    for (size_t t = 0; t < per_tile.size(); ++t) {
+        for (auto &x : per_tile[t]) {
+            o.push_back(x.first);
+            ix.push_back(x.second);
+        }
+        st[t + 1] = (int)o.size();
+    }
+    if (o.empty()) {
+        o.push_back(0);
+        ix.push_back(0);
+    }
+    start.release(); off.release(); idx.release();
+    if (start.upload(st) || off.upload(o) || idx.upload(ix)) return GBH_ERR_CUDA;
+    (void)e;
+    return GBH_OK;
+}
+
 InPlan in_plan(const gbh_engine *e)
 {
     InPlan pl;
@@ -1430,6 +1457,43 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
         return GBH_ERR_CUDA;
     e->n_in = n;
     e->n_tgt = (int)taddr.size();
+    // the fused form: only set-inputs on lane tiles' inject rows (M_BEGIN's
+    // second operand); the last one registered for a row wins, as h_in_msgs
+    e->fuse_in = true;
+    std::vector<std::vector<std::pair<int, int>>> per_tile(e->tiles.size());
+    std::map<std::pair<int, int>, int> last;   // (tile, offset) -> input
+    for (size_t q = 0; q < e->dec.neurons.size() && e->fuse_in; ++q) {
+        const Neuron &N = e->dec.neurons[q];
+        const int ti = e->neuron_tile[q];
+        const Tile &t = e->tiles[ti];
+        const int l = e->neuron_lane[q];
+        std::vector<char> inject(N.fsrc.size(), 0);
+        for (size_t pc = 0; pc < N.prog.size();) {
+            const int code = N.prog[pc];
+            const int m = micro_operands(code);
+            if (m < 0) break;
+            if (code == M_BEGIN) inject[N.prog[pc + 2]] = 1;
+            pc += 1 + m;
+        }
+        for (size_t f = 0; f < N.fsrc.size(); ++f) {
+            if (N.fsrc[f].kind != FS_CHIP) continue;
+            auto it = want_chip.find(e->chip_start[N.solver] + N.fsrc[f].idx);
+            if (it == want_chip.end()) continue;
+            for (int i : it->second) {
+                if ((kind && kind[i] != GBH_IN_SET) || !inject[f] || e->types[t.type].wide) {
+                    e->fuse_in = false;
+                    break;
+                }
+                const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
+                last[{ti, (int)(f * LANES + l) | (packed ? (1 << 30) : 0)}] = i;
+            }
+        }
+    }
+    if (!want_conc.empty()) e->fuse_in = false;
+    if (e->fuse_in) {
+        for (auto &kv : last) per_tile[kv.first.first].push_back({kv.first.second, kv.second});
+        if (upload_tile_lists(e, per_tile, e->d_tin_start, e->d_tin_off, e->d_tin_idx)) return GBH_ERR_CUDA;
+    }
     return GBH_OK;
 }
 
@@ -1470,6 +1534,18 @@ int gbh_register_outputs(gbh_engine *e, int n, const int *solver, const int *row
     e->d_out_vals.release(); e->d_out_addr.release();
     if (e->d_out_vals.alloc(n) || e->d_out_addr.upload(addr)) return GBH_ERR_CUDA;
     e->n_out = n;
+    std::vector<std::vector<std::pair<int, int>>> per_tile(e->tiles.size());
+    for (int i = 0; i < n; ++i) {   // the tile of each output, from its address
+        for (size_t t = 0; t < e->tiles.size(); ++t) {
+            const Tile &tl = e->tiles[t];
+            const int64_t rows = rows_of(e->types[tl.type].nslots, e->types[tl.type].wide != 0);
+            if (addr[i] >= tl.vm * LANES && addr[i] < (tl.vm + rows) * LANES) {
+                per_tile[t].push_back({(int)(addr[i] - tl.vm * LANES), i});
+                break;
+            }
+        }
+    }
+    if (upload_tile_lists(e, per_tile, e->d_tout_start, e->d_tout_off, e->d_tout_idx)) return GBH_ERR_CUDA;
     return GBH_OK;
 }
 
@@ -1602,6 +1678,12 @@ int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nstep
     }
     const int nio = std::max(n_in ? e->n_tgt : 0, n_out);
     const InPlan plan = in_plan(e);
+    // every launch group specialised (lane tiles), no synapses: the step
+    // kernels apply each step's inputs and gather its outputs themselves, and
+    // a block of steps runs as multi-step launches
+    bool fused = !e->has_network && !e->givals_enabled && !e->net_coop && (n_in == 0 || e->fuse_in) &&
+                 !e->launches.empty();
+    for (const Launch &L : e->launches) fused = fused && L.jit >= 0 && !L.wide;
     const unsigned grid = (unsigned)((nio + 255) / 256);
     int last = 0;
     for (int s0 = 0, j = 0; s0 < nsteps; s0 += B, ++j) {
@@ -1614,10 +1696,39 @@ int gbh_run_io(gbh_engine *e, const double *host_in, double *host_out, int nstep
                                cudaMemcpyHostToDevice, e->io_stream));
             CK(cudaEventRecord(e->blk_in_copied[b], e->io_stream));
             CK(cudaStreamWaitEvent(st, e->blk_in_copied[b], 0));
-            k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, 0, nullptr, din, plan, e->d_P.p, e->d_F.p);
-            CK(cudaGetLastError());
+            if (!fused) {
+                k_io<<<grid, 256, 0, st>>>(e->d_V.p, e->d_out_addr.p, 0, nullptr, din, plan, e->d_P.p, e->d_F.p);
+                CK(cudaGetLastError());
+            }
         }
         if (n_out) CK(cudaStreamWaitEvent(st, e->blk_out_copied[b], 0));   // its outputs were copied out
+        if (fused) {
+            DevView v = view_of(e);
+            v.io_in = n_in ? din : nullptr;
+            v.io_out = n_out ? dout : nullptr;
+            v.io_nin = n_in;
+            v.io_nout = n_out;
+            v.io_step0 = e->step;
+            v.tin_start = e->d_tin_start.p;
+            v.tin_off = e->d_tin_off.p;
+            v.tin_idx = e->d_tin_idx.p;
+            v.tout_start = e->d_tout_start.p;
+            v.tout_off = e->d_tout_off.p;
+            v.tout_idx = e->d_tout_idx.p;
+            e->dstep_valid = false;   // absolute step numbers in the launches
+            rc = issue_steps(e, v, nb, e->step, false, st, nullptr);
+            if (rc) return rc;
+            e->step += nb;
+            CK(cudaEventRecord(e->blk_done[b], st));
+            if (n_out) {
+                CK(cudaStreamWaitEvent(e->io_out_stream, e->blk_done[b], 0));
+                CK(cudaMemcpyAsync(host_out + (int64_t)s0 * n_out, dout, (size_t)nb * n_out * sizeof(double),
+                                   cudaMemcpyDeviceToHost, e->io_out_stream));
+                CK(cudaEventRecord(e->blk_out_copied[b], e->io_out_stream));
+            }
+            last = b;
+            continue;
+        }
         for (int k = 0; k < nb; ++k) {
             rc = run_steps(e, 1, st);
             if (rc) return rc;
@@ -2409,6 +2520,8 @@ void gbh_destroy(gbh_engine *e)
     e->d_gbar.release(); e->d_spiked.release(); e->d_rstart.release(); e->d_rbase.release(); e->d_rdelay.release(); e->d_rbits.release();
     e->d_in_vals.release(); e->d_in_start.release(); e->d_in_addr.release();
     e->d_in_item.release(); e->d_in_sa.release(); e->d_in_sb.release();
+    e->d_tin_start.release(); e->d_tin_off.release(); e->d_tin_idx.release();
+    e->d_tout_start.release(); e->d_tout_off.release(); e->d_tout_idx.release();
     e->d_out_vals.release(); e->d_out_addr.release();
     drop_graphs(e);
     if (e->cap_stream) cudaStreamDestroy(e->cap_stream);

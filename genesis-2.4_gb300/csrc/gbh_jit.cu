@@ -176,11 +176,14 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
         switch (code) {
         case M_BEGIN:
             if (mx) {
-                o << "      { const df emrm = " << E.ldr(a[0]) << "; ichan = df_add(emrm, " << E.ldr(a[1]) << ");";
+                // the inject row is read coherently: per-step inputs are written into it
+                // by the kernel itself (fused host I/O)
+                o << "      { const df emrm = " << E.ldr(a[0]) << "; ichan = df_add(emrm, " << (E.stream ? "ld_df_cg(" : "ld_df(")
+                  << E.pP(a[1]) << "));";
                 if (giv) o << " Im = df2d(emrm) - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
                 o << " }\n";
             } else {
-                o << "      { const double emrm = " << E.Pr(a[0]) << "; ichan = emrm + " << E.Pr(a[1]) << ";";
+                o << "      { const double emrm = " << E.Pr(a[0]) << "; ichan = emrm + " << E.P(a[1]) << ";";
                 if (giv) o << " Im = emrm - Vm / " << E.P(a[2]) << "; " << E.G(a[3]) << " = Im;";
                 o << " }\n";
             }
@@ -555,7 +558,14 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     o << "  const " << (E.stream ? "RoStream" : "RoRow")
       << "<double> Aw{v.A + tl.topo * 32 + lane}, Bw{v.B + tl.topo * 32 + lane}, Cbw{v.Cb + tl.topo * 32 + lane};\n";
     o << "  for (int it = 0; it < nsteps; ++it) {\n"
-      << "    const long long step = sbase + step0 + it; (void)step;\n";
+      << "    const long long step = sbase + step0 + it; (void)step;\n"
+      << "    if (v.io_in) {   // this step's inputs into the tile's fields, then visible to every lane\n"
+      << "      const double *src = v.io_in + (step - v.io_step0) * v.io_nin; double *Pt = v.P + tl.fld * 32;\n"
+      << "      for (int q = v.tin_start[t] + lane; q < v.tin_start[t + 1]; q += 32) {\n"
+      << "        const int o = v.tin_off[q]; const double x = src[v.tin_idx[q]];\n"
+      << "        if (o & (1 << 30)) { const float hi = __double2float_rn(x); st_df(&Pt[o & ~(1 << 30)], df_make(hi, __double2float_rn(x - (double)hi))); }\n"
+      << "        else Pt[o] = x; }\n"
+      << "      __syncwarp(); }\n";
     if (mixed) {
         o << "    DCursor vc, cc, c1; vc.row = vc.base = 0; vc.frac = df_make(0.f, 0.f); cc = vc; c1 = vc;\n"
           << "    df Ek = df_make(0.f, 0.f), Gk = Ek, gmax = Ek; (void)gmax;\n";
@@ -717,6 +727,9 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
         t << " }\n";
     }
+    t << "    if (v.io_out) {   // this step's outputs\n"
+      << "      __syncwarp(); double *dst = v.io_out + (step - v.io_step0) * v.io_nout; const double *Vt = v.V + tl.vm * 32;\n"
+      << "      for (int q = v.tout_start[t] + lane; q < v.tout_start[t + 1]; q += 32) dst[v.tout_idx[q]] = Vt[v.tout_off[q]]; }\n";
     t << "  }\n}\n";
     return t.str();
 }
