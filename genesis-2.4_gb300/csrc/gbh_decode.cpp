@@ -118,6 +118,82 @@ struct NB {
     }
 };
 
+// funcs[] of symmetric compartments (h_funcs_init's symflag branch,
+// hines_init.c:361-1273, emits COPY_ARRAY, FASTSIBARRAY_ELIM and
+// SIBARRAY_ELIM): walked with the reference's operand counts and ravals
+// cursor (hines_solve.c:223-296), every index checked against the rows and
+// ravals, and written out as SymOp triples. `sym` is false when no such token
+// occurs (the program is then a tree, handled by parse_funcs).
+int parse_funcs_sym(Ctx &c, const int *f, int64_t nf, int64_t nra, int n, std::vector<int> &prog, bool &sym)
+{
+    prog.clear();
+    sym = false;
+    if (n < 2) return GBH_OK;
+    int64_t fi = 0, ri = 0;
+    int cur = 1;
+    auto row_of = [&](int64_t at, int &row) -> bool {
+        const int x = f[at];
+        if (x < 0 || (x & 1) || x / 2 >= n) return false;
+        row = x / 2;
+        return true;
+    };
+    auto rav_ok = [&](int64_t k) { return k >= 0 && k < nra; };
+    for (int pass = 0; pass < 2; ++pass) {
+        for (;;) {
+            if (fi >= nf) return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "funcs[] ends inside an elimination pass");
+            const int op = f[fi++];
+            int a = 0, b = 0;
+            if (op == F_ELIM) {
+                if (fi >= nf || !row_of(fi, a) || !rav_ok(ri) || (pass == 0 && !rav_ok(ri + 1)))
+                    return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "ELIM operand or ravals cursor out of range");
+                ++fi;
+                b = (int)ri;
+                ri += pass == 0 ? 2 : 1;
+            } else if (pass == 0 && (op == F_SET_DIAG || op == F_SKIP_DIAG)) {
+                cur += op == F_SET_DIAG ? 1 : 2;
+                if (cur >= n) return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "forward cursor past the last row");
+            } else if (pass == 0 && (op == F_FASTSIB || op == F_COPY)) {
+                if (fi >= nf || !rav_ok(f[fi]) || !rav_ok(ri))
+                    return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "ravals index out of range");
+                a = f[fi++];
+                b = (int)ri++;
+                sym = true;
+            } else if (op == F_SIB) {
+                if (fi + 1 >= nf || !rav_ok(f[fi]))
+                    return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "SIBARRAY_ELIM operand out of range");
+                a = f[fi];
+                if (pass == 0) {
+                    if (!rav_ok(f[fi + 1]))
+                        return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "SIBARRAY_ELIM operand out of range");
+                    b = f[fi + 1];
+                } else if (!row_of(fi + 1, b)) {
+                    return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "SIBARRAY_ELIM row out of range");
+                }
+                fi += 2;
+                sym = true;
+            } else if (pass == 1 && op == F_CALC) {
+                if (cur < 0) return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "CALC_RESULTS below row 0");
+                cur -= 1;
+            } else if (op == F_FINISH) {
+                prog.insert(prog.end(), {SY_FINISH, 0, 0});
+                break;
+            } else {
+                return fail(c, GBH_ERR_FUNCS, cur, op, fi - 1, "funcs token %d in the %s pass", op,
+                            pass == 0 ? "forward" : "backward");
+            }
+            prog.insert(prog.end(), {op, a, b});
+        }
+        if (pass == 0) {
+            if (cur != n - 1)
+                return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "forward pass ends at row %d, expected %d", cur, n - 1);
+            cur = n - 2;
+        } else if (cur != -1) {
+            return fail(c, GBH_ERR_FUNCS, cur, 0, fi, "backward pass stops at row %d", cur);
+        }
+    }
+    return GBH_OK;
+}
+
 // Symbolic execution of funcs[] (asymmetric compartments).
 int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra, int n,
                 std::vector<int> &parent, std::vector<double> &A, std::vector<double> &B,
@@ -224,16 +300,33 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         if (ts < 0 || ts >= d->ntables) return fail(c, GBH_ERR_ARG, -1, 0, -1, "table set %d out of range", ts);
 
         // elimination structure
-        std::vector<int> parent, ridx;
+        std::vector<int> parent, ridx, symprog;
         std::vector<double> A, B, Cc;
-        int rc = parse_funcs(c, d->funcs + d->funcs_start[si], d->funcs_start[si + 1] - d->funcs_start[si],
-                             d->ravals + d->ravals_start[si], d->ravals_start[si + 1] - d->ravals_start[si],
-                             n, parent, A, B, Cc, ridx);
+        const int *fs = d->funcs + d->funcs_start[si];
+        const int64_t nfs = d->funcs_start[si + 1] - d->funcs_start[si];
+        const int64_t nra = d->ravals_start[si + 1] - d->ravals_start[si];
+        bool sym = false;
+        int rc = parse_funcs_sym(c, fs, nfs, nra, n, symprog, sym);
         if (rc) return rc;
+        if (sym) {   // the whole solver is one neuron; its rows are coupled beyond a tree
+            parent.assign(n, -1);
+            A.assign(n, 0.0);
+            B.assign(n, 0.0);
+            Cc.assign(n, 0.0);
+            ridx.assign(3 * (size_t)n, -1);
+        } else {
+            rc = parse_funcs(c, fs, nfs, d->ravals + d->ravals_start[si], nra, n, parent, A, B, Cc, ridx);
+            if (rc) return rc;
+        }
         // trees: parents always have higher rows (Hines numbering)
         std::vector<int> tree(n, -1);
         std::vector<int> tmin, tmax;
-        for (int r = n - 1; r >= 0; --r) {
+        if (sym) {
+            tree.assign(n, 0);
+            tmin.push_back(0);
+            tmax.push_back(n - 1);
+        }
+        for (int r = n - 1; r >= 0 && !sym; --r) {
             if (parent[r] < 0) {
                 tree[r] = (int)tmin.size();
                 tmin.push_back(r);
@@ -271,6 +364,10 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                 nn.B.push_back(B[r]);
                 nn.C.push_back(Cc[r]);
                 for (int q = 0; q < 3; ++q) nn.ridx.push_back(ridx[3 * r + q]);
+            }
+            if (sym) {
+                nn.sym = symprog;
+                nn.rav.assign(d->ravals + d->ravals_start[si], d->ravals + d->ravals_start[si + 1]);
             }
             tree_neuron[order[k]] = nbase + k;
             out.neurons.push_back(std::move(nn));
@@ -813,6 +910,9 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             put(N.has_cd); put(N.nscratch);
             put((int)N.prog.size());
             for (int v : N.prog) put(v);
+            put((int)N.sym.size());
+            for (int v : N.sym) put(v);
+            put((int)N.rav.size());
             for (int v : N.pool_prog) put(v);
             N.key = std::move(key);
         }

@@ -17,7 +17,8 @@ struct FieldSrc {
     bool state;      // written back on sync (gate states, synchan X/Y)
 };
 
-// One neuron = one tree of one solver.
+// One neuron = one tree of one solver (a solver with symmetric compartments:
+// the whole solver, its elimination program run as written).
 struct Neuron {
     int solver = 0;
     int row0 = 0, nrows = 0;
@@ -34,6 +35,8 @@ struct Neuron {
     std::vector<int> parent;      // per slot
     std::vector<double> A, B, C;  // per slot
     std::vector<int> ridx;        // per slot: ravals index of A, B, C (-1: none)
+    std::vector<int> sym;         // symmetric compartments: SymOp triples (empty: a tree)
+    std::vector<double> rav;      // symmetric compartments: the solver's ravals
     int spike_op = -1;
     bool has_cd = false;          // diffusion systems: codiag/coresult rows in use
     int nscratch = 0;             // scratch rows of its diffusion solves

@@ -48,6 +48,8 @@ struct DevView {
     double *CR, *CD, *S;
     // wide tiles (one neuron per block): per-tile elimination schedules
     const int *wtop;
+    // ravals rows of the solvers with symmetric compartments
+    double *RV;
     // Per-step host I/O inside a multi-step launch of the specialised kernels
     // (gbh_run_io): io_in[k * io_nin + i] is input i of step io_step0 + k and
     // io_out likewise. Per tile, tin_* list (offset in the tile's field block,
@@ -60,6 +62,65 @@ struct DevView {
     const int *tin_start, *tin_off, *tin_idx;
     const int *tout_start, *tout_off, *tout_idx;
 };
+
+// Elimination of one solver with symmetric compartments (SymOp program at
+// sp, rows at stride STR): do_euler_hsolve / do_crank_hsolve
+// (hines_solve.c:140-296) with the same operations in the same order,
+// including the in-place updates of the ravals the program rewrites
+// (COPY_ARRAY, FASTSIBARRAY_ELIM, SIBARRAY_ELIM). R and D hold each row's
+// right-hand side and diagonal on entry, R the solution on exit; V is Vm.
+// The decoder has checked every index against the solver's rows and ravals.
+template <int STR>
+__device__ __forceinline__ void sym_eliminate(const int *sp, double *R, double *D, double *RV, double *V, bool crank)
+{
+    int cur = 1;
+    double rv = R[STR], dv = D[STR], temp = 0.0;
+    for (;; sp += 3) {
+        const int op = sp[0], a = sp[1], b = sp[2];
+        if (op == SY_ELIM) {
+            temp = RV[b * STR] / D[a * STR];
+            dv -= RV[(b + 1) * STR] * temp;
+            rv -= R[a * STR] * temp;
+        } else if (op == SY_SET || op == SY_SKIP) {
+            R[cur * STR] = rv;
+            D[cur * STR] = dv;
+            cur += op == SY_SET ? 1 : 2;
+            rv = R[cur * STR];
+            dv = D[cur * STR];
+        } else if (op == SY_FASTSIB) {
+            RV[a * STR] -= RV[b * STR] * temp;
+        } else if (op == SY_COPY) {
+            RV[a * STR] = RV[b * STR];
+        } else if (op == SY_SIB) {
+            RV[b * STR] -= RV[a * STR] * temp;
+        } else {
+            break;
+        }
+    }
+    {
+        const double x = rv / dv;
+        V[cur * STR] = crank ? x + x - V[cur * STR] : x;
+        R[cur * STR] = x;
+    }
+    cur -= 1;
+    rv = R[cur * STR];
+    for (sp += 3;; sp += 3) {
+        const int op = sp[0], a = sp[1], b = sp[2];
+        if (op == SY_ELIM) {
+            rv -= RV[b * STR] * R[a * STR];
+        } else if (op == SY_CALC) {
+            const double x = rv / D[cur * STR];
+            V[cur * STR] = crank ? x + x - V[cur * STR] : x;
+            R[cur * STR] = x;
+            cur -= 1;
+            if (cur >= 0) rv = R[cur * STR];
+        } else if (op == SY_SIB) {
+            rv -= RV[a * STR] * R[b * STR];
+        } else {
+            break;
+        }
+    }
+}
 
 // Barrier over all blocks of a cooperative launch: the last block to arrive
 // resets the count and advances the generation; the others wait for the

@@ -115,6 +115,7 @@ struct gbh_engine {
     DBuf<double> d_P, d_V, d_C, d_F, d_A, d_B, d_Cb, d_giv, d_stab;
     DBuf<double> d_CR, d_CD, d_S;   // coresult / codiag rows, diffusion scratch
     DBuf<int> d_wtop;               // elimination schedules of wide tiles
+    DBuf<double> d_RV;              // ravals rows of solvers with symmetric compartments
     DBuf<int> d_I, d_par;
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
@@ -133,7 +134,7 @@ struct gbh_engine {
     DBuf<int> d_status;
     int ring_len = 2;
     int64_t rows_fld = 0, rows_int = 0, rows_pool = 0, rows_giv = 0, rows_vm = 0, rows_topo = 0,
-            rows_syn = 0, rows_scr = 0;
+            rows_syn = 0, rows_scr = 0, rows_rav = 0;
     std::vector<Launch> launches;
     int steps_per_launch = 1;
     bool has_network = false;
@@ -451,6 +452,12 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             tt.nsyn = (int)N.syn_op.size();
             tt.has_cd = N.has_cd;
             tt.nscratch = N.nscratch;
+            if (!N.sym.empty()) {
+                tt.sym = 1;
+                tt.sym_off = (int)prog_pool.size();
+                prog_pool.insert(prog_pool.end(), N.sym.begin(), N.sym.end());
+                tt.nrav = (int)N.rav.size();
+            }
             type_of_key[N.key] = (int)e->types.size();
             e->types.push_back(tt);
             members.emplace_back();
@@ -467,7 +474,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         // cables ran 20 % slower one per warp than 32 per warp.
         for (size_t ti = 0; ti < e->types.size(); ++ti) {
             TileType &tt = e->types[ti];
-            const bool by_size = tt.nslots >= (e->opt.wide_min > 0 ? e->opt.wide_min : 32);
+            const bool by_size = tt.nslots >= (e->opt.wide_min > 0 ? e->opt.wide_min : 32) && !tt.sym;
             std::vector<int> meta;
             if (by_size && wide_plan(prog_pool, tt, meta)) {
                 tt.wide = 1;
@@ -522,6 +529,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             t.topo = e->rows_topo; e->rows_topo += rows_of(tt.nslots, w);
             t.syn = e->rows_syn; e->rows_syn += (int64_t)tt.nsyn * e->ring_len;
             t.scr = e->rows_scr; e->rows_scr += rows_of(tt.nscratch, w);
+            t.rav = e->rows_rav; e->rows_rav += rows_of(tt.nrav, w);
             t.first_neuron = gneuron;
             gneuron += LANES;
             if (w) {
@@ -542,6 +550,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     std::vector<double> P(e->rows_fld * L, 0.0), V(e->rows_vm * L, 0.0), C(e->rows_pool * L, 0.0),
         A(e->rows_topo * L, 0.0), B(e->rows_topo * L, 0.0), Cb(e->rows_topo * L, 0.0);
     std::vector<int> I(e->rows_int * L, 0), par(e->rows_topo * L, -1);
+    std::vector<double> RV(std::max<int64_t>(e->rows_rav, 1) * L, 0.0);
     // padding lanes: a passive row that solves to zero and never spikes
     for (const Tile &t : e->tiles) {
         const TileType &tt = e->types[t.type];
@@ -567,6 +576,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             Cb[at(t.topo, s, l, w)] = N.C[s];
         }
         for (size_t f = 0; f < N.fsrc.size(); ++f) P[at(t.fld, f, l, w)] = N.fval[f];
+        for (size_t k = 0; k < N.rav.size(); ++k) RV[at(t.rav, k, l, w)] = N.rav[k];
         for (size_t r = 0; r < N.iops.size(); ++r) I[at(t.ints, r, l, w)] = N.ival[r];
         for (size_t p = 0; p < N.pool_conc.size(); ++p)
             C[at(t.pools, p, l, w)] = d->conc[d->conc_start[N.solver] + N.pool_conc[p]];
@@ -721,6 +731,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_C.upload(C);
     rc |= e->d_F.upload(std::vector<double>(C.size(), 0.0));
     rc |= e->d_wtop.upload(wtop.empty() ? std::vector<int>(1, 0) : wtop);
+    rc |= e->d_RV.upload(RV);
     bool any_cd = false;
     for (const TileType &tt : e->types) any_cd = any_cd || tt.has_cd;
     if (any_cd) {   // coresult 0, codiag 1 (hines_conc_init.c:121-126), solve scratch
@@ -762,7 +773,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         // the looped forms keep 2 x nslots x 32 rows per warp in shared memory:
         // 4-warp blocks of more than 96 compartments would not fit
         for (int ti : torder)
-            if (type_t0[ti] >= 0 && !e->types[ti].wide && e->types[ti].nslots <= 96) cand.push_back(ti);
+            if (type_t0[ti] >= 0 && !e->types[ti].wide && !e->types[ti].sym && e->types[ti].nslots <= 96)
+                cand.push_back(ti);
         std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
             return (type_t1[a] - type_t0[a]) > (type_t1[b] - type_t0[b]);
         });
@@ -904,6 +916,7 @@ DevView view_of(gbh_engine *e)
     v.C = e->d_C.p;
     v.F = e->d_F.p;
     v.wtop = e->d_wtop.p;
+    v.RV = e->d_RV.p;
     v.CR = e->d_CR.p;
     v.CD = e->d_CD.p;
     v.S = e->d_S.p;
@@ -1155,6 +1168,7 @@ int autotune_trials(gbh_engine *e)
     rc |= keep(e->d_C.p, e->d_C.n * sizeof(double));
     rc |= keep(e->d_CR.p, e->d_CR.n * sizeof(double));
     rc |= keep(e->d_CD.p, e->d_CD.n * sizeof(double));
+    rc |= keep(e->d_RV.p, e->d_RV.n * sizeof(double));
     rc |= keep(e->d_I.p, e->d_I.n * sizeof(int));
     rc |= keep(e->d_ring.p, e->d_ring.n * sizeof(unsigned));
     rc |= keep(e->d_spikes.p, e->d_spikes.n * sizeof(unsigned long long));
@@ -1802,6 +1816,7 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
             tt.interp = N.interp;
             tt.has_cd = N.has_cd;
             tt.nscratch = N.nscratch;
+            tt.sym = !N.sym.empty();
             keys[N.key] = (int)types.size();
             types.push_back(tt);
             parents.push_back(N.parent);
@@ -2166,6 +2181,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         if (tt.wide)
             return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
                             "gbh_loss_gradient: create the engine with wide_min < 0 (one neuron per lane)");
+        if (tt.sym)
+            return fail_err(nullptr, GBH_ERR_UNSUPPORTED,
+                            "gbh_loss_gradient: symmetric compartments are not differentiated");
         AdjType &at = atypes[ti];
         at.nslots = tt.nslots;
         at.snap_off = (int)snap_field.size();
@@ -2513,7 +2531,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_A.release(); e->d_B.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_A.release(); e->d_B.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

@@ -68,6 +68,22 @@ enum PoolOp {
     PO_DIFF = 12      // ms w nfix crank sbase nq nb, ms*w rows p, nq rows f, nb rows f
 };
 
+// Elimination program of a solver with symmetric compartments: the funcs[]
+// tokens of do_euler_hsolve / do_crank_hsolve (hines_solve.c:140-296) as
+// triples {token, a, b} with the ravals cursor resolved into an index.
+//   forward:  SY_ELIM   row ra   temp = rav[ra] / diag[row]; diag -= rav[ra+1] temp;
+//                                rhs -= rhs[row] temp
+//             SY_SET / SY_SKIP   store the current row, move on by 1 / 2 rows
+//             SY_FASTSIB dst ra  rav[dst] -= rav[ra] temp
+//             SY_COPY  dst ra    rav[dst] = rav[ra]
+//             SY_SIB   src dst   rav[dst] -= rav[src] temp
+//   backward: SY_ELIM  row ra    rhs -= rav[ra] x[row]
+//             SY_CALC            solve the current row, move down one row
+//             SY_SIB   src row   rhs -= rav[src] x[row]
+//   SY_FINISH ends each pass.
+enum SymOp { SY_ELIM = 0, SY_SET = 1, SY_SKIP = 2, SY_FASTSIB = 3, SY_COPY = 4, SY_SIB = 5, SY_CALC = 6,
+             SY_FINISH = 7 };
+
 // Lanes per tile: one neuron per lane of a warp.
 constexpr int LANES = 32;
 
@@ -101,6 +117,9 @@ struct TileType {
     int wide;        // one neuron per tile, its compartments across a block's threads
     int wide_off;    // wide: prog-pool offset of [slot program offsets | previous NEWVOLT slot |
                      //        previous NEWCONC1 slot | NEWCONC1 conc row], nslots each
+    int sym;         // symmetric compartments: the solver's funcs program runs as written
+    int sym_off;     // sym: prog-pool offset of its decoded triples (SymOp)
+    int nrav;        // sym: ravals rows (rewritten during each step, as in the reference)
 };
 
 struct Tile {
@@ -115,6 +134,7 @@ struct Tile {
     int64_t syn;     // event-ring rows (nsyn * ring_len)
     int64_t scr;     // diffusion scratch rows (nscratch)
     int64_t wtop;    // wide: offset into DevView::wtop of its elimination schedule
+    int64_t rav;     // sym: ravals rows (nrav)
     int64_t first_neuron; // global neuron index of lane 0
 };
 

@@ -511,7 +511,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                        const std::vector<int> *uniform_parent, int min_blocks, bool compact, bool smem_rows,
                        int warps)
 {
-    if (tt.has_cd || tt.nscratch) return std::string();   // diffusion systems: interpreted
+    if (tt.has_cd || tt.nscratch || tt.sym) return std::string();   // diffusion, symmetric: interpreted
     if (compact) uniform_parent = nullptr;   // rows in shared-memory columns, looped elimination
     const bool cols = !uniform_parent || smem_rows;   // D/R rows in shared-memory columns
     Emit E;

@@ -446,6 +446,9 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
         }
 
         // ---------------- elimination ----------------
+        if (ty.sym) {
+            sym_eliminate<LANES>(v.prog + ty.sym_off, Rcol, Dcol, v.RV + tl.rav * LANES + lane, Vw, ty.crank != 0);
+        } else {
         for (int s = 0; s < S; ++s) {
             const int p = par[s * LANES];
             if (p >= 0) {
@@ -467,6 +470,7 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
             } else {
                 Vw[s * LANES] = r;
             }
+        }
         }
         // cooperative multi-step launch: every tile's events of this step
         // are in the rings before any tile starts the next step

@@ -394,7 +394,11 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
             }
         }
 
-        // elimination (FP64, one refined reciprocal per row)
+        // elimination (FP64, one refined reciprocal per row; symmetric
+        // compartments: the reference's program with its divisions)
+        if (ty.sym) {
+            sym_eliminate<LANES>(v.prog + ty.sym_off, Rcol, Dcol, v.RV + tl.rav * LANES + lane, Vw, ty.crank != 0);
+        } else {
         for (int s = 0; s < S; ++s) {
             const int p = par[s * LANES];
             const double ri = rcp_newton(Dcol[s * LANES]);
@@ -417,6 +421,7 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
             } else {
                 Vw[s * LANES] = r;
             }
+        }
         }
         // cooperative multi-step launch: every tile's events of this step
         // are in the rings before any tile starts the next step

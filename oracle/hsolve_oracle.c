@@ -771,7 +771,7 @@ void orc_solve(orc_solver *s)
             else vmv[vrow] = rv;
             res[cur] = rv;
             cur -= 2;
-            rv = res[cur];
+            if (cur >= 0) rv = res[cur];   /* the reference reads one row below results[] here */
         } else if (op == F_SIB) {
             rv -= ra[f[fi]] * res[f[fi + 1]];
             fi += 2;

@@ -55,10 +55,12 @@ def test_storemode_is_rejected():
 
 
 @pytest.mark.parametrize("token", [3, 4, 5])
-def test_symmetric_compartment_elimination_is_rejected(token):
+def test_symmetric_token_with_index_out_of_range_is_rejected(token):
+    """Symmetric-compartment tokens are run as written; one whose ravals
+    index lies outside the solver's ravals[] is a funcs error."""
     h = A.solver([_hh(), _hh()], A.tables(12, 20), parents=[1, -1])
     f = list(h.funcs)
-    f.insert(0, token)
+    f[0:0] = [token, 10 ** 6] if token != 5 else [token, 0, 10 ** 6]
     h.funcs = np.array(f, np.int32)
     e = _err([h])
     assert e.code == -3 and e.opcode == token
