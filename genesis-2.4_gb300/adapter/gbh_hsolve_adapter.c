@@ -44,7 +44,8 @@ typedef struct gbh_hstate {
 static Hsolve *gbh_registry[GBH_MAX_SOLVERS];
 static int gbh_nreg = 0;
 
-static int gbh_fill_desc(Hsolve *h, gbh_batch_desc *d, gbh_tables *t, int *scalars, int64_t (*st)[2])
+static int gbh_fill_desc(Hsolve *h, gbh_batch_desc *d, gbh_tables *t, int *scalars /* [5] */,
+                         int64_t (*st)[2])
 {
     memset(d, 0, sizeof(*d));
     memset(t, 0, sizeof(*t));
@@ -62,6 +63,7 @@ static int gbh_fill_desc(Hsolve *h, gbh_batch_desc *d, gbh_tables *t, int *scala
     scalars[1] = h->chanmode;
     scalars[2] = h->calcmode;
     scalars[3] = 0;
+    scalars[4] = h->storemode;
     d->abi_version = GBH_ABI_VERSION;
     d->nsolvers = 1;
     d->dt = h->dt;
@@ -104,6 +106,12 @@ static int gbh_fill_desc(Hsolve *h, gbh_batch_desc *d, gbh_tables *t, int *scala
         d->bufvals_start = st[12];
         d->bufvals = h->bufvals;
     }
+    if (h->storemode && h->itotal) {   /* itotal[nelm_names] (hines_chip_init.c:753) */
+        st[13][0] = 0;
+        st[13][1] = h->nelm_names;
+        d->storemode = &scalars[4];
+        d->itotal_start = st[13];
+    }
     return 0;
 }
 
@@ -113,7 +121,7 @@ int gbh_init(Hsolve *h)
     gbh_tables t;
     gbh_options opt;
     gbh_error err;
-    int scalars[4];
+    int scalars[5];
     gbh_hstate *s;
     Iinfo *ii;
     int n, i;
@@ -199,6 +207,7 @@ int gbh_chip_update(Hsolve *h)
         return -1;
     }
     if (h->outinfo && gbh_get_state(s->e, h->vm, NULL, NULL, NULL) != GBH_OK) return -1;
+    if (h->outinfo && h->storemode && h->itotal && gbh_get_itotal(s->e, h->itotal) != GBH_OK) return -1;
     return 1;   /* vm is ready: hines.c skips the conc update and the CPU solve */
 }
 
@@ -206,6 +215,7 @@ void gbh_sync_chip(Hsolve *h)
 {
     gbh_hstate *s = (gbh_hstate *)h->accel_state;
     if (s) gbh_get_state(s->e, h->vm, h->chip, h->conc, h->ops);
+    if (s && h->storemode && h->itotal) gbh_get_itotal(s->e, h->itotal);
 }
 
 void gbh_cleanup(void)

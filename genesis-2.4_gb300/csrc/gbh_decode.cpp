@@ -298,6 +298,13 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         if (n <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "solver without compartments");
         if (cm != 4 && cm != 5) return fail(c, GBH_ERR_UNSUPPORTED, -1, cm, -1, "chanmode %d (engine runs 4 and 5)", cm);
         if (ts < 0 || ts >= d->ntables) return fail(c, GBH_ERR_ARG, -1, 0, -1, "table set %d out of range", ts);
+        // storemode: itotal is a sum over the whole solver, accumulated in row
+        // order (hines_chip.c:134-166, 314-322), so the solver stays one neuron
+        const int smode = d->storemode ? d->storemode[si] : 0;
+        const int64_t nelm = smode ? d->itotal_start[si + 1] - d->itotal_start[si] : 0;
+        if (smode < 0 || smode > 2) return fail(c, GBH_ERR_ARG, -1, 0, -1, "storemode %d (0, 1 or 2)", smode);
+        if (smode && (nelm < 1 || nelm > (1 << 20)))
+            return fail(c, GBH_ERR_ARG, -1, 0, -1, "storemode %d with %lld itotal entries", smode, (long long)nelm);
 
         // elimination structure
         std::vector<int> parent, ridx, symprog;
@@ -321,12 +328,13 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         // trees: parents always have higher rows (Hines numbering)
         std::vector<int> tree(n, -1);
         std::vector<int> tmin, tmax;
-        if (sym) {
+        const bool whole = sym || smode;   // one neuron holds every row of the solver
+        if (whole) {
             tree.assign(n, 0);
             tmin.push_back(0);
             tmax.push_back(n - 1);
         }
-        for (int r = n - 1; r >= 0 && !sym; --r) {
+        for (int r = n - 1; r >= 0 && !whole; --r) {
             if (parent[r] < 0) {
                 tree[r] = (int)tmin.size();
                 tmin.push_back(r);
@@ -369,6 +377,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                 nn.sym = symprog;
                 nn.rav.assign(d->ravals + d->ravals_start[si], d->ravals + d->ravals_start[si + 1]);
             }
+            nn.nitot = (int)nelm;
             tree_neuron[order[k]] = nbase + k;
             out.neurons.push_back(std::move(nn));
         }
@@ -402,6 +411,12 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             P.push_back(nb.fld(FS_CHIP, ch + 1, chip[ch + 1]));
             P.push_back(nb.fld(FS_GIV, g, giv[g]));
             P.push_back(nb.giv(g + 1));
+            if (smode == 1) {   // itotal[0] += leak current (hines_chip.c:166)
+                P.push_back(M_ITLEAK);
+                P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
+                P.push_back(nb.fld(FS_GIV, g, giv[g]));
+                P.push_back(0);
+            }
             ch += 2;
             g += 2;
             auto sel_pool = [&](int64_t at) -> int {
@@ -487,9 +502,18 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                     break;
                 }
                 case R_STORE_ALLI:
-                case R_STORE_ALLC:
-                    return fail(c, GBH_ERR_UNSUPPORTED, row, code, o - 1,
-                                "storemode (itotal accumulation) is not supported by the engine");
+                case R_STORE_ALLC: {   // itotal[k] += Ik / Gk (hines_chip.c:314-322)
+                    if (!need(1)) return fail(c, GBH_ERR_OPCODE, row, code, o, "truncated STORE_ALL op");
+                    const int k = ops[o++];
+                    if (!smode)
+                        return fail(c, GBH_ERR_ARG, row, code, o - 2, "STORE_ALL op in a solver without storemode");
+                    if (k < 0 || k >= nelm)
+                        return fail(c, GBH_ERR_ARG, row, code, o - 1, "itotal index %d out of range", k);
+                    P.push_back(M_STORE);
+                    P.push_back(code == R_STORE_ALLI ? 0 : 1);
+                    P.push_back(k);
+                    break;
+                }
                 case R_GHK:
                 case R_NERNST: {
                     int p = sel_pool(o - 1);
@@ -907,7 +931,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             put(N.nrows); put(N.table_set); put(N.crank); put(N.c5); put(N.interp);
             put((int)N.fsrc.size()); put((int)N.iops.size()); put((int)N.pool_conc.size());
             put((int)N.giv_ref.size()); put((int)N.syn_op.size()); put(N.spike_op >= 0);
-            put(N.has_cd); put(N.nscratch);
+            put(N.has_cd); put(N.nscratch); put(N.nitot);
             put((int)N.prog.size());
             for (int v : N.prog) put(v);
             put((int)N.sym.size());

@@ -40,6 +40,7 @@ struct Neuron {
     int spike_op = -1;
     bool has_cd = false;          // diffusion systems: codiag/coresult rows in use
     int nscratch = 0;             // scratch rows of its diffusion solves
+    int nitot = 0;                // storemode: itotal rows (the solver's nelm_names)
     std::string key;              // grouping signature
 };
 

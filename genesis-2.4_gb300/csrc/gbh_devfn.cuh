@@ -48,8 +48,9 @@ struct DevView {
     double *CR, *CD, *S;
     // wide tiles (one neuron per block): per-tile elimination schedules
     const int *wtop;
-    // ravals rows of the solvers with symmetric compartments
-    double *RV;
+    // ravals rows of the solvers with symmetric compartments; itotal rows
+    // of the storemode solvers
+    double *RV, *IT;
     // Per-step host I/O inside a multi-step launch of the specialised kernels
     // (gbh_run_io): io_in[k * io_nin + i] is input i of step io_step0 + k and
     // io_out likewise. Per tile, tin_* list (offset in the tile's field block,

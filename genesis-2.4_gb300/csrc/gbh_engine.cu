@@ -99,7 +99,7 @@ struct gbh_engine {
     std::vector<TileType> types;
     std::vector<Tile> tiles;
     std::vector<int> neuron_tile, neuron_lane;   // placement of every neuron
-    std::vector<int64_t> chip_start, conc_start, ops_start, vm_start, giv_start, rav_start;
+    std::vector<int64_t> chip_start, conc_start, ops_start, vm_start, giv_start, rav_start, itot_start;
     std::vector<double> chip_orig;              // reference chip[] for sync copies
     std::vector<int> ops_orig;
     int64_t ngiv_total = 0;
@@ -116,6 +116,7 @@ struct gbh_engine {
     DBuf<double> d_CR, d_CD, d_S;   // coresult / codiag rows, diffusion scratch
     DBuf<int> d_wtop;               // elimination schedules of wide tiles
     DBuf<double> d_RV;              // ravals rows of solvers with symmetric compartments
+    DBuf<double> d_IT;              // itotal rows of storemode solvers
     DBuf<int> d_I, d_par;
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
@@ -134,7 +135,7 @@ struct gbh_engine {
     DBuf<int> d_status;
     int ring_len = 2;
     int64_t rows_fld = 0, rows_int = 0, rows_pool = 0, rows_giv = 0, rows_vm = 0, rows_topo = 0,
-            rows_syn = 0, rows_scr = 0, rows_rav = 0;
+            rows_syn = 0, rows_scr = 0, rows_rav = 0, rows_itot = 0;
     std::vector<Launch> launches;
     int steps_per_launch = 1;
     bool has_network = false;
@@ -229,7 +230,7 @@ int micro_operands(int code)
     case M_CONCVAL: case M_DOMAIN: case M_NEWCONC2: case M_SCALE_FLUX: case M_SAME_GHK:
     case M_CHAN_G: case M_ADDCURR: return 1;
     case M_NERNST: case M_CHAN: case M_STORE: return 2;
-    case M_SPIKE: case M_GHK: case M_END: return 3;
+    case M_SPIKE: case M_GHK: case M_END: case M_ITLEAK: return 3;
     case M_ELMMPUMP: case M_GATE: case M_MGBLOCK: return 4;
     case M_SYN: return 6;
     default: return -1;
@@ -348,7 +349,7 @@ bool wide_plan(const std::vector<int> &prog, const TileType &tt, std::vector<int
             if (n < 0) return false;
             const int *o = &prog[pc + 1];
             switch (code) {
-            case M_DOMAIN: case M_NEWCONC2: case M_SAME_GHK: case M_DO_TABGHK: case M_STORE:
+            case M_DOMAIN: case M_NEWCONC2: case M_SAME_GHK: case M_DO_TABGHK: case M_STORE: case M_ITLEAK:
                 return false;
             case M_CONCVAL: sel = true; selrow = o[0]; break;
             case M_NEWVOLT: if (++nv > 1) return false; break;
@@ -458,6 +459,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 prog_pool.insert(prog_pool.end(), N.sym.begin(), N.sym.end());
                 tt.nrav = (int)N.rav.size();
             }
+            tt.nitot = N.nitot;
             type_of_key[N.key] = (int)e->types.size();
             e->types.push_back(tt);
             members.emplace_back();
@@ -474,7 +476,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         // cables ran 20 % slower one per warp than 32 per warp.
         for (size_t ti = 0; ti < e->types.size(); ++ti) {
             TileType &tt = e->types[ti];
-            const bool by_size = tt.nslots >= (e->opt.wide_min > 0 ? e->opt.wide_min : 32) && !tt.sym;
+            const bool by_size = tt.nslots >= (e->opt.wide_min > 0 ? e->opt.wide_min : 32) && !tt.sym && !tt.nitot;
             std::vector<int> meta;
             if (by_size && wide_plan(prog_pool, tt, meta)) {
                 tt.wide = 1;
@@ -530,6 +532,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             t.syn = e->rows_syn; e->rows_syn += (int64_t)tt.nsyn * e->ring_len;
             t.scr = e->rows_scr; e->rows_scr += rows_of(tt.nscratch, w);
             t.rav = e->rows_rav; e->rows_rav += rows_of(tt.nrav, w);
+            t.itot = e->rows_itot; e->rows_itot += rows_of(tt.nitot, w);
             t.first_neuron = gneuron;
             gneuron += LANES;
             if (w) {
@@ -732,6 +735,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_F.upload(std::vector<double>(C.size(), 0.0));
     rc |= e->d_wtop.upload(wtop.empty() ? std::vector<int>(1, 0) : wtop);
     rc |= e->d_RV.upload(RV);
+    rc |= e->d_IT.upload(std::vector<double>(std::max<int64_t>(e->rows_itot, 1) * L, 0.0));
     bool any_cd = false;
     for (const TileType &tt : e->types) any_cd = any_cd || tt.has_cd;
     if (any_cd) {   // coresult 0, codiag 1 (hines_conc_init.c:121-126), solve scratch
@@ -773,7 +777,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         // the looped forms keep 2 x nslots x 32 rows per warp in shared memory:
         // 4-warp blocks of more than 96 compartments would not fit
         for (int ti : torder)
-            if (type_t0[ti] >= 0 && !e->types[ti].wide && !e->types[ti].sym && e->types[ti].nslots <= 96)
+            if (type_t0[ti] >= 0 && !e->types[ti].wide && !e->types[ti].sym && !e->types[ti].nitot &&
+                e->types[ti].nslots <= 96)
                 cand.push_back(ti);
         std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) {
             return (type_t1[a] - type_t0[a]) > (type_t1[b] - type_t0[b]);
@@ -917,6 +922,7 @@ DevView view_of(gbh_engine *e)
     v.F = e->d_F.p;
     v.wtop = e->d_wtop.p;
     v.RV = e->d_RV.p;
+    v.IT = e->d_IT.p;
     v.CR = e->d_CR.p;
     v.CD = e->d_CD.p;
     v.S = e->d_S.p;
@@ -1817,6 +1823,7 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
             tt.has_cd = N.has_cd;
             tt.nscratch = N.nscratch;
             tt.sym = !N.sym.empty();
+            tt.nitot = N.nitot;
             keys[N.key] = (int)types.size();
             types.push_back(tt);
             parents.push_back(N.parent);
@@ -1897,6 +1904,8 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
     e->ops_start.assign(desc->ops_start, desc->ops_start + ns + 1);
     e->vm_start.assign(desc->vm_start, desc->vm_start + ns + 1);
     e->giv_start.assign(desc->givals_start, desc->givals_start + ns + 1);
+    if (desc->storemode) e->itot_start.assign(desc->itotal_start, desc->itotal_start + ns + 1);
+    else e->itot_start.assign(ns + 1, 0);
     e->rav_start.assign(desc->ravals_start, desc->ravals_start + ns + 1);
     e->chip_orig.assign(desc->chip, desc->chip + desc->chip_start[ns]);
     e->ops_orig.assign(desc->ops, desc->ops + desc->ops_start[ns]);
@@ -2094,6 +2103,23 @@ int gbh_get_givals(gbh_engine *e, double *givals)
         const bool w = e->types[t.type].wide != 0;
         for (size_t r = 0; r < N.giv_ref.size(); ++r)
             givals[e->giv_start[N.solver] + N.giv_ref[r]] = Gv[at(t.giv, r, l, w)];
+    }
+    return GBH_OK;
+}
+
+int gbh_get_itotal(gbh_engine *e, double *itotal)
+{
+    if (!e || !itotal) return GBH_ERR_ARG;
+    if (e->rows_itot == 0) return GBH_OK;
+    const size_t L = LANES;
+    CK(cudaStreamSynchronize(e->stream));
+    std::vector<double> It(e->rows_itot * L);
+    CK(cudaMemcpy(It.data(), e->d_IT.p, It.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < e->dec.neurons.size(); ++i) {
+        const Neuron &N = e->dec.neurons[i];
+        const Tile &t = e->tiles[e->neuron_tile[i]];
+        const int l = e->neuron_lane[i];
+        for (int k = 0; k < N.nitot; ++k) itotal[e->itot_start[N.solver] + k] = It[at(t.itot, k, l, false)];
     }
     return GBH_OK;
 }
@@ -2531,7 +2557,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_A.release(); e->d_B.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

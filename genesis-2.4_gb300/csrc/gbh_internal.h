@@ -45,8 +45,9 @@ enum MicroOp {
     M_SYN,           // fFreq stab sRow fX fY fWdt                      (SYN2/SYN3)
     M_MGBLOCK,       // fKA fKBinv fCMg gOut                            (after M_SYN)
     M_ADDCURR,       // gOut
-    M_STORE,         // kind(0 I, 1 G) name                              (storemode itotal)
-    M_END            // fTbyc fDiag gIm
+    M_STORE,         // kind(0 I, 1 G) k                                 (itotal[k] += Ik / Gk)
+    M_END,           // fTbyc fDiag gIm
+    M_ITLEAK         // fEmRm fRm k                                      (itotal[k] += leak current)
 };
 enum GateKind { GK_1V = 0, GK_1C = 1, GK_2V = 2, GK_2C = 3 };
 // Pool-phase micro-ops (do_h4_conc_chip_update, hines_conc_chip.c:59-221, and
@@ -120,6 +121,7 @@ struct TileType {
     int sym;         // symmetric compartments: the solver's funcs program runs as written
     int sym_off;     // sym: prog-pool offset of its decoded triples (SymOp)
     int nrav;        // sym: ravals rows (rewritten during each step, as in the reference)
+    int nitot;       // storemode: itotal rows, zeroed at the start of every step
 };
 
 struct Tile {
@@ -135,6 +137,7 @@ struct Tile {
     int64_t scr;     // diffusion scratch rows (nscratch)
     int64_t wtop;    // wide: offset into DevView::wtop of its elimination schedule
     int64_t rav;     // sym: ravals rows (nrav)
+    int64_t itot;    // storemode: itotal rows (nitot)
     int64_t first_neuron; // global neuron index of lane 0
 };
 

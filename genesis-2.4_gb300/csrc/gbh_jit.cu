@@ -149,7 +149,7 @@ int nops_of(int code)
     case M_CONCVAL: case M_DOMAIN: case M_NEWCONC2: case M_SCALE_FLUX: case M_SAME_GHK:
     case M_CHAN_G: case M_ADDCURR: return 1;
     case M_NERNST: case M_CHAN: case M_STORE: return 2;
-    case M_SPIKE: case M_GHK: case M_END: return 3;
+    case M_SPIKE: case M_GHK: case M_END: case M_ITLEAK: return 3;
     case M_ELMMPUMP: case M_GATE: case M_MGBLOCK: return 4;
     case M_SYN: return 6;
     default: return -1;
@@ -511,7 +511,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                        const std::vector<int> *uniform_parent, int min_blocks, bool compact, bool smem_rows,
                        int warps)
 {
-    if (tt.has_cd || tt.nscratch || tt.sym) return std::string();   // diffusion, symmetric: interpreted
+    if (tt.has_cd || tt.nscratch || tt.sym || tt.nitot)   // diffusion, symmetric, storemode: interpreted
+        return std::string();
     if (compact) uniform_parent = nullptr;   // rows in shared-memory columns, looped elimination
     const bool cols = !uniform_parent || smem_rows;   // D/R rows in shared-memory columns
     Emit E;

@@ -66,7 +66,7 @@ __device__ __forceinline__ void chan_state_reset(ChanState &cs, int ncols)
 struct ChanRows {
     double *P;
     int *I;
-    double *C, *F, *G, *CD;
+    double *C, *F, *G, *CD, *IT;
     unsigned *ring;
     int64_t neuron;
     bool active;
@@ -164,7 +164,11 @@ __device__ __forceinline__ bool chan_compartment(const DevView &v, const ChanEnv
             N.F[(sel) * STR] += N.P[(pc[1]) * STR] * Ik;
             pc += 2;
         } else if (code == M_STORE) {
-            pc += 3;  // itotal accumulation is host-visible only; rejected at setup
+            N.IT[pc[2] * STR] += pc[1] ? Gk : Ik;
+            pc += 3;
+        } else if (code == M_ITLEAK) {
+            N.IT[pc[3] * STR] += N.P[(pc[1]) * STR] - Vm / N.P[(pc[2]) * STR];
+            pc += 4;
         } else if (code == M_END) {
             const double tbyc = N.P[(pc[1]) * STR];
             R = Vm + ichan * tbyc;
@@ -407,12 +411,14 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
     NR.F = Fw;
     NR.G = Gw;
     NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.IT = v.IT + tl.itot * LANES + lane;
     NR.ring = v.ring + tl.syn * LANES + lane;
     NR.neuron = neuron;
     NR.active = active;
 
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
+        for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
         // ---------------- channel phase ----------------
         ChanState cs;
         chan_state_reset(cs, tg.ncols);
@@ -599,6 +605,7 @@ k_wide(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
     NR.F = v.F + tl.pools * LANES;
     NR.G = v.giv + tl.giv * LANES;
     NR.CD = v.CD ? v.CD + tl.pools * LANES : nullptr;
+    NR.IT = nullptr;   // storemode types never run wide
     NR.ring = v.ring + tl.syn * LANES;
     NR.neuron = tl.first_neuron;
     NR.active = true;

@@ -134,7 +134,11 @@ __device__ __forceinline__ bool chan_compartment_df(const DevView &v, const Chan
             N.F[(sel) * STR] += N.P[(pc[1]) * STR] * Ik;
             pc += 2;
         } else if (code == M_STORE) {
+            N.IT[pc[2] * STR] += pc[1] ? df2d(Gk) : Ik;
             pc += 3;
+        } else if (code == M_ITLEAK) {
+            N.IT[pc[3] * STR] += df2d(ld_df(&N.P[(pc[1]) * STR])) - Vm / N.P[(pc[2]) * STR];
+            pc += 4;
         } else if (code == M_END) {
             const df tbyc = ld_df(&N.P[(pc[1]) * STR]);
             const df dv = df_mul(ichan, tbyc);
@@ -357,12 +361,14 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
     NR.F = Fw;
     NR.G = Gw;
     NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.IT = v.IT + tl.itot * LANES + lane;
     NR.ring = v.ring + tl.syn * LANES + lane;
     NR.neuron = neuron;
     NR.active = active;
 
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
+        for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
         ChanStateDF cs;
         chan_state_reset_df(cs);
         const int *pc = v.prog + ty.prog_off;
@@ -475,6 +481,7 @@ k_wide_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long st
     NR.F = v.F + tl.pools * LANES;
     NR.G = v.giv + tl.giv * LANES;
     NR.CD = v.CD ? v.CD + tl.pools * LANES : nullptr;
+    NR.IT = nullptr;   // storemode types never run wide
     NR.ring = v.ring + tl.syn * LANES;
     NR.neuron = tl.first_neuron;
     NR.active = true;

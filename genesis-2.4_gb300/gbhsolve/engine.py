@@ -22,7 +22,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_int64)
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 PREC_FP64, PREC_MIXED = 0, 1
 IN_SET, IN_ADD, IN_FLUX = 0, 1, 2     # gbh_register_inputs_typed kinds
 
@@ -54,7 +54,7 @@ class GbhBatchDesc(C.Structure):
                 ("concchip_start", _lp), ("concchip", _dp),
                 ("diff_start", _lp), ("dconc", _ip), ("nshells", _ip), ("nshrows", _ip), ("nshfix", _ip),
                 ("fbufval", _ip), ("covals0_start", _lp), ("covals0", _dp), ("bufvals_start", _lp),
-                ("bufvals", _dp)]
+                ("bufvals", _dp), ("storemode", _ip), ("itotal_start", _lp)]
 
 
 class GbhSynapses(C.Structure):
@@ -91,7 +91,7 @@ EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
             "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync", "gbh_run_io",
-            "gbh_register_inputs_typed"]
+            "gbh_register_inputs_typed", "gbh_get_itotal"]
 
 _LIB = None
 
@@ -254,6 +254,12 @@ class Batch:
                 setattr(d, k, _ptr(getattr(self, k), _ip))
             d.covals0_start, d.covals0 = _ptr(self.covals0_start, _lp), _ptr(self.covals0, _dp)
             d.bufvals_start, d.bufvals = _ptr(self.bufvals_start, _lp), _ptr(self.bufvals, _dp)
+        # storemode (optional `storemode` / `nelm_names` on a solver)
+        self.storemode = np.array([int(getattr(s, "storemode", 0)) for s in self.solvers], dtype=np.int32)
+        nelm = [int(getattr(s, "nelm_names", 0)) if m else 0 for s, m in zip(self.solvers, self.storemode)]
+        self.itotal_start = np.concatenate([[0], np.cumsum(nelm)]).astype(np.int64)
+        if self.storemode.any():
+            d.storemode, d.itotal_start = _ptr(self.storemode, _ip), _ptr(self.itotal_start, _lp)
         self.desc = d
         self.syn = None
         if synapses is not None:
@@ -387,6 +393,13 @@ class Engine:
         g = np.array(b.givals, copy=True)
         self._check(self.lib.gbh_get_givals(self.h, _ptr(g, _dp)))
         return b.split(g, b.givals_start)
+
+    def itotal(self):
+        """gbh_get_itotal: hsolve->itotal of every solver (empty for storemode 0)."""
+        b = self.batch
+        t = np.zeros(max(int(b.itotal_start[-1]), 1))
+        self._check(self.lib.gbh_get_itotal(self.h, _ptr(t, _dp)))
+        return b.split(t, b.itotal_start)
 
     def register_inputs(self, solver, chip_index, kind=None, sa=None, sb=None):
         """Inputs of h_in_msgs: kind IN_SET (chip[index] = v, the default),

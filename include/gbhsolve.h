@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define GBH_ABI_VERSION 2
+#define GBH_ABI_VERSION 3
 
 /* precision of gate/table arithmetic (elimination, Vm and Ca are always FP64) */
 #define GBH_PREC_FP64 0
@@ -98,6 +98,13 @@ typedef struct gbh_batch_desc {
     const int *dconc, *nshells, *nshrows, *nshfix, *fbufval;
     const int64_t *covals0_start; const double *covals0;
     const int64_t *bufvals_start; const double *bufvals;
+    /* storemode (hsolve->storemode, hines_chip.c:134-166, 314-322): per
+     * solver 0 (off), 1 (each compartment's leak current and the currents
+     * of the STORE_ALLI_OP children) or 2 (the conductances of the
+     * STORE_ALLC_OP children), summed over the solver every step into
+     * itotal[nelm_names] (gbh_get_itotal). storemode NULL = 0 everywhere. */
+    const int *storemode;          /* [nsolvers] */
+    const int64_t *itotal_start;   /* [nsolvers+1]: nelm_names of each solver */
 } gbh_batch_desc;
 
 /*
@@ -256,6 +263,14 @@ int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const dou
  */
 int gbh_enable_givals(gbh_engine *e, int enable);
 int gbh_get_givals(gbh_engine *e, double *givals);
+
+/*
+ * Copies hsolve->itotal of every storemode solver after the last completed
+ * step (layout itotal_start; solvers with storemode 0 are left untouched).
+ * Replaces the host reads of hsolve->itotal (hines.c:285-290, element field
+ * `itotal`).
+ */
+int gbh_get_itotal(gbh_engine *e, double *itotal);
 
 /*
  * Per-step inputs and outputs, the engine side of h_in_msgs / h_out_msgs

@@ -133,7 +133,8 @@ class Solver:
         s.ops, s.chip, s.funcs = _p(self.ops, _ip), _p(self.chip, _dp), _p(self.funcs, _ip)
         s.ravals, s.results, s.vm = _p(self.ravals, _dp), _p(self.results, _dp), _p(self.vm, _dp)
         s.givals = _p(self.givals, _dp)
-        s.chanmode, s.calcmode, s.storemode = h.chanmode, h.calcmode, 0
+        s.chanmode, s.calcmode = h.chanmode, h.calcmode
+        s.storemode = int(getattr(h, "storemode", 0))
         s.crank, s.dt = h.crank, h.dt
         s.ncols, s.xdivs, s.ydivs = h.ncols, h.xdivs, h.ydivs
         s.xmin, s.invdx, s.ymin, s.invdy = h.xmin, h.invdx, h.ymin, h.invdy
@@ -167,8 +168,10 @@ class Solver:
         else:
             s.ndiffs = 0
         s.nconcchips_used = 1 if len(self.concchip) else 0
-        s.itotal = C.cast(0, _dp)
-        s.nelm_names = 0
+        # storemode: itotal[nelm_names] summed every step (hines_chip.c:134-166)
+        self.itotal = np.zeros(max(int(getattr(h, "nelm_names", 0)), 1))
+        s.itotal = _p(self.itotal, _dp) if s.storemode else C.cast(0, _dp)
+        s.nelm_names = int(getattr(h, "nelm_names", 0)) if s.storemode else 0
         s.childops, s.childchips = _p(self.childops, _ip), _p(self.childchips, _ip)
         self.s = s
 

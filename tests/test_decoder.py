@@ -47,11 +47,11 @@ def test_unknown_conductance_opcode_is_rejected():
     assert e.code == -2 and e.opcode == 4099
 
 
-def test_storemode_is_rejected():
+def test_store_op_without_storemode_is_rejected():
     c = _hh()
     c.op(A.STORE_ALLI, 0)
     e = _err([A.solver([c], A.tables(12, 20))])
-    assert e.code == -6 and e.opcode == A.STORE_ALLI
+    assert e.code == -1 and e.opcode == A.STORE_ALLI
 
 
 @pytest.mark.parametrize("token", [3, 4, 5])
