@@ -433,7 +433,11 @@ def main():
     M = args.neurons * NCOMP
     results = {}
     for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
+        # engine setup: descriptor packing, decode (threaded over solvers),
+        # layout, upload, specialisation (NVRTC) and autotuning
+        tc = time.perf_counter()
         eng = engine.Engine(hs, precision=prec, steps_per_launch=args.steps_per_launch, device=local)
+        setup_s = time.perf_counter() - tc
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -445,11 +449,13 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             ms = float(t.item())
         results[form] = dict(ms=ms, launches=launches, spl=st.steps_per_launch,
-                             value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng)
+                             value=M * ws * args.steps / (ms / 1e3), clocks=clk.summary(), eng=eng,
+                             setup_s=setup_s)
         log("%s: %.3f ms for %d steps, %d launches, %d specialised kernels (min blocks %d, %s form),"
-            " %d steps/launch -> %.3e cs/s" % (form, ms, args.steps, launches, st.jit_kernels, st.jit_min_blocks,
-                                               ["unrolled", "compact", "unrolled/shared-rows"][st.jit_compact],
-                                               st.steps_per_launch, results[form]["value"]))
+            " %d steps/launch -> %.3e cs/s (engine setup %.2f s)"
+            % (form, ms, args.steps, launches, st.jit_kernels, st.jit_min_blocks,
+               ["unrolled", "compact", "unrolled/shared-rows"][st.jit_compact], st.steps_per_launch,
+               results[form]["value"], setup_s))
         if form == "fp64":
             eng.close()
 
@@ -579,8 +585,9 @@ def main():
                        "steps_per_launch": r["spl"], "autotuned": args.steps_per_launch == 0,
                        "l2": "state 1.6M compartments > L2, no flush"},
             "forms": {"fp64": {"value": results["fp64"]["value"], "ms_per_step": results["fp64"]["ms"] / args.steps,
-                               "dtype": "f64"},
+                               "dtype": "f64", "engine_setup_s": results["fp64"]["setup_s"]},
                       "mixed": {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
+                                "engine_setup_s": r["setup_s"],
                                 "max_abs_dvm_vs_fp64_oracle_V": acc, "accuracy_steps": ACC_STEPS,
                                 "spike_time_max_dev_s": spk_dev, "spikes_compared": nspk,
                                 "spike_count_mismatches": spk_mismatch,

@@ -17,7 +17,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <functional>
 #include <map>
+#include <thread>
 #include <unordered_map>
 
 namespace gbh {
@@ -272,20 +275,31 @@ int parse_funcs(Ctx &c, const int *f, int64_t nf, const double *ra, int64_t nra,
     return GBH_OK;
 }
 
-}  // namespace
-
-int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
+// Grouping key: everything the kernel's control flow depends on.
+void make_key(Neuron &N)
 {
-    Ctx c{d, err, -1};
-    if (!d || d->abi_version != GBH_ABI_VERSION)
-        return fail(c, GBH_ERR_ARG, -1, 0, -1, "descriptor missing or ABI version mismatch");
-    if (d->nsolvers <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "no solvers");
-    out.neurons.clear();
-    out.stablist.clear();
-    out.solver_first_neuron.assign(d->nsolvers + 1, 0);
-    for (int si = 0; si < d->nsolvers; ++si) {
-        c.solver = si;
-        out.solver_first_neuron[si] = (int)out.neurons.size();
+    std::string key;
+    auto put = [&](int v) { key.append(reinterpret_cast<const char *>(&v), sizeof(int)); };
+    put(N.nrows); put(N.table_set); put(N.crank); put(N.c5); put(N.interp);
+    put((int)N.fsrc.size()); put((int)N.iops.size()); put((int)N.pool_conc.size());
+    put((int)N.giv_ref.size()); put((int)N.syn_op.size()); put(N.spike_op >= 0);
+    put(N.has_cd); put(N.nscratch); put(N.nitot);
+    put((int)N.prog.size());
+    for (int v : N.prog) put(v);
+    put((int)N.sym.size());
+    for (int v : N.sym) put(v);
+    put((int)N.rav.size());
+    for (int v : N.pool_prog) put(v);
+    N.key = std::move(key);
+}
+
+// Decodes solver si into neurons (appended); synchan constant sets go to
+// stabs (deduplicated within it), their indices recorded in Neuron::stab_pos.
+int decode_solver(const gbh_batch_desc *d, int si, std::vector<Neuron> &neurons, std::vector<double> &stabs,
+                  gbh_error *err)
+{
+    Ctx c{d, err, si};
+    {
         const int *ops = d->ops + d->ops_start[si];
         const int64_t nops = d->ops_start[si + 1] - d->ops_start[si];
         const double *chip = d->chip + d->chip_start[si];
@@ -356,7 +370,7 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             order[ntrees - 1 - t] = t;  // trees were found from the top row down
         }
         std::vector<int> tree_neuron(ntrees);
-        const int nbase = (int)out.neurons.size();
+        const int nbase = (int)neurons.size();
         for (int k = 0; k < ntrees; ++k) {
             Neuron nn;
             nn.solver = si;
@@ -379,10 +393,10 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             }
             nn.nitot = (int)nelm;
             tree_neuron[order[k]] = nbase + k;
-            out.neurons.push_back(std::move(nn));
+            neurons.push_back(std::move(nn));
         }
         std::vector<NB> nbs(ntrees);
-        for (int k = 0; k < ntrees; ++k) nbs[k].n = &out.neurons[nbase + k];
+        for (int k = 0; k < ntrees; ++k) nbs[k].n = &neurons[nbase + k];
 
         // ---- walk ops[] ----
         int64_t o = 0, ch = 0, g = 1;   // givals[0] is unused
@@ -631,14 +645,15 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
                         // of different solvers keep identical programs
                         const double *sv = d->stablist + d->stab_start[si] + stab;
                         int gstab = -1;
-                        for (size_t q = 0; q + 4 <= out.stablist.size(); q += 4)
-                            if (memcmp(&out.stablist[q], sv, 4 * sizeof(double)) == 0) { gstab = (int)q; break; }
+                        for (size_t q = 0; q + 4 <= stabs.size(); q += 4)
+                            if (memcmp(&stabs[q], sv, 4 * sizeof(double)) == 0) { gstab = (int)q; break; }
                         if (gstab < 0) {
-                            gstab = (int)out.stablist.size();
-                            out.stablist.insert(out.stablist.end(), sv, sv + 4);
+                            gstab = (int)stabs.size();
+                            stabs.insert(stabs.end(), sv, sv + 4);
                         }
                         P.push_back(M_SYN);
                         P.push_back(ffreq);
+                        N.stab_pos.push_back((int)P.size());
                         P.push_back(gstab);
                         P.push_back(srow);
                         P.push_back(nb.fld(FS_CHIP, ch, chip[ch], true));
@@ -923,25 +938,93 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
             }
         }
         for (int k = 0; k < ntrees; ++k) {
-            Neuron &N = *nbs[k].n;
-            N.pool_prog.push_back(0);
-            // grouping key: everything the kernel's control flow depends on
-            std::string key;
-            auto put = [&](int v) { key.append(reinterpret_cast<const char *>(&v), sizeof(int)); };
-            put(N.nrows); put(N.table_set); put(N.crank); put(N.c5); put(N.interp);
-            put((int)N.fsrc.size()); put((int)N.iops.size()); put((int)N.pool_conc.size());
-            put((int)N.giv_ref.size()); put((int)N.syn_op.size()); put(N.spike_op >= 0);
-            put(N.has_cd); put(N.nscratch); put(N.nitot);
-            put((int)N.prog.size());
-            for (int v : N.prog) put(v);
-            put((int)N.sym.size());
-            for (int v : N.sym) put(v);
-            put((int)N.rav.size());
-            for (int v : N.pool_prog) put(v);
-            N.key = std::move(key);
+            nbs[k].n->pool_prog.push_back(0);
+            make_key(*nbs[k].n);
         }
     }
-    out.solver_first_neuron[d->nsolvers] = (int)out.neurons.size();
+    return GBH_OK;
+}
+
+}  // namespace
+
+// Solvers are independent, so chunks of them decode on separate threads; the
+// chunks are then concatenated in solver order and their synchan constant
+// sets merged first-come (the indices a sequential pass would assign; the
+// programs and grouping keys of a chunk whose indices move are updated).
+// The first error in solver order is the one reported.
+int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
+{
+    Ctx c{d, err, -1};
+    if (!d || d->abi_version != GBH_ABI_VERSION)
+        return fail(c, GBH_ERR_ARG, -1, 0, -1, "descriptor missing or ABI version mismatch");
+    if (d->nsolvers <= 0) return fail(c, GBH_ERR_ARG, -1, 0, -1, "no solvers");
+    const int ns = d->nsolvers;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nchunk = std::max(1, std::min({(int)std::min(hw, 32u), ns / 256, ns}));
+    struct Chunk {
+        int s0 = 0, s1 = 0, rc = GBH_OK;
+        std::vector<Neuron> neurons;
+        std::vector<double> stab;
+        std::vector<int> first;   // neurons before each of its solvers
+        gbh_error err{};
+    };
+    std::vector<Chunk> ch(nchunk);
+    auto work = [&](Chunk &k) {
+        for (int si = k.s0; si < k.s1; ++si) {
+            k.first.push_back((int)k.neurons.size());
+            k.rc = decode_solver(d, si, k.neurons, k.stab, &k.err);
+            if (k.rc) return;
+        }
+    };
+    for (int i = 0; i < nchunk; ++i) {
+        ch[i].s0 = (int)((int64_t)ns * i / nchunk);
+        ch[i].s1 = (int)((int64_t)ns * (i + 1) / nchunk);
+    }
+    if (nchunk == 1) {
+        work(ch[0]);
+    } else {
+        std::vector<std::thread> th;
+        for (int i = 0; i < nchunk; ++i) th.emplace_back(work, std::ref(ch[i]));
+        for (auto &t : th) t.join();
+    }
+    out.neurons.clear();
+    out.stablist.clear();
+    out.solver_first_neuron.assign(ns + 1, 0);
+    size_t total = 0;
+    for (const Chunk &k : ch) {
+        if (k.rc) {
+            if (err) *err = k.err;
+            return k.rc;
+        }
+        total += k.neurons.size();
+    }
+    out.neurons.reserve(total);
+    for (Chunk &k : ch) {
+        std::vector<int> remap(k.stab.size() / 4);
+        bool moved = false;
+        for (size_t q = 0; q + 4 <= k.stab.size(); q += 4) {
+            int g = -1;
+            for (size_t r = 0; r + 4 <= out.stablist.size(); r += 4)
+                if (memcmp(&out.stablist[r], &k.stab[q], 4 * sizeof(double)) == 0) { g = (int)r; break; }
+            if (g < 0) {
+                g = (int)out.stablist.size();
+                out.stablist.insert(out.stablist.end(), k.stab.begin() + q, k.stab.begin() + q + 4);
+            }
+            remap[q / 4] = g;
+            moved = moved || g != (int)q;
+        }
+        const int base = (int)out.neurons.size();
+        for (int si = k.s0; si < k.s1; ++si) out.solver_first_neuron[si] = base + k.first[si - k.s0];
+        for (Neuron &N : k.neurons) {
+            if (moved && !N.stab_pos.empty()) {
+                for (int p : N.stab_pos) N.prog[p] = remap[N.prog[p] / 4];
+                make_key(N);
+            }
+            out.neurons.push_back(std::move(N));
+        }
+        std::vector<Neuron>().swap(k.neurons);
+    }
+    out.solver_first_neuron[ns] = (int)out.neurons.size();
     return GBH_OK;
 }
 

@@ -32,6 +32,7 @@ struct Neuron {
     std::vector<int> pool_conc;   // solver conc index of each pool row
     std::vector<int64_t> giv_ref; // solver givals index of each givals row
     std::vector<int> syn_op;      // solver ops index of each synchan row
+    std::vector<int> stab_pos;    // prog positions holding a stablist index
     std::vector<int> parent;      // per slot
     std::vector<double> A, B, C;  // per slot
     std::vector<int> ridx;        // per slot: ravals index of A, B, C (-1: none)

@@ -80,3 +80,39 @@ def test_error_names_the_solver():
     bad = A.solver([c], A.tables(12, 20))
     e = _err([good, good, bad])
     assert e.solver == 2
+
+
+def _syn_solver(order):
+    """One compartment with two synchans whose constant sets (stablist
+    entries 0 and 4 of its own stablist) are used in the given order."""
+    c = A.Compt(-2e-10, 1e-10, 2.0, 1.01, 3e8, -0.06)
+    for stab in order:
+        c.op(A.CHAN_EK, chips=[0.0, 1e-9]).op(A.SYN2, stab, -1, 1, chips=[0.4, 0.7], giv=3)
+    sa = [0.99, 9.5e-5, 0.98, 9.9e-5 / 2e-5]
+    sb = [0.95, 8.0e-5, 0.97, 9.0e-5 / 2e-5]
+    return A.solver([c], A.tables(12, 20), stablist=sa + sb)
+
+
+def test_parallel_decode_merges_synchan_constants():
+    """Large batches decode in chunks on several threads; the chunks'
+    synchan constant sets are renumbered into the batch's first-come order
+    and the programs regrouped. Solvers using the sets in opposite orders
+    are two program types however the batch is chunked."""
+    from gbhsolve import engine
+    n = 4096
+    hs = [_syn_solver([0, 4])] * (n // 2) + [_syn_solver([4, 0])] * (n // 2)
+    assert engine.validate(hs) == (n, 2)
+    assert engine.validate(hs[n // 2:]) == (n // 2, 1)
+
+
+def test_parallel_decode_reports_first_error_in_solver_order():
+    good = _syn_solver([0, 4])
+    bad = A.solver([_hh()], A.tables(12, 20))
+    bad.chip = bad.chip[:4]
+    worse = _syn_solver([0, 4])
+    worse.ops = worse.ops.copy()
+    worse.ops[1] = 7777
+    hs = [good] * 4096
+    hs[1500], hs[3900] = bad, worse
+    e = _err(hs)
+    assert e.solver == 1500 and e.code == -1
