@@ -13,7 +13,8 @@ step code.
 * The rest of each model (ops[], chip[], tables, pools) is what
   gbhsolve.model builds for the same cell; chip[]'s diagonal terms are
   replaced by the reference's symmetric ones.
-* shared/tablist, xvals, yvals: the channel tables, the same for every case.
+* shared/tablist, xvals, yvals: the channel tables of the HH cases; a case
+  with another channel mix carries its own (<case>/tablist ...).
 * vm_ref/chip_ref: after `nsteps` steps of do_chip_hh4_update +
   do_h4_conc_chip_update + do_euler_hsolve/do_crank_hsolve (oracle/_ref/
   libhsolve_ref.so).
@@ -43,20 +44,28 @@ SETUP_LIB = os.path.join(REPO, "oracle", "_ref", "libhsetup_ref.so")
 _HH = []
 
 
-def branched_cell(parents, seed, inject=0.3e-9, gk_dend=36.0, dend_len=20e-6, dia_range=(0.5e-6, 3e-6)):
-    """Soma (HH Na/K) plus dendrites on the given parent list, dendritic K
-    channel on every dendrite; diameters seeded. Every cell shares one pair
-    of channel types (one set of tables)."""
+def branched_cell(parents, seed, inject=0.3e-9, gk_dend=36.0, dend_len=20e-6, dia_range=(0.5e-6, 3e-6),
+                  with_ca=False):
+    """Soma (HH Na/K; with_ca: a Ca channel feeding a Ca_concen pool and a
+    Ca-dependent K channel) plus dendrites on the given parent list, dendritic
+    K channel on every dendrite; diameters seeded. Every cell shares the same
+    channel types (one set of tables per channel mix)."""
     rng = np.random.default_rng(seed)
     if not _HH:
         _HH.extend(configs.hh_channels(-0.065))
-    na, k = _HH
+        _HH.extend(configs.ca_channels())
+    na, k, ca, kca = _HH
     sli, PI = configs.sli, configs.PI
     sl, sd = 30e-6, 30e-6
     sa, sx = sl * PI * sd, PI * (sd / 2) ** 2
     s = model.Compartment(Em=sli(-0.065), Rm=sli(0.33 / sa), Cm=sli(0.01 * sa), Ra=sli(0.3 * sl / sx),
                           initVm=sli(-0.065), inject=sli(inject), parent=parents[0])
     s.children = [model.TabChannel(na, Gbar=sli(1200.0 * sa)), model.TabChannel(k, Gbar=sli(360.0 * sa))]
+    if with_ca:
+        B = 1.0 / (2 * 96485.3415 * sa * 0.1e-6)
+        s.children += [model.TabChannel(ca, Gbar=sli(40.0 * sa), flux_to=4),
+                       model.TabChannel(kca, Gbar=sli(100.0 * sa), conc_src=4),
+                       model.CaConcen(tau=0.02, B=B, Ca_base=5e-5, thick=0.1e-6)]
     out = [s]
     for c in range(1, len(parents)):
         dd = float(rng.uniform(*dia_range))
@@ -104,6 +113,9 @@ def cases():
     out.append(("sym_two_trees_euler", model.Model(two, dt=configs.sli(20e-6)), 300))
     t48 = configs.random_binary_tree(rng, 48)   # above the engine's one-neuron-per-warp threshold
     out.append(("sym_binary48_euler", model.Model(branched_cell(t48, 17, inject=0.6e-9), dt=configs.sli(20e-6)), 300))
+    t20 = configs.random_binary_tree(rng, 20)
+    out.append(("sym_binary20_ca_crank", model.Model(branched_cell(t20, 18, inject=0.8e-9, with_ca=True),
+                                                     dt=configs.sli(20e-6), method=model.CRANK), 400))
     return out
 
 
@@ -160,10 +172,11 @@ def main():
         for k in ("ops", "chip", "funcs", "ravals", "vm", "givals", "stablist",
                   "conc", "concops", "concchip", "childops", "childchips"):
             out[name + "/" + k] = np.asarray(getattr(h, k))
-        for k in ("tablist", "xvals", "yvals"):   # every case uses the same channel tables
-            if "shared/" + k in out:
-                assert np.array_equal(out["shared/" + k], getattr(h, k))
-            out["shared/" + k] = np.asarray(getattr(h, k))
+        for k in ("tablist", "xvals", "yvals"):   # stored once unless a case's channel mix differs
+            if "shared/" + k not in out:
+                out["shared/" + k] = np.asarray(getattr(h, k))
+            elif not np.array_equal(out["shared/" + k], getattr(h, k)):
+                out[name + "/" + k] = np.asarray(getattr(h, k))
         out[name + "/scalars"] = np.array([h.ncompts, h.ncols, h.xdivs, h.xmin, h.invdx, h.ydivs, h.ymin, h.invdy,
                                            h.dt, h.crank, h.chanmode, h.calcmode], dtype=np.float64)
         out[name + "/nsteps"] = np.array(nsteps)

@@ -32,12 +32,13 @@ def _load():
 
 def _case(d, name):
     g = lambda k: d[name + "/" + k]  # noqa: E731
+    t = lambda k: d[name + "/" + k] if name + "/" + k in d.files else d["shared/" + k]  # noqa: E731
     sc = g("scalars")
     return SimpleNamespace(
         ncompts=int(sc[0]), ops=g("ops"), chip=g("chip").copy(), funcs=g("funcs"), ravals=g("ravals").copy(),
         vm=g("vm").copy(), givals=g("givals"), ncols=int(sc[1]), xdivs=int(sc[2]), xmin=float(sc[3]),
-        invdx=float(sc[4]), tablist=d["shared/tablist"], xvals=d["shared/xvals"], ydivs=int(sc[5]),
-        ymin=float(sc[6]), invdy=float(sc[7]), yvals=d["shared/yvals"], stablist=g("stablist"), conc=g("conc"),
+        invdx=float(sc[4]), tablist=t("tablist"), xvals=t("xvals"), ydivs=int(sc[5]),
+        ymin=float(sc[6]), invdy=float(sc[7]), yvals=t("yvals"), stablist=g("stablist"), conc=g("conc"),
         concops=g("concops"), concchip=g("concchip"), childops=g("childops"), childchips=g("childchips"),
         dt=float(sc[8]), crank=int(sc[9]), chanmode=int(sc[10]), calcmode=int(sc[11]),
         method=11 if int(sc[9]) else 10)
@@ -58,7 +59,7 @@ def _cases_module():
 
 def test_fixtures_carry_symmetric_tokens():
     d = _load()
-    assert len(_names(d)) == 6
+    assert len(_names(d)) == 7
     for name in _names(d):
         toks = set(int(t) for t in d[name + "/funcs"])
         assert {3, 4, 5} <= toks, name
