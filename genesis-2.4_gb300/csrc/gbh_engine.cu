@@ -1252,6 +1252,7 @@ int autotune_trials(gbh_engine *e)
     }
     for (Save &s : saves) cudaFree(s.dst);
     if (e->d_spiked.p) CK(cudaMemset(e->d_spiked.p, 0, e->d_spiked.n * sizeof(unsigned)));   // trial spikes
+    if (e->rows_itot) CK(cudaMemset(e->d_IT.p, 0, e->d_IT.n * sizeof(double)));   // trial itotal sums
     for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
     e->jit_choice = best_v;
     e->steps_per_launch = best_s;

@@ -107,6 +107,7 @@ def test_engine_fp64_bitwise(oracle, gpu_engine, jit, crank):
     for k in range(6):
         hs.append(_solver(k % 3, TWO_TREES if k % 2 else CHAIN, seed=k, crank=crank))
     eng = gpu_engine.Engine(hs * 3, jit=jit, steps_per_launch=23)
+    assert all(not np.any(t) for t in eng.itotal())   # no step run yet
     eng.run(250)
     st = eng.get_state()
     it = eng.itotal()
