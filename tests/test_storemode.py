@@ -126,7 +126,8 @@ def test_engine_fp64_bitwise(oracle, gpu_engine, jit, crank):
 @pytest.mark.gpu
 def test_engine_mixed_within_tolerance(oracle, gpu_engine):
     hs = [_solver(1, CHAIN, seed=7), _solver(2, TWO_TREES, seed=8)]
-    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_MIXED)
+    eng = gpu_engine.Engine(hs, precision=gpu_engine.PREC_MIXED)   # autotuned: trial steps run here
+    assert all(not np.any(t) for t in eng.itotal())
     eng.run(300)
     it = eng.itotal()
     vm = eng.get_state()["vm"]
