@@ -308,10 +308,12 @@ def other_configs(device, n_trees=50_000):
            "drive": "inject U(0.05, 0.3) nA, seed 1"}
     for graph in (False, True):
         eng = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_FP64, device=device, use_graph=graph)
+        st = eng.stats()
         ms = rate(eng, 5000, 100)
         key = "graph" if graph else "launches"
         net[key] = {"ms": ms, "steps_per_s": 5000 / (ms / 1e3), "value": 4000 * 5000 / (ms / 1e3),
-                    "spikes": int(eng.spike_counts().sum())}
+                    "spikes": int(eng.spike_counts().sum()), "cooperative": int(st.cooperative),
+                    "specialised_kernels": int(st.jit_kernels)}
         eng.close()
     out["hh-network-4000"] = net
 
