@@ -13,6 +13,12 @@
  *   void gbh_sync_chip(Hsolve *)     -- cuda_sync_chip:   device -> chip/vm/conc
  *   void gbh_cleanup(void)           -- cuda_cleanup
  *
+ * plus one the reference has no counterpart for:
+ *
+ *   int  gbh_push_state(Hsolve *)    -- chip/vm/conc -> device, after the host
+ *                                       wrote them (RESTORE2, hines.c:560-571;
+ *                                       HPUT; RESET's element values)
+ *
  * and maps one Hsolve onto the array-level C ABI of include/gbhsolve.h. The
  * engine runs the chip update, the Ca pools and the Hines elimination, so
  * hines.c must skip do_h4_conc_chip_update and the CPU solve when
@@ -216,6 +222,17 @@ void gbh_sync_chip(Hsolve *h)
     gbh_hstate *s = (gbh_hstate *)h->accel_state;
     if (s) gbh_get_state(s->e, h->vm, h->chip, h->conc, h->ops);
     if (s && h->storemode && h->itotal) gbh_get_itotal(s->e, h->itotal);
+}
+
+int gbh_push_state(Hsolve *h)
+{
+    gbh_hstate *s = (gbh_hstate *)h->accel_state;
+    if (!s) return 0;   /* no engine yet: gbh_init copies the host arrays */
+    if (gbh_set_state(s->e, h->vm, h->chip, h->nconcs ? h->conc : NULL) != GBH_OK) {
+        fprintf(stderr, "gbh_push_state %s: %s\n", h->name, gbh_last_error());
+        return -1;
+    }
+    return 0;
 }
 
 void gbh_cleanup(void)
