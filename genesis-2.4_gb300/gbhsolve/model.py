@@ -322,6 +322,9 @@ def _belongs_before(a, b):
     return False
 
 
+_TABLE_CACHE = {}
+
+
 def build(model: Model, exact: bool = False) -> HsolveArrays:
     """SETUP + RESET of one hsolve over ``model``; returns the flat arrays.
 
@@ -446,7 +449,14 @@ def build(model: Model, exact: bool = False) -> HsolveArrays:
     tablist = np.zeros(0)
     xvals = np.zeros(0)
     yvals = np.zeros(0)
-    if ntab:
+    # cells built from the same channel types at the same dt get the same
+    # composite table: one shared (read-only) copy instead of one per cell
+    tkey = (tuple((sl, id(t), fl) for sl, (t, fl) in sorted(slots.items())), xdivs, xmin, invdx, ydivs, ymin,
+            invdy, dt)
+    cached = _TABLE_CACHE.get(tkey) if ntab else None
+    if cached is not None:
+        tabindex, tablist, xvals, yvals = cached[0]
+    elif ntab:
         tabsize = xdivs + 1
         if ydivs and not xdivs:
             tabsize = ydivs + 1
@@ -486,6 +496,12 @@ def build(model: Model, exact: bool = False) -> HsolveArrays:
         # padding row: the reference reads one row past the end when the
         # index is clamped to xdivs; a copy keeps that read finite.
         tablist[tabsize * ncols:] = tablist[(tabsize - 1) * ncols:tabsize * ncols]
+        for a in (tablist, xvals, yvals):
+            a.flags.writeable = False
+        if len(_TABLE_CACHE) >= 64:
+            _TABLE_CACHE.clear()
+        # the Interpol objects are kept with the entry so their ids stay unique
+        _TABLE_CACHE[tkey] = ((dict(tabindex), tablist, xvals, yvals), [t for t, _ in slots.values()])
     if ntab == 0:
         xmin = invdx = ymin = invdy = 0.0
 
