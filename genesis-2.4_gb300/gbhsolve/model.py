@@ -25,6 +25,7 @@ olf/olf_struct.h:142-155, sim/struct_defs.h:118-134).
 from __future__ import annotations
 
 import math
+import struct
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -51,9 +52,13 @@ SING_TINY = 1e-6                # olf_defs.h:58
 MAXTABC = 40                    # first voltage-table slot (hines_defs.h:59)
 
 
+_F32 = struct.Struct("f")
+
+
 def f32(x: float) -> float:
-    """Value as stored in a GENESIS ``float`` field."""
-    return float(np.float32(x))
+    """Value as stored in a GENESIS ``float`` field (IEEE single, round to
+    nearest even, as the C double-to-float conversion does)."""
+    return _F32.unpack(_F32.pack(x))[0]
 
 
 _f32_field = f32
