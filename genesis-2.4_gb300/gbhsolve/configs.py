@@ -158,11 +158,14 @@ def random_tree_neuron(rng, ncomp, na, k, ca, kca, inject, erest=-0.065, dend_le
                        TabChannel(kca, Gbar=sli(100.0 * sa), conc_src=4),
                        CaConcen(tau=0.02, B=B, Ca_base=5e-5, thick=0.1e-6)]
     out.append(s)
+    # one draw per dendrite, in order (the same stream as scalar draws)
+    dias = rng.uniform(dia_range[0], dia_range[1], size=ncomp - 1).tolist() if ncomp > 1 else []
+    em = sli(erest)
     for c in range(1, ncomp):
-        dd = float(rng.uniform(*dia_range))
+        dd = dias[c - 1]
         da, dx = dend_len * PI * dd, PI * (dd / 2) ** 2
-        out.append(Compartment(Em=sli(erest), Rm=sli(rm / da), Cm=sli(cm * da),
-                               Ra=sli(ra * dend_len / dx), initVm=sli(erest), parent=parents[c]))
+        out.append(Compartment(Em=em, Rm=sli(rm / da), Cm=sli(cm * da),
+                               Ra=sli(ra * dend_len / dx), initVm=em, parent=parents[c]))
     return out
 
 
