@@ -137,3 +137,12 @@ def test_engine_mixed_within_tolerance(oracle, gpu_engine):
         np.testing.assert_allclose(vm[i], ref.vm, rtol=0, atol=1e-9)
         np.testing.assert_allclose(it[i], ref.itotal, rtol=1e-6, atol=1e-6 * np.max(np.abs(ref.itotal)))
     eng.close()
+
+
+def test_storemode_types_are_not_specialised():
+    """storemode solvers run on the interpreting kernels: the code generator
+    declines their tile type (empty source), as it does for symmetric
+    compartments."""
+    from gbhsolve import engine
+    assert engine.jit_source([_solver(1, CHAIN)]) == ""
+    assert engine.jit_source([_solver(0, CHAIN)]) != ""

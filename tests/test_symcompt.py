@@ -173,3 +173,15 @@ def test_gradient_refuses_symmetric(gpu_engine):
     with pytest.raises(RuntimeError):
         eng.loss_gradient(10, [0], [0], trace)
     eng.close()
+
+
+def test_symmetric_types_are_not_specialised():
+    """The code generator declines symmetric-compartment tile types (they run
+    on the interpreting kernels); the same cell as asymmetric compartments
+    is specialised."""
+    from gbhsolve import engine
+    d = _load()
+    assert engine.jit_source([_case(d, "sym_star2x3_euler")]) == ""
+    mk = _cases_module()
+    m = [c for c in mk.cases() if c[0] == "sym_star2x3_euler"][0][1]
+    assert engine.jit_source([model.build(m)]) != ""
