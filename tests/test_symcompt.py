@@ -185,3 +185,31 @@ def test_symmetric_types_are_not_specialised():
     mk = _cases_module()
     m = [c for c in mk.cases() if c[0] == "sym_star2x3_euler"][0][1]
     assert engine.jit_source([model.build(m)]) != ""
+
+
+@pytest.mark.parametrize("damage", ["truncate", "extra_set", "bad_row", "odd_row"])
+def test_decoder_rejects_malformed_symmetric_programs(damage):
+    """A symmetric program is checked as it is decoded: it must end both
+    passes on the right rows, and every row operand must be an even results
+    index inside the solver."""
+    from gbhsolve import engine
+    d = _load()
+    h = _case(d, "sym_star2x3_euler")
+    f = [int(x) for x in h.funcs]
+    fin = f.index(7)                          # end of the forward pass
+    if damage == "truncate":
+        f = f[:fin - 3]
+    elif damage == "extra_set":
+        f.insert(fin, 1)                      # one row too many
+    else:
+        # walk the backward pass token by token to its last SIBARRAY_ELIM
+        i, k = fin + 1, None
+        while f[i] != 7:
+            if f[i] == 5:
+                k = i
+            i += {0: 2, 6: 1, 5: 3}[f[i]]
+        f[k + 2] = 2 * h.ncompts if damage == "bad_row" else f[k + 2] + 1
+    h.funcs = np.array(f, np.int32)
+    with pytest.raises(engine.EngineError) as ei:
+        engine.validate([h])
+    assert ei.value.code == -3
