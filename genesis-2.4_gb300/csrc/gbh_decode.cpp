@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <exception>
 #include <functional>
 #include <map>
 #include <thread>
@@ -952,7 +953,9 @@ int decode_solver(const gbh_batch_desc *d, int si, std::vector<Neuron> &neurons,
 // sets merged first-come (the indices a sequential pass would assign; the
 // programs and grouping keys of a chunk whose indices move are updated).
 // The first error in solver order is the one reported.
-int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
+namespace {
+
+int decode_chunks(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
 {
     Ctx c{d, err, -1};
     if (!d || d->abi_version != GBH_ABI_VERSION)
@@ -969,11 +972,19 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         gbh_error err{};
     };
     std::vector<Chunk> ch(nchunk);
+    // no C++ exception leaves the C ABI: host memory exhaustion is an error code
     auto work = [&](Chunk &k) {
-        for (int si = k.s0; si < k.s1; ++si) {
-            k.first.push_back((int)k.neurons.size());
-            k.rc = decode_solver(d, si, k.neurons, k.stab, &k.err);
-            if (k.rc) return;
+        int si = k.s0;
+        try {
+            for (; si < k.s1; ++si) {
+                k.first.push_back((int)k.neurons.size());
+                k.rc = decode_solver(d, si, k.neurons, k.stab, &k.err);
+                if (k.rc) return;
+            }
+        } catch (const std::exception &ex) {
+            Ctx ce{d, &k.err, si};
+            k.rc = fail(ce, GBH_ERR_ARG, -1, 0, -1, "decoding needs more host memory than is available (%s)",
+                        ex.what());
         }
     };
     for (int i = 0; i < nchunk; ++i) {
@@ -984,7 +995,14 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
         work(ch[0]);
     } else {
         std::vector<std::thread> th;
-        for (int i = 0; i < nchunk; ++i) th.emplace_back(work, std::ref(ch[i]));
+        int started = 0;
+        try {
+            th.reserve(nchunk);
+            for (; started < nchunk; ++started) th.emplace_back(work, std::ref(ch[started]));
+        } catch (const std::exception &) {
+            // no more threads to be had: the remaining chunks run here
+        }
+        for (int i = started; i < nchunk; ++i) work(ch[i]);
         for (auto &t : th) t.join();
     }
     out.neurons.clear();
@@ -1026,6 +1044,19 @@ int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
     }
     out.solver_first_neuron[ns] = (int)out.neurons.size();
     return GBH_OK;
+}
+
+}  // namespace
+
+int decode_batch(const gbh_batch_desc *d, Decoded &out, gbh_error *err)
+{
+    try {
+        return decode_chunks(d, out, err);
+    } catch (const std::exception &ex) {
+        Ctx c{d, err, -1};
+        out.neurons.clear();
+        return fail(c, GBH_ERR_ARG, -1, 0, -1, "decoding needs more host memory than is available (%s)", ex.what());
+    }
 }
 
 }  // namespace gbh

@@ -1873,17 +1873,18 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
     return gbh_create_dist(desc, syn, nullptr, opt, err);
 }
 
-gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
-                            const gbh_options *opt, gbh_error *err)
+namespace {
+
+gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
+                        const gbh_options *opt, gbh_error *err, gbh_engine *&made)
 {
-    gbh_error local{};
-    if (!err) err = &local;
     memset(err, 0, sizeof(*err));
     if (!desc) {
         fail_err(err, GBH_ERR_ARG, "NULL descriptor");
         return nullptr;
     }
     gbh_engine *e = new gbh_engine();
+    made = e;
     if (opt) e->opt = *opt;
     e->nsolvers = desc->nsolvers;
     e->dt = desc->dt;
@@ -1969,6 +1970,25 @@ gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn,
         fprintf(stderr, "gbhsolve: specialised kernels: %d; compiler log:\n%.4000s\n", e->jit_compiled,
                 e->jit_log.c_str());
     return e;
+}
+
+}  // namespace
+
+// No C++ exception leaves the C ABI: running out of host memory (or threads)
+// while building the engine is an error code, the partial engine released.
+gbh_engine *gbh_create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
+                            const gbh_options *opt, gbh_error *err)
+{
+    gbh_error local{};
+    if (!err) err = &local;
+    gbh_engine *made = nullptr;
+    try {
+        return create_dist(desc, syn, remote, opt, err, made);
+    } catch (const std::exception &ex) {
+        if (made) gbh_destroy(made);
+        fail_err(err, GBH_ERR_ARG, "engine setup needs more host resources than are available (%s)", ex.what());
+        return nullptr;
+    }
 }
 
 int gbh_run_async(gbh_engine *e, int nsteps, void *stream)
