@@ -350,10 +350,11 @@ int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
  *
  * No counterpart in the reference: its CUDA backend allocates per solver.
  * This exists for hosts that are not allowed to allocate device memory while
- * the simulation steps, for example a GENESIS build that issues the step
- * inside CUDA stream capture (allocation calls are not permitted there) or
- * one that sizes a device memory pool once at start-up. Results equal
- * gbh_run's on the same engine.
+ * the simulation steps: a GENESIS process that shares the GPU with another
+ * runtime which reserved the device memory at start-up (a caching pool sized
+ * once, so a later cudaMalloc fails or steals from it), or a step loop with a
+ * latency budget, where cudaMalloc/cudaFree may synchronise the whole device.
+ * Results equal gbh_run's on the same engine.
  *
  * The step kernel's per-step scratch -- the Ca flux rows, one double per Ca
  * pool per neuron slot, padded to 32 lanes -- comes from a fixed array of

@@ -1,8 +1,9 @@
 """gbh_run_noalloc: the step entry point that allocates no device memory.
 
-It is for hosts that may not allocate device memory while stepping (the
-step issued inside CUDA stream capture, or a device memory pool sized once
-at start-up). Its Ca-flux scratch is a fixed array inside the library, so
+It is for hosts that may not allocate device memory while stepping: the
+GPU's memory was reserved at start-up by a pool another runtime owns, or
+the step loop cannot afford cudaMalloc/cudaFree, which may synchronise the
+whole device. Its Ca-flux scratch is a fixed array inside the library, so
 this test uses a model with Ca pools, where that scratch is really used, and
 checks two consecutive calls against gbh_run on an identical engine. The
 FP64 step is exact, so the comparison is bit for bit, the same tolerance the
@@ -10,6 +11,7 @@ other FP64 engine tests use. This file is collected last on purpose.
 """
 import numpy as np
 import pytest
+import torch
 
 from gbhsolve import configs, model
 
@@ -24,7 +26,6 @@ def test_run_noalloc_matches_run_twice(gpu_engine):
         ref.run(120)
         new.run_noalloc(120)          # queued on the default stream
         a = ref.get_state()           # get_state synchronises the device copy
-        import torch
         torch.cuda.synchronize()
         b = new.get_state()
         for i in range(len(hs)):
