@@ -29,3 +29,17 @@ def test_library_loads_and_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(lib, name), name
     assert sorted(engine.EXPORTED) == declared_functions()
+
+
+def test_step_entry_points_reject_a_null_engine_before_any_device_call():
+    """A NULL engine or a negative step count is GBH_ERR_ARG, decided on the
+    host before any CUDA call, so it holds on a machine without a GPU."""
+    lib = ctypes.CDLL(build.build())
+    GBH_ERR_ARG = -1
+    for name in ("gbh_run", "gbh_run_noalloc", "gbh_step_io", "gbh_run_io"):
+        getattr(lib, name).restype = ctypes.c_int
+    assert lib.gbh_run(None, 1) == GBH_ERR_ARG
+    assert lib.gbh_run_noalloc(None, 1, None) == GBH_ERR_ARG
+    assert lib.gbh_run_noalloc(None, -1, None) == GBH_ERR_ARG
+    assert lib.gbh_step_io(None, None, None, 1, None) == GBH_ERR_ARG
+    assert lib.gbh_run_io(None, None, None, 1, 16, None) == GBH_ERR_ARG
