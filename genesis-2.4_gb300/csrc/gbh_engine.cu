@@ -1262,9 +1262,12 @@ int autotune_trials(gbh_engine *e)
 }
 
 // Internal: the step loop of run_steps with the flux scratch supplied by the
-// caller (used by gbh_run_noalloc). Reports the flux elements the engine needs.
+// caller (used by gbh_run_noalloc). Reports the flux elements the engine needs,
+// the engine's own flux rows, device and stream.
 int64_t gbh_internal_flux_elems(const gbh_engine *e) { return e->rows_pool * (int64_t)LANES; }
+double *gbh_internal_flux_rows(const gbh_engine *e) { return e->d_F.p; }
 int gbh_internal_device(const gbh_engine *e) { return e->opt.device; }
+cudaStream_t gbh_internal_stream(const gbh_engine *e) { return e->stream; }
 
 int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, double *flux)
 {
@@ -1274,6 +1277,7 @@ int gbh_internal_run_with_flux(gbh_engine *e, int nsteps, cudaStream_t st, doubl
     const int rc = issue_steps(e, v, nsteps, e->step, e->givals_enabled, st, nullptr);
     if (rc) return rc;
     e->step += nsteps;
+    e->stats.steps += nsteps;
     if (e->givals_enabled) e->givals_valid = true;
     return GBH_OK;
 }

@@ -354,20 +354,26 @@ int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
  * runtime which reserved the device memory at start-up (a caching pool sized
  * once, so a later cudaMalloc fails or steals from it), or a step loop with a
  * latency budget, where cudaMalloc/cudaFree may synchronise the whole device.
- * Results equal gbh_run's on the same engine.
+ * Results equal gbh_run's on the same engine, registered inputs included.
  *
  * The step kernel's per-step scratch -- the Ca flux rows, one double per Ca
  * pool per neuron slot, padded to 32 lanes -- comes from a fixed array of
  * GBH_NOALLOC_FLUX_MAX doubles (8 MiB) compiled into the library, which every
  * GPU that loads the library keeps until the process exits. Engines that need
- * more are rejected with GBH_ERR_ARG. The call makes no cudaMalloc/cudaFree
- * or other allocating call; it clears the part of the array it uses before
- * stepping. The first call on a device looks up the array's device address
+ * more are rejected with GBH_ERR_ARG before anything is queued. The call
+ * makes no cudaMalloc/cudaFree or other allocating call: it copies the
+ * engine's flux rows (FLUX inputs set by gbh_set_inputs_async, flux carried
+ * from the previous step) into the array, steps on it, and copies the rows
+ * back, two device-to-device copies between buffers that already exist. The
+ * first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the one array: calls that may overlap on the GPU (other
  * streams, other engines) race on it and must be serialised by the caller.
- * stream is a cudaStream_t passed as void* (NULL = default stream); the call
- * returns once the work is queued.
+ * stream is a cudaStream_t passed as void* (NULL = the engine's own stream,
+ * as for gbh_run_async); the call returns once the work is queued and leaves
+ * the caller's current device as it found it. A device status word raised
+ * by these steps (event ring overflow, unimplemented micro-op) is reported by
+ * the engine's next synchronous call (gbh_run).
  */
 #define GBH_NOALLOC_FLUX_MAX (1 << 20)
 int gbh_run_noalloc(gbh_engine *e, int nsteps, void *stream);

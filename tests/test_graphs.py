@@ -60,10 +60,8 @@ def test_network_graph_with_noalloc_between(oracle, gpu_engine):
     step counter stale; the next replay must resynchronise it."""
     hs, esyn, child = _network(60, 0.1, seed=11)
     eng = gpu_engine.Engine(hs, synapses=esyn, use_graph=True)
-    import torch
     eng.run(400)
-    eng.run_noalloc(250)        # queued on the default stream
-    torch.cuda.synchronize()
+    eng.run_noalloc(250)        # NULL stream: queued on the engine's own stream
     eng.run(350)
     solvers = [oracle.Solver(h, i) for i, h in enumerate(hs)]
     net = oracle.Network(solvers, esyn["src_start"], esyn["target_solver"], child, esyn["target_op"],
