@@ -22,7 +22,7 @@
  * and maps one Hsolve onto the array-level C ABI of include/gbhsolve.h. The
  * engine runs the chip update, the Ca pools and the Hines elimination, so
  * hines.c must skip do_h4_conc_chip_update and the CPU solve when
- * gbh_chip_update returns 1 (see INTEGRATION.md for the patch).
+ * gbh_chip_update returns 1.
  *
  * Per step it forwards the values h_in_msgs wrote into chip[] (INJECT, BASE,
  * THRESH targets listed in hsolve->ininfo) and, when the solver has output

@@ -461,12 +461,20 @@ int decode_solver(const gbh_batch_desc *d, int si, std::vector<Neuron> &neurons,
                     break;
                 }
                 case R_DOMAIN:
+                    // the concentration axis (yvals) exists only in a solver
+                    // with concentrations (hines_chip.c:131-140); without one
+                    // the reference's lookup reads through a NULL yvals
+                    if (d->conc_start[si + 1] == d->conc_start[si])
+                        return fail(c, GBH_ERR_ARG, row, code, o - 1, "DOMAIN_OP in a solver without concentrations");
                     P.push_back(M_DOMAIN);
                     P.push_back(nb.fld(FS_CHIP, ch, chip[ch]));
                     ch++;
                     break;
                 case R_NEWCONC2: {
+                    if (!need(1)) return fail(c, GBH_ERR_OPCODE, row, code, o, "truncated NEWCONC2_OP");
                     const int k = ops[o++];
+                    const int64_t nconc = d->conc_start[si + 1] - d->conc_start[si];
+                    if (k < 0 || k >= nconc) return fail(c, GBH_ERR_ARG, row, code, o - 1, "conc index %d out of range", k);
                     P.push_back(M_NEWCONC2);
                     P.push_back(nb.pool(k));
                     break;

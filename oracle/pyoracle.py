@@ -60,8 +60,26 @@ def ensure_built(with_reference: bool = True) -> None:
         subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
+_ref_src = None
+
+
+def reference_src() -> str:
+    """The reference's genesis/src directory: GENESIS_REF_SRC in the
+    environment, else the default that oracle/Makefile builds from."""
+    global _ref_src
+    if _ref_src is None:
+        env = os.environ.get("GENESIS_REF_SRC")
+        if env:
+            _ref_src = env
+        else:
+            r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+            _ref_src = r.stdout.strip() if r.returncode == 0 else ""
+    return _ref_src
+
+
 def reference_sources_present() -> bool:
-    return os.path.exists("/root/reference/genesis/src/hines/hines_chip.c")
+    src = reference_src()
+    return bool(src) and os.path.exists(os.path.join(src, "hines", "hines_chip.c"))
 
 
 _libs = {}

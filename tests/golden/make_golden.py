@@ -1,8 +1,16 @@
-"""Generates tests/golden/ref_trajectories.npz: small hsolve models (arrays
-as the SETUP restatement builds them) and their state after N steps of the
-reference's OWN step code (genesis/src/hines/hines_4chip.c, hines_solve.c,
-hines_conc_4chip.c compiled from the reference sources by oracle/Makefile
-into oracle/_ref/libhsolve_ref.so).
+"""Generates the reference-run fixtures under tests/golden/:
+
+* ref_trajectories.npz: small hsolve models (arrays as the SETUP
+  restatement builds them) and their state after N steps of the reference's
+  OWN step code (genesis/src/hines/hines_4chip.c, hines_4nichip.c,
+  hines_solve.c, hines_conc_4chip.c compiled from the reference sources by
+  oracle/Makefile into oracle/_ref/libhsolve_ref.so);
+* ref_opcodes.npz: every hand-assembled opcode program of tests/opprograms.py
+  in each of its three step modes (chanmode 4, chanmode 5 under
+  Crank-Nicolson, calcmode 0), with its state (vm, chip, conc, givals, ops)
+  after NSTEPS steps of the same reference code, and a digest of its input
+  arrays so that a test notices when a program is no longer the one the
+  fixture was made from.
 
 Run in a container that has the reference sources:
     python tests/golden/make_golden.py
@@ -16,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, "genesis-2.4_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
+sys.path.insert(0, os.path.dirname(HERE))
 
 import pyoracle  # noqa: E402
 from gbhsolve import configs, model  # noqa: E402
@@ -33,8 +42,30 @@ def _calc0(h):
     return h
 
 
+def opcode_fixtures():
+    import opprograms as P
+    out = {"tags": [], "nsteps": np.array(P.NSTEPS)}
+    for name in sorted(P.PROGRAMS):
+        for mode in P.MODES:
+            h, libm = P.build(name, *mode)
+            tag = P.mode_tag(name, *mode)
+            s = pyoracle.Solver(h)
+            s.run(P.NSTEPS, "reference")
+            out["tags"].append(tag)
+            out[tag + "/digest"] = np.array(P.input_digest(h))
+            out[tag + "/libm"] = np.array(bool(libm))
+            P.to_fixture(h, tag, out)
+            for k in ("vm", "chip", "givals", "ops"):
+                out[tag + "/" + k] = getattr(s, k).copy()
+            out[tag + "/conc"] = s.conc[:len(h.conc)].copy()
+            print(tag, "vm[0] = %.12g" % s.vm[0])
+    out["tags"] = np.array(out["tags"])
+    np.savez_compressed(os.path.join(HERE, "ref_opcodes.npz"), **out)
+
+
 def main():
     pyoracle.ensure_built(with_reference=True)
+    opcode_fixtures()
     out = {"names": np.array([c[0] for c in CASES])}
     for name, make, nsteps in CASES:
         h = make()

@@ -10,12 +10,14 @@ import pytest
 
 from gbhsolve import build
 
-REF = "/root/reference/genesis/src"
+import pyoracle
+
+REF = pyoracle.reference_src()
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ADAPTER = os.path.join(REPO, "genesis-2.4_gb300", "adapter", "gbh_hsolve_adapter.c")
 
 
-@pytest.mark.skipif(not os.path.exists(REF + "/hines/hines_ext.h"), reason="reference headers not present")
+@pytest.mark.skipif(not REF or not os.path.exists(REF + "/hines/hines_ext.h"), reason="reference headers not present")
 def test_adapter_compiles_against_reference_headers(tmp_path):
     inc = sum((["-I", REF + "/" + d] for d in ("hines", "sim", "ss", "shell", "segment", "olf", "concen",
                                                  "device", "newconn", "sys")), [])

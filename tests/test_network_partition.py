@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 from gbhsolve import configs, model, shard
+from oracle_rank import OracleRank
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -63,7 +64,7 @@ def test_partitioned_oracle_in_process(oracle, world):
     for r in range(world):
         lo, hi = shard.shard_range(n, r, world)
         loc, rem = shard.partition_network(esyn, lo, hi, target_child=child)
-        ranks.append(shard.OracleRank(oracle, hs[lo:hi], loc, rem))
+        ranks.append(OracleRank(oracle, hs[lo:hi], loc, rem))
     for _ in range(nsteps):
         for rk in ranks:
             rk.run(1)
@@ -79,6 +80,8 @@ def test_partitioned_oracle_in_process(oracle, world):
 def _gloo_worker(rank, world, port, out):
     sys.path.insert(0, os.path.join(REPO, "genesis-2.4_gb300"))
     sys.path.insert(0, os.path.join(REPO, "oracle"))
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    from oracle_rank import OracleRank
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     import torch
     import torch.distributed as dist
@@ -88,7 +91,7 @@ def _gloo_worker(rank, world, port, out):
     n = len(hs)
     lo, hi = shard.shard_range(n, rank, world)
     loc, rem = shard.partition_network(esyn, lo, hi, target_child=child)
-    rk = shard.OracleRank(pyoracle, hs[lo:hi], loc, rem)
+    rk = OracleRank(pyoracle, hs[lo:hi], loc, rem)
     shard.run_partitioned(rk, 700, n, dist)
     vm = np.zeros(n * hs[0].ncompts)
     sp = np.zeros(n)

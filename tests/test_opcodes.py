@@ -1,173 +1,72 @@
-"""Opcode coverage: hand-assembled compartment programs through the GPU
-engine (specialised and interpreted paths, FP64 and mixed) against the CPU
-oracle. Programs without libm calls must match bit for bit in FP64;
+"""Opcode coverage: hand-assembled compartment programs (tests/opprograms.py)
+through the GPU engine (specialised and interpreted paths, FP64 and mixed)
+against the reference's own step code, run once into the committed fixture
+tests/golden/ref_opcodes.npz (tests/golden/make_golden.py), and against the
+CPU oracle. Programs without libm calls must match bit for bit in FP64;
 programs using exp/log (GHK, Nernst, Mg block) compare within 1e-12
 relative, the distance between the CPU's libm and CUDA's math library."""
+import os
+
 import numpy as np
 import pytest
 
-import ophelpers as A
+import opprograms as P
 
 pytestmark = pytest.mark.gpu
 
-DT = 2e-5
+FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "ref_opcodes.npz")
 
 
-def _c(vm0=-0.062, inj=1e-10):
-    # Em/Rm, inject, tbyc, diagterm, Rm, initial Vm
-    return A.Compt(-0.065 / 3e8, inj, DT / 1e-11, 1.0 + DT / (1e-11 * 3e8), 3e8, vm0)
-
-
-def prog_hh_like():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.05, 1e-8]).op(A.IPOL1V, 0, 3, chips=[0.1])
-    c.op(A.IPOL1V, 2, 1, chips=[0.6]).op(A.ADD_CURR, giv=3)
-    c.op(A.CHAN_EK, chips=[-0.08, 3e-8]).op(A.IPOL1V, 4, 4, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40)), False
-
-
-def prog_instant_powers():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.02, 2e-8]).op(A.IPOL1V, 0, -2, chips=[0.2])
-    c.op(A.IPOL1V, 2, 5, chips=[0.4]).op(A.IPOL1V, 4, 6, chips=[0.5]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=1)), False
-
-
-def prog_chan_carry_two_compartments():
-    c0 = _c(-0.06)
-    c0.op(A.NEWVOLT).op(A.CHAN_EK, chips=[-0.07, 1e-8]).op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    c0.op(A.CHAN, chips=[2e-8]).op(A.IPOL1V, 2, 1, chips=[0.5]).op(A.ADD_CURR, giv=3)
-    c1 = _c(-0.064)
-    c1.op(A.NEWVOLT).op(A.CHAN, chips=[3e-8]).op(A.IPOL1V, 4, 3, chips=[0.2]).op(A.ADD_CURR, giv=3)
-    return [c0, c1], dict(tabs=A.tables(12, 40, seed=2), parents=[1, -1]), False
-
-
-def prog_tabcurrent():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.0, 1e-8]).op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    c.op(A.CHAN, chips=[5e-9]).op(A.IPOL1V, 6, 0, giv=3)          # tabcurrent: current added at once
-    c.op(A.CHAN_EK, chips=[-0.08, 1e-8]).op(A.IPOL1V, 8, 1, chips=[0.4]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=3)), False
-
-
-def prog_nernst():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CONC_VAL, 0).op(A.NERNST, chips=[0.0125, 2e-8]).op(A.IPOL1V, 0, 2, chips=[0.3])
-    c.op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=4), conc=[5e-5, 2.0]), True
-
-
-def prog_ghk_same_ghk_flux():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CONC_VAL, 0).op(A.GHK, chips=[2 * 96485.3 / (8.314 * 300), 2 * 96485.3, 1e-12])
-    c.op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3).op(A.FLUX)
-    c.op(A.SAME_GHK, chips=[2e-12]).op(A.IPOL1V, 2, 1, chips=[0.4]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=5), conc=[5e-5, 2.0]), True
-
-
-def prog_tabghk():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.DO_TABGHK).op(A.IPOL1V, 0, 0)
-    c.op(A.SAME_GHK, chips=[3e-9]).op(A.IPOL1V, 2, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=6)), False
-
-
-def prog_domain():
-    c = _c()
-    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.1, 1e-8]).op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    c.op(A.DOMAIN, chips=[1e7]).op(A.CHAN_EK, chips=[-0.08, 2e-8]).op(A.IPOL1C, 4, 1, chips=[0.2])
-    c.op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=7, ydivs=40)), False
-
-
-def prog_conc_gate_pool():
-    c = _c()
-    c.op(A.CONC_VAL, 0).op(A.NEWCONC1).op(A.NEWVOLT).op(A.CHAN_EK, chips=[-0.08, 1e-8])
-    c.op(A.IPOL1V, 0, 1, chips=[0.3]).op(A.IPOL1C, 2, 2, chips=[0.2]).op(A.ADD_CURR, giv=3)
-    c.op(A.CHAN_EK, chips=[0.12, 5e-9]).op(A.IPOL1V, 4, 2, chips=[0.1]).op(A.ADD_CURR, giv=3).op(A.FLUX)
-    kw = dict(tabs=A.tables(12, 40, seed=8, ydivs=40, ymax=0.5), conc=[1e-4],
-              concops=[A.CACONC, 0, A.LCACONC], concchip=[5e-5, 1.0 + DT / 0.04, DT * 3e11])
-    return [c], kw, False
-
-
-def prog_2d_tables():
-    c = _c()
-    c.op(A.CONC_VAL, 0).op(A.NEWCONC1).op(A.NEWVOLT).op(A.CHAN_EK, chips=[-0.08, 1e-8])
-    c.op(A.IPOL2V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    c.op(A.NEWCONC2, 1).op(A.CHAN_EK, chips=[0.05, 2e-9]).op(A.IPOL2C, 4, 1, chips=[0.4]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(30, 10, seed=9, ydivs=10, ymax=0.5), conc=[0.17, 0.31]), False
-
-
-def prog_syn_mgblock():
-    c = _c()
-    xc2, yc1, yc2, xc1 = 0.99, 9.5e-5, 0.98, 9.9e-5
-    c.op(A.CHAN_EK, chips=[0.0, 1e-9]).op(A.SYN2, 0, -1, 1, chips=[0.4, 0.7])
-    c.op(A.MGBLOCK, chips=[0.3, 1 / 0.062, 1.2], giv=6)           # blocked and unblocked currents
-    return [c], dict(tabs=A.tables(12, 40), stablist=[xc2, yc1, yc2, xc1 / DT]), True
-
-
-def prog_elmmpump():
-    c = _c()
-    c.op(A.CONC_VAL, 0).op(A.ELMMPUMP, chips=[2e-4, 3e-12, 1e-3], giv=1)
-    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[-0.08, 1e-8]).op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=10), conc=[1e-4]), False
-
-
-def prog_spike():
-    c = _c(-0.02, 5e-9)
-    c.op(A.NEWVOLT).op(A.SPIKE, 0, 5, chips=[-0.03]).op(A.CHAN_EK, chips=[-0.08, 1e-8])
-    c.op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
-    return [c], dict(tabs=A.tables(12, 40, seed=11)), False
-
-
-PROGRAMS = {f.__name__[5:]: f for f in (
-    prog_hh_like, prog_instant_powers, prog_chan_carry_two_compartments, prog_tabcurrent, prog_nernst,
-    prog_ghk_same_ghk_flux, prog_tabghk, prog_domain, prog_conc_gate_pool, prog_2d_tables, prog_syn_mgblock,
-    prog_elmmpump, prog_spike)}
-
-
-def _build(name, chanmode=4, calcmode=1, crank=False):
-    compts, kw, libm = PROGRAMS[name]()
-    tabs = kw.pop("tabs")
-    h = A.solver(compts, tabs, dt=DT, chanmode=chanmode, calcmode=calcmode, crank=crank, **kw)
-    return h, libm
-
-
-def _compare(a, b, libm):
+def _compare(a, b, libm, tag=""):
     if libm:
-        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-18)
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-18, err_msg=tag)
     else:
-        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, b, err_msg=tag)
+
+
+@pytest.fixture(scope="module")
+def ref_states():
+    return np.load(FIXTURE, allow_pickle=False)
 
 
 @pytest.mark.parametrize("jit", [True, False, 2, 3])
-@pytest.mark.parametrize("name", sorted(PROGRAMS))
-def test_program_fp64(oracle, gpu_engine, name, jit):
-    for chanmode, calcmode, crank in ((4, 1, False), (5, 1, True), (4, 0, False)):
-        h, libm = _build(name, chanmode, calcmode, crank)
+@pytest.mark.parametrize("name", sorted(P.PROGRAMS))
+def test_program_fp64(oracle, gpu_engine, ref_states, name, jit):
+    for mode in P.MODES:
+        tag = P.mode_tag(name, *mode)
+        h = P.from_fixture(ref_states, tag)        # the exact inputs the reference stepped
+        libm = bool(ref_states[tag + "/libm"])
         eng = gpu_engine.Engine([h], jit=jit)
         eng.enable_givals(True)
-        eng.run(400)
+        eng.run(P.NSTEPS)
         st = eng.get_state()
         giv = eng.givals()[0]
-        ref = oracle.Solver(h)
-        ref.run(400)
-        tag = "%s cm%d calc%d crank%d" % (name, chanmode, calcmode, crank)
-        _compare(st["vm"][0], ref.vm, libm)
-        _compare(st["chip"][0], ref.chip, libm)
+        # the reference's own step code (fixture)
+        _compare(st["vm"][0], ref_states[tag + "/vm"], libm, tag)
+        _compare(st["chip"][0], ref_states[tag + "/chip"], libm, tag)
+        _compare(giv, ref_states[tag + "/givals"], libm, tag)
         if len(h.conc):
-            _compare(st["conc"][0], ref.conc[:len(h.conc)], libm)
-        _compare(giv, ref.givals, libm)
-        if name == "spike":
-            np.testing.assert_array_equal(st["ops"][0], ref.ops, err_msg=tag)
+            _compare(st["conc"][0], ref_states[tag + "/conc"], libm, tag)
+        np.testing.assert_array_equal(st["ops"][0], ref_states[tag + "/ops"], err_msg=tag)
+        # the oracle restatement, run here
+        ref = oracle.Solver(h)
+        ref.run(P.NSTEPS)
+        _compare(st["vm"][0], ref.vm, libm, tag)
+        _compare(st["chip"][0], ref.chip, libm, tag)
+        if len(h.conc):
+            _compare(st["conc"][0], ref.conc[:len(h.conc)], libm, tag)
+        _compare(giv, ref.givals, libm, tag)
         eng.close()
 
 
-@pytest.mark.parametrize("name", sorted(PROGRAMS))
-def test_program_mixed(oracle, gpu_engine, name):
-    h, _ = _build(name)
+@pytest.mark.parametrize("name", sorted(P.PROGRAMS))
+def test_program_mixed(oracle, gpu_engine, ref_states, name):
+    tag = P.mode_tag(name, *P.MODES[0])
+    h = P.from_fixture(ref_states, tag)
     eng = gpu_engine.Engine([h], precision=gpu_engine.PREC_MIXED)
-    eng.run(400)
+    eng.run(P.NSTEPS)
+    np.testing.assert_allclose(eng.vm(), ref_states[tag + "/vm"], rtol=0, atol=1e-9)
     ref = oracle.Solver(h)
-    ref.run(400)
+    ref.run(P.NSTEPS)
     np.testing.assert_allclose(eng.vm(), ref.vm, rtol=0, atol=1e-9)
+    eng.close()

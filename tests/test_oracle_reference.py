@@ -51,8 +51,9 @@ def _from_npz(d, name):
         crank=int(sc[9]), chanmode=int(sc[10]), calcmode=int(sc[11]), method=11 if int(sc[9]) else 10)
 
 
-needs_ref = pytest.mark.skipif(not os.path.exists("/root/reference/genesis/src/hines/hines_chip.c"),
-                               reason="reference sources not present")
+import pyoracle  # noqa: E402
+
+needs_ref = pytest.mark.skipif(not pyoracle.reference_sources_present(), reason="reference sources not present")
 
 
 @needs_ref
@@ -89,3 +90,63 @@ def test_oracle_network_matches_reference_step_code(oracle):
     assert runs[0][1].sum() > 0
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
+
+
+def test_opcode_programs_equal_reference_fixture(oracle):
+    """Every opcode program of tests/opprograms.py in all three step modes:
+    the oracle against the reference's own step code (committed fixture)."""
+    import opprograms as P
+    d = np.load(os.path.join(GOLDEN, "ref_opcodes.npz"), allow_pickle=False)
+    tags = [str(t) for t in d["tags"]]
+    assert len(tags) == len(P.PROGRAMS) * len(P.MODES)
+    for name in sorted(P.PROGRAMS):
+        for mode in P.MODES:
+            h, libm = P.build(name, *mode)
+            tag = P.mode_tag(name, *mode)
+            assert str(d[tag + "/digest"]) == P.input_digest(h), tag
+            hf = P.from_fixture(d, tag)
+            assert P.input_digest(hf) == P.input_digest(h), tag
+            s = oracle.Solver(hf)
+            s.run(int(d["nsteps"]))
+            for k in ("vm", "chip", "givals"):
+                if libm:    # exp/log: libm of the machine running the test
+                    np.testing.assert_allclose(getattr(s, k), d[tag + "/" + k], rtol=1e-12, atol=1e-18,
+                                               err_msg=tag)
+                else:
+                    np.testing.assert_array_equal(getattr(s, k), d[tag + "/" + k], err_msg=tag)
+            np.testing.assert_array_equal(s.ops, d[tag + "/ops"], err_msg=tag)
+            if len(h.conc):
+                np.testing.assert_allclose(s.conc[:len(h.conc)], d[tag + "/conc"], rtol=1e-12 if libm else 0,
+                                           atol=0, err_msg=tag)
+
+
+@needs_ref
+def test_opcode_programs_oracle_equals_live_reference(oracle):
+    """The same programs run live through the compiled reference here."""
+    import opprograms as P
+    oracle.ensure_built(with_reference=True)
+    for name in sorted(P.PROGRAMS):
+        for mode in P.MODES:
+            h, _ = P.build(name, *mode)
+            a, b = oracle.Solver(h), oracle.Solver(h)
+            a.run(P.NSTEPS, "oracle")
+            b.run(P.NSTEPS, "reference")
+            for k in ("vm", "chip", "conc", "givals", "ops"):
+                np.testing.assert_array_equal(getattr(a, k), getattr(b, k), err_msg=P.mode_tag(name, *mode))
+
+
+def test_domain_without_concentrations_is_a_setup_error():
+    """DOMAIN_OP needs the concentration axis, which a solver has only when it
+    holds concentrations (hines_chip.c:131-140); the reference would read
+    through a NULL yvals, the engine refuses the model at setup."""
+    import ophelpers as A
+    import opprograms as P
+    from gbhsolve import engine
+    c = P._c()
+    c.op(A.NEWVOLT).op(A.CHAN_EK, chips=[0.1, 1e-8]).op(A.IPOL1V, 0, 2, chips=[0.3]).op(A.ADD_CURR, giv=3)
+    c.op(A.DOMAIN, chips=[1e7]).op(A.CHAN_EK, chips=[-0.08, 2e-8]).op(A.IPOL1C, 4, 1, chips=[0.2])
+    c.op(A.ADD_CURR, giv=3)
+    h = A.solver([c], A.tables(12, 40, seed=7, ydivs=40), dt=P.DT)
+    with pytest.raises(engine.EngineError) as ei:
+        engine.validate([h])
+    assert ei.value.opcode == A.DOMAIN

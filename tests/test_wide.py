@@ -9,7 +9,8 @@ import pytest
 
 import ophelpers as A
 import test_conc_diffusion as CD
-import test_opcodes as OP
+import opprograms as OP
+from test_opcodes import FIXTURE, _compare
 from gbhsolve import configs, model
 
 pytestmark = pytest.mark.gpu
@@ -65,18 +66,23 @@ def test_random_trees_wide_mixed(oracle, gpu_engine):
 
 @pytest.mark.parametrize("name", sorted(OP.PROGRAMS))
 def test_opcode_programs_forced_wide(oracle, gpu_engine, name):
-    for chanmode, calcmode, crank in ((4, 1, False), (5, 1, True), (4, 0, False)):
-        h, libm = OP._build(name, chanmode, calcmode, crank)
+    d = np.load(FIXTURE, allow_pickle=False)
+    for mode in OP.MODES:
+        tag = OP.mode_tag(name, *mode)
+        h, libm = OP.from_fixture(d, tag), bool(d[tag + "/libm"])
         eng = gpu_engine.Engine([h], wide_min=1)
         eng.enable_givals(True)
-        eng.run(400)
+        eng.run(OP.NSTEPS)
         st = eng.get_state()
-        ref = _oracle_run(oracle, h, 400)
-        OP._compare(st["vm"][0], ref.vm, libm)
-        OP._compare(st["chip"][0], ref.chip, libm)
+        # the reference's own step code (fixture) and the oracle
+        _compare(st["vm"][0], d[tag + "/vm"], libm, tag)
+        _compare(st["chip"][0], d[tag + "/chip"], libm, tag)
+        ref = _oracle_run(oracle, h, OP.NSTEPS)
+        _compare(st["vm"][0], ref.vm, libm, tag)
+        _compare(st["chip"][0], ref.chip, libm, tag)
         if len(h.conc):
-            OP._compare(st["conc"][0], ref.conc[:len(h.conc)], libm)
-        OP._compare(eng.givals()[0], ref.givals, libm)
+            _compare(st["conc"][0], ref.conc[:len(h.conc)], libm, tag)
+        _compare(eng.givals()[0], ref.givals, libm, tag)
         eng.close()
 
 

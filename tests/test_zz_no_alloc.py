@@ -19,7 +19,7 @@ import ophelpers as A
 
 pytestmark = pytest.mark.gpu
 DT = 2e-5
-GBH_ERR_ARG = 1
+GBH_ERR_ARG = -1
 FLUX_MAX = 1 << 20
 
 
