@@ -389,6 +389,8 @@ def main():
                     help="time only this form's step loop (for profiler launch lists and captures)")
     ap.add_argument("--profile-adjoint", type=int, nargs=2, metavar=("NEURONS", "STEPS"),
                     help="run only the gradient workload at this size")
+    ap.add_argument("--wide-min", type=int, default=0,
+                    help="--profile-trees: the engine's wide_min (0 autotuned mapping, < 0 never wide)")
     ap.add_argument("--profile-trees", type=int, metavar="NEURONS",
                     help="run only random trees (8-256 compartments, Ca) of this many neurons, the form of "
                          "--profile-form (default mixed), steps_per_launch --steps-per-launch (default 64); "
@@ -410,7 +412,8 @@ def main():
         from gbhsolve import configs, model
         ht = [model.build(m) for m in configs.random_trees(args.profile_trees, seed=2)]
         prec = engine.PREC_FP64 if args.profile_form == "fp64" else engine.PREC_MIXED
-        eng = engine.Engine(ht, precision=prec, steps_per_launch=args.steps_per_launch or 64, device=local)
+        eng = engine.Engine(ht, precision=prec, steps_per_launch=args.steps_per_launch or 64, device=local,
+                            wide_min=args.wide_min)
         eng.run(args.warmup)
         eng.vm()
         torch.cuda.profiler.start()

@@ -9,6 +9,16 @@
 
 namespace gbh {
 
+// A synchan whose synapses carry different weights: its events are kept as
+// one bit per incoming synapse per future step (ring slot), the bits ranked
+// in the order the reference sums them, and weight/dt of each rank.
+struct SynW {
+    int64_t mbase;   // word of slot 0 in DevView::wmask (slot q at mbase + q * nwords)
+    int64_t wbase;   // weight/dt of rank 0 in DevView::wval
+    int nwords;      // 32 ranks per word
+    int pad;
+};
+
 struct DevView {
     const Tile *tiles;
     const TileType *types;
@@ -62,7 +72,105 @@ struct DevView {
     long long io_step0;
     const int *tin_start, *tin_off, *tin_idx;
     const int *tout_start, *tout_off, *tout_idx;
+    // stack elimination (TileType::stack): per-row flags (StackFlag) and a
+    // column of (right-hand side, diagonal or its reciprocal) per row, both
+    // at the tile's topo rows
+    const int *ltop;
+    double2 *col;
+    // synapses of weighted synchans (SynW): per synapse its bit's word for
+    // slot 0 (-1 for a synchan of one weight) and bit | nwords << 5
+    const int64_t *syn_out_mword;
+    const int *syn_out_mbit;
+    unsigned *wmask;
+    const SynW *synw;
+    const double *wval;
+    // spike detection runs in a pass of its own before each step (k_spikes),
+    // for networks with synapses that act in the step of the spike
+    int spike_pre;
 };
+
+// A neuron whose Vm is no longer finite: a NaN or infinity anywhere in its
+// tree reaches every row through the elimination within the step, so one
+// row per neuron per step is checked (after back substitution).
+__device__ __forceinline__ void finite_check(const DevView &v, double x, bool active)
+{
+    if (!(fabs(x) <= 1.7976931348623157e308) && active && v.status) atomicOr(v.status, ST_NONFINITE);
+}
+
+// Prefetch of the cache line holding *p into L1 (the loads of a later row).
+__device__ __forceinline__ void prefetch_l1(const void *p)
+{
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// One synaptic event, counted in the target synchan's ring slot for the step
+// it acts in; for a weighted synchan also its synapse's rank bit.
+__device__ __forceinline__ void put_event(unsigned *ring, int ring_len, unsigned *wmask, int64_t base, int delay,
+                                          int64_t mword, int mbit, long long step)
+{
+    const int slot = (int)((step + delay) % ring_len);
+    atomicAdd(&ring[base + (int64_t)slot * LANES], 1u);
+    if (mword >= 0) atomicOr(&wmask[mword + (int64_t)slot * (mbit >> 5)], 1u << (mbit & 31));
+}
+
+// h_dospike_event (hines_conn.c:44-58): an event on every synapse of the
+// neuron, counted as a spike.
+__device__ __forceinline__ void deliver_spike(const DevView &v, int64_t neuron, long long step)
+{
+    const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
+    for (int64_t e = e0; e < e1; ++e)
+        put_event(v.ring, v.ring_len, v.wmask, v.syn_out_base[e], v.syn_out_delay[e],
+                  v.syn_out_mword ? v.syn_out_mword[e] : -1, v.syn_out_mbit ? v.syn_out_mbit[e] : 0, step);
+    v.spikes[neuron] += 1ULL;
+    if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
+}
+
+// SPIKE_OP (hines_chip.c:266-276): the refractory counter counts down every
+// step; above threshold with the counter spent, the neuron fires and the
+// counter restarts. Returns the new counter.
+__device__ __forceinline__ int spike_op(const DevView &v, double Vm, double thresh, int cnt, int refract,
+                                        bool active, int64_t neuron, long long step)
+{
+    cnt -= 1;
+    if (Vm > thresh && cnt <= 0 && active) {
+        deliver_spike(v, neuron, step);
+        cnt = refract;
+    }
+    return cnt;
+}
+
+// The events due now in one synchan's ring cell (h_dosynchan ->
+// synchan HPROCESS, hines_conn.c:62-89, synchan.c:307-350): false if none;
+// otherwise act = the sum of weight/dt over them, from zero, in the
+// reference's order (its pending list puts a new event before the events
+// due the same step, so the newest is summed first). w_dt >= 0: every
+// synapse carries this weight/dt, one addition per event; w_dt < 0: the
+// synchan has weights per synapse, described by synw[-w_dt - 1], its due
+// bits summed in rank order. Clears what it consumed.
+__device__ __forceinline__ bool syn_due(const DevView &v, unsigned *cell, double w_dt, long long step, double &act)
+{
+    const unsigned n = *cell;
+    if (!n) return false;
+    *cell = 0u;
+    act = 0.0;
+    if (w_dt >= 0.0) {
+        for (unsigned q = 0; q < n; ++q) act += w_dt;
+    } else {
+        const SynW d = v.synw[(int64_t)(-w_dt) - 1];
+        unsigned *m = v.wmask + d.mbase + (int64_t)(step % v.ring_len) * d.nwords;
+        const double *w = v.wval + d.wbase;
+        for (int k = 0; k < d.nwords; ++k) {
+            unsigned b = m[k];
+            m[k] = 0u;
+            while (b) {
+                const int j = __ffs(b) - 1;
+                b &= b - 1;
+                act += w[k * 32 + j];
+            }
+        }
+    }
+    return true;
+}
 
 // Elimination of one solver with symmetric compartments (SymOp program at
 // sp, rows at stride STR): do_euler_hsolve / do_crank_hsolve

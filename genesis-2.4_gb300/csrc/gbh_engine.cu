@@ -70,11 +70,19 @@ struct DBuf {
     }
 };
 
+// A neuron's spike detector, for the pass before each step (k_spikes):
+// element indices of its compartment's Vm, its threshold field and its
+// counter rows, and its global neuron index.
+struct SpikeSrc {
+    int64_t vm, thresh, cnt, refr, neuron;
+};
+
 struct Launch {
     int tile0, tile1, smax, warps;
     int jit = -1;        // index of a specialised kernel, or -1 to interpret
     bool uniform = false; // every neuron of the type has the same tree
     bool wide = false;    // one neuron per block (wide tiles)
+    bool stack = false;   // stack elimination (smax = shared doubles per lane)
 };
 
 // Element idx of a block of rows starting at row `base`: lane-interleaved
@@ -118,9 +126,21 @@ struct gbh_engine {
     DBuf<double> d_RV;              // ravals rows of solvers with symmetric compartments
     DBuf<double> d_IT;              // itotal rows of storemode solvers
     DBuf<int> d_I, d_par;
+    DBuf<int> d_ltop;              // stack elimination: per-row flags (topo rows)
+    DBuf<double2> d_col;           // stack elimination: (rhs, diagonal) per row
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
     DBuf<int> d_out_delay;
+    // synchans whose synapses carry different weights (SynW)
+    DBuf<int64_t> d_out_mword, d_rmword;
+    DBuf<int> d_out_mbit, d_rmbit;
+    DBuf<SynW> d_synw;
+    DBuf<double> d_wval;
+    DBuf<unsigned> d_wmask;
+    // spike detection in a pass of its own (synapses acting in the spike's step)
+    bool spike_pre = false;
+    int nspike_src = 0;
+    DBuf<SpikeSrc> d_spike_src;
     DBuf<unsigned long long> d_spikes;
     // networks: cooperative multi-step launches (grid barrier every step)
     DBuf<unsigned> d_gbar;
@@ -201,6 +221,9 @@ struct gbh_engine {
     bool fuse_in = false;
 };
 
+// The spike-detection pass before a step (k_spikes), on stream st.
+int launch_spikes(gbh_engine *e, const gbh::DevView &v, long long step, cudaStream_t st);
+
 namespace {
 
 int fail_err(gbh_error *err, int code, const char *fmt, ...)
@@ -235,6 +258,79 @@ int micro_operands(int code)
     case M_SYN: return 6;
     default: return -1;
     }
+}
+
+// Which operands of a micro-op are field rows (bit i: operand i).
+int field_operands(int code)
+{
+    switch (code) {
+    case M_BEGIN: return 0x7;
+    case M_DOMAIN: case M_SCALE_FLUX: case M_SAME_GHK: case M_CHAN_G: return 0x1;
+    case M_SPIKE: return 0x1;
+    case M_ELMMPUMP: return 0x7;
+    case M_GHK: return 0x7;
+    case M_NERNST: case M_CHAN: case M_END: case M_ITLEAK: return 0x3;
+    case M_GATE: return 0x8;
+    case M_SYN: return 0x39;
+    case M_MGBLOCK: return 0x7;
+    default: return 0;
+    }
+}
+
+// Per slot of a type's program, the first and last field row it reads
+// (rows are allocated in program order, so a slot's fields are mostly one
+// contiguous range): what the stack kernels prefetch a few rows ahead.
+std::vector<int> slot_field_ranges(const std::vector<int> &prog, const TileType &tt)
+{
+    std::vector<int> out;
+    size_t pc = tt.prog_off;
+    for (int s = 0; s < tt.nslots; ++s) {
+        int lo = INT32_MAX, hi = -1;
+        for (;;) {
+            const int code = prog[pc];
+            const int n = micro_operands(code);
+            if (n < 0) break;
+            const int fm = field_operands(code);
+            for (int i = 0; i < n; ++i)
+                if ((fm >> i) & 1) {
+                    const int f = prog[pc + 1 + i];
+                    if (f >= 0) {
+                        lo = std::min(lo, f);
+                        hi = std::max(hi, f);
+                    }
+                }
+            pc += 1 + n;
+            if (code == M_END) break;
+        }
+        if (hi < 0) lo = hi = 0;
+        out.push_back(lo);
+        out.push_back(std::min(hi, lo + 31));
+    }
+    return out;
+}
+
+// Slot and rows of the spike detector in a type's program (M_SPIKE operands:
+// threshold field, counter and refractory int rows).
+bool spike_rows(const std::vector<int> &prog, const TileType &tt, int &slot, int &fth, int &icnt, int &iref)
+{
+    size_t pc = tt.prog_off;
+    for (int s = 0; s < tt.nslots; ++s) {
+        for (;;) {
+            const int code = prog[pc];
+            const int n = micro_operands(code);
+            if (n < 0) return false;
+            if (code == M_SPIKE) {
+                slot = s;
+                fth = prog[pc + 1];
+                icnt = prog[pc + 2];
+                iref = prog[pc + 3];
+                return true;
+            }
+            pc += 1 + n;
+            if (code == M_END) break;
+        }
+    }
+    return false;
 }
 
 // Fields the mixed-precision kernel reads as packed double-float pairs.
@@ -279,6 +375,12 @@ double unpack_df(double d)
 
 // Shared-memory budget per block for the elimination columns.
 constexpr int kSmemPerBlock = 96 * 1024;
+// Lane-mapped types of at least this many compartments that are not
+// specialised run the stack elimination (k_stack*) rather than the
+// interpreter's shared-memory columns (2 x compartments x 32 doubles a warp).
+constexpr int kStackMin = 32;
+// Shared memory a stack-elimination warp may take (doubles per lane).
+constexpr int kStackCapMax = 200 * 1024 / (LANES * (int)sizeof(double));
 
 // Composite tables on the device: FP64 copy (plus one padding row), axis
 // value pools and their geometry.
@@ -377,6 +479,70 @@ bool wide_plan(const std::vector<int> &prog, const TileType &tt, std::vector<int
     meta.insert(meta.end(), vprev.begin(), vprev.end());
     meta.insert(meta.end(), cprev.begin(), cprev.end());
     meta.insert(meta.end(), cpool.begin(), cpool.end());
+    return true;
+}
+
+// Stack elimination plan of one neuron (see k_stack): per-row StackFlag words
+// and the shared memory the two stacks need, in doubles per lane. Returns
+// false unless the rows are a post-order of the tree -- each row's last
+// child the row before it, its other children the top entries of the
+// forward stack, and on the way back the parent's solution on the top of the
+// backward stack -- which the Hines numbering of do_hnum
+// (hines_init.c:317-345) always gives; the neuron then runs another kernel.
+bool stack_plan(const std::vector<int> &parent, std::vector<int> &flags, int &cap)
+{
+    const int S = (int)parent.size();
+    std::vector<int> nk(S, 0), first(S, -1);
+    for (int s = 0; s < S; ++s) {
+        const int p = parent[s];
+        if (p < 0) continue;
+        if (p <= s || p >= S) return false;
+        if (nk[p]++ == 0) first[p] = s;
+    }
+    flags.assign(S, 0);
+    std::vector<int> st;
+    size_t fmax = 0, bmax = 0;
+    for (int s = 0; s < S; ++s) {
+        int f = 0;
+        if (nk[s] > 0) {
+            const int np = nk[s] - 1;
+            if (parent[s - 1] != s || np > FL_NPOP || (int)st.size() < np) return false;
+            for (int j = 0; j < np; ++j)
+                if (parent[st[st.size() - np + j]] != s) return false;
+            st.resize(st.size() - np);
+            f |= np | FL_CARRY_IN;
+        }
+        if (parent[s] >= 0) {
+            f |= FL_PARENT;
+            if (parent[s] == s + 1) {
+                f |= FL_CARRY_OUT;
+            } else {
+                f |= FL_PUSH;
+                st.push_back(s);
+                fmax = std::max(fmax, st.size());
+            }
+        }
+        flags[s] = f;
+    }
+    if (!st.empty()) return false;
+    for (int s = S - 1; s >= 0; --s) {
+        const int p = parent[s];
+        if (p >= 0 && p != s + 1) {
+            if (st.empty() || st.back() != p) return false;
+            flags[s] |= FL_XLOAD;
+            if (first[p] == s) {
+                flags[s] |= FL_XPOP;
+                st.pop_back();
+            }
+        }
+        if (nk[s] >= 2) {
+            flags[s] |= FL_XPUSH;
+            st.push_back(s);
+            bmax = std::max(bmax, st.size());
+        }
+    }
+    if (!st.empty()) return false;
+    cap = (int)std::max<size_t>(std::max(2 * fmax, bmax), 1);
     return true;
 }
 
@@ -485,6 +651,29 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             }
         }
     }
+    // ---- stack elimination for the remaining large lane-mapped types ----
+    for (size_t ti = 0; ti < e->types.size(); ++ti) {
+        TileType &tt = e->types[ti];
+        if (tt.wide || tt.sym || tt.nslots < kStackMin) continue;
+        int cap = 1;
+        bool ok = true;
+        std::vector<int> fl;
+        for (int i : members[ti]) {
+            int c = 0;
+            if (!stack_plan(dec.neurons[i].parent, fl, c)) {
+                ok = false;
+                break;
+            }
+            cap = std::max(cap, c);
+        }
+        if (ok && cap <= kStackCapMax) {
+            tt.stack = 1;
+            tt.scap = cap;
+            const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
+            tt.pf_off = (int)prog_pool.size();
+            prog_pool.insert(prog_pool.end(), pf.begin(), pf.end());
+        }
+    }
     // ---- event ring length from the synapse delays ----
     const bool local_syn = syn && syn->nsynapses > 0;
     const int64_t nrsyn = (remote && remote->nsources > 0) ? remote->src_start[remote->nsources] : 0;
@@ -492,9 +681,9 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     int maxd = 1;
     if (local_syn) {
         for (int64_t s = 0; s < syn->nsynapses; ++s) {
-            if (syn->delay_steps[s] < 1)
-                return fail_err(err, GBH_ERR_UNSUPPORTED, "synapse %lld has a delay below one step",
-                                (long long)s);
+            // (int)(delay/dt + 0.9) steps (synchan.c:199-200): zero for a delay under 0.1 dt
+            if (syn->delay_steps[s] < 0)
+                return fail_err(err, GBH_ERR_ARG, "synapse %lld has a negative delay", (long long)s);
             maxd = std::max(maxd, syn->delay_steps[s] + 1);
         }
     }
@@ -553,6 +742,9 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     std::vector<double> P(e->rows_fld * L, 0.0), V(e->rows_vm * L, 0.0), C(e->rows_pool * L, 0.0),
         A(e->rows_topo * L, 0.0), B(e->rows_topo * L, 0.0), Cb(e->rows_topo * L, 0.0);
     std::vector<int> I(e->rows_int * L, 0), par(e->rows_topo * L, -1);
+    bool any_stack = false;
+    for (const TileType &tt : e->types) any_stack = any_stack || tt.stack;
+    std::vector<int> LT(any_stack ? e->rows_topo * L : 1, 0);
     std::vector<double> RV(std::max<int64_t>(e->rows_rav, 1) * L, 0.0);
     // padding lanes: a passive row that solves to zero and never spikes
     for (const Tile &t : e->tiles) {
@@ -578,6 +770,12 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             B[at(t.topo, s, l, w)] = N.B[s];
             Cb[at(t.topo, s, l, w)] = N.C[s];
         }
+        if (e->types[t.type].stack) {
+            std::vector<int> fl;
+            int cap = 0;
+            stack_plan(N.parent, fl, cap);
+            for (int s = 0; s < N.nrows; ++s) LT[at(t.topo, s, l, false)] = fl[s];
+        }
         for (size_t f = 0; f < N.fsrc.size(); ++f) P[at(t.fld, f, l, w)] = N.fval[f];
         for (size_t k = 0; k < N.rav.size(); ++k) RV[at(t.rav, k, l, w)] = N.rav[k];
         for (size_t r = 0; r < N.iops.size(); ++r) I[at(t.ints, r, l, w)] = N.ival[r];
@@ -598,8 +796,21 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         }
     }
     // ---- synapses: CSR over global neuron index ----
-    std::vector<int64_t> out_start(gneuron + 1, 0), out_base;
-    std::vector<int> out_delay;
+    // Every synapse targets one synchan (a SYN2/SYN3 op of a neuron). A
+    // synchan whose synapses all carry one weight keeps weight/dt in its
+    // field and counts events; one with different weights gets a SynW
+    // descriptor (field value -(1 + index)): a bit per incoming synapse per
+    // ring slot, ranked in the order the reference sums the events due in
+    // one step -- newest first (synchan.c:239-300 inserts a new event before
+    // the pending ones due the same step): by effective delay ascending
+    // (later spikes), then by source in the global solver order descending,
+    // then by the source's message order descending.
+    std::vector<int64_t> out_start(gneuron + 1, 0), out_base, out_mword;
+    std::vector<int> out_delay, out_mbit;
+    std::vector<SynW> synw;
+    std::vector<double> wval;
+    int64_t nmask = 0;
+    e->spike_pre = false;
     if (e->has_network) {
         // synchan lookup: (solver, op) -> (neuron, syn row)
         std::unordered_map<int64_t, std::pair<int, int>> syn_at;
@@ -611,8 +822,16 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         std::vector<int> src_neuron(e->nsolvers, -1);
         for (int i = 0; i < nneu; ++i)
             if (dec.neurons[i].spike_op >= 0) src_neuron[dec.neurons[i].solver] = i;
-        std::vector<std::vector<std::pair<int64_t, int>>> per(gneuron);
-        std::unordered_map<int64_t, double> wset;
+        const int64_t first = remote ? remote->first_solver : 0;   // global index of local solver 0
+        // one record per synapse, local ones first (CSR order), then remote
+        struct SynRec {
+            int tn, srow;             // target neuron and synchan row
+            int dl;                   // effective delay (steps)
+            int64_t gsrc, k;          // global source index, index in its table
+            double wdt;               // weight / dt
+            int rank;
+        };
+        std::vector<SynRec> recs;
         for (int s = 0; s < e->nsolvers && local_syn; ++s) {
             for (int64_t k = syn->src_start[s]; k < syn->src_start[s + 1]; ++k) {
                 if (src_neuron[s] < 0)
@@ -625,74 +844,140 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 if (it == syn_at.end())
                     return fail_err(err, GBH_ERR_ARG, "synapse %lld: ops[%d] of solver %d is not a SYN2/SYN3 op",
                                     (long long)k, syn->target_op[k], ts);
-                const int tn = it->second.first, srow = it->second.second;
-                const double w = syn->weight[k] / e->dt;
-                const int64_t wkey = (int64_t)tn * 4096 + srow;
-                auto wi = wset.find(wkey);
-                if (wi == wset.end()) wset[wkey] = w;
-                else if (wi->second != w)
-                    return fail_err(err, GBH_ERR_UNSUPPORTED,
-                                    "synapses into one synchan (solver %d, ops[%d]) carry different weights", ts,
-                                    syn->target_op[k]);
                 const Neuron &SN = dec.neurons[src_neuron[s]];
                 int dl = syn->delay_steps[k];
                 // a target whose SYN2 op runs before the source's SPIKE op in the
                 // same step sees the event one step later (the countdown of this
                 // step is already spent)
                 if (ts < s || (ts == s && syn->target_op[k] < SN.spike_op)) dl += 1;
-                const Tile &tt = e->tiles[e->neuron_tile[tn]];
-                const int64_t base = (tt.syn + (int64_t)srow * e->ring_len) * LANES + e->neuron_lane[tn];
-                const int64_t gsrc = e->tiles[e->neuron_tile[src_neuron[s]]].first_neuron +
-                                     e->neuron_lane[src_neuron[s]];
-                per[gsrc].push_back({base, dl});
+                if (dl == 0) e->spike_pre = true;   // acts in the step of the spike
+                recs.push_back({it->second.first, it->second.second, dl, first + s, k, syn->weight[k] / e->dt, 0});
             }
         }
-        for (int64_t g = 0; g < gneuron; ++g) {
-            out_start[g + 1] = out_start[g] + (int64_t)per[g].size();
-            for (auto &pr : per[g]) {
-                out_base.push_back(pr.first);
-                out_delay.push_back(pr.second);
-            }
-        }
-        // synapses from remote sources: ring bases and effective delays, the
-        // same uniform-weight rule per target synchan
+        const size_t nlocal = recs.size();
         if (remote && remote->nsources > 0) {
             e->nremote = remote->nsources;
-            std::vector<int64_t> rbase;
-            std::vector<int> rdelay;
-            for (int64_t k = 0; k < nrsyn; ++k) {
-                const int ts = remote->target_solver[k];
-                if (ts < 0 || ts >= e->nsolvers)
-                    return fail_err(err, GBH_ERR_ARG, "remote synapse %lld targets solver %d", (long long)k, ts);
-                auto it = syn_at.find((int64_t)ts * (1LL << 32) + remote->target_op[k]);
-                if (it == syn_at.end())
-                    return fail_err(err, GBH_ERR_ARG, "remote synapse %lld: ops[%d] of solver %d is not a SYN2/SYN3 op",
-                                    (long long)k, remote->target_op[k], ts);
-                const int tn = it->second.first, srow = it->second.second;
-                const double w = remote->weight[k] / e->dt;
-                const int64_t wkey = (int64_t)tn * 4096 + srow;
-                auto wi = wset.find(wkey);
-                if (wi == wset.end()) wset[wkey] = w;
-                else if (wi->second != w)
-                    return fail_err(err, GBH_ERR_UNSUPPORTED,
-                                    "synapses into one synchan (solver %d, ops[%d]) carry different weights", ts,
-                                    remote->target_op[k]);
-                const Tile &tt = e->tiles[e->neuron_tile[tn]];
-                rbase.push_back((tt.syn + (int64_t)srow * e->ring_len) * LANES + e->neuron_lane[tn]);
-                rdelay.push_back(remote->delay_steps[k]);
+            for (int g = 0; g < remote->nsources; ++g) {
+                for (int64_t k = remote->src_start[g]; k < remote->src_start[g + 1]; ++k) {
+                    const int ts = remote->target_solver[k];
+                    if (ts < 0 || ts >= e->nsolvers)
+                        return fail_err(err, GBH_ERR_ARG, "remote synapse %lld targets solver %d", (long long)k, ts);
+                    if (remote->delay_steps[k] < 1)
+                        return fail_err(err, GBH_ERR_UNSUPPORTED,
+                                        "remote synapse %lld acts within the step of the spike: spikes are exchanged "
+                                        "between steps", (long long)k);
+                    auto it = syn_at.find((int64_t)ts * (1LL << 32) + remote->target_op[k]);
+                    if (it == syn_at.end())
+                        return fail_err(err, GBH_ERR_ARG,
+                                        "remote synapse %lld: ops[%d] of solver %d is not a SYN2/SYN3 op",
+                                        (long long)k, remote->target_op[k], ts);
+                    recs.push_back({it->second.first, it->second.second, remote->delay_steps[k], (int64_t)g, k,
+                                    remote->weight[k] / e->dt, 0});
+                }
+            }
+        }
+        // group by target synchan; weights and ranks
+        std::map<int64_t, std::vector<size_t>> by_tgt;
+        for (size_t r = 0; r < recs.size(); ++r) by_tgt[(int64_t)recs[r].tn * 4096 + recs[r].srow].push_back(r);
+        std::vector<int64_t> rec_mword(recs.size(), -1);
+        std::vector<int> rec_mbit(recs.size(), 0);
+        std::unordered_map<int64_t, double> wfield;   // synchan -> value of its weight field
+        for (auto &kv : by_tgt) {
+            std::vector<size_t> &v = kv.second;
+            bool uniform = true;
+            for (size_t r : v) uniform = uniform && recs[r].wdt == recs[v[0]].wdt;
+            if (uniform) {
+                wfield[kv.first] = recs[v[0]].wdt;
+                continue;
+            }
+            std::sort(v.begin(), v.end(), [&](size_t a, size_t b) {
+                const SynRec &x = recs[a], &y = recs[b];
+                if (x.dl != y.dl) return x.dl < y.dl;
+                if (x.gsrc != y.gsrc) return x.gsrc > y.gsrc;
+                return x.k > y.k;
+            });
+            SynW d{};
+            d.nwords = (int)((v.size() + 31) / 32);
+            d.mbase = nmask;
+            d.wbase = (int64_t)wval.size();
+            nmask += (int64_t)d.nwords * e->ring_len;
+            for (size_t q = 0; q < v.size(); ++q) {
+                wval.push_back(recs[v[q]].wdt);
+                rec_mword[v[q]] = d.mbase + (int64_t)(q >> 5);
+                rec_mbit[v[q]] = (int)(q & 31) | (d.nwords << 5);
+            }
+            wfield[kv.first] = -(double)(synw.size() + 1);
+            synw.push_back(d);
+        }
+        const bool weighted = !synw.empty();
+        std::vector<std::vector<size_t>> per(gneuron);
+        for (size_t r = 0; r < nlocal; ++r) {
+            const int s = (int)(recs[r].gsrc - first);
+            const int64_t gs = e->tiles[e->neuron_tile[src_neuron[s]]].first_neuron + e->neuron_lane[src_neuron[s]];
+            per[gs].push_back(r);
+        }
+        auto ring_base = [&](const SynRec &x) {
+            const Tile &tt = e->tiles[e->neuron_tile[x.tn]];
+            return (tt.syn + (int64_t)x.srow * e->ring_len) * LANES + e->neuron_lane[x.tn];
+        };
+        for (int64_t g = 0; g < gneuron; ++g) {
+            out_start[g + 1] = out_start[g] + (int64_t)per[g].size();
+            for (size_t r : per[g]) {
+                out_base.push_back(ring_base(recs[r]));
+                out_delay.push_back(recs[r].dl);
+                if (weighted) {
+                    out_mword.push_back(rec_mword[r]);
+                    out_mbit.push_back(rec_mbit[r]);
+                }
+            }
+        }
+        // synapses from remote sources: ring bases, effective delays and rank bits
+        if (remote && remote->nsources > 0) {
+            std::vector<int64_t> rbase, rmword;
+            std::vector<int> rdelay, rmbit;
+            for (size_t r = nlocal; r < recs.size(); ++r) {
+                rbase.push_back(ring_base(recs[r]));
+                rdelay.push_back(recs[r].dl);
+                rmword.push_back(rec_mword[r]);
+                rmbit.push_back(rec_mbit[r]);
             }
             std::vector<int64_t> rstart(remote->src_start, remote->src_start + remote->nsources + 1);
             if (e->d_rstart.upload(rstart) || e->d_rbase.upload(rbase) || e->d_rdelay.upload(rdelay) ||
-                e->d_rbits.alloc(((size_t)remote->nsources + 7) / 8))
+                e->d_rbits.alloc(((size_t)remote->nsources + 7) / 8) ||
+                (weighted && (e->d_rmword.upload(rmword) || e->d_rmbit.upload(rmbit))))
                 return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
         }
-        for (auto &kv : wset) {
+        for (auto &kv : wfield) {
             const int tn = (int)(kv.first / 4096), srow = (int)(kv.first % 4096);
             const Neuron &N = dec.neurons[tn];
             const Tile &t = e->tiles[e->neuron_tile[tn]];
             for (size_t f = 0; f < N.fsrc.size(); ++f)
                 if (N.fsrc[f].kind == FS_WDT && N.fsrc[f].idx == srow)
                     P[at(t.fld, (int64_t)f, e->neuron_lane[tn], e->types[t.type].wide != 0)] = kv.second;
+        }
+        // spike detection before each step: every neuron with a spike detector
+        if (e->spike_pre) {
+            std::vector<SpikeSrc> ss;
+            for (int i = 0; i < nneu; ++i) {
+                const Neuron &N = dec.neurons[i];
+                if (N.spike_op < 0) continue;
+                const Tile &t = e->tiles[e->neuron_tile[i]];
+                const TileType &tt = e->types[t.type];
+                const int l = e->neuron_lane[i];
+                const bool w = tt.wide != 0;
+                int slot = -1, fth = -1, icnt = -1, iref = -1;
+                if (!spike_rows(prog_pool, tt, slot, fth, icnt, iref))
+                    return fail_err(err, GBH_ERR_ARG, "solver %d: spike detector not found in its program", N.solver);
+                SpikeSrc x;
+                x.vm = at(t.vm, slot, l, w);
+                x.thresh = at(t.fld, fth, l, w);
+                x.cnt = at(t.ints, icnt, l, w);
+                x.refr = at(t.ints, iref, l, w);
+                x.neuron = t.first_neuron + l;
+                ss.push_back(x);
+            }
+            e->nspike_src = (int)ss.size();
+            if (e->d_spike_src.upload(ss)) return fail_err(err, GBH_ERR_CUDA, "%s", g_last_error);
         }
     }
     // ---- tables ----
@@ -748,12 +1033,21 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_Cb.upload(Cb);
     rc |= e->d_I.upload(I);
     rc |= e->d_par.upload(par);
+    rc |= e->d_ltop.upload(LT);
+    if (any_stack) rc |= e->d_col.alloc(e->rows_topo * L);
     rc |= e->d_giv.upload(std::vector<double>(e->rows_giv * L, 0.0));
     rc |= e->d_stab.upload(stab);
     rc |= e->d_ring.upload(std::vector<unsigned>(e->rows_syn * L, 0u));
     rc |= e->d_out_start.upload(out_start);
     rc |= e->d_out_base.upload(out_base);
     rc |= e->d_out_delay.upload(out_delay);
+    if (!synw.empty()) {
+        rc |= e->d_out_mword.upload(out_mword);
+        rc |= e->d_out_mbit.upload(out_mbit);
+        rc |= e->d_synw.upload(synw);
+        rc |= e->d_wval.upload(wval);
+        rc |= e->d_wmask.upload(std::vector<unsigned>(nmask, 0u));
+    }
     rc |= e->d_spikes.upload(std::vector<unsigned long long>(gneuron + 1, 0ULL));
     if (e->has_network) rc |= e->d_spiked.upload(std::vector<unsigned>((gneuron + 31) / 32 + 1, 0u));
     rc |= e->d_status.upload(std::vector<int>(1, 0));
@@ -876,6 +1170,18 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         }
         const int smax = e->types[ty0].nslots;
         size_t t1 = t0;
+        if (e->types[ty0].stack) {   // one warp per tile, every size in one launch
+            int cap = 1;
+            while (t1 < e->tiles.size() && type_jit[e->tiles[t1].type] < 0 && e->types[e->tiles[t1].type].stack) {
+                cap = std::max(cap, e->types[e->tiles[t1].type].scap);
+                ++t1;
+            }
+            Launch L{(int)t0, (int)t1, cap, 1};
+            L.stack = true;
+            e->launches.push_back(L);
+            t0 = t1;
+            continue;
+        }
         if (e->types[ty0].wide) {   // one block per neuron
             while (t1 < e->tiles.size() && e->types[e->tiles[t1].type].wide &&
                    e->types[e->tiles[t1].type].nslots * 2 > smax)
@@ -927,6 +1233,8 @@ DevView view_of(gbh_engine *e)
     v.CD = e->d_CD.p;
     v.S = e->d_S.p;
     v.parent = e->d_par.p;
+    v.ltop = e->d_ltop.p;
+    v.col = e->d_col.p;
     v.A = e->d_A.p;
     v.B = e->d_B.p;
     v.Cb = e->d_Cb.p;
@@ -936,6 +1244,12 @@ DevView view_of(gbh_engine *e)
     v.syn_out_start = e->d_out_start.p;
     v.syn_out_base = e->d_out_base.p;
     v.syn_out_delay = e->d_out_delay.p;
+    v.syn_out_mword = e->d_out_mword.p;
+    v.syn_out_mbit = e->d_out_mbit.p;
+    v.wmask = e->d_wmask.p;
+    v.synw = e->d_synw.p;
+    v.wval = e->d_wval.p;
+    v.spike_pre = e->spike_pre ? 1 : 0;
     v.spikes = e->d_spikes.p;
     v.spiked = e->has_network ? e->d_spiked.p : nullptr;
     v.stablist = e->d_stab.p;
@@ -961,7 +1275,10 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
         return GBH_OK;
     }
     cudaError_t ce;
-    if (L.wide)
+    if (L.stack)
+        ce = mixed ? launch_mixed_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, st)
+                   : launch_fp64_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, st);
+    else if (L.wide)
         ce = mixed ? launch_mixed_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st)
                    : launch_fp64_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st);
     else
@@ -988,9 +1305,16 @@ int issue_steps(gbh_engine *e, const DevView &v, int nsteps, long long step0, bo
     const int nl = (int)e->launches.size();
     const int ns = (int)e->side.size();
     const int plain = giv_last ? nsteps - 1 : nsteps;
+    auto spikes = [&](long long step, cudaStream_t s) {   // spike detection before the step
+        if (!e->spike_pre) return GBH_OK;
+        const int rc = launch_spikes(e, v, step, s);
+        if (!rc && kernels) ++*kernels;
+        return rc;
+    };
     if (nl <= 1 || ns == 0) {
         for (int done = 0; done < plain;) {
-            const int k = std::min(e->steps_per_launch, plain - done);
+            const int k = e->spike_pre ? 1 : std::min(e->steps_per_launch, plain - done);
+            if (spikes(step0 + done, st)) return GBH_ERR_CUDA;
             for (const Launch &L : e->launches) {
                 const int rc = launch_one(e, v, L, k, step0 + done, mixed, false, st);
                 if (rc) return rc;
@@ -1002,6 +1326,7 @@ int issue_steps(gbh_engine *e, const DevView &v, int nsteps, long long step0, bo
         const int span = e->has_network ? 1 : std::max(plain, 1);
         for (int done = 0; done < plain; done += span) {
             const int n = std::min(span, plain - done);
+            if (spikes(step0 + done, st)) return GBH_ERR_CUDA;
             CK(cudaEventRecord(e->ev_fork, st));
             for (int i = 0; i < ns; ++i) CK(cudaStreamWaitEvent(e->side[i], e->ev_fork, 0));
             for (int li = 0; li < nl; ++li) {
@@ -1022,6 +1347,7 @@ int issue_steps(gbh_engine *e, const DevView &v, int nsteps, long long step0, bo
         }
     }
     if (giv_last && nsteps > 0) {
+        if (spikes(step0 + nsteps - 1, st)) return GBH_ERR_CUDA;
         for (const Launch &L : e->launches) {
             const int rc = launch_one(e, v, L, 1, step0 + nsteps - 1, mixed, true, st);
             if (rc) return rc;
@@ -1212,7 +1538,7 @@ int autotune_trials(gbh_engine *e)
     // networks: the cooperative multi-step launch against the best per-step plan
     bool any_wide = false;
     for (const TileType &tt : e->types) any_wide = any_wide || tt.wide;
-    if (e->has_network && e->nremote == 0 && e->d_gbar.p && !any_wide) {
+    if (e->has_network && e->nremote == 0 && e->d_gbar.p && !any_wide && !e->spike_pre) {
         for (size_t k = 0; k < e->jits.size(); ++k) e->jits[k] = e->jit_var[k][best_v];
         e->jit_choice = best_v;
         e->steps_per_launch = best_s;
@@ -1350,14 +1676,39 @@ __global__ void k_io(const double *V, const int64_t *out_addr, int n_out, double
 // synapses adds one event to its target synchan's ring slot for the step
 // the spike acts in.
 __global__ void k_deliver_remote(const unsigned char *bits, int n, const int64_t *start, const int64_t *base,
-                                 const int *delay, unsigned *ring, int ring_len, long long step)
+                                 const int *delay, const int64_t *mword, const int *mbit, unsigned *ring,
+                                 unsigned *wmask, int ring_len, long long step)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !(bits[i >> 3] & (1u << (i & 7)))) return;
-    for (int64_t k = start[i]; k < start[i + 1]; ++k) {
-        const int slot = (int)((step + delay[k]) % ring_len);
-        atomicAdd(&ring[base[k] + (int64_t)slot * LANES], 1u);
+    for (int64_t k = start[i]; k < start[i + 1]; ++k)
+        put_event(ring, ring_len, wmask, base[k], delay[k], mword ? mword[k] : -1, mbit ? mbit[k] : 0, step);
+}
+
+// Spike detection of every neuron with a spike detector, before the step's
+// channel programs (networks whose synapses can act in the step of the
+// spike): SPIKE_OP reads only the compartment's Vm at the start of the step
+// and the neuron's own counters, so the step kernels then skip it.
+__global__ void k_spikes(DevView v, const SpikeSrc *src, int n, long long step0)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long step = (v.step_dev ? *v.step_dev : 0) + step0;
+    const SpikeSrc x = src[i];
+    v.I[x.cnt] = spike_op(v, v.V[x.vm], v.P[x.thresh], v.I[x.cnt], v.I[x.refr], true, x.neuron, step);
+}
+
+int launch_spikes(gbh_engine *e, const DevView &v, long long step, cudaStream_t st)
+{
+    const int threads = 128, blocks = (e->nspike_src + threads - 1) / threads;
+    if (blocks > 0) k_spikes<<<blocks, threads, 0, st>>>(v, e->d_spike_src.p, e->nspike_src, step);
+    const cudaError_t ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+        set_last("spike detection launch failed: %s", cudaGetErrorString(ce));
+        return GBH_ERR_CUDA;
     }
+    e->stats.launches++;
+    return GBH_OK;
 }
 
 __global__ void k_gather_outputs(const double *V, const int64_t *addr, int n, double *out)
@@ -1938,7 +2289,8 @@ gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, con
     e->steps_per_launch = e->opt.steps_per_launch > 0 ? e->opt.steps_per_launch : 64;
     bool wide_tiles = false;
     for (const TileType &tt : e->types) wide_tiles = wide_tiles || tt.wide;
-    if (e->opt.steps_per_launch < 0 && e->has_network && e->nremote == 0 && !wide_tiles) {   // forced cooperative plan
+    if (e->opt.steps_per_launch < 0 && e->has_network && e->nremote == 0 && !wide_tiles &&
+        !e->spike_pre) {   // forced cooperative plan
         e->net_coop = true;
         e->net_spl = -e->opt.steps_per_launch;
     }
@@ -1955,6 +2307,10 @@ gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, con
     for (const Neuron &N : e->dec.neurons) comps += N.nrows;
     e->stats.compartments = comps;
     e->stats.tiles = (int64_t)e->tiles.size();
+    for (const Launch &L : e->launches) {
+        if (L.wide) e->stats.wide_tiles += L.tile1 - L.tile0;
+        if (L.stack) e->stats.stack_tiles += L.tile1 - L.tile0;
+    }
     e->stats.precision = e->opt.precision;
     e->stats.steps_per_launch = e->net_coop ? e->net_spl : e->steps_per_launch;
     e->stats.cooperative = e->net_coop ? 1 : 0;
@@ -2019,9 +2375,10 @@ int gbh_run(gbh_engine *e, int nsteps)
     CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {
         set_last("device status word 0x%x (%s)", status,
-                 (status & ST_SMEM) ? "kernel launched with too little shared memory"
-                                    : (status & ST_EVENT_OVERFLOW) ? "synaptic event ring overflow"
-                                                                   : "unimplemented micro-op reached");
+                 (status & ST_SMEM)        ? "kernel launched with too little shared memory"
+                 : (status & ST_NONFINITE) ? "a neuron's Vm is NaN or infinite"
+                 : (status & ST_BARRIER)   ? "a grid barrier wait ran out"
+                                           : "unimplemented micro-op reached");
         return GBH_ERR_DEVICE;
     }
     return GBH_OK;
@@ -2176,7 +2533,8 @@ int gbh_deliver_remote(gbh_engine *e, const uint8_t *source_bits)
     CK(cudaMemcpyAsync(e->d_rbits.p, source_bits, nb, cudaMemcpyHostToDevice, e->stream));
     const int threads = 256, blocks = (e->nremote + threads - 1) / threads;
     k_deliver_remote<<<blocks, threads, 0, e->stream>>>(e->d_rbits.p, e->nremote, e->d_rstart.p, e->d_rbase.p,
-                                                        e->d_rdelay.p, e->d_ring.p, e->ring_len, e->step - 1);
+                                                        e->d_rdelay.p, e->d_rmword.p, e->d_rmbit.p, e->d_ring.p,
+                                                        e->d_wmask.p, e->ring_len, e->step - 1);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e->stream));   // the host bitmap may be reused on return
     e->stats.launches++;
@@ -2582,7 +2940,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

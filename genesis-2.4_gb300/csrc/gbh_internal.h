@@ -122,6 +122,28 @@ struct TileType {
     int sym_off;     // sym: prog-pool offset of its decoded triples (SymOp)
     int nrav;        // sym: ravals rows (rewritten during each step, as in the reference)
     int nitot;       // storemode: itotal rows, zeroed at the start of every step
+    int stack;       // lane-mapped with the stack elimination (k_stack*): every neuron's rows are
+                     // a post-order of its tree (each subtree contiguous, its root last)
+    int scap;        // stack: shared-memory doubles per lane its neurons need
+    int pf_off;      // stack: prog-pool offset of each slot's [first, last] field row (prefetch)
+};
+
+// Per-row flags of the stack elimination (DevView::ltop, topo rows, one word
+// per lane). Forward, rows ascending: a row's last child is the row before
+// it, whose contribution is carried in registers; its other children's
+// contributions wait on a per-lane stack (they are its top FL_NPOP entries,
+// in ascending row order). Backward, rows descending: the solution of the
+// row after is in a register; a row whose parent is further away reads the
+// parent's solution from a per-lane stack of branch points.
+enum StackFlag {
+    FL_NPOP = 0xff,          // stack entries to apply: children other than the last
+    FL_CARRY_IN = 1 << 8,    // the previous row is this row's last child
+    FL_PARENT = 1 << 9,      // the row has a parent
+    FL_CARRY_OUT = 1 << 10,  // the parent is the next row
+    FL_PUSH = 1 << 11,       // the parent is further away: push the contribution
+    FL_XLOAD = 1 << 12,      // backward: the parent's solution is on the stack top
+    FL_XPOP = 1 << 13,       // backward: the last reader of that entry (the parent's first child)
+    FL_XPUSH = 1 << 14       // backward: two or more children read this row's solution later
 };
 
 struct Tile {
@@ -142,7 +164,10 @@ struct Tile {
 };
 
 // Device status word bits
-enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_EVENT_OVERFLOW = 2, ST_SMEM = 4 /* launched with too little shared memory */,
-              ST_BARRIER = 8 /* a grid barrier wait ran out */ };
+// (bit 2 is unused: an event ring slot is consumed ring_len - 1 steps before
+// it is reused, every delay being shorter than the ring, so it cannot overflow)
+enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_SMEM = 4 /* launched with too little shared memory */,
+              ST_BARRIER = 8 /* a grid barrier wait ran out */,
+              ST_NONFINITE = 16 /* a neuron's Vm became NaN or infinite */ };
 
 }  // namespace gbh

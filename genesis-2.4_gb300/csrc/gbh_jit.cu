@@ -223,15 +223,8 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
                   << ", yvals, " << ncols << ", interp); ctab_base = cc.base;\n";
             break;
         case M_SPIKE:
-            o << "      { int cnt = " << E.I(a[1]) << " - 1;\n"
-              << "        if (Vm > " << E.P(a[0]) << " && cnt <= 0 && active) {\n"
-              << "          const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];\n"
-              << "          for (int64_t e = e0; e < e1; ++e) {\n"
-              << "            const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);\n"
-              << "            atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * 32], 1u); }\n"
-              << "          v.spikes[neuron] += 1ULL; if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));"
-              << " cnt = " << E.I(a[2]) << "; }\n"
-              << "        " << E.I(a[1]) << " = cnt; }\n";
+            o << "      if (!v.spike_pre) " << E.I(a[1]) << " = spike_op(v, Vm, " << E.P(a[0]) << ", " << E.I(a[1])
+              << ", " << E.I(a[2]) << ", active, neuron, step);\n";
             break;
         case M_ELMMPUMP:
             o << "      { const double cx = Cw[sel * 32]; const double X = 1.0 / (cx + " << E.P(a[0])
@@ -383,9 +376,7 @@ bool emit_slot(Emit &E, int s, const int *&pc, const TableGeom &tg)
                     o << "        double X = *px * sl[0];\n"
                       << "        unsigned *cell = v.ring + ((tl.syn + (int64_t)" << srow
                       << " * v.ring_len + (int64_t)(step % v.ring_len)) * 32 + lane);\n"
-                      << "        const unsigned n = *cell;\n"
-                      << "        if (n) { const double wdt = " << E.P(fw)
-                      << "; double act = 0.0; for (unsigned q = 0; q < n; ++q) act += wdt; X += v.dt * act * sl[3]; *cell = 0u; }\n"
+                      << "        { double act; if (syn_due(v, cell, " << E.P(fw) << ", step, act)) X += v.dt * act * sl[3]; }\n"
                       << "        *px = X; const double Y = X * sl[1] + *py * sl[2]; *py = Y;";
                     if (mx) o << " Gk = df_mul(Gk, d2df(Y)); }\n";
                     else o << " Gk *= Y; }\n";
@@ -728,6 +719,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
         t << " }\n";
     }
+    t << "    finite_check(v, Vw[0], active);\n";
     t << "    if (v.io_out) {   // this step's outputs\n"
       << "      __syncwarp(); double *dst = v.io_out + (step - v.io_step0) * v.io_nout; const double *Vt = v.V + tl.vm * 32;\n"
       << "      for (int q = v.tout_start[t] + lane; q < v.tout_start[t + 1]; q += 32) dst[v.tout_idx[q]] = Vt[v.tout_off[q]]; }\n";

@@ -16,6 +16,12 @@ cudaError_t launch_mixed_wide(const DevView &v, int tile0, int tile1, int smax, 
                : wide_launch(k_wide_mixed<false>, v, tile0, tile1, smax, nsteps, step, st);
 }
 
+cudaError_t launch_mixed_stack(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step,
+                               bool giv, cudaStream_t st)
+{
+    return stack_launch_mixed(v, tile0, tile1, cap, nsteps, step, giv, st);
+}
+
 cudaError_t launch_mixed_coop(const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st)
 {
     return coop_launch(k_steps_mixed<false>, v, ntiles, smax, nsteps, step, st);

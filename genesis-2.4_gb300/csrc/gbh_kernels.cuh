@@ -132,21 +132,9 @@ __device__ __forceinline__ bool chan_compartment(const DevView &v, const ChanEnv
             ctab_base = cc.base;
             pc += 1;
         } else if (code == M_SPIKE) {
-            int cnt = N.I[(pc[2]) * STR] - 1;
-            if (Vm > N.P[(pc[1]) * STR]) {
-                if (cnt <= 0 && active) {
-                    // h_dospike_event: deliver to every target synchan
-                    const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
-                    for (int64_t e = e0; e < e1; ++e) {
-                        const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
-                        atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
-                    }
-                    v.spikes[neuron] += 1ULL;
-                    if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
-                    cnt = N.I[(pc[3]) * STR];
-                }
-            }
-            N.I[(pc[2]) * STR] = cnt;
+            if (!v.spike_pre)   // else done by k_spikes before the step
+                N.I[(pc[2]) * STR] = spike_op(v, Vm, N.P[(pc[1]) * STR], N.I[(pc[2]) * STR], N.I[(pc[3]) * STR],
+                                              active, neuron, step);
             pc += 4;
         } else if (code == M_ELMMPUMP) {
             const double cx = N.C[(sel) * STR];
@@ -298,14 +286,8 @@ __device__ __forceinline__ bool chan_compartment(const DevView &v, const ChanEnv
                     double X = *px * sl[0];
                     unsigned *cell = N.ring + ((int64_t)pc[3] * v.ring_len +
                                                (int64_t)(step % v.ring_len)) * LANES;
-                    const unsigned n = *cell;
-                    if (n) {
-                        const double wdt = N.P[(pc[6]) * STR];
-                        double act = 0.0;
-                        for (unsigned q = 0; q < n; ++q) act += wdt;
-                        X += v.dt * act * sl[3];
-                        *cell = 0u;
-                    }
+                    double act;
+                    if (syn_due(v, cell, N.P[(pc[6]) * STR], step, act)) X += v.dt * act * sl[3];
                     *px = X;
                     const double Y = X * sl[1] + *py * sl[2];
                     *py = Y;
@@ -478,10 +460,196 @@ k_steps(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
             }
         }
         }
+        finite_check(v, Vw[0], active);
         // cooperative multi-step launch: every tile's events of this step
         // are in the rings before any tile starts the next step
         if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
     }
+}
+
+// ------------------------------------------------------------ stack elimination
+// Lane-mapped tiles of large neurons (TileType::stack): one neuron per lane
+// as in k_steps, but the rows never sit in shared memory as columns. Each
+// neuron's rows are a post-order of its tree (the Hines numbering of
+// do_hnum, hines_init.c:317-345: every subtree contiguous, its root last), so
+// the forward elimination runs fused with the channel phase, row by row: the
+// row's own right-hand side and diagonal, minus its children's contributions
+// in ascending row order -- the older children's from a per-lane stack in
+// shared memory, the last child's (the previous row) from registers -- and
+// then its own contribution, pushed or carried. The pool phase follows (it
+// reads Vm and concentrations, never a row's diagonal), then back
+// substitution in descending row order from the per-row (rhs, diagonal)
+// column in global memory. The operations and their order per row are those
+// of the sequential sweep (hines_solve.c:223-296), so FP64 results are the
+// reference's bit for bit. Shared memory: cap doubles per lane (16 bytes per
+// pending contribution, 8 per pending branch-point solution).
+template <typename G, bool GIV>
+__global__ void __launch_bounds__(32, 16)
+k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
+{
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x;
+    const int t = tile0 + blockIdx.x;
+    if (t >= tile1) return;
+    {
+        unsigned dsz;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsz));
+        if (dsz < (unsigned)cap * LANES * sizeof(double)) {
+            if (v.status && lane == 0) atomicOr(v.status, ST_SMEM);
+            return;
+        }
+    }
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const double *xvals = v.xyvals + tg.xv_off;
+    const double *yvals = tg.yv_off >= 0 ? v.xyvals + tg.yv_off : xvals;
+    const bool active = lane < tl.nlanes;
+
+    double *Pw = v.P + tl.fld * LANES + lane;
+    double *Vw = v.V + tl.vm * LANES + lane;
+    double *Cw = v.C + tl.pools * LANES + lane;
+    double *Fw = v.F + tl.pools * LANES + lane;
+    const int *lt = v.ltop + tl.topo * LANES + lane;
+    const double *Aw = v.A + tl.topo * LANES + lane;
+    const double *Bw = v.B + tl.topo * LANES + lane;
+    const double *Cbw = v.Cb + tl.topo * LANES + lane;
+    double2 *col = v.col + tl.topo * LANES + lane;
+    double *stk = sm + lane;      // entry j at stk[j * 32]
+    const int S = ty.nslots;
+    const int *pf = v.prog + ty.pf_off;   // per slot: first and last field row
+    constexpr int kPf = 2;                // rows of lookahead
+
+    ChanEnv<G> E;
+    E.tab = tab_ptr<G>(v, tg.tab_off);
+    E.xvals = xvals;
+    E.yvals = yvals;
+    E.tg = tg;
+    E.ncols = tg.ncols;
+    E.interp = ty.interp != 0;
+    E.c5 = ty.chanmode5 != 0;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = Pw;
+    NR.I = v.I + tl.ints * LANES + lane;
+    NR.C = Cw;
+    NR.F = Fw;
+    NR.G = v.giv + tl.giv * LANES + lane;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.IT = v.IT + tl.itot * LANES + lane;
+    NR.ring = v.ring + tl.syn * LANES + lane;
+    NR.neuron = tl.first_neuron + lane;
+    NR.active = active;
+
+    for (int it = 0; it < nsteps; ++it) {
+        const long long step = sbase + step0 + it;
+        for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
+        ChanState cs;
+        chan_state_reset(cs, tg.ncols);
+        const int *pc = v.prog + ty.prog_off;
+        int top = 0;                    // stack entries (two doubles each)
+        double cd = 0.0, cr = 0.0;      // contribution carried to the next row
+        for (int s = 0; s < S; ++s) {
+            if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
+                const int q = s + kPf;
+                const int f0 = pf[2 * q], f1 = pf[2 * q + 1];
+                for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
+                prefetch_l1(&Vw[q * LANES]);
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&Aw[q * LANES]);
+                prefetch_l1(&Bw[q * LANES]);
+            }
+            double R, D;
+            if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
+            }
+            const int f = lt[s * LANES];
+            const int np = f & FL_NPOP;
+            top -= np;
+            for (int j = 0; j < np; ++j) {
+                D -= stk[(2 * (top + j)) * LANES];
+                R -= stk[(2 * (top + j) + 1) * LANES];
+            }
+            if (f & FL_CARRY_IN) {
+                D -= cd;
+                R -= cr;
+            }
+            col[s * LANES] = make_double2(R, D);
+            if (f & FL_PARENT) {
+                const double temp = Aw[s * LANES] / D;
+                const double pd = Bw[s * LANES] * temp, pr = R * temp;
+                if (f & FL_CARRY_OUT) {
+                    cd = pd;
+                    cr = pr;
+                } else {
+                    stk[(2 * top) * LANES] = pd;
+                    stk[(2 * top + 1) * LANES] = pr;
+                    ++top;
+                }
+            }
+        }
+        {
+            PoolLane PL;
+            PL.C = Cw;
+            PL.F = Fw;
+            PL.CR = v.CR ? v.CR + tl.pools * LANES + lane : nullptr;
+            PL.CD = NR.CD;
+            PL.S = v.S ? v.S + tl.scr * LANES + lane : nullptr;
+            PL.P = Pw;
+            PL.V = Vw;
+            PL.dt = v.dt;
+            PL.crank = ty.crank;
+            if (!pool_phase<LANES>(v.prog + ty.pool_off, PL)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
+            }
+        }
+        double xn = 0.0;   // solution of the row after
+        top = 0;
+        for (int s = S - 1; s >= 0; --s) {
+            if (s >= kPf) {
+                const int q = s - kPf;
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&col[q * LANES]);
+                prefetch_l1(&Cbw[q * LANES]);
+                if (ty.crank) prefetch_l1(&Vw[q * LANES]);
+            }
+            const int f = lt[s * LANES];
+            const double2 rd = col[s * LANES];
+            double r = rd.x;
+            if (f & FL_PARENT) {
+                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
+                if (f & FL_XPOP) --top;
+                r -= Cbw[s * LANES] * xp;
+            }
+            r = r / rd.y;
+            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
+            xn = r;
+            if (ty.crank) {
+                const double old = Vw[s * LANES];
+                Vw[s * LANES] = r + r - old;
+            } else {
+                Vw[s * LANES] = r;
+            }
+        }
+        finite_check(v, xn, active);   // row 0's solution
+    }
+}
+
+template <typename G>
+cudaError_t stack_launch(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step, bool giv,
+                         cudaStream_t st)
+{
+    const size_t smem = (size_t)cap * LANES * sizeof(double);
+    auto fn = giv ? k_stack<G, true> : k_stack<G, false>;
+    if (smem > 48 * 1024) {
+        const cudaError_t ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ce != cudaSuccess) return ce;
+    }
+    fn<<<tile1 - tile0, LANES, smem, st>>>(v, tile0, tile1, cap, nsteps, step);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ wide tiles
@@ -682,6 +850,7 @@ k_wide(DevView v, int tile0, int tile1, int smax, int nsteps, long long step0)
             }
             __syncthreads();
         }
+        if (tid == 0) finite_check(v, V[0], true);
     }
 }
 
@@ -716,6 +885,13 @@ cudaError_t launch_fp64(const DevView &v, int tile0, int tile1, int smax, int wa
                         long long step, bool giv, cudaStream_t st);
 cudaError_t launch_mixed(const DevView &v, int tile0, int tile1, int smax, int warps, int nsteps,
                          long long step, bool giv, cudaStream_t st);
+
+// Stack elimination tiles (TileType::stack), one warp per tile, cap doubles
+// of shared memory per lane.
+cudaError_t launch_fp64_stack(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step, bool giv,
+                              cudaStream_t st);
+cudaError_t launch_mixed_stack(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step,
+                               bool giv, cudaStream_t st);
 
 // Cooperative multi-step launch over tiles [0, ntiles), one warp per block,
 // with a grid barrier after every step (v.gbar set): every block must be

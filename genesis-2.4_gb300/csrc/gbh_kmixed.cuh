@@ -102,20 +102,9 @@ __device__ __forceinline__ bool chan_compartment_df(const DevView &v, const Chan
             locate_df(cc, d2df(N.C[(sel) * STR]), ynmin, yinv, tg.ydivs, ncols);
             pc += 1;
         } else if (code == M_SPIKE) {
-            int cnt = N.I[(pc[2]) * STR] - 1;
-            if (Vm > N.P[(pc[1]) * STR]) {
-                if (cnt <= 0 && active) {
-                    const int64_t e0 = v.syn_out_start[neuron], e1 = v.syn_out_start[neuron + 1];
-                    for (int64_t e = e0; e < e1; ++e) {
-                        const int slot = (int)((step + v.syn_out_delay[e]) % v.ring_len);
-                        atomicAdd(&v.ring[v.syn_out_base[e] + (int64_t)slot * LANES], 1u);
-                    }
-                    v.spikes[neuron] += 1ULL;
-                    if (v.spiked) atomicOr(&v.spiked[neuron >> 5], 1u << (neuron & 31));
-                    cnt = N.I[(pc[3]) * STR];
-                }
-            }
-            N.I[(pc[2]) * STR] = cnt;
+            if (!v.spike_pre)   // else done by k_spikes before the step
+                N.I[(pc[2]) * STR] = spike_op(v, Vm, N.P[(pc[1]) * STR], N.I[(pc[2]) * STR], N.I[(pc[3]) * STR],
+                                              active, neuron, step);
             pc += 4;
         } else if (code == M_ELMMPUMP) {
             const double cx = N.C[(sel) * STR];
@@ -257,14 +246,8 @@ __device__ __forceinline__ bool chan_compartment_df(const DevView &v, const Chan
                     }
                     double X = *px * sl[0];
                     unsigned *cell = N.ring + ((int64_t)pc[3] * v.ring_len + (int64_t)(step % v.ring_len)) * LANES;
-                    const unsigned n = *cell;
-                    if (n) {
-                        const double wdt = N.P[(pc[6]) * STR];
-                        double act = 0.0;
-                        for (unsigned q = 0; q < n; ++q) act += wdt;
-                        X += v.dt * act * sl[3];
-                        *cell = 0u;
-                    }
+                    double act;
+                    if (syn_due(v, cell, N.P[(pc[6]) * STR], step, act)) X += v.dt * act * sl[3];
                     *px = X;
                     const double Y = X * sl[1] + *py * sl[2];
                     *py = Y;
@@ -429,10 +412,182 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
             }
         }
         }
+        finite_check(v, Vw[0], active);
         // cooperative multi-step launch: every tile's events of this step
         // are in the rings before any tile starts the next step
         if (v.gbar && !grid_sync(v.gbar, gridDim.x, v.status)) return;
     }
+}
+
+// Stack elimination of the mixed form (see k_stack in gbh_kernels.cuh): the
+// same row order and per-lane stacks; the diagonal's reciprocal is formed
+// once per row (rcp_newton) and kept in the column for back substitution.
+template <bool GIV>
+__global__ void __launch_bounds__(32, 16)
+k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
+{
+    extern __shared__ double sm[];
+    const int lane = threadIdx.x;
+    const int t = tile0 + blockIdx.x;
+    if (t >= tile1) return;
+    {
+        unsigned dsz;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsz));
+        if (dsz < (unsigned)cap * LANES * sizeof(double)) {
+            if (v.status && lane == 0) atomicOr(v.status, ST_SMEM);
+            return;
+        }
+    }
+    const long long sbase = v.step_dev ? *v.step_dev : 0;
+    const Tile tl = v.tiles[t];
+    const TileType ty = v.types[tl.type];
+    const TableGeom tg = v.tgeom[ty.table_set];
+    const bool active = lane < tl.nlanes;
+
+    double *Pw = v.P + tl.fld * LANES + lane;
+    double *Vw = v.V + tl.vm * LANES + lane;
+    double *Cw = v.C + tl.pools * LANES + lane;
+    double *Fw = v.F + tl.pools * LANES + lane;
+    const int *lt = v.ltop + tl.topo * LANES + lane;
+    const double *Aw = v.A + tl.topo * LANES + lane;
+    const double *Bw = v.B + tl.topo * LANES + lane;
+    const double *Cbw = v.Cb + tl.topo * LANES + lane;
+    double2 *col = v.col + tl.topo * LANES + lane;
+    double *stk = sm + lane;
+    const int S = ty.nslots;
+    const int *pf = v.prog + ty.pf_off;   // per slot: first and last field row
+    constexpr int kPf = 2;                // rows of lookahead
+
+    ChanEnvDF E;
+    E.tab = v.tabdf + tg.tab_off;
+    E.tg = tg;
+    E.ncols = tg.ncols;
+    E.xnmin = df_make(-tg.xmin_hi, -tg.xmin_lo);
+    E.xinv = df_make(tg.invdx_hi, tg.invdx_lo);
+    E.ynmin = df_make(-tg.ymin_hi, -tg.ymin_lo);
+    E.yinv = df_make(tg.invdy_hi, tg.invdy_lo);
+    E.c5 = ty.chanmode5 != 0;
+    E.has_cd = ty.has_cd != 0;
+    ChanRows NR;
+    NR.P = Pw;
+    NR.I = v.I + tl.ints * LANES + lane;
+    NR.C = Cw;
+    NR.F = Fw;
+    NR.G = v.giv + tl.giv * LANES + lane;
+    NR.CD = v.CD ? v.CD + tl.pools * LANES + lane : nullptr;
+    NR.IT = v.IT + tl.itot * LANES + lane;
+    NR.ring = v.ring + tl.syn * LANES + lane;
+    NR.neuron = tl.first_neuron + lane;
+    NR.active = active;
+
+    for (int it = 0; it < nsteps; ++it) {
+        const long long step = sbase + step0 + it;
+        for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
+        ChanStateDF cs;
+        chan_state_reset_df(cs);
+        const int *pc = v.prog + ty.prog_off;
+        int top = 0;
+        double cd = 0.0, cr = 0.0;
+        for (int s = 0; s < S; ++s) {
+            if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
+                const int q = s + kPf;
+                const int f0 = pf[2 * q], f1 = pf[2 * q + 1];
+                for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
+                prefetch_l1(&Vw[q * LANES]);
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&Aw[q * LANES]);
+                prefetch_l1(&Bw[q * LANES]);
+            }
+            double R, D;
+            if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
+            }
+            const int f = __ldg(&lt[s * LANES]);
+            const int np = f & FL_NPOP;
+            top -= np;
+            for (int j = 0; j < np; ++j) {
+                D -= stk[(2 * (top + j)) * LANES];
+                R -= stk[(2 * (top + j) + 1) * LANES];
+            }
+            if (f & FL_CARRY_IN) {
+                D -= cd;
+                R -= cr;
+            }
+            const double ri = rcp_newton(D);
+            col[s * LANES] = make_double2(R, ri);
+            if (f & FL_PARENT) {
+                const double temp = __ldg(&Aw[s * LANES]) * ri;
+                const double pd = __ldg(&Bw[s * LANES]) * temp, pr = R * temp;
+                if (f & FL_CARRY_OUT) {
+                    cd = pd;
+                    cr = pr;
+                } else {
+                    stk[(2 * top) * LANES] = pd;
+                    stk[(2 * top + 1) * LANES] = pr;
+                    ++top;
+                }
+            }
+        }
+        {
+            PoolLane PL;
+            PL.C = Cw;
+            PL.F = Fw;
+            PL.CR = v.CR ? v.CR + tl.pools * LANES + lane : nullptr;
+            PL.CD = NR.CD;
+            PL.S = v.S ? v.S + tl.scr * LANES + lane : nullptr;
+            PL.P = Pw;
+            PL.V = Vw;
+            PL.dt = v.dt;
+            PL.crank = ty.crank;
+            if (!pool_phase<LANES>(v.prog + ty.pool_off, PL)) {
+                if (v.status) atomicOr(v.status, ST_BAD_OP);
+                return;
+            }
+        }
+        double xn = 0.0;
+        top = 0;
+        for (int s = S - 1; s >= 0; --s) {
+            if (s >= kPf) {
+                const int q = s - kPf;
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&col[q * LANES]);
+                prefetch_l1(&Cbw[q * LANES]);
+                if (ty.crank) prefetch_l1(&Vw[q * LANES]);
+            }
+            const int f = __ldg(&lt[s * LANES]);
+            const double2 rd = col[s * LANES];
+            double r = rd.x;
+            if (f & FL_PARENT) {
+                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
+                if (f & FL_XPOP) --top;
+                r = fma(-__ldg(&Cbw[s * LANES]), xp, r);
+            }
+            r = r * rd.y;
+            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
+            xn = r;
+            if (ty.crank) {
+                const double old = Vw[s * LANES];
+                Vw[s * LANES] = fma(2.0, r, -old);
+            } else {
+                Vw[s * LANES] = r;
+            }
+        }
+        finite_check(v, xn, active);   // row 0's solution
+    }
+}
+
+inline cudaError_t stack_launch_mixed(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step,
+                                      bool giv, cudaStream_t st)
+{
+    const size_t smem = (size_t)cap * LANES * sizeof(double);
+    auto fn = giv ? k_stack_mixed<true> : k_stack_mixed<false>;
+    if (smem > 48 * 1024) {
+        const cudaError_t ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (ce != cudaSuccess) return ce;
+    }
+    fn<<<tile1 - tile0, LANES, smem, st>>>(v, tile0, tile1, cap, nsteps, step);
+    return cudaGetLastError();
 }
 
 // Wide tiles of the mixed form (see k_wide): the double-float lookups keep
@@ -545,6 +700,7 @@ k_wide_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long st
             }
             __syncthreads();
         }
+        if (tid == 0) finite_check(v, V[0], true);
     }
 }
 

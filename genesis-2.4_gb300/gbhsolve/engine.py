@@ -22,7 +22,7 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lp = C.POINTER(C.c_int64)
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 PREC_FP64, PREC_MIXED = 0, 1
 IN_SET, IN_ADD, IN_FLUX = 0, 1, 2     # gbh_register_inputs_typed kinds
 
@@ -64,7 +64,7 @@ class GbhSynapses(C.Structure):
 
 class GbhRemoteSynapses(C.Structure):
     _fields_ = [("nsources", C.c_int), ("src_start", _lp), ("target_solver", _ip), ("target_op", _ip),
-                ("weight", _dp), ("delay_steps", _ip)]
+                ("weight", _dp), ("delay_steps", _ip), ("first_solver", C.c_int64)]
 
 
 class GbhOptions(C.Structure):
@@ -83,7 +83,7 @@ class GbhStats(C.Structure):
                 ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int),
                 ("jit_kernels", C.c_int), ("jit_min_blocks", C.c_int),
                 ("grad_forward_ms", C.c_double), ("grad_reverse_ms", C.c_double), ("jit_compact", C.c_int),
-                ("cooperative", C.c_int)]
+                ("cooperative", C.c_int), ("wide_tiles", C.c_int64), ("stack_tiles", C.c_int64)]
 
 
 EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",
@@ -336,7 +336,8 @@ class Engine:
             r = self._remote
             self.nremote = len(r["src_start"]) - 1
             rs = GbhRemoteSynapses(self.nremote, _ptr(r["src_start"], _lp), _ptr(r["target_solver"], _ip),
-                                   _ptr(r["target_op"], _ip), _ptr(r["weight"], _dp), _ptr(r["delay_steps"], _ip))
+                                   _ptr(r["target_op"], _ip), _ptr(r["weight"], _dp), _ptr(r["delay_steps"], _ip),
+                                   int(remote.get("first_solver", 0)))
             h = self.lib.gbh_create_dist(C.byref(self.batch.desc), syn_p, C.byref(rs), C.byref(opt), C.byref(err))
         if not h:
             raise EngineError(err)

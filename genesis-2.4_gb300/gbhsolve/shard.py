@@ -51,7 +51,8 @@ def partition_network(syn, lo, hi, spike_op=None, target_child=None):
               contiguous range);
       remote  synapses from cells of other ranks to this rank's cells, CSR
               over all n sources (global index; a local source's range is
-              empty), target solvers counted from lo, effective delays: the
+              empty), first_solver = lo, target solvers counted from lo,
+              effective delays: the
               delay plus 1 when the target's global index precedes the
               source's (the reference steps solvers in order, so such a
               target sees the spike one step later).
@@ -83,7 +84,7 @@ def partition_network(syn, lo, hi, spike_op=None, target_child=None):
             loc_start.append(len(loc["weight"]))
         rem_start.append(len(rem["weight"]))
     local = {"src_start": np.asarray(loc_start, dtype=np.int64)}
-    remote = {"src_start": np.asarray(rem_start, dtype=np.int64)}
+    remote = {"src_start": np.asarray(rem_start, dtype=np.int64), "first_solver": int(lo)}
     for k, t in (("target_solver", np.int32), ("target_op", np.int32), ("weight", np.float64),
                  ("delay_steps", np.int32), ("target_child", np.int32)):
         local[k] = np.asarray(loc[k], dtype=t)

@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define GBH_ABI_VERSION 3
+#define GBH_ABI_VERSION 4
 
 /* precision of gate/table arithmetic (elimination, Vm and Ca are always FP64) */
 #define GBH_PREC_FP64 0
@@ -112,9 +112,16 @@ typedef struct gbh_batch_desc {
  * h_dospike_event / synchan EVENT / HSEVENT do through GENESIS messages,
  * hines_conn.c:44-108, newconn/synchan.c:160-313). CSR over source solvers
  * (the solver holding the spikegen). Each synapse targets the SYN2_OP whose
- * ops[] index (within the target solver) is target_op, with weight and delay
- * in steps ((int)(delay/dt + 0.9), synchan.c:199-200). All synapses into one
- * synchan must carry the same weight; delays must be >= 1 step.
+ * ops[] index (within the target solver) is target_op, with its own weight
+ * and delay in steps ((int)(delay/dt + 0.9), synchan.c:199-200; 0 for a
+ * delay under a tenth of a step). The events due in one step are summed into
+ * the synchan's activation as weight/dt each, newest first, the order of the
+ * reference's pending-event list (synchan.c:239-350): later spikes first,
+ * then sources later in the solver order, then later synapses of a source.
+ * A spike acts in step s + delay, one step later when the target's synapse
+ * op runs before the source's spike op in the sequential order (an earlier
+ * solver, or an earlier op of the same solver); with delay 0 the spike
+ * detectors run in a pass of their own before each step.
  */
 typedef struct gbh_synapses {
     int64_t nsynapses;
@@ -141,7 +148,9 @@ typedef struct gbh_remote_synapses {
     const int *target_solver;  /* local solver */
     const int *target_op;
     const double *weight;
-    const int *delay_steps;
+    const int *delay_steps;    /* >= 1: spikes are exchanged between steps */
+    int64_t first_solver;      /* global index of this engine's solver 0 (the
+                                  order events due in one step are summed in) */
 } gbh_remote_synapses;
 
 typedef struct gbh_options {
@@ -192,6 +201,10 @@ typedef struct gbh_stats {
                                   with its rows in shared memory              */
     int cooperative;           /* network steps run K per cooperative launch
                                   with a grid barrier between steps           */
+    int64_t wide_tiles;        /* tiles holding one neuron across a warp's
+                                  threads (level-by-level elimination)        */
+    int64_t stack_tiles;       /* tiles of 32 large neurons, one per lane,
+                                  eliminated with per-lane stacks             */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
@@ -372,7 +385,7 @@ int gbh_get_stats(const gbh_engine *e, gbh_stats *st);
  * stream is a cudaStream_t passed as void* (NULL = the engine's own stream,
  * as for gbh_run_async); the call returns once the work is queued and leaves
  * the caller's current device as it found it. A device status word raised
- * by these steps (event ring overflow, unimplemented micro-op) is reported by
+ * by these steps (a non-finite Vm, an unimplemented micro-op) is reported by
  * the engine's next synchronous call (gbh_run).
  */
 #define GBH_NOALLOC_FLUX_MAX (1 << 20)

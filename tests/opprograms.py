@@ -190,3 +190,21 @@ def from_fixture(d, tag):
     for k, v in zip(SCALARS, sc):
         kw[k] = float(v) if k in ("xmin", "invdx", "ymin", "invdy", "dt") else int(v)
     return SimpleNamespace(diff=None, **kw)
+
+
+def syn_countdown_words(ops):
+    """Positions of the SYN2_OP/SYN3_OP countdown words in ops[] (the word
+    after the stablist index). The reference keeps each synchan's time to
+    its next event there, set by HSEVENT and h_dosynchan (hines.c:352-357,
+    hines_conn.c:62-89); the engine keeps its events in per-step rings
+    instead and does not maintain this word."""
+    ops = np.asarray(ops)
+    out = []
+    i = 0
+    while i < len(ops) and ops[i] != A.LCOMPT:
+        if ops[i] in (A.SYN2, A.SYN3):
+            out.append(i + 2)
+            i += 4
+        else:
+            i += 1
+    return np.array(out, dtype=np.int64)

@@ -88,3 +88,52 @@ def test_network_cooperative_mixed_matches_launches(gpu_engine):
     assert a.spike_counts().sum() > n
     a.close()
     b.close()
+
+
+def _weighted(esyn, seed, zero_frac=0.3, max_delay=6):
+    """Seeded weights per synapse (a float field in the reference, so rounded
+    through float) and delays of 0..max_delay steps, a share of them 0
+    (a synapse delay under a tenth of a step)."""
+    rng = np.random.default_rng(seed)
+    n = len(esyn["weight"])
+    w = rng.uniform(0.2, 2.0, size=n).astype(np.float32).astype(np.float64)
+    d = rng.integers(1, max_delay + 1, size=n)
+    d[rng.random(n) < zero_frac] = 0
+    out = dict(esyn)
+    out["weight"] = w
+    out["delay_steps"] = d.astype(np.int32)
+    return out
+
+
+@pytest.mark.parametrize("jit", [True, False])
+def test_network_weights_per_synapse_and_zero_delays(oracle, gpu_engine, jit):
+    """Every synapse its own weight, some acting in the step of the spike:
+    activations summed newest first as the reference's pending list does;
+    identical spike counts and Vm bit for bit."""
+    rng = np.random.default_rng(12)
+    n = 150
+    hs, esyn, child = _network(n, 0.08, seed=13, inject=rng.uniform(0.0, 0.3e-9, size=n))
+    ws = _weighted(esyn, 14)
+    assert (ws["delay_steps"] == 0).any() and len(np.unique(ws["weight"])) > 100
+    eng = gpu_engine.Engine(hs, synapses=ws, jit=jit)
+    for m in (1000, 777, 1223):
+        eng.run(m)
+    solvers, ref_spikes = _oracle_net(oracle, hs, ws, child, 3000)
+    assert ref_spikes.sum() > n
+    np.testing.assert_array_equal(eng.spike_counts(), ref_spikes)
+    np.testing.assert_array_equal(eng.vm(), np.concatenate([s.vm for s in solvers]))
+    eng.close()
+
+
+def test_network_weights_graph_replay(oracle, gpu_engine):
+    rng = np.random.default_rng(15)
+    n = 100
+    hs, esyn, child = _network(n, 0.1, seed=16, inject=rng.uniform(0.0, 0.3e-9, size=n))
+    ws = _weighted(esyn, 17, zero_frac=0.5, max_delay=3)
+    eng = gpu_engine.Engine(hs, synapses=ws, use_graph=True)
+    for _ in range(4):
+        eng.run(500)
+    solvers, ref_spikes = _oracle_net(oracle, hs, ws, child, 2000)
+    np.testing.assert_array_equal(eng.spike_counts(), ref_spikes)
+    np.testing.assert_array_equal(eng.vm(), np.concatenate([s.vm for s in solvers]))
+    eng.close()

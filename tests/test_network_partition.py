@@ -140,3 +140,46 @@ def test_partitioned_engines_match_oracle(oracle, gpu_engine, use_graph):
     np.testing.assert_array_equal(np.concatenate([e.vm() for e in engs]), ref_vm)
     for e in engs:
         e.close()
+
+
+@pytest.mark.gpu
+def test_partitioned_engines_weights_per_synapse(oracle, gpu_engine):
+    """Weights per synapse across ranks: each rank sums the events due in a
+    step in the global order (its first solver's global index places its own
+    sources among the remote ones), so two engines equal the single-process
+    oracle bit for bit."""
+    hs, esyn, child = _network(90, 0.1, seed=14)
+    rng = np.random.default_rng(15)
+    ws = dict(esyn)
+    ws["weight"] = rng.uniform(0.2, 2.0, size=len(esyn["weight"])).astype(np.float32).astype(np.float64)
+    ws["delay_steps"] = rng.integers(1, 5, size=len(esyn["weight"])).astype(np.int32)
+    n, nsteps, world = len(hs), 1200, 2
+    ref_vm, ref_sp = _oracle_whole(oracle, hs, ws, child, nsteps)
+    assert ref_sp.sum() > n
+    engs = []
+    for r in range(world):
+        lo, hi = shard.shard_range(n, r, world)
+        loc, rem = shard.partition_network(ws, lo, hi)
+        engs.append(gpu_engine.Engine(hs[lo:hi], synapses=loc, remote=rem))
+    for _ in range(nsteps):
+        for e in engs:
+            e.run(1)
+        glob = np.concatenate([e.get_spiked() for e in engs])
+        for e in engs:
+            e.deliver_remote(glob)
+    np.testing.assert_array_equal(np.concatenate([e.spike_counts() for e in engs]), ref_sp)
+    np.testing.assert_array_equal(np.concatenate([e.vm() for e in engs]), ref_vm)
+    for e in engs:
+        e.close()
+
+
+@pytest.mark.gpu
+def test_partitioned_zero_delay_across_ranks_is_refused(gpu_engine):
+    """A spike exchanged between steps cannot act in the step it happened."""
+    hs, esyn, _ = _network(40, 0.2, seed=16)
+    ws = dict(esyn)
+    ws["delay_steps"] = np.zeros(len(esyn["weight"]), dtype=np.int32)
+    loc, rem = shard.partition_network(ws, 20, 40)   # remote sources precede the rank's cells
+    assert (rem["delay_steps"] == 0).any()
+    with pytest.raises(gpu_engine.EngineError):
+        gpu_engine.Engine(hs[20:40], synapses=loc, remote=rem)

@@ -47,7 +47,9 @@ def test_program_fp64(oracle, gpu_engine, ref_states, name, jit):
         _compare(giv, ref_states[tag + "/givals"], libm, tag)
         if len(h.conc):
             _compare(st["conc"][0], ref_states[tag + "/conc"], libm, tag)
-        np.testing.assert_array_equal(st["ops"][0], ref_states[tag + "/ops"], err_msg=tag)
+        keep = np.ones(len(h.ops), bool)
+        keep[P.syn_countdown_words(h.ops)] = False
+        np.testing.assert_array_equal(st["ops"][0][keep], ref_states[tag + "/ops"][keep], err_msg=tag)
         # the oracle restatement, run here
         ref = oracle.Solver(h)
         ref.run(P.NSTEPS)

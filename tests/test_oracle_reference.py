@@ -150,3 +150,29 @@ def test_domain_without_concentrations_is_a_setup_error():
     with pytest.raises(engine.EngineError) as ei:
         engine.validate([h])
     assert ei.value.opcode == A.DOMAIN
+
+
+@needs_ref
+def test_oracle_network_weights_zero_delay_matches_reference_step_code(oracle):
+    """Per-synapse weights and zero-step delays through the reference's own
+    step code (do_chip_hh4_update calling h_dosynchan) under the oracle's
+    event layer, against the oracle's own step."""
+    oracle.ensure_built(with_reference=True)
+    ms, syn = configs.hh_network(40, p_conn=0.2, seed=3)
+    rng = np.random.default_rng(1)
+    for m in ms:
+        m.compartments[0].inject = float(rng.uniform(0, 0.3e-9))
+    hs = [model.build(m) for m in ms]
+    esyn, child = configs.network_synapses(hs, syn)
+    w = rng.uniform(0.2, 2.0, size=len(esyn["weight"])).astype(np.float32).astype(np.float64)
+    d = rng.integers(0, 4, size=len(w)).astype(np.int32)
+    runs = []
+    for impl in ("oracle", "reference"):
+        sv = [oracle.Solver(h, i) for i, h in enumerate(hs)]
+        net = oracle.Network(sv, esyn["src_start"], esyn["target_solver"], child, esyn["target_op"], w, d,
+                             impl=impl)
+        net.run(1500)
+        runs.append((np.concatenate([s.vm for s in sv]), net.spikes.copy()))
+    assert runs[0][1].sum() > 0
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
