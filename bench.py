@@ -23,9 +23,9 @@ step over all compartments (channel program, elimination, Vm update).
   roofline HBM roofline of the step kernel (algorithmic bytes per
            compartment-step x compartment-steps per launch / launch time)
 
-``--impl reference`` times the CPU restatement of the reference solver (the
-oracle port: the reference's own C step code cannot be built on this host)
-on every host core over a bounded sample of the same workload.
+``--impl reference`` times the reference's own CPU step code (compiled from
+its sources into oracle/_ref; the oracle's restatement where they are not
+available) on every host core over a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -189,25 +189,57 @@ def accuracy_sample(hs, precision, nsteps=ACC_STEPS, nsample=ACC_SAMPLE):
     return worst, dev, nspk, mismatch
 
 
-def cpu_sample_rate(hs, seconds=12.0):
-    """Oracle (one core) compartment-steps/s over a bounded sample."""
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_impl():
+    """The CPU step code timed: the reference's own (compiled from its
+    sources into oracle/_ref where they are available), else the oracle's
+    restatement of it (bit-equal to it)."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
-    pyoracle.ensure_built(with_reference=False)
+    pyoracle.ensure_built(with_reference=True)
+    if os.path.exists(pyoracle.LIB_REF):
+        return "reference", "reference"
+    return "oracle", "port"
+
+
+def cpu_sample_rate(hs, seconds=12.0):
+    """The reference's step code (one core) compartment-steps/s over a
+    bounded sample."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+    impl, kind = cpu_impl()
     solvers = [pyoracle.Solver(h) for h in hs[:256]]
     steps = 0
     t0 = time.perf_counter()
     while time.perf_counter() - t0 < seconds:
         for s in solvers:
-            s.run(20)
+            s.run(20, impl)
         steps += 20
     el = time.perf_counter() - t0
     cs = steps * len(solvers) * NCOMP
-    return cs / el, "%d neurons x %d compartments x %d steps (%.1f s)" % (len(solvers), NCOMP, steps, el)
+    return cs / el, kind, "%d neurons x %d compartments x %d steps (%.1f s)" % (len(solvers), NCOMP, steps, el)
 
 
 def _cpu_worker(args):
-    n, steps, seed = args
+    n, steps, seed, impl = args
     sys.path.insert(0, os.path.join(REPO, "genesis-2.4_gb300"))
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import pyoracle
@@ -216,7 +248,7 @@ def _cpu_worker(args):
     solvers = [pyoracle.Solver(h) for h in hs]
     t0 = time.perf_counter()
     for s in solvers:
-        s.run(steps)
+        s.run(steps, impl)
     return n * NCOMP * steps, time.perf_counter() - t0
 
 
@@ -333,27 +365,27 @@ def other_configs(device, n_trees=50_000):
 
 
 def run_reference(args, ws, rank, dist):
-    """CPU restatement of the reference solver on every host core."""
+    """The reference's CPU step code on every host core."""
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
     import multiprocessing as mp
-    import pyoracle
-    pyoracle.ensure_built(with_reference=False)
+    impl, kind = cpu_impl()
     cores = os.cpu_count() or 1
     per = 96                       # neurons per worker per step batch
     nst = 100                      # steps per neuron per timed sample (amortises the per-call overhead)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        pool.map(_cpu_worker, [(8, 5, k) for k in range(cores)])   # warm the workers
+        pool.map(_cpu_worker, [(8, 5, k, impl) for k in range(cores)])   # warm the workers
         vals = []
         for _ in range(args.warmup):
-            pool.map(_cpu_worker, [(per, nst, k) for k in range(cores)])
+            pool.map(_cpu_worker, [(per, nst, k, impl) for k in range(cores)])
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            res = pool.map(_cpu_worker, [(per, nst, k) for k in range(cores)])
+            res = pool.map(_cpu_worker, [(per, nst, k, impl) for k in range(cores)])
             wall = time.perf_counter() - t0
             cs = sum(r[0] for r in res)
+            # each worker's in-process time; the slowest one sets the step
+            # (pool dispatch, the workers' model build excluded)
             vals.append(cs / max(max(r[1] for r in res), 1e-9))
     value = float(np.median(vals))
     line = {
@@ -363,8 +395,12 @@ def run_reference(args, ws, rank, dist):
         "data": "synthetic",
         "config": {"workload": "cables-100k-x16 (config 3 morphology, dendritic K)", "sample_neurons":
                    per * cores, "steps_per_sample": nst},
-        "cpu_baseline": {"value": value, "unit": "compartment-steps/s", "cores": cores, "kind": "port",
-                         "sample": "%d workers x %d neurons x 16 compartments x %d steps per timed step"
+        "cpu_baseline": {"value": value, "unit": "compartment-steps/s", "cores": cores, "kind": kind,
+                         "cpu": cpu_model(),
+                         "code": "the reference's own step code (hines_4chip.c, hines_solve.c, ...) compiled "
+                                 "with its -O2" if kind == "reference" else "the oracle's restatement",
+                         "sample": "%d workers x %d neurons x 16 compartments x %d steps per timed step; value: "
+                                   "compartment-steps over the slowest worker's in-process time"
                                    % (cores, per, nst)},
         "e2e": {"value": value, "unit": "compartment-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -563,8 +599,9 @@ def main():
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        v, sample = cpu_sample_rate(hs)
-        cpu = {"value": v, "unit": "compartment-steps/s", "cores": 1, "kind": "port", "sample": sample}
+        v, kind, sample = cpu_sample_rate(hs)
+        cpu = {"value": v, "unit": "compartment-steps/s", "cores": 1, "kind": kind, "cpu": cpu_model(),
+               "sample": sample}
 
     peak, peak_kind = peaks()
     r = results["mixed"]

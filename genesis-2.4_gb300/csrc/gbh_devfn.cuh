@@ -91,10 +91,13 @@ struct DevView {
 
 // A neuron whose Vm is no longer finite: a NaN or infinity anywhere in its
 // tree reaches every row through the elimination within the step, so one
-// row per neuron per step is checked (after back substitution).
+// row per neuron per step is checked (after back substitution). The mixed
+// form's exact float<->double conversions run on the integer pipe and turn a
+// NaN or infinity into a finite value near 2^128, so any |Vm| above 1e30 --
+// no voltage in any unit system -- counts as lost as well.
 __device__ __forceinline__ void finite_check(const DevView &v, double x, bool active)
 {
-    if (!(fabs(x) <= 1.7976931348623157e308) && active && v.status) atomicOr(v.status, ST_NONFINITE);
+    if (!(fabs(x) <= 1.0e30) && active && v.status) atomicOr(v.status, ST_NONFINITE);
 }
 
 // Prefetch of the cache line holding *p into L1 (the loads of a later row).

@@ -277,15 +277,20 @@ int field_operands(int code)
     }
 }
 
-// Per slot of a type's program, the first and last field row it reads
-// (rows are allocated in program order, so a slot's fields are mostly one
-// contiguous range): what the stack kernels prefetch a few rows ahead.
+// Per slot of a type's program, 6 ints for the stack kernels: the first and
+// last field row it reads (rows are allocated in program order, so a slot's
+// fields are mostly one contiguous range; prefetched a few rows ahead), and
+// for a passive compartment -- a program of M_BEGIN and M_END alone -- the
+// rows of Em/Rm, inject, dt/Cm and the diagonal term (else -1): such rows
+// skip the interpreter.
 std::vector<int> slot_field_ranges(const std::vector<int> &prog, const TileType &tt)
 {
     std::vector<int> out;
     size_t pc = tt.prog_off;
     for (int s = 0; s < tt.nslots; ++s) {
         int lo = INT32_MAX, hi = -1;
+        const size_t pc0 = pc;
+        const bool passive = prog[pc0] == M_BEGIN && prog[pc0 + 5] == M_END;
         for (;;) {
             const int code = prog[pc];
             const int n = micro_operands(code);
@@ -305,6 +310,14 @@ std::vector<int> slot_field_ranges(const std::vector<int> &prog, const TileType 
         if (hi < 0) lo = hi = 0;
         out.push_back(lo);
         out.push_back(std::min(hi, lo + 31));
+        if (passive) {
+            out.push_back(prog[pc0 + 1]);   // Em/Rm
+            out.push_back(prog[pc0 + 2]);   // inject
+            out.push_back(prog[pc0 + 6]);   // dt/Cm
+            out.push_back(prog[pc0 + 7]);   // diagonal term
+        } else {
+            out.insert(out.end(), {-1, -1, -1, -1});
+        }
     }
     return out;
 }

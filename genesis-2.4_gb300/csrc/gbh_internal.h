@@ -168,6 +168,6 @@ struct Tile {
 // it is reused, every delay being shorter than the ring, so it cannot overflow)
 enum Status { ST_OK = 0, ST_BAD_OP = 1, ST_SMEM = 4 /* launched with too little shared memory */,
               ST_BARRIER = 8 /* a grid barrier wait ran out */,
-              ST_NONFINITE = 16 /* a neuron's Vm became NaN or infinite */ };
+              ST_NONFINITE = 16 /* a neuron's Vm became NaN, infinite or beyond 1e30 */ };
 
 }  // namespace gbh

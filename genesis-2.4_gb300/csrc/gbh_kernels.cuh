@@ -518,7 +518,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     double2 *col = v.col + tl.topo * LANES + lane;
     double *stk = sm + lane;      // entry j at stk[j * 32]
     const int S = ty.nslots;
-    const int *pf = v.prog + ty.pf_off;   // per slot: first and last field row
+    const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
     constexpr int kPf = 2;                // rows of lookahead
 
     ChanEnv<G> E;
@@ -553,7 +553,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         for (int s = 0; s < S; ++s) {
             if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
                 const int q = s + kPf;
-                const int f0 = pf[2 * q], f1 = pf[2 * q + 1];
+                const int f0 = pf[6 * q], f1 = pf[6 * q + 1];
                 for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
                 prefetch_l1(&Vw[q * LANES]);
                 prefetch_l1(&lt[q * LANES]);
@@ -561,7 +561,18 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 prefetch_l1(&Bw[q * LANES]);
             }
             double R, D;
-            if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+            const int *ps = pf + 6 * s;
+            if (!GIV && ps[2] >= 0) {
+                // passive compartment: the interpreter's M_BEGIN / M_END
+                // arithmetic without decoding them
+                const double Vm = Vw[s * LANES];
+                const double ichan = Pw[ps[2] * LANES] + Pw[ps[3] * LANES];
+                const double tbyc = Pw[ps[4] * LANES];
+                const double sumg = 0.0;
+                R = Vm + ichan * tbyc;
+                D = sumg * tbyc + Pw[ps[5] * LANES];
+                pc += 9;
+            } else if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
                 if (v.status) atomicOr(v.status, ST_BAD_OP);
                 return;
             }

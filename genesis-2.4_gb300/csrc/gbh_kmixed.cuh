@@ -455,7 +455,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
     double2 *col = v.col + tl.topo * LANES + lane;
     double *stk = sm + lane;
     const int S = ty.nslots;
-    const int *pf = v.prog + ty.pf_off;   // per slot: first and last field row
+    const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
     constexpr int kPf = 2;                // rows of lookahead
 
     ChanEnvDF E;
@@ -491,7 +491,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         for (int s = 0; s < S; ++s) {
             if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
                 const int q = s + kPf;
-                const int f0 = pf[2 * q], f1 = pf[2 * q + 1];
+                const int f0 = pf[6 * q], f1 = pf[6 * q + 1];
                 for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
                 prefetch_l1(&Vw[q * LANES]);
                 prefetch_l1(&lt[q * LANES]);
@@ -499,7 +499,17 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 prefetch_l1(&Bw[q * LANES]);
             }
             double R, D;
-            if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+            const int *ps = pf + 6 * s;
+            if (!GIV && ps[2] >= 0) {
+                // passive compartment: the interpreter's M_BEGIN / M_END
+                // arithmetic without decoding them
+                const double Vm = Vw[s * LANES];
+                const df ichan = df_add(ld_df(&Pw[ps[2] * LANES]), ld_df(&Pw[ps[3] * LANES]));
+                const df tbyc = ld_df(&Pw[ps[4] * LANES]);
+                R = df2d(df_add(d2df(Vm), df_mul(ichan, tbyc)));
+                D = df2d(df_add(df_mul(df_make(0.f, 0.f), tbyc), ld_df(&Pw[ps[5] * LANES])));
+                pc += 9;
+            } else if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
                 if (v.status) atomicOr(v.status, ST_BAD_OP);
                 return;
             }

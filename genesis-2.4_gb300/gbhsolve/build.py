@@ -6,6 +6,7 @@ The CUDA/C++ translation units are compiled in parallel:
   gbh_adjoint.cu adjoint (gradient) kernels of the FP64 form, --fmad=false
   gbh_engine.cu host layout, launches and the C ABI
   gbh_decode.cpp ops[]/funcs[] decoder
+  gbh_hsolve.cpp hsolve-level ABI: many hsolves in one batch engine
 """
 from __future__ import annotations
 
@@ -33,7 +34,7 @@ def nvcc() -> str:
 
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))
-            if f.endswith((".cu", ".cpp", ".cuh", ".h"))] + [os.path.join(INCLUDE, "gbhsolve.h")]
+            if f.endswith((".cu", ".cpp", ".cuh", ".h"))] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 
 
 def up_to_date() -> bool:
@@ -83,6 +84,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         ("gbh_engine.cu", []),
         ("gbh_noalloc.cu", []),
         ("gbh_decode.cpp", []),
+        ("gbh_hsolve.cpp", []),
         ("gbh_jit.cu", []),
     ]
 

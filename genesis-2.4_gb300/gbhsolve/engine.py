@@ -91,7 +91,10 @@ EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_
             "gbh_register_outputs", "gbh_get_outputs_async", "gbh_get_spike_counts", "gbh_get_stats",
             "gbh_destroy", "gbh_last_error", "gbh_run_noalloc", "gbh_loss_gradient", "gbh_create_dist",
             "gbh_get_spiked", "gbh_deliver_remote", "gbh_step_io", "gbh_io_sync", "gbh_run_io",
-            "gbh_register_inputs_typed", "gbh_get_itotal"]
+            "gbh_register_inputs_typed", "gbh_get_itotal",
+            # hsolve-level ABI (include/gbh_hsolve.h, mirrored in gbhsolve/hsolve.py)
+            "gbh_hs_register", "gbh_hs_set_synapses", "gbh_hs_step", "gbh_hs_sync", "gbh_hs_push",
+            "gbh_hs_stats", "gbh_hs_count", "gbh_hs_cleanup"]
 
 _LIB = None
 

@@ -35,14 +35,65 @@ enum { F_ELIM = 0, F_SET_DIAG = 1, F_SKIP_DIAG = 2, F_FASTSIB = 3, F_COPY = 4,
 
 #define ORC_TINY 1.0e-6 /* hines_defs.h TINY */
 
-/* The single-uniform deviate used by SYN3_OP (G_RNG in the reference). The
- * oracle uses a fixed-seed 64-bit LCG rounded to float (G_RNG returns float);
- * SYN3 parity against a real GENESIS run is therefore statistical only. */
-static unsigned long long orc_rng_state = 0x9E3779B97F4A7C15ULL;
+/* SYN3_OP's uniform deviate, urandom() = G_RNG() in the reference: with its
+ * default generator selected (sim/sim_random.c:45-100, 197-210) that is
+ * "ran1" of Numerical Recipes in C (Press et al., 1st ed., sec. 7.1): three
+ * linear congruential generators; the first two make a value in [0, 1),
+ * the third picks which of 97 stored values to return and to replace with
+ * the new one. Restated here with the published constants; values are
+ * stored and returned as float, as G_RNG returns them. One stream for the
+ * process, (re)seeded by orc_seed_rng (G_SEEDRNG's ran1(-seed)); unseeded,
+ * it starts as ran1(0) does on its first call. */
+enum { R1_M1 = 259200, R1_A1 = 7141, R1_C1 = 54773, R1_M2 = 134456, R1_A2 = 8121, R1_C2 = 28411,
+       R1_M3 = 243000, R1_A3 = 4561, R1_C3 = 51349 };
+static struct {
+    long x1, x2, x3;
+    float tab[98];
+    int ready;
+} orc_rng;
+
+/* a generated value: (x1 + x2 / M2) / M1, evaluated in that order (the
+ * reference's constants RM1, RM2 are unparenthesised (1.0)/M quotients) */
+static float orc_ran1_value(void)
+{
+    return (float)(((double)orc_rng.x1 + (double)orc_rng.x2 / R1_M2) / R1_M1);
+}
+
+static void orc_ran1_init(long seed)
+{
+    int j;
+    orc_rng.x1 = (R1_C1 + seed) % R1_M1;
+    orc_rng.x1 = (R1_A1 * orc_rng.x1 + R1_C1) % R1_M1;
+    orc_rng.x2 = orc_rng.x1 % R1_M2;
+    orc_rng.x1 = (R1_A1 * orc_rng.x1 + R1_C1) % R1_M1;
+    orc_rng.x3 = orc_rng.x1 % R1_M3;
+    for (j = 1; j <= 97; j++) {
+        orc_rng.x1 = (R1_A1 * orc_rng.x1 + R1_C1) % R1_M1;
+        orc_rng.x2 = (R1_A2 * orc_rng.x2 + R1_C2) % R1_M2;
+        orc_rng.tab[j] = orc_ran1_value();
+    }
+    orc_rng.ready = 1;
+}
+
 static double orc_urandom(void)
 {
-    orc_rng_state = orc_rng_state * 6364136223846793005ULL + 1442695040888963407ULL;
-    return (double)(float)((double)(orc_rng_state >> 11) * (1.0 / 9007199254740992.0));
+    int j;
+    float out;
+    if (!orc_rng.ready) orc_ran1_init(0);
+    orc_rng.x1 = (R1_A1 * orc_rng.x1 + R1_C1) % R1_M1;
+    orc_rng.x2 = (R1_A2 * orc_rng.x2 + R1_C2) % R1_M2;
+    orc_rng.x3 = (R1_A3 * orc_rng.x3 + R1_C3) % R1_M3;
+    j = 1 + (int)((97 * orc_rng.x3) / R1_M3);
+    out = orc_rng.tab[j];
+    orc_rng.tab[j] = orc_ran1_value();
+    return (double)out;
+}
+
+/* G_SEEDRNG(seed): ran1(-seed), which reinitialises and then draws once */
+void orc_seed_rng(long seed)
+{
+    orc_ran1_init(seed);
+    (void)orc_urandom();
 }
 
 /*

@@ -126,6 +126,8 @@ void orc_net_set_process(orc_net *n, int (*process)(orc_solver *));
 long long orc_net_step_count(const orc_net *n);
 void orc_net_deliver(orc_net *n, int count, const int *tgt_solver, const int *tgt_child, const int *tgt_op,
                      const double *w, const long long *fire_step);
+/* Seeds SYN3_OP's generator as G_SEEDRNG does (sim/sim_random.c:212-222). */
+void orc_seed_rng(long seed);
 
 #ifdef __cplusplus
 }

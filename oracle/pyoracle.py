@@ -85,6 +85,13 @@ def reference_sources_present() -> bool:
 _libs = {}
 
 
+def seed_rng(seed: int, impl: str = "oracle") -> None:
+    """Seeds SYN3_OP's generator (G_SEEDRNG) of the oracle or of the
+    reference's own code."""
+    lib = _lib(impl)
+    (lib.orc_seed_rng if impl == "oracle" else lib.G_SEEDRNG)(int(seed))
+
+
 def _lib(which: str):
     if which not in _libs:
         path = LIB_ORACLE if which == "oracle" else LIB_REF
@@ -102,9 +109,13 @@ def _lib(which: str):
             lib.orc_net_deliver.argtypes = [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, C.POINTER(C.c_longlong)]
             lib.orc_net_step_count.restype = C.c_longlong
             lib.orc_net_step_count.argtypes = [C.c_void_p]
+            lib.orc_seed_rng.argtypes = [C.c_long]
+            lib.orc_seed_rng.restype = None
         else:
             lib.ref_process.argtypes = [C.POINTER(OrcSolver)]
             lib.ref_run.argtypes = [C.POINTER(OrcSolver), C.c_int]
+            lib.G_SEEDRNG.argtypes = [C.c_long]
+            lib.G_SEEDRNG.restype = None
         _libs[which] = lib
     return _libs[which]
 

@@ -9,7 +9,8 @@
  *
  * It supplies the symbols those files need from the rest of GENESIS:
  *   Error()            -- message banner (sim/)
- *   G_RNG()            -- SPRNG uniform deviate used by SYN3_OP
+ *   the option-parsing symbols of sim/sim_random.c, whose G_RNG (the
+ *                         uniform deviate SYN3_OP draws) is linked in as is
  *   h_dospike_event()  -- hines_conn.c:44-58, routed to the solver's hook
  *   h_dosynchan()      -- hines_conn.c:62-89, routed to the solver's hook
  *   BaseObject()       -- the element's object, for its integration method
@@ -38,14 +39,14 @@ GenesisObject *BaseObject(Element *e)
     return &ref_object;
 }
 
-static unsigned long long ref_rng_state = 0x9E3779B97F4A7C15ULL;
-float G_RNG()
-{
-    /* same fixed-seed LCG as the oracle's SYN3 deviate, rounded to float as
-     * the reference's G_RNG returns float (sys/header.h) */
-    ref_rng_state = ref_rng_state * 6364136223846793005ULL + 1442695040888963407ULL;
-    return (float)((double)(ref_rng_state >> 11) * (1.0 / 9007199254740992.0));
-}
+/* G_RNG / G_SEEDRNG come from the reference's own sim/sim_random.c, linked
+ * beside this file; its option parsing (do_setRNG) is never called here and
+ * needs only these symbols */
+char *G_optopt;
+int G_getopt() { return -1; }
+int initopt() { return 0; }
+void printoptusage() {}
+int IsSilent() { return 1; }
 
 void h_dospike_event(Hsolve *hsolve)
 {

@@ -208,3 +208,16 @@ def syn_countdown_words(ops):
         else:
             i += 1
     return np.array(out, dtype=np.int64)
+
+
+def syn3_solver(p_fire, stablist, n_compts=1, seed_vm=-0.062):
+    """Compartments each with one SYN3_OP synchan (randomly triggered,
+    channelC3): chip layout per compartment [Em/Rm, inject, Ek, gmax,
+    dt*frequency, X, Y, dt/Cm, diagonal term]; X sits at 9 * c + 5."""
+    comps = []
+    for c in range(n_compts):
+        cc = _c(seed_vm)
+        # a synapse op adds its channel's current itself (hines_chip.c:551-567)
+        cc.op(A.CHAN_EK, chips=[0.0, 1e-9]).op(A.SYN3, 0, -1, 1, chips=[p_fire, 0.0, 0.0], giv=3)
+        comps.append(cc)
+    return A.solver(comps, A.tables(12, 40), dt=DT, stablist=stablist)

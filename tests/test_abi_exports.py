@@ -1,5 +1,6 @@
 """The C-ABI library builds, loads without a GPU, and exports every function
-declared in include/gbhsolve.h."""
+declared in include/*.h (gbhsolve.h: the array-level ABI; gbh_hsolve.h: the
+hsolve-level ABI)."""
 import ctypes
 import os
 import re
@@ -10,16 +11,21 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_functions():
-    src = open(os.path.join(REPO, "include", "gbhsolve.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(gbh_[a-z_0-9]+)\s*\(", src, flags=re.M)
+    names = []
+    inc = os.path.join(REPO, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        src = open(os.path.join(inc, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(gbh_[a-z_0-9]+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
 def test_header_declares_the_boundary():
     names = declared_functions()
     for required in ("gbh_create", "gbh_run", "gbh_get_state", "gbh_destroy", "gbh_validate",
-                     "gbh_run_noalloc"):
+                     "gbh_run_noalloc", "gbh_hs_register", "gbh_hs_step", "gbh_hs_sync", "gbh_hs_push"):
         assert required in names
 
 

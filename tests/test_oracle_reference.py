@@ -176,3 +176,46 @@ def test_oracle_network_weights_zero_delay_matches_reference_step_code(oracle):
     assert runs[0][1].sum() > 0
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
     np.testing.assert_array_equal(runs[0][1], runs[1][1])
+
+
+@needs_ref
+def test_syn3_draws_equal_reference_generator(oracle):
+    """SYN3_OP (channelC3) draws urandom() = G_RNG() each step; the oracle's
+    restatement of GENESIS's default generator (Numerical Recipes ran1) gives
+    the reference's own sim/sim_random.c stream: equal trajectories from the
+    same seed."""
+    import opprograms as P
+    oracle.ensure_built(with_reference=True)
+    h = P.syn3_solver(0.1, [0.99, 9.5e-5, 0.98, 9.9e-5 / P.DT], n_compts=3)
+    runs = []
+    for impl in ("oracle", "reference"):
+        oracle.seed_rng(7, impl)
+        s = oracle.Solver(h)
+        s.run(3000, impl)
+        runs.append((s.vm.copy(), s.chip.copy()))
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
+    assert runs[0][1][5] != 0.0
+
+
+def test_syn3_oracle_firing_statistics(oracle):
+    """The criterion the engine's SYN3 draws are held to, applied to the
+    reference's generator (restated): X counts firings exactly when
+    xconst2 = 1 and the increment is 1; counts are Binomial(N, p)."""
+    import opprograms as P
+    n, nsteps, p = 96, 2000, 0.1
+    h = P.syn3_solver(p, [1.0, 0.0, 0.0, 1.0], n_compts=n)
+    oracle.seed_rng(3)
+    s = oracle.Solver(h)
+    s.run(nsteps)
+    counts = s.chip[5::9][:n]
+    check_binomial(counts, nsteps, p)
+
+
+def check_binomial(counts, nsteps, p):
+    counts = np.asarray(counts)
+    assert np.all(counts == np.round(counts))
+    mean, var = nsteps * p, nsteps * p * (1 - p)
+    assert abs(counts.mean() - mean) < 5 * np.sqrt(var / len(counts)), counts.mean()
+    assert 0.6 * var < counts.var() < 1.5 * var, counts.var()
+    assert len(np.unique(counts)) > 10          # neurons draw independent streams
