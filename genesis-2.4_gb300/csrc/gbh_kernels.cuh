@@ -519,7 +519,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     double *stk = sm + lane;      // entry j at stk[j * 32]
     const int S = ty.nslots;
     const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
-    constexpr int kPf = 2;                // rows of lookahead
+    constexpr int kCh = 8;                // rows per chunk
 
     ChanEnv<G> E;
     E.tab = tab_ptr<G>(v, tg.tab_off);
@@ -550,33 +550,11 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         const int *pc = v.prog + ty.prog_off;
         int top = 0;                    // stack entries (two doubles each)
         double cd = 0.0, cr = 0.0;      // contribution carried to the next row
-        for (int s = 0; s < S; ++s) {
-            if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
-                const int q = s + kPf;
-                const int f0 = pf[6 * q], f1 = pf[6 * q + 1];
-                for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
-                prefetch_l1(&Vw[q * LANES]);
-                prefetch_l1(&lt[q * LANES]);
-                prefetch_l1(&Aw[q * LANES]);
-                prefetch_l1(&Bw[q * LANES]);
-            }
-            double R, D;
-            const int *ps = pf + 6 * s;
-            if (!GIV && ps[2] >= 0) {
-                // passive compartment: the interpreter's M_BEGIN / M_END
-                // arithmetic without decoding them
-                const double Vm = Vw[s * LANES];
-                const double ichan = Pw[ps[2] * LANES] + Pw[ps[3] * LANES];
-                const double tbyc = Pw[ps[4] * LANES];
-                const double sumg = 0.0;
-                R = Vm + ichan * tbyc;
-                D = sumg * tbyc + Pw[ps[5] * LANES];
-                pc += 9;
-            } else if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
-                if (v.status) atomicOr(v.status, ST_BAD_OP);
-                return;
-            }
-            const int f = lt[s * LANES];
+        // the forward step of row s from its own (R, D): children's
+        // contributions (stack, then the carried last child) in ascending row
+        // order, its (R, D) into the column, its own contribution pushed or
+        // carried -- the operations of the sequential sweep (hines_solve.c:247-252)
+        auto fwd = [&](int s, double R, double D, int f, double a, double bb) {
             const int np = f & FL_NPOP;
             top -= np;
             for (int j = 0; j < np; ++j) {
@@ -589,8 +567,8 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
             }
             col[s * LANES] = make_double2(R, D);
             if (f & FL_PARENT) {
-                const double temp = Aw[s * LANES] / D;
-                const double pd = Bw[s * LANES] * temp, pr = R * temp;
+                const double temp = a / D;
+                const double pd = bb * temp, pr = R * temp;
                 if (f & FL_CARRY_OUT) {
                     cd = pd;
                     cr = pr;
@@ -599,6 +577,55 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                     stk[(2 * top + 1) * LANES] = pr;
                     ++top;
                 }
+            }
+        };
+        // the interpreter's M_BEGIN / M_END arithmetic of a passive row
+        auto passive = [&](int s, const int *ps, double &R, double &D) {
+            const double Vm = Vw[s * LANES];
+            const double ichan = Pw[ps[2] * LANES] + Pw[ps[3] * LANES];
+            const double tbyc = Pw[ps[4] * LANES];
+            const double sumg = 0.0;
+            R = Vm + ichan * tbyc;
+            D = sumg * tbyc + Pw[ps[5] * LANES];
+        };
+        for (int s0 = 0; s0 < S; s0 += kCh) {
+            for (int q = s0 + kCh; q < min(s0 + 2 * kCh, S); ++q) {   // the next chunk's rows, into L1
+                for (int f = pf[6 * q]; f <= pf[6 * q + 1]; ++f) prefetch_l1(&Pw[f * LANES]);
+                prefetch_l1(&Vw[q * LANES]);
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&Aw[q * LANES]);
+                prefetch_l1(&Bw[q * LANES]);
+            }
+            bool all_passive = !GIV && s0 + kCh <= S;
+            for (int k = 0; k < kCh && all_passive; ++k) all_passive = pf[6 * (s0 + k) + 2] >= 0;
+            if (all_passive) {
+                // every row's own terms first (independent of each other),
+                // then the elimination chain through them
+                double R[kCh], D[kCh], a[kCh], bb[kCh];
+                int f[kCh];
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) {
+                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k]);
+                    f[k] = lt[(s0 + k) * LANES];
+                    a[k] = Aw[(s0 + k) * LANES];
+                    bb[k] = Bw[(s0 + k) * LANES];
+                }
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) fwd(s0 + k, R[k], D[k], f[k], a[k], bb[k]);
+                pc += 9 * kCh;
+                continue;
+            }
+            for (int s = s0; s < min(s0 + kCh, S); ++s) {
+                double R, D;
+                const int *ps = pf + 6 * s;
+                if (!GIV && ps[2] >= 0) {
+                    passive(s, ps, R, D);
+                    pc += 9;
+                } else if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                    if (v.status) atomicOr(v.status, ST_BAD_OP);
+                    return;
+                }
+                fwd(s, R, D, lt[s * LANES], Aw[s * LANES], Bw[s * LANES]);
             }
         }
         {
@@ -619,32 +646,44 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         }
         double xn = 0.0;   // solution of the row after
         top = 0;
-        for (int s = S - 1; s >= 0; --s) {
-            if (s >= kPf) {
-                const int q = s - kPf;
+        // back substitution of row s (hines_solve.c:270-289): its solution
+        // from the parent's (the row after, or the branch point on the stack)
+        auto bwd = [&](int s, int f, double2 rd, double c, double old) {
+            double r = rd.x;
+            if (f & FL_PARENT) {
+                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
+                if (f & FL_XPOP) --top;
+                r -= c * xp;
+            }
+            r = r / rd.y;
+            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
+            xn = r;
+            Vw[s * LANES] = ty.crank ? r + r - old : r;
+        };
+        int s1 = S - 1;
+        for (; s1 + 1 >= kCh; s1 -= kCh) {   // chunks: every row's loads, then the chain
+            for (int q = s1 - kCh; q > s1 - 2 * kCh && q >= 0; --q) {
                 prefetch_l1(&lt[q * LANES]);
                 prefetch_l1(&col[q * LANES]);
                 prefetch_l1(&Cbw[q * LANES]);
                 if (ty.crank) prefetch_l1(&Vw[q * LANES]);
             }
-            const int f = lt[s * LANES];
-            const double2 rd = col[s * LANES];
-            double r = rd.x;
-            if (f & FL_PARENT) {
-                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
-                if (f & FL_XPOP) --top;
-                r -= Cbw[s * LANES] * xp;
+            int f[kCh];
+            double2 rd[kCh];
+            double c[kCh], old[kCh];
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) {
+                const int s = s1 - k;
+                f[k] = lt[s * LANES];
+                rd[k] = col[s * LANES];
+                c[k] = Cbw[s * LANES];
+                old[k] = ty.crank ? Vw[s * LANES] : 0.0;
             }
-            r = r / rd.y;
-            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
-            xn = r;
-            if (ty.crank) {
-                const double old = Vw[s * LANES];
-                Vw[s * LANES] = r + r - old;
-            } else {
-                Vw[s * LANES] = r;
-            }
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) bwd(s1 - k, f[k], rd[k], c[k], old[k]);
         }
+        for (; s1 >= 0; --s1)
+            bwd(s1, lt[s1 * LANES], col[s1 * LANES], Cbw[s1 * LANES], ty.crank ? Vw[s1 * LANES] : 0.0);
         finite_check(v, xn, active);   // row 0's solution
     }
 }

@@ -456,7 +456,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
     double *stk = sm + lane;
     const int S = ty.nslots;
     const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
-    constexpr int kPf = 2;                // rows of lookahead
+    constexpr int kCh = 8;                // rows per chunk
 
     ChanEnvDF E;
     E.tab = v.tabdf + tg.tab_off;
@@ -488,32 +488,10 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         const int *pc = v.prog + ty.prog_off;
         int top = 0;
         double cd = 0.0, cr = 0.0;
-        for (int s = 0; s < S; ++s) {
-            if (s + kPf < S) {   // the loads of a later row, into L1 while this one computes
-                const int q = s + kPf;
-                const int f0 = pf[6 * q], f1 = pf[6 * q + 1];
-                for (int f = f0; f <= f1; ++f) prefetch_l1(&Pw[f * LANES]);
-                prefetch_l1(&Vw[q * LANES]);
-                prefetch_l1(&lt[q * LANES]);
-                prefetch_l1(&Aw[q * LANES]);
-                prefetch_l1(&Bw[q * LANES]);
-            }
-            double R, D;
-            const int *ps = pf + 6 * s;
-            if (!GIV && ps[2] >= 0) {
-                // passive compartment: the interpreter's M_BEGIN / M_END
-                // arithmetic without decoding them
-                const double Vm = Vw[s * LANES];
-                const df ichan = df_add(ld_df(&Pw[ps[2] * LANES]), ld_df(&Pw[ps[3] * LANES]));
-                const df tbyc = ld_df(&Pw[ps[4] * LANES]);
-                R = df2d(df_add(d2df(Vm), df_mul(ichan, tbyc)));
-                D = df2d(df_add(df_mul(df_make(0.f, 0.f), tbyc), ld_df(&Pw[ps[5] * LANES])));
-                pc += 9;
-            } else if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
-                if (v.status) atomicOr(v.status, ST_BAD_OP);
-                return;
-            }
-            const int f = __ldg(&lt[s * LANES]);
+        // the forward step of row s from its own (R, D): children's
+        // contributions (stack, then the carried last child), the row's
+        // reciprocal into the column, its own contribution pushed or carried
+        auto fwd = [&](int s, double R, double D, int f, double a, double bb) {
             const int np = f & FL_NPOP;
             top -= np;
             for (int j = 0; j < np; ++j) {
@@ -527,8 +505,8 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             const double ri = rcp_newton(D);
             col[s * LANES] = make_double2(R, ri);
             if (f & FL_PARENT) {
-                const double temp = __ldg(&Aw[s * LANES]) * ri;
-                const double pd = __ldg(&Bw[s * LANES]) * temp, pr = R * temp;
+                const double temp = a * ri;
+                const double pd = bb * temp, pr = R * temp;
                 if (f & FL_CARRY_OUT) {
                     cd = pd;
                     cr = pr;
@@ -537,6 +515,54 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                     stk[(2 * top + 1) * LANES] = pr;
                     ++top;
                 }
+            }
+        };
+        // the interpreter's M_BEGIN / M_END arithmetic of a passive row
+        auto passive = [&](int s, const int *ps, double &R, double &D) {
+            const double Vm = Vw[s * LANES];
+            const df ichan = df_add(ld_df(&Pw[ps[2] * LANES]), ld_df(&Pw[ps[3] * LANES]));
+            const df tbyc = ld_df(&Pw[ps[4] * LANES]);
+            R = df2d(df_add(d2df(Vm), df_mul(ichan, tbyc)));
+            D = df2d(df_add(df_mul(df_make(0.f, 0.f), tbyc), ld_df(&Pw[ps[5] * LANES])));
+        };
+        for (int s0 = 0; s0 < S; s0 += kCh) {
+            for (int q = s0 + kCh; q < min(s0 + 2 * kCh, S); ++q) {   // the next chunk's rows, into L1
+                for (int f = pf[6 * q]; f <= pf[6 * q + 1]; ++f) prefetch_l1(&Pw[f * LANES]);
+                prefetch_l1(&Vw[q * LANES]);
+                prefetch_l1(&lt[q * LANES]);
+                prefetch_l1(&Aw[q * LANES]);
+                prefetch_l1(&Bw[q * LANES]);
+            }
+            bool all_passive = !GIV && s0 + kCh <= S;
+            for (int k = 0; k < kCh && all_passive; ++k) all_passive = pf[6 * (s0 + k) + 2] >= 0;
+            if (all_passive) {
+                // every row's own terms first (independent of each other),
+                // then the elimination chain through them
+                double R[kCh], D[kCh], a[kCh], bb[kCh];
+                int f[kCh];
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) {
+                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k]);
+                    f[k] = __ldg(&lt[(s0 + k) * LANES]);
+                    a[k] = __ldg(&Aw[(s0 + k) * LANES]);
+                    bb[k] = __ldg(&Bw[(s0 + k) * LANES]);
+                }
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) fwd(s0 + k, R[k], D[k], f[k], a[k], bb[k]);
+                pc += 9 * kCh;
+                continue;
+            }
+            for (int s = s0; s < min(s0 + kCh, S); ++s) {
+                double R, D;
+                const int *ps = pf + 6 * s;
+                if (!GIV && ps[2] >= 0) {
+                    passive(s, ps, R, D);
+                    pc += 9;
+                } else if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
+                    if (v.status) atomicOr(v.status, ST_BAD_OP);
+                    return;
+                }
+                fwd(s, R, D, __ldg(&lt[s * LANES]), __ldg(&Aw[s * LANES]), __ldg(&Bw[s * LANES]));
             }
         }
         {
@@ -557,32 +583,45 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         }
         double xn = 0.0;
         top = 0;
-        for (int s = S - 1; s >= 0; --s) {
-            if (s >= kPf) {
-                const int q = s - kPf;
+        // back substitution of row s: its solution from the parent's (the row
+        // after, or the branch point on the stack)
+        auto bwd = [&](int s, int f, double2 rd, double c, double old) {
+            double r = rd.x;
+            if (f & FL_PARENT) {
+                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
+                if (f & FL_XPOP) --top;
+                r = fma(-c, xp, r);
+            }
+            r = r * rd.y;
+            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
+            xn = r;
+            Vw[s * LANES] = ty.crank ? fma(2.0, r, -old) : r;
+        };
+        int s1 = S - 1;
+        for (; s1 + 1 >= kCh; s1 -= kCh) {   // chunks: every row's loads, then the chain
+            for (int q = s1 - kCh; q > s1 - 2 * kCh && q >= 0; --q) {
                 prefetch_l1(&lt[q * LANES]);
                 prefetch_l1(&col[q * LANES]);
                 prefetch_l1(&Cbw[q * LANES]);
                 if (ty.crank) prefetch_l1(&Vw[q * LANES]);
             }
-            const int f = __ldg(&lt[s * LANES]);
-            const double2 rd = col[s * LANES];
-            double r = rd.x;
-            if (f & FL_PARENT) {
-                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
-                if (f & FL_XPOP) --top;
-                r = fma(-__ldg(&Cbw[s * LANES]), xp, r);
+            int f[kCh];
+            double2 rd[kCh];
+            double c[kCh], old[kCh];
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) {
+                const int s = s1 - k;
+                f[k] = __ldg(&lt[s * LANES]);
+                rd[k] = col[s * LANES];
+                c[k] = __ldg(&Cbw[s * LANES]);
+                old[k] = ty.crank ? Vw[s * LANES] : 0.0;
             }
-            r = r * rd.y;
-            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
-            xn = r;
-            if (ty.crank) {
-                const double old = Vw[s * LANES];
-                Vw[s * LANES] = fma(2.0, r, -old);
-            } else {
-                Vw[s * LANES] = r;
-            }
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) bwd(s1 - k, f[k], rd[k], c[k], old[k]);
         }
+        for (; s1 >= 0; --s1)
+            bwd(s1, __ldg(&lt[s1 * LANES]), col[s1 * LANES], __ldg(&Cbw[s1 * LANES]),
+                ty.crank ? Vw[s1 * LANES] : 0.0);
         finite_check(v, xn, active);   // row 0's solution
     }
 }

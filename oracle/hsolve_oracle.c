@@ -858,6 +858,26 @@ int orc_run_loss(orc_solver *s, int nsteps, int ntargets, const int *rows, const
     return 0;
 }
 
+/* Runs nsteps steps recording vm[rows[j]] after every step into
+ * out[i * nrows + j], and the voltage-table row each compartment's Vm falls
+ * in after every step into tab_rows[i * ncompts + c] (NULL: not recorded). */
+int orc_run_trace(orc_solver *s, int nsteps, int nrows, const int *rows, double *out, int *tab_rows)
+{
+    int i, j, c;
+    for (i = 0; i < nsteps; i++) {
+        if (orc_process(s)) return -1;
+        for (j = 0; j < nrows; j++) out[(long)i * nrows + j] = s->vm[rows[j]];
+        if (tab_rows)
+            for (c = 0; c < s->ncompts; c++) {
+                double f = (s->vm[c] - s->xmin) * s->invdx;
+                if (f < 0.0) f = 0.0;
+                else if (f > s->xdivs) f = s->xdivs;
+                tab_rows[(long)i * s->ncompts + c] = (int)f;
+            }
+    }
+    return 0;
+}
+
 int orc_run(orc_solver *s, int nsteps)
 {
     int i;

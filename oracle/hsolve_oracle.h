@@ -103,6 +103,10 @@ int orc_run(orc_solver *s, int nsteps);
  * trace[n*ntargets + j])^2 in *loss: the loss of the engine's differentiated
  * form, for finite-difference checks. */
 int orc_run_loss(orc_solver *s, int nsteps, int ntargets, const int *rows, const double *trace, double *loss);
+/* nsteps steps recording vm[rows[j]] after each into out[i * nrows + j] and,
+ * when tab_rows is not NULL, each compartment's voltage-table row into
+ * tab_rows[i * ncompts + c]. */
+int orc_run_trace(orc_solver *s, int nsteps, int nrows, const int *rows, double *out, int *tab_rows);
 
 /* ---- network of solvers with spike -> synchan event delivery ---- */
 typedef struct orc_net orc_net;

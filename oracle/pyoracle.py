@@ -100,6 +100,7 @@ def _lib(which: str):
             lib.orc_process.argtypes = [C.POINTER(OrcSolver)]
             lib.orc_run.argtypes = [C.POINTER(OrcSolver), C.c_int]
             lib.orc_run_loss.argtypes = [C.POINTER(OrcSolver), C.c_int, C.c_int, _ip, _dp, _dp]
+            lib.orc_run_trace.argtypes = [C.POINTER(OrcSolver), C.c_int, C.c_int, _ip, _dp, _ip]
             lib.orc_net_create.restype = C.c_void_p
             lib.orc_net_create.argtypes = [C.c_int, C.POINTER(C.POINTER(OrcSolver)), _ip, _ip, _ip,
                                            _ip, _dp, _ip]
@@ -211,6 +212,19 @@ class Solver:
         if rc != 0:
             raise RuntimeError("%s step failed at op %d" % (impl, self.s.err_op))
 
+
+    def run_trace(self, nsteps: int, rows, table_rows: bool = False):
+        """Runs nsteps steps; returns vm[rows] after every step (nsteps x
+        len(rows)) and, with table_rows, every compartment's voltage-table
+        row after every step (nsteps x ncompts), else None."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        out = np.empty((int(nsteps), len(r)))
+        tr = np.empty((int(nsteps), self.h.ncompts), dtype=np.int32) if table_rows else None
+        rc = _lib("oracle").orc_run_trace(C.byref(self.s), int(nsteps), len(r), _p(r, _ip), _p(out, _dp),
+                                          _p(tr, _ip) if tr is not None else C.cast(0, _ip))
+        if rc != 0:
+            raise RuntimeError("oracle step failed at op %d" % self.s.err_op)
+        return out, tr
 
     def run_loss(self, nsteps: int, rows, trace) -> float:
         """Runs nsteps steps; returns sum over steps and targets of

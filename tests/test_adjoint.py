@@ -57,44 +57,40 @@ def _rel(a, b):
 FD_TOL = 1e-4
 
 
-def _table_rows(oracle, h, nsteps):
-    """Voltage-table row of every compartment after every step (the bracket
-    the next step's gates interpolate in)."""
-    s = oracle.Solver(h)
-    out = np.empty((nsteps, h.ncompts), dtype=np.int64)
-    for n in range(nsteps):
-        s.run(1)
-        out[n] = np.clip(np.floor((s.vm - h.xmin) * h.invdx), 0, h.xdivs)
-    return out
-
-
 def fd_rule(oracle, tree, chans, j, g, nsteps, rows, trace, rel_h=1e-6):
     """Per-sample finite-difference rule for the gradient g of parameter j.
 
-    The loss is piecewise smooth: the gates interpolate tables linearly, so
-    its slope jumps where a perturbation moves some compartment's Vm across
-    a table node at some step. A central difference (h = rel_h x |p|) must
-    agree with g within FD_TOL. If it does not and the runs at p - h and
-    p + h put some compartment in different table rows at some step (the
-    interval straddles a node), g is the slope on one side of the kink: the
-    forward or the backward difference must agree with it within FD_TOL.
+    Differences of the loss between two runs are formed from their traces,
+    L(a) - L(b) = sum (a - b)(a + b - 2 target), which keeps the digits a
+    difference of two 10,000-step sums would cancel. The loss is piecewise
+    smooth: the gates interpolate tables linearly, so its slope jumps where
+    a perturbation moves some compartment's Vm across a table node at some
+    step. A central difference (h = rel_h x |p|) must agree with g within
+    FD_TOL. If it does not and the runs at p - h and p + h put some
+    compartment in different table rows at some step (the interval straddles
+    a node), g is the slope on one side of the kink: the forward or the
+    backward difference must agree with it within FD_TOL.
     Returns (kind, rel err): kind "central", "one-sided" or "fail"."""
     na, k = chans
     v = tree.vector()
     step = rel_h * abs(v[j])
-    built = {}
-    loss = {}
+    tr, rw = {}, {}
+    target = np.asarray(trace, dtype=np.float64).reshape(int(nsteps), len(rows))
     for sgn in (1, 0, -1):
         w = v.copy()
         w[j] += sgn * step
-        built[sgn] = model.build(tree.with_vector(w).model(na, k, dt=DT), exact=True)
-        loss[sgn] = oracle.Solver(built[sgn]).run_loss(nsteps, rows, trace)
-    central = _rel((loss[1] - loss[-1]) / (2 * step), g)
+        hh = model.build(tree.with_vector(w).model(na, k, dt=DT), exact=True)
+        tr[sgn], rw[sgn] = oracle.Solver(hh).run_trace(nsteps, rows, table_rows=sgn != 0)
+
+    def dloss(a, b):
+        return float(np.sum((tr[a] - tr[b]) * (tr[a] + tr[b] - 2.0 * target)))
+
+    central = _rel(dloss(1, -1) / (2 * step), g)
     if central <= FD_TOL:
         return "central", central
-    if np.array_equal(_table_rows(oracle, built[1], nsteps), _table_rows(oracle, built[-1], nsteps)):
+    if np.array_equal(rw[1], rw[-1]):
         return "fail", central
-    one = min(_rel((loss[1] - loss[0]) / step, g), _rel((loss[0] - loss[-1]) / step, g))
+    one = min(_rel(dloss(1, 0) / step, g), _rel(dloss(0, -1) / step, g))
     return ("one-sided" if one <= FD_TOL else "fail"), one
 
 
