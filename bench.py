@@ -51,6 +51,10 @@ IO_BLOCK = 16       # steps per host<->device transfer block of the end-to-end r
 # pass over per-compartment state and coefficients, tables on chip):
 # FP64 (16+32)*16 + 28*15 + 17*16 + 18*16 = 1748 B per neuron; mixed 1469 B
 ALG_BYTES = {"fp64": 1748.0 / NCOMP, "mixed": 1469.0 / NCOMP}
+# random trees (8-256 compartments, Ca pools): algorithmic bytes per
+# compartment-step, the per-compartment streaming pass of the mixed form
+# (~76 B) plus the soma's channels and Ca pool spread over the mean tree
+TREE_BYTES = 78.0
 ACC_STEPS = 10_000
 ACC_SAMPLE = 32
 # differentiated form (gradient of a somatic-trace loss)
@@ -323,12 +327,27 @@ def other_configs(device, n_trees=50_000):
         eng.run(steps)
         return eng.stats().device_ms - ms0
 
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import pyoracle
+
     hs0 = [model.build(m) for m in configs.cables(1000, per_neuron_solvers=True)]
     eng = engine.Engine(hs0, precision=engine.PREC_FP64, device=device)
     ms = rate(eng, 200, 20)
     out["cables-1k-x16"] = {"compartments": 16_000, "steps": 200, "ms": ms, "value": 16_000 * 200 / (ms / 1e3),
                             "dtype": "f64"}
     eng.close()
+    # the mixed form against the reference's FP64 step (the oracle) over the
+    # configured 200 steps, every neuron
+    ref = []
+    for h in hs0:
+        o = pyoracle.Solver(h)
+        o.run(200)
+        ref.append(o.vm.copy())
+    mx = engine.Engine(hs0, precision=engine.PREC_MIXED, device=device)
+    mx.run(200)
+    out["cables-1k-x16"]["mixed_max_abs_dvm_vs_fp64_oracle_V"] = float(
+        max(np.max(np.abs(a - b)) for a, b in zip(mx.get_state()["vm"], ref)))
+    mx.close()
 
     ms1, syn = configs.hh_network(4000)
     drive = np.random.default_rng(1).uniform(0.05e-9, 0.3e-9, size=len(ms1))   # tonic drive, recorded choice
@@ -338,6 +357,7 @@ def other_configs(device, n_trees=50_000):
     esyn, _ = configs.network_synapses(hs1, syn)
     net = {"cells": 4000, "synapses": int(len(esyn["target_solver"])), "steps": 5000, "dtype": "f64",
            "drive": "inject U(0.05, 0.3) nA, seed 1"}
+    fp64_counts = fp64_vm = None
     for graph in (False, True):
         eng = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_FP64, device=device, use_graph=graph)
         st = eng.stats()
@@ -346,19 +366,42 @@ def other_configs(device, n_trees=50_000):
         net[key] = {"ms": ms, "steps_per_s": 5000 / (ms / 1e3), "value": 4000 * 5000 / (ms / 1e3),
                     "spikes": int(eng.spike_counts().sum()), "cooperative": int(st.cooperative),
                     "specialised_kernels": int(st.jit_kernels)}
+        if not graph:
+            fp64_counts, fp64_vm = eng.spike_counts(), eng.vm()
         eng.close()
+    # the mixed form over the same 5,100 steps against the FP64 engine (which
+    # equals the reference's step code bit for bit): spike counts per cell
+    mx = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_MIXED, device=device)
+    mx.run(5100)
+    mc = mx.spike_counts()
+    net["mixed"] = {"spike_count_mismatch_cells": int(np.sum(mc != fp64_counts)), "spikes": int(mc.sum()),
+                    "max_abs_dvm_vs_fp64_V": float(np.max(np.abs(mx.vm() - fp64_vm))), "steps": 5100}
+    mx.close()
     out["hh-network-4000"] = net
 
     hs2 = [model.build(m) for m in configs.random_trees(n_trees, seed=2)]
     M2 = sum(h.ncompts for h in hs2)
-    trees = {"neurons": n_trees, "compartments": M2, "steps": 500}
+    trees = {"neurons": n_trees, "compartments": M2, "steps": 500,
+             "timed": "500 of the configured 5,000 steps (a rate; neurons are independent)"}
     for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
+        tc = time.perf_counter()
         eng = engine.Engine(hs2, precision=prec, device=device, use_graph=True)
+        setup = time.perf_counter() - tc
         st = eng.stats()
         ms = rate(eng, 500, 20)
         trees[form] = {"ms": ms, "value": M2 * 500 / (ms / 1e3), "tiles": int(st.tiles),
-                       "specialised_kernels": int(st.jit_kernels), "steps_per_launch": int(st.steps_per_launch)}
+                       "wide_tiles": int(st.wide_tiles), "stack_tiles": int(st.stack_tiles),
+                       "specialised_kernels": int(st.jit_kernels), "steps_per_launch": int(st.steps_per_launch),
+                       "engine_setup_s": setup,
+                       "hbm_frac": TREE_BYTES * M2 * 500 / (ms / 1e3) / 1e9 / peaks()[0]}
         eng.close()
+    # the mixed form against the reference's FP64 step over the configured
+    # 5,000 steps on a seeded 1-in-500 sample of the trees
+    sample = hs2[::500]
+    acc, dev, nspk, mism = accuracy_sample(sample, engine.PREC_MIXED, nsteps=5000, nsample=len(sample))
+    trees["mixed"].update({"max_abs_dvm_vs_fp64_oracle_V": acc, "spike_time_max_dev_s": dev, "spikes_compared": nspk,
+                           "spike_count_mismatches": mism, "accuracy_sample_neurons": len(sample),
+                           "accuracy_steps": 5000})
     out["random-trees-ca"] = trees
     log("other configs: %s" % json.dumps(out))
     return out
@@ -426,7 +469,11 @@ def main():
     ap.add_argument("--profile-adjoint", type=int, nargs=2, metavar=("NEURONS", "STEPS"),
                     help="run only the gradient workload at this size")
     ap.add_argument("--wide-min", type=int, default=0,
-                    help="--profile-trees: the engine's wide_min (0 autotuned mapping, < 0 never wide)")
+                    help="--profile-trees: the engine's wide_min (0 mapping chosen by trial, < 0 never wide)")
+    ap.add_argument("--no-jit", action="store_true",
+                    help="--profile-trees / --profile-network: interpret every program (no specialised kernels)")
+    ap.add_argument("--profile-network", type=int, metavar="STEPS",
+                    help="run only the 4,000-cell network (FP64, tonic drive) for this many steps")
     ap.add_argument("--profile-trees", type=int, metavar="NEURONS",
                     help="run only random trees (8-256 compartments, Ca) of this many neurons, the form of "
                          "--profile-form (default mixed), steps_per_launch --steps-per-launch (default 64); "
@@ -449,7 +496,7 @@ def main():
         ht = [model.build(m) for m in configs.random_trees(args.profile_trees, seed=2)]
         prec = engine.PREC_FP64 if args.profile_form == "fp64" else engine.PREC_MIXED
         eng = engine.Engine(ht, precision=prec, steps_per_launch=args.steps_per_launch or 64, device=local,
-                            wide_min=args.wide_min)
+                            wide_min=args.wide_min, jit=not args.no_jit)
         eng.run(args.warmup)
         eng.vm()
         torch.cuda.profiler.start()
@@ -460,6 +507,22 @@ def main():
         torch.cuda.profiler.stop()
         log("random trees %d: %d steps in %.1f ms, %d tiles" % (args.profile_trees, args.steps, dt * 1e3,
                                                               eng.stats().tiles))
+        eng.close()
+        return 0
+    if args.profile_network:
+        from gbhsolve import configs, model
+        ms1, syn = configs.hh_network(4000)
+        drive = np.random.default_rng(1).uniform(0.05e-9, 0.3e-9, size=len(ms1))
+        for m, x in zip(ms1, drive):
+            m.compartments[0].inject = float(x)
+        hs1 = [model.build(m) for m in ms1]
+        esyn, _ = configs.network_synapses(hs1, syn)
+        eng = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_FP64, device=local, jit=not args.no_jit)
+        eng.run(args.warmup)
+        ms0 = eng.stats().device_ms
+        eng.run(args.profile_network)
+        ms = eng.stats().device_ms - ms0
+        log("network 4000: %.2f us/step, %d spikes" % (ms / args.profile_network * 1e3, eng.spike_counts().sum()))
         eng.close()
         return 0
     hs, injects = build_workload(args.neurons)

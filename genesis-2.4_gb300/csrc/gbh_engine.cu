@@ -2244,7 +2244,61 @@ gbh_engine *gbh_create(const gbh_batch_desc *desc, const gbh_synapses *syn, cons
 namespace {
 
 gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
-                        const gbh_options *opt, gbh_error *err, gbh_engine *&made)
+                        const gbh_options *opt, gbh_error *err, gbh_engine *&made, const Decoded *pre = nullptr);
+
+// The neuron-to-warp mapping, chosen by trial (gbh_options.wide_min 0): for
+// each candidate -- neurons of at least 32, 64 or 128 compartments one per
+// warp (wide tiles), or none (every large neuron lane-mapped, 32 per warp,
+// with the stack elimination) -- an engine over the same decoded batch,
+// interpreted (the specialised kernels serve the small types the same way
+// under every candidate) at 16 steps per launch, times 32 steps after 16;
+// the fastest candidate is kept. Returns the chosen wide_min.
+int choose_mapping(gbh_engine *e, const gbh_batch_desc *desc, const gbh_synapses *syn,
+                   const gbh_remote_synapses *remote)
+{
+    int maxrows = 0;
+    for (const Neuron &N : e->dec.neurons) maxrows = std::max(maxrows, N.nrows);
+    std::vector<int> cand;
+    for (int w : {32, 64, 128})
+        if (w <= maxrows) cand.push_back(w);
+    if (cand.empty()) return -1;   // nothing large enough to run wide
+    cand.push_back(-1);
+    int best = cand[0];
+    double best_ms = 1e300;
+    for (int w : cand) {
+        gbh_options o = e->opt;
+        o.wide_min = w;
+        o.jit = -1;
+        o.steps_per_launch = 16;
+        o.use_graph = 0;
+        gbh_error te{};
+        gbh_engine *made = nullptr, *t = nullptr;
+        try {
+            t = create_dist(desc, syn, remote, &o, &te, made, &e->dec);
+        } catch (const std::exception &) {
+            if (made) gbh_destroy(made);
+            t = nullptr;
+        }
+        if (!t) continue;   // a candidate that cannot be built is not chosen
+        double ms = 1e300;
+        if (gbh_run(t, 16) == GBH_OK) {
+            const double ms0 = t->stats.device_ms;
+            if (gbh_run(t, 32) == GBH_OK) ms = t->stats.device_ms - ms0;
+        }
+        if (getenv("GBH_VERBOSE"))
+            fprintf(stderr, "gbhsolve: mapping trial wide_min %d: %.2f us/step (%lld wide, %lld stack tiles)\n", w,
+                    ms / 32 * 1e3, (long long)t->stats.wide_tiles, (long long)t->stats.stack_tiles);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = w;
+        }
+        gbh_destroy(t);
+    }
+    return best;
+}
+
+gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, const gbh_remote_synapses *remote,
+                        const gbh_options *opt, gbh_error *err, gbh_engine *&made, const Decoded *pre)
 {
     memset(err, 0, sizeof(*err));
     if (!desc) {
@@ -2261,12 +2315,15 @@ gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, con
         delete e;
         return nullptr;
     }
-    int rc = decode_batch(desc, e->dec, err);
+    int rc = GBH_OK;
+    if (pre) e->dec = *pre;   // a trial engine over a batch already decoded
+    else rc = decode_batch(desc, e->dec, err);
     if (rc) {
         set_last("%s", err->message);
         delete e;
         return nullptr;
     }
+    if (!pre && e->opt.wide_min == 0) e->opt.wide_min = choose_mapping(e, desc, syn, remote);
     // keep the reference layout for state sync
     const int ns = desc->nsolvers;
     e->chip_start.assign(desc->chip_start, desc->chip_start + ns + 1);

@@ -325,7 +325,7 @@ class Engine:
         # jit: True (autotuned forms), False (interpreter), or the ABI value
         jit_v = (0 if jit else -1) if isinstance(jit, bool) else int(jit)
         # wide_min: neurons of at least this many compartments run one per
-        # block (0: 32, negative: never)
+        # warp (0: chosen by timing candidates at creation, negative: never)
         opt = GbhOptions(precision, steps_per_launch, warps_per_block, 1 if use_graph else 0, device, jit_v,
                          int(wide_min))
         err = GbhError()

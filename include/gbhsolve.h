@@ -174,9 +174,12 @@ typedef struct gbh_options {
                             shared-memory rows only; -1 = interpret the
                             programs                                          */
     int wide_min;        /* neurons with at least this many compartments run
-                            one per warp, compartments across its threads
-                            (0 = 32; < 0 = never; gbh_loss_gradient needs
-                            < 0)                                             */
+                            one per warp, compartments across its threads;
+                            the other large neurons run 32 per warp, one per
+                            lane, with the stack elimination. 0 = chosen by
+                            trial at creation (candidates 32, 64, 128, never:
+                            an interpreted engine per candidate times a few
+                            steps); < 0 = never (gbh_loss_gradient needs it) */
 } gbh_options;
 
 typedef struct gbh_stats {
