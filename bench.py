@@ -379,10 +379,15 @@ def other_configs(device, n_trees=50_000):
     mx.close()
     out["hh-network-4000"] = net
 
-    hs2 = [model.build(m) for m in configs.random_trees(n_trees, seed=2)]
+    # SETUP of the 50,000 hsolves (the restated h_hh_chip_init / do_hget_children
+    # / h_funcs_init, with the model generation) on every host core
+    ts = time.perf_counter()
+    hs2 = model.build_generated(configs.random_trees, n_trees, seed=2)
+    setup_s = time.perf_counter() - ts
     M2 = sum(h.ncompts for h in hs2)
     trees = {"neurons": n_trees, "compartments": M2, "steps": 500,
-             "timed": "500 of the configured 5,000 steps (a rate; neurons are independent)"}
+             "timed": "500 of the configured 5,000 steps (a rate; neurons are independent)",
+             "hsolve_setup_s": setup_s, "hsolve_setup_processes": model.setup_workers()}
     for form, prec in (("fp64", engine.PREC_FP64), ("mixed", engine.PREC_MIXED)):
         tc = time.perf_counter()
         eng = engine.Engine(hs2, precision=prec, device=device, use_graph=True)
@@ -493,20 +498,24 @@ def main():
         return 0
     if args.profile_trees:
         from gbhsolve import configs, model
-        ht = [model.build(m) for m in configs.random_trees(args.profile_trees, seed=2)]
+        ht = model.build_generated(configs.random_trees, args.profile_trees, seed=2)
         prec = engine.PREC_FP64 if args.profile_form == "fp64" else engine.PREC_MIXED
         eng = engine.Engine(ht, precision=prec, steps_per_launch=args.steps_per_launch or 64, device=local,
                             wide_min=args.wide_min, jit=not args.no_jit)
         eng.run(args.warmup)
         eng.vm()
+        ms0 = eng.stats().device_ms
         torch.cuda.profiler.start()
-        t0 = time.time()
         eng.run(args.steps)
         eng.vm()
-        dt = time.time() - t0
         torch.cuda.profiler.stop()
-        log("random trees %d: %d steps in %.1f ms, %d tiles" % (args.profile_trees, args.steps, dt * 1e3,
-                                                              eng.stats().tiles))
+        st = eng.stats()
+        us = (st.device_ms - ms0) / args.steps * 1e3
+        ncs = sum(h.ncompts for h in ht)
+        log("random trees %d (%s): %.1f us/step on the device (%.3g compartment-steps/s), %d tiles "
+            "(%d wide, %d stack), %d steps per launch" % (args.profile_trees, args.profile_form, us,
+                                                          ncs / (us * 1e-6), st.tiles, st.wide_tiles,
+                                                          st.stack_tiles, st.steps_per_launch))
         eng.close()
         return 0
     if args.profile_network:

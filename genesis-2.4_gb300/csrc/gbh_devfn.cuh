@@ -72,11 +72,13 @@ struct DevView {
     long long io_step0;
     const int *tin_start, *tin_off, *tin_idx;
     const int *tout_start, *tout_off, *tout_idx;
-    // stack elimination (TileType::stack): per-row flags (StackFlag) and a
-    // column of (right-hand side, diagonal or its reciprocal) per row, both
-    // at the tile's topo rows
+    // stack elimination (TileType::stack): per-row flags (StackFlag), a
+    // column of (right-hand side, diagonal or its reciprocal) per row, and
+    // for the rows below nstatic their step-invariant (rhs term, coupling
+    // factor), all at the tile's topo rows
     const int *ltop;
     double2 *col;
+    double2 *kst;
     // synapses of weighted synchans (SynW): per synapse its bit's word for
     // slot 0 (-1 for a synchan of one weight) and bit | nwords << 5
     const int64_t *syn_out_mword;

@@ -128,6 +128,7 @@ struct gbh_engine {
     DBuf<int> d_I, d_par;
     DBuf<int> d_ltop;              // stack elimination: per-row flags (topo rows)
     DBuf<double2> d_col;           // stack elimination: (rhs, diagonal) per row
+    DBuf<double2> d_kst;           // stack elimination: static rows' (rhs term, coupling factor)
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
     DBuf<int> d_out_delay;
@@ -683,6 +684,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             tt.stack = 1;
             tt.scap = cap;
             const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
+            tt.nstatic = 0;
+            while (tt.nstatic < tt.nslots && pf[6 * tt.nstatic + 2] >= 0) ++tt.nstatic;
             tt.pf_off = (int)prog_pool.size();
             prog_pool.insert(prog_pool.end(), pf.begin(), pf.end());
         }
@@ -787,7 +790,9 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             std::vector<int> fl;
             int cap = 0;
             stack_plan(N.parent, fl, cap);
-            for (int s = 0; s < N.nrows; ++s) LT[at(t.topo, s, l, false)] = fl[s];
+            const int nst = e->types[t.type].nstatic;
+            for (int s = 0; s < N.nrows; ++s)
+                LT[at(t.topo, s, l, false)] = fl[s] | (s < nst && N.parent[s] >= nst ? FL_PD : 0);
         }
         for (size_t f = 0; f < N.fsrc.size(); ++f) P[at(t.fld, f, l, w)] = N.fval[f];
         for (size_t k = 0; k < N.rav.size(); ++k) RV[at(t.rav, k, l, w)] = N.rav[k];
@@ -1047,7 +1052,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_I.upload(I);
     rc |= e->d_par.upload(par);
     rc |= e->d_ltop.upload(LT);
-    if (any_stack) rc |= e->d_col.alloc(e->rows_topo * L);
+    if (any_stack) rc |= e->d_col.alloc(e->rows_topo * L) | e->d_kst.alloc(e->rows_topo * L);
     rc |= e->d_giv.upload(std::vector<double>(e->rows_giv * L, 0.0));
     rc |= e->d_stab.upload(stab);
     rc |= e->d_ring.upload(std::vector<unsigned>(e->rows_syn * L, 0u));
@@ -1248,6 +1253,7 @@ DevView view_of(gbh_engine *e)
     v.parent = e->d_par.p;
     v.ltop = e->d_ltop.p;
     v.col = e->d_col.p;
+    v.kst = e->d_kst.p;
     v.A = e->d_A.p;
     v.B = e->d_B.p;
     v.Cb = e->d_Cb.p;
@@ -3010,7 +3016,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_kst.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

@@ -126,6 +126,9 @@ struct TileType {
                      // a post-order of its tree (each subtree contiguous, its root last)
     int scap;        // stack: shared-memory doubles per lane its neurons need
     int pf_off;      // stack: prog-pool offset of each slot's [first, last] field row (prefetch)
+    int nstatic;     // stack: rows [0, nstatic) are passive and so is every row below them in their
+                     // trees (the first non-passive slot; post-order keeps subtrees below their roots):
+                     // their diagonals, reciprocals and coupling factors are the same every step
 };
 
 // Per-row flags of the stack elimination (DevView::ltop, topo rows, one word
@@ -143,7 +146,9 @@ enum StackFlag {
     FL_PUSH = 1 << 11,       // the parent is further away: push the contribution
     FL_XLOAD = 1 << 12,      // backward: the parent's solution is on the stack top
     FL_XPOP = 1 << 13,       // backward: the last reader of that entry (the parent's first child)
-    FL_XPUSH = 1 << 14       // backward: two or more children read this row's solution later
+    FL_XPUSH = 1 << 14,      // backward: two or more children read this row's solution later
+    FL_PD = 1 << 15          // a row below nstatic whose parent is at or above it: the parent's
+                             // forward step needs this row's diagonal contribution
 };
 
 struct Tile {

@@ -516,9 +516,11 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     const double *Bw = v.B + tl.topo * LANES + lane;
     const double *Cbw = v.Cb + tl.topo * LANES + lane;
     double2 *col = v.col + tl.topo * LANES + lane;
+    double2 *kst = v.kst + tl.topo * LANES + lane;
     double *stk = sm + lane;      // entry j at stk[j * 32]
     const int S = ty.nslots;
     const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
+    const int nst = GIV ? 0 : ty.nstatic; // static rows (givals off: they would write Im)
     constexpr int kCh = 8;                // rows per chunk
 
     ChanEnv<G> E;
@@ -544,6 +546,11 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
 
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
+        // after a launch's first step the static rows' (rhs term, coupling
+        // factor) are in kst: their diagonals do not change within a launch
+        // (nothing but channels changes a diagonal; inputs and state writes
+        // come between launches), so they skip the diagonal's elimination
+        const bool fast = it > 0;
         for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
         ChanState cs;
         chan_state_reset(cs, tg.ncols);
@@ -553,8 +560,9 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         // the forward step of row s from its own (R, D): children's
         // contributions (stack, then the carried last child) in ascending row
         // order, its (R, D) into the column, its own contribution pushed or
-        // carried -- the operations of the sequential sweep (hines_solve.c:247-252)
-        auto fwd = [&](int s, double R, double D, int f, double a, double bb) {
+        // carried -- the operations of the sequential sweep (hines_solve.c:247-252).
+        // A static row also keeps its rhs term K and its factor a / D.
+        auto fwd = [&](int s, double R, double D, int f, double a, double bb, double K) {
             const int np = f & FL_NPOP;
             top -= np;
             for (int j = 0; j < np; ++j) {
@@ -566,8 +574,9 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 R -= cr;
             }
             col[s * LANES] = make_double2(R, D);
+            double temp = 0.0;
             if (f & FL_PARENT) {
-                const double temp = a / D;
+                temp = a / D;
                 const double pd = bb * temp, pr = R * temp;
                 if (f & FL_CARRY_OUT) {
                     cd = pd;
@@ -578,17 +587,62 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                     ++top;
                 }
             }
+            if (s < nst) kst[s * LANES] = make_double2(K, temp);
         };
-        // the interpreter's M_BEGIN / M_END arithmetic of a passive row
-        auto passive = [&](int s, const int *ps, double &R, double &D) {
+        // the same for a static row on later steps: its diagonal and factor
+        // are those of the first step, so only the rhs is eliminated (the
+        // same operations on R as above); its diagonal contribution bb * temp
+        // is formed only for a parent above the static rows
+        auto fwd_static = [&](int s, double R, double T, int f) {
+            const int np = f & FL_NPOP;
+            top -= np;
+            for (int j = 0; j < np; ++j) R -= stk[(2 * (top + j) + 1) * LANES];
+            if (f & FL_CARRY_IN) R -= cr;
+            reinterpret_cast<double *>(col + s * LANES)[0] = R;
+            if (f & FL_PARENT) {
+                const double pd = (f & FL_PD) ? Bw[s * LANES] * T : 0.0, pr = R * T;
+                if (f & FL_CARRY_OUT) {
+                    cd = pd;
+                    cr = pr;
+                } else {
+                    stk[(2 * top) * LANES] = pd;
+                    stk[(2 * top + 1) * LANES] = pr;
+                    ++top;
+                }
+            }
+        };
+        // the interpreter's M_BEGIN / M_END arithmetic of a passive row; K
+        // is the rhs term ichan * tbyc
+        auto passive = [&](int s, const int *ps, double &R, double &D, double &K) {
             const double Vm = Vw[s * LANES];
             const double ichan = Pw[ps[2] * LANES] + Pw[ps[3] * LANES];
             const double tbyc = Pw[ps[4] * LANES];
             const double sumg = 0.0;
-            R = Vm + ichan * tbyc;
+            K = ichan * tbyc;
+            R = Vm + K;
             D = sumg * tbyc + Pw[ps[5] * LANES];
         };
         for (int s0 = 0; s0 < S; s0 += kCh) {
+            if (fast && s0 + kCh <= nst) {
+                for (int q = s0 + kCh; q < min(s0 + 2 * kCh, nst); ++q) {   // the next chunk's rows
+                    prefetch_l1(&Vw[q * LANES]);
+                    prefetch_l1(&lt[q * LANES]);
+                    prefetch_l1(&kst[q * LANES]);
+                }
+                double R[kCh], T[kCh];
+                int f[kCh];
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) {
+                    const double2 kt = kst[(s0 + k) * LANES];
+                    f[k] = lt[(s0 + k) * LANES];
+                    R[k] = Vw[(s0 + k) * LANES] + kt.x;
+                    T[k] = kt.y;
+                }
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) fwd_static(s0 + k, R[k], T[k], f[k]);
+                pc += 9 * kCh;
+                continue;
+            }
             for (int q = s0 + kCh; q < min(s0 + 2 * kCh, S); ++q) {   // the next chunk's rows, into L1
                 for (int f = pf[6 * q]; f <= pf[6 * q + 1]; ++f) prefetch_l1(&Pw[f * LANES]);
                 prefetch_l1(&Vw[q * LANES]);
@@ -601,31 +655,44 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
             if (all_passive) {
                 // every row's own terms first (independent of each other),
                 // then the elimination chain through them
-                double R[kCh], D[kCh], a[kCh], bb[kCh];
+                double R[kCh], D[kCh], K[kCh], a[kCh], bb[kCh];
                 int f[kCh];
 #pragma unroll
                 for (int k = 0; k < kCh; ++k) {
-                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k]);
+                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k], K[k]);
                     f[k] = lt[(s0 + k) * LANES];
                     a[k] = Aw[(s0 + k) * LANES];
                     bb[k] = Bw[(s0 + k) * LANES];
                 }
 #pragma unroll
-                for (int k = 0; k < kCh; ++k) fwd(s0 + k, R[k], D[k], f[k], a[k], bb[k]);
+                for (int k = 0; k < kCh; ++k) {
+                    const int s = s0 + k;
+                    if (fast && s < nst) {
+                        fwd_static(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
+                    } else {
+                        fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
+                    }
+                }
                 pc += 9 * kCh;
                 continue;
             }
             for (int s = s0; s < min(s0 + kCh, S); ++s) {
-                double R, D;
+                double R, D, K = 0.0;
                 const int *ps = pf + 6 * s;
+                if (fast && s < nst) {
+                    const double2 kt = kst[s * LANES];
+                    fwd_static(s, Vw[s * LANES] + kt.x, kt.y, lt[s * LANES]);
+                    pc += 9;
+                    continue;
+                }
                 if (!GIV && ps[2] >= 0) {
-                    passive(s, ps, R, D);
+                    passive(s, ps, R, D, K);
                     pc += 9;
                 } else if (!chan_compartment<G, GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
                     if (v.status) atomicOr(v.status, ST_BAD_OP);
                     return;
                 }
-                fwd(s, R, D, lt[s * LANES], Aw[s * LANES], Bw[s * LANES]);
+                fwd(s, R, D, lt[s * LANES], Aw[s * LANES], Bw[s * LANES], K);
             }
         }
         {

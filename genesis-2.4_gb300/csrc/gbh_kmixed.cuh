@@ -453,9 +453,11 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
     const double *Bw = v.B + tl.topo * LANES + lane;
     const double *Cbw = v.Cb + tl.topo * LANES + lane;
     double2 *col = v.col + tl.topo * LANES + lane;
+    double2 *kst = v.kst + tl.topo * LANES + lane;
     double *stk = sm + lane;
     const int S = ty.nslots;
     const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
+    const int nst = GIV ? 0 : ty.nstatic; // static rows (givals off: they would write Im)
     constexpr int kCh = 8;                // rows per chunk
 
     ChanEnvDF E;
@@ -482,6 +484,9 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
 
     for (int it = 0; it < nsteps; ++it) {
         const long long step = sbase + step0 + it;
+        // after a launch's first step the static rows' (rhs term, coupling
+        // factor) are in kst (see k_stack)
+        const bool fast = it > 0;
         for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
         ChanStateDF cs;
         chan_state_reset_df(cs);
@@ -490,8 +495,9 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         double cd = 0.0, cr = 0.0;
         // the forward step of row s from its own (R, D): children's
         // contributions (stack, then the carried last child), the row's
-        // reciprocal into the column, its own contribution pushed or carried
-        auto fwd = [&](int s, double R, double D, int f, double a, double bb) {
+        // reciprocal into the column, its own contribution pushed or carried;
+        // a static row also keeps its rhs term K and its factor a / D
+        auto fwd = [&](int s, double R, double D, int f, double a, double bb, double K) {
             const int np = f & FL_NPOP;
             top -= np;
             for (int j = 0; j < np; ++j) {
@@ -504,8 +510,9 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             }
             const double ri = rcp_newton(D);
             col[s * LANES] = make_double2(R, ri);
+            double temp = 0.0;
             if (f & FL_PARENT) {
-                const double temp = a * ri;
+                temp = a * ri;
                 const double pd = bb * temp, pr = R * temp;
                 if (f & FL_CARRY_OUT) {
                     cd = pd;
@@ -516,16 +523,58 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                     ++top;
                 }
             }
+            if (s < nst) kst[s * LANES] = make_double2(K, temp);
         };
-        // the interpreter's M_BEGIN / M_END arithmetic of a passive row
-        auto passive = [&](int s, const int *ps, double &R, double &D) {
-            const double Vm = Vw[s * LANES];
+        // a static row on later steps: only its rhs is eliminated; its
+        // diagonal contribution is formed only for a parent above the static rows
+        auto fwd_static = [&](int s, double R, double T, int f) {
+            const int np = f & FL_NPOP;
+            top -= np;
+            for (int j = 0; j < np; ++j) R -= stk[(2 * (top + j) + 1) * LANES];
+            if (f & FL_CARRY_IN) R -= cr;
+            reinterpret_cast<double *>(col + s * LANES)[0] = R;
+            if (f & FL_PARENT) {
+                const double pd = (f & FL_PD) ? __ldg(&Bw[s * LANES]) * T : 0.0, pr = R * T;
+                if (f & FL_CARRY_OUT) {
+                    cd = pd;
+                    cr = pr;
+                } else {
+                    stk[(2 * top) * LANES] = pd;
+                    stk[(2 * top + 1) * LANES] = pr;
+                    ++top;
+                }
+            }
+        };
+        // a passive row (M_BEGIN / M_END): its current term ichan * tbyc in
+        // double-float, added to Vm in FP64 (part of the Vm update); the
+        // diagonal is the row's diagonal term (its conductance sum is zero)
+        auto passive = [&](int s, const int *ps, double &R, double &D, double &K) {
             const df ichan = df_add(ld_df(&Pw[ps[2] * LANES]), ld_df(&Pw[ps[3] * LANES]));
-            const df tbyc = ld_df(&Pw[ps[4] * LANES]);
-            R = df2d(df_add(d2df(Vm), df_mul(ichan, tbyc)));
-            D = df2d(df_add(df_mul(df_make(0.f, 0.f), tbyc), ld_df(&Pw[ps[5] * LANES])));
+            K = df2d(df_mul(ichan, ld_df(&Pw[ps[4] * LANES])));
+            R = Vw[s * LANES] + K;
+            D = df2d(ld_df(&Pw[ps[5] * LANES]));
         };
         for (int s0 = 0; s0 < S; s0 += kCh) {
+            if (fast && s0 + kCh <= nst) {
+                for (int q = s0 + kCh; q < min(s0 + 2 * kCh, nst); ++q) {   // the next chunk's rows
+                    prefetch_l1(&Vw[q * LANES]);
+                    prefetch_l1(&lt[q * LANES]);
+                    prefetch_l1(&kst[q * LANES]);
+                }
+                double R[kCh], T[kCh];
+                int f[kCh];
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) {
+                    const double2 kt = kst[(s0 + k) * LANES];
+                    f[k] = __ldg(&lt[(s0 + k) * LANES]);
+                    R[k] = Vw[(s0 + k) * LANES] + kt.x;
+                    T[k] = kt.y;
+                }
+#pragma unroll
+                for (int k = 0; k < kCh; ++k) fwd_static(s0 + k, R[k], T[k], f[k]);
+                pc += 9 * kCh;
+                continue;
+            }
             for (int q = s0 + kCh; q < min(s0 + 2 * kCh, S); ++q) {   // the next chunk's rows, into L1
                 for (int f = pf[6 * q]; f <= pf[6 * q + 1]; ++f) prefetch_l1(&Pw[f * LANES]);
                 prefetch_l1(&Vw[q * LANES]);
@@ -538,31 +587,44 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             if (all_passive) {
                 // every row's own terms first (independent of each other),
                 // then the elimination chain through them
-                double R[kCh], D[kCh], a[kCh], bb[kCh];
+                double R[kCh], D[kCh], K[kCh], a[kCh], bb[kCh];
                 int f[kCh];
 #pragma unroll
                 for (int k = 0; k < kCh; ++k) {
-                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k]);
+                    passive(s0 + k, pf + 6 * (s0 + k), R[k], D[k], K[k]);
                     f[k] = __ldg(&lt[(s0 + k) * LANES]);
                     a[k] = __ldg(&Aw[(s0 + k) * LANES]);
                     bb[k] = __ldg(&Bw[(s0 + k) * LANES]);
                 }
 #pragma unroll
-                for (int k = 0; k < kCh; ++k) fwd(s0 + k, R[k], D[k], f[k], a[k], bb[k]);
+                for (int k = 0; k < kCh; ++k) {
+                    const int s = s0 + k;
+                    if (fast && s < nst) {
+                        fwd_static(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
+                    } else {
+                        fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
+                    }
+                }
                 pc += 9 * kCh;
                 continue;
             }
             for (int s = s0; s < min(s0 + kCh, S); ++s) {
-                double R, D;
+                double R, D, K = 0.0;
                 const int *ps = pf + 6 * s;
+                if (fast && s < nst) {
+                    const double2 kt = kst[s * LANES];
+                    fwd_static(s, Vw[s * LANES] + kt.x, kt.y, __ldg(&lt[s * LANES]));
+                    pc += 9;
+                    continue;
+                }
                 if (!GIV && ps[2] >= 0) {
-                    passive(s, ps, R, D);
+                    passive(s, ps, R, D, K);
                     pc += 9;
                 } else if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
                     if (v.status) atomicOr(v.status, ST_BAD_OP);
                     return;
                 }
-                fwd(s, R, D, __ldg(&lt[s * LANES]), __ldg(&Aw[s * LANES]), __ldg(&Bw[s * LANES]));
+                fwd(s, R, D, __ldg(&lt[s * LANES]), __ldg(&Aw[s * LANES]), __ldg(&Bw[s * LANES]), K);
             }
         }
         {

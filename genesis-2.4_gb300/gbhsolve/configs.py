@@ -170,8 +170,12 @@ def random_tree_neuron(rng, ncomp, na, k, ca, kca, inject, erest=-0.065, dend_le
 
 
 def random_trees(n_neurons, seed=2, size_range=(8, 256), dt=20e-6, with_ca=True,
-                 inject_range=(0.0, 1e-9), method=BEULER):
-    """Config 2: one hsolve per neuron, log-uniform sizes."""
+                 inject_range=(0.0, 1e-9), method=BEULER, start=0, stop=None):
+    """Config 2: one hsolve per neuron, log-uniform sizes. Sizes and injects
+    are drawn for all ``n_neurons`` from ``seed``; neuron i's branching and
+    diameters from its own generator seeded by (seed, i). So neurons
+    [start, stop) can be generated alone (model.build_generated sets up
+    the 50,000 on every core) and equal those of the whole set."""
     rng = np.random.default_rng(seed)
     na, k = hh_channels(-0.065)
     ca, kca = ca_channels()
@@ -180,9 +184,9 @@ def random_trees(n_neurons, seed=2, size_range=(8, 256), dt=20e-6, with_ca=True,
     sizes = np.clip(sizes, lo, hi)
     injects = rng.uniform(inject_range[0], inject_range[1], size=n_neurons)
     models = []
-    for i in range(n_neurons):
-        comps = random_tree_neuron(rng, int(sizes[i]), na, k, ca, kca, float(injects[i]),
-                                   with_ca=with_ca)
+    for i in range(start, n_neurons if stop is None else stop):
+        comps = random_tree_neuron(np.random.default_rng((seed, i)), int(sizes[i]), na, k, ca, kca,
+                                   float(injects[i]), with_ca=with_ca)
         models.append(Model(comps, dt=sli(dt), method=method))
     return models
 

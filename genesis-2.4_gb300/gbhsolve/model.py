@@ -25,6 +25,7 @@ olf/olf_struct.h:142-155, sim/struct_defs.h:118-134).
 from __future__ import annotations
 
 import math
+import pickle
 import struct
 from dataclasses import dataclass, field
 from typing import List, Optional
@@ -752,3 +753,102 @@ def _child_pos(row_children, orig_pos):
         if p == orig_pos:
             return p
     raise ValueError("child %d not found" % orig_pos)
+
+
+# --------------------------------------------------------------------------
+# SETUP of many hsolves on every host core
+# --------------------------------------------------------------------------
+_SENT_TABLES = set()      # in a worker: table keys already returned to the parent
+_TABLE_KEYS = {}          # in a worker: id(tablist) -> content key
+
+
+def _table_key(a: HsolveArrays):
+    import hashlib
+    k = _TABLE_KEYS.get(id(a.tablist))
+    if k is None:
+        h = hashlib.blake2b(digest_size=16)
+        h.update(struct.pack("<iiidddd", a.ncols, a.xdivs, a.ydivs, a.xmin, a.invdx, a.ymin, a.invdy))
+        for arr in (a.tablist, a.xvals, a.yvals):
+            h.update(np.ascontiguousarray(arr, dtype=np.float64).tobytes())
+        k = h.hexdigest()
+        _TABLE_KEYS[id(a.tablist)] = k     # the tables stay alive in _TABLE_CACHE
+    return k
+
+
+def _build_chunk(args):
+    """Worker: builds one chunk -- a list of models, or the models
+    ``factory(n, start=a, stop=b, **kw)`` generates -- and returns the arrays
+    without their tables plus the tables this worker has not returned
+    before."""
+    what, exact = args
+    if isinstance(what, list):
+        models = what
+    else:
+        factory, n, kw, a, b = what
+        models = factory(n, start=a, stop=b, **kw)
+    out, new = [], {}
+    for m in models:
+        a = build(m, exact)
+        key = None
+        if a.ncols:
+            key = _table_key(a)
+            if key not in _SENT_TABLES:
+                _SENT_TABLES.add(key)
+                new[key] = (a.tablist, a.xvals, a.yvals)
+            a.tablist = a.xvals = a.yvals = None
+        out.append((a, key))
+    return out, new
+
+
+def setup_workers(workers: Optional[int] = None) -> int:
+    """Processes build_many / build_generated use: ``workers``, else every
+    host core this process may run on."""
+    import os
+    if workers is not None:
+        return workers
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def _run_chunks(chunks, workers):
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    tables, out = {}, []
+    with ProcessPoolExecutor(min(workers, len(chunks)), mp_context=mp.get_context("spawn")) as pool:
+        # results arrive in chunk order, and a worker's chunks in increasing
+        # order, so a table is received before any solver that refers to it
+        for arrs, new in pool.map(_build_chunk, chunks):
+            for k, v in new.items():
+                tables.setdefault(k, v)
+            for a, key in arrs:
+                if key is not None:
+                    a.tablist, a.xvals, a.yvals = tables[key]
+                out.append(a)
+    return out
+
+
+def build_many(models, exact: bool = False, workers: Optional[int] = None, chunk: int = 2048):
+    """``build`` of every model, in order, on ``workers`` processes (default:
+    every host core). The reference sets up each hsolve on its own at RESET
+    (h_hh_chip_init, do_hget_children, h_funcs_init: hines_chip_init.c:465-
+    1260, hines_child.c:81-1549, hines_init.c:361-1273), one after another;
+    hsolves are independent, so they are set up here in chunks on a pool of
+    spawned processes. Solvers whose composite tables are equal share one
+    copy of them, as ``build`` does within one process. The arrays equal
+    ``build``'s exactly."""
+    models = list(models)
+    workers = setup_workers(workers)
+    if workers <= 1 or len(models) <= chunk:
+        return [build(m, exact) for m in models]
+    return _run_chunks([(models[i:i + chunk], exact) for i in range(0, len(models), chunk)], workers)
+
+
+def build_generated(factory, n: int, exact: bool = False, workers: Optional[int] = None, chunk: int = 512,
+                    **kw):
+    """``build_many(factory(n, **kw))`` for a generator whose models [a, b)
+    come from ``factory(n, start=a, stop=b, **kw)`` alone (configs.random_trees):
+    each worker generates its own chunks, so the models never cross a process
+    boundary, only the built arrays."""
+    workers = setup_workers(workers)
+    if workers <= 1 or n <= chunk:
+        return [build(m, exact) for m in factory(n, **kw)]
+    return _run_chunks([((factory, n, kw, a, min(a + chunk, n)), exact) for a in range(0, n, chunk)], workers)

@@ -123,3 +123,45 @@ def test_non_postorder_tree_falls_back(oracle, gpu_engine):
     np.testing.assert_array_equal(vm[0], ref.vm)
     np.testing.assert_array_equal(vm[32], ref.vm)
     eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_static_rows_follow_inputs_and_state_between_launches(oracle, gpu_engine, prec):
+    """Passive rows below every channel keep their diagonal terms in a launch
+    after its first step; inputs (the soma's and a dendrite's inject) and
+    state writes (a dendrite's Em/Rm term) between launches must reach them."""
+    hs = _trees(model.BEULER, seed=41)
+    p = gpu_engine.PREC_FP64 if prec == "fp64" else gpu_engine.PREC_MIXED
+    eng = gpu_engine.Engine(hs, precision=p, wide_min=-1, jit=False, steps_per_launch=20)
+    assert eng.stats().stack_tiles == eng.stats().tiles
+    rows = []
+    for i, h in enumerate(hs):
+        rows.append((i, int(h.compchips[h.ncompts - 1]) + 1))      # the soma's inject
+        rows.append((i, int(h.compchips[3]) + 1))                  # a dendrite's inject
+    eng.register_inputs(np.array([r[0] for r in rows], np.int32), np.array([r[1] for r in rows]))
+    refs = [oracle.Solver(h) for h in hs]
+    rng = np.random.default_rng(42)
+    worst = 0.0
+    for k in range(6):
+        v = rng.uniform(0.0, 1e-9, size=len(rows))
+        eng.set_inputs_async(v, 0)
+        for (i, c), x in zip(rows, v):
+            refs[i].chip[c] = x
+        if k == 3:                                  # a state write between launches
+            st = eng.get_state()
+            for i, h in enumerate(hs):
+                c = int(h.compchips[5])             # row 5's Em/Rm term
+                st["chip"][i][c] *= 1.25
+                refs[i].chip[c] = st["chip"][i][c]
+            eng.set_state(chip=st["chip"])
+        eng.run(20)
+        for r in refs:
+            r.run(20)
+        vm = eng.get_state()["vm"]
+        for i, r in enumerate(refs):
+            if prec == "fp64":
+                np.testing.assert_array_equal(vm[i], r.vm)
+            else:
+                worst = max(worst, float(np.max(np.abs(vm[i] - r.vm))))
+    assert worst <= 1e-9, worst
+    eng.close()
