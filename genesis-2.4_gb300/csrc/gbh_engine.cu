@@ -83,6 +83,7 @@ struct Launch {
     bool uniform = false; // every neuron of the type has the same tree
     bool wide = false;    // one neuron per block (wide tiles)
     bool stack = false;   // stack elimination (smax = shared doubles per lane)
+    bool split = false;   // stack: some tile's rows above its static ones go to a second warp
 };
 
 // Element idx of a block of rows starting at row `base`: lane-interleaved
@@ -394,7 +395,7 @@ constexpr int kSmemPerBlock = 96 * 1024;
 // interpreter's shared-memory columns (2 x compartments x 32 doubles a warp).
 constexpr int kStackMin = 32;
 // Shared memory a stack-elimination warp may take (doubles per lane).
-constexpr int kStackCapMax = 200 * 1024 / (LANES * (int)sizeof(double));
+constexpr int kStackCapMax = 200 * 1024 / (LANES * (int)sizeof(double)) - 2 * kSplitRows;
 
 // Composite tables on the device: FP64 copy (plus one padding row), axis
 // value pools and their geometry.
@@ -669,8 +670,8 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     for (size_t ti = 0; ti < e->types.size(); ++ti) {
         TileType &tt = e->types[ti];
         if (tt.wide || tt.sym || tt.nslots < kStackMin) continue;
-        int cap = 1;
-        bool ok = true;
+        int cap = 2;   // at least one stack entry: the sweeps read an entry whether or not they use it
+        bool ok = true, np1 = true;
         std::vector<int> fl;
         for (int i : members[ti]) {
             int c = 0;
@@ -679,10 +680,12 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
                 break;
             }
             cap = std::max(cap, c);
+            for (int f : fl) np1 = np1 && (f & FL_NPOP) <= 1;
         }
         if (ok && cap <= kStackCapMax) {
             tt.stack = 1;
             tt.scap = cap;
+            tt.np1 = np1;
             const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
             tt.nstatic = 0;
             while (tt.nstatic < tt.nslots && pf[6 * tt.nstatic + 2] >= 0) ++tt.nstatic;
@@ -1196,6 +1199,10 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             }
             Launch L{(int)t0, (int)t1, cap, 1};
             L.stack = true;
+            for (size_t u = t0; u < t1; ++u) {
+                const TileType &tt = e->types[e->tiles[u].type];
+                L.split = L.split || (tt.nstatic > 0 && tt.nslots - tt.nstatic <= kSplitRows);
+            }
             e->launches.push_back(L);
             t0 = t1;
             continue;
@@ -1295,8 +1302,8 @@ int launch_one(gbh_engine *e, const DevView &v, const Launch &L, int k, long lon
     }
     cudaError_t ce;
     if (L.stack)
-        ce = mixed ? launch_mixed_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, st)
-                   : launch_fp64_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, st);
+        ce = mixed ? launch_mixed_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, L.split, st)
+                   : launch_fp64_stack(v, L.tile0, L.tile1, L.smax, k, step, giv, L.split, st);
     else if (L.wide)
         ce = mixed ? launch_mixed_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st)
                    : launch_fp64_wide(v, L.tile0, L.tile1, L.smax, k, step, giv, st);

@@ -129,6 +129,8 @@ struct TileType {
     int nstatic;     // stack: rows [0, nstatic) are passive and so is every row below them in their
                      // trees (the first non-passive slot; post-order keeps subtrees below their roots):
                      // their diagonals, reciprocals and coupling factors are the same every step
+    int np1;         // stack: no row of any of its neurons has more than one stacked child (binary
+                     // trees): the forward sweep pops at most one entry per row, without a loop
 };
 
 // Per-row flags of the stack elimination (DevView::ltop, topo rows, one word
@@ -138,6 +140,10 @@ struct TileType {
 // in ascending row order). Backward, rows descending: the solution of the
 // row after is in a register; a row whose parent is further away reads the
 // parent's solution from a per-lane stack of branch points.
+// Rows above the static ones (TileType::nstatic) that a second warp of a
+// stack tile computes in shared memory while the first sweeps the static rows
+constexpr int kSplitRows = 8;
+
 enum StackFlag {
     FL_NPOP = 0xff,          // stack entries to apply: children other than the last
     FL_CARRY_IN = 1 << 8,    // the previous row is this row's last child

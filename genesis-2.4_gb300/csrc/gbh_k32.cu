@@ -17,9 +17,9 @@ cudaError_t launch_mixed_wide(const DevView &v, int tile0, int tile1, int smax, 
 }
 
 cudaError_t launch_mixed_stack(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step,
-                               bool giv, cudaStream_t st)
+                               bool giv, bool split, cudaStream_t st)
 {
-    return stack_launch_mixed(v, tile0, tile1, cap, nsteps, step, giv, st);
+    return stack_launch_mixed(v, tile0, tile1, cap, nsteps, step, giv, split, st);
 }
 
 cudaError_t launch_mixed_coop(const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st)

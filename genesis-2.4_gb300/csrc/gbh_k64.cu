@@ -17,9 +17,9 @@ cudaError_t launch_fp64_wide(const DevView &v, int tile0, int tile1, int smax, i
 }
 
 cudaError_t launch_fp64_stack(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step, bool giv,
-                              cudaStream_t st)
+                              bool split, cudaStream_t st)
 {
-    return stack_launch<double>(v, tile0, tile1, cap, nsteps, step, giv, st);
+    return stack_launch<double>(v, tile0, tile1, cap, nsteps, step, giv, split, st);
 }
 
 cudaError_t launch_fp64_coop(const DevView &v, int ntiles, int smax, int nsteps, long long step, cudaStream_t st)

@@ -422,22 +422,35 @@ k_steps_mixed(DevView v, int tile0, int tile1, int smax, int nsteps, long long s
 // Stack elimination of the mixed form (see k_stack in gbh_kernels.cuh): the
 // same row order and per-lane stacks; the diagonal's reciprocal is formed
 // once per row (rcp_newton) and kept in the column for back substitution.
-template <bool GIV>
-__global__ void __launch_bounds__(32, 16)
+//
+// SPLIT: two warps per tile. After a launch's first step the second warp
+// runs the channel phase of the rows above the static ones (kSplitRows at
+// most; the soma of a tree whose dendrites are passive) and the pool phase,
+// leaving each row's (R, D) in shared memory, while the first warp sweeps
+// the static rows; the first warp then finishes those rows' forward steps
+// and the back substitution. Both warps pass two barriers per step.
+template <bool GIV, bool SPLIT>
+__global__ void __launch_bounds__(SPLIT ? 64 : 32, SPLIT ? 8 : 16)
 k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
 {
     extern __shared__ double sm[];
-    const int lane = threadIdx.x;
+    __shared__ int sbad;
+    const int lane = threadIdx.x & (LANES - 1);
     const int t = tile0 + blockIdx.x;
     if (t >= tile1) return;
     {
         unsigned dsz;
         asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsz));
-        if (dsz < (unsigned)cap * LANES * sizeof(double)) {
-            if (v.status && lane == 0) atomicOr(v.status, ST_SMEM);
+        if (dsz < ((unsigned)cap + (SPLIT ? 2u * kSplitRows : 0u)) * LANES * sizeof(double)) {
+            if (v.status && threadIdx.x == 0) atomicOr(v.status, ST_SMEM);
             return;
         }
     }
+    if (SPLIT) {
+        if (threadIdx.x == 0) sbad = 0;
+        __syncthreads();
+    }
+    const int wid = SPLIT ? (int)(threadIdx.x >> 5) : 0;   // 0 sweeps, 1 computes the channel rows
     const long long sbase = v.step_dev ? *v.step_dev : 0;
     const Tile tl = v.tiles[t];
     const TileType ty = v.types[tl.type];
@@ -455,10 +468,12 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
     double2 *col = v.col + tl.topo * LANES + lane;
     double2 *kst = v.kst + tl.topo * LANES + lane;
     double *stk = sm + lane;
+    double *rdb = sm + cap * LANES + lane;  // SPLIT: (R, D) of the rows above the static ones
     const int S = ty.nslots;
     const int *pf = v.prog + ty.pf_off;   // per slot: field rows to prefetch; passive rows' fields
     const int nst = GIV ? 0 : ty.nstatic; // static rows (givals off: they would write Im)
     constexpr int kCh = 8;                // rows per chunk
+    const bool sp = SPLIT && nst > 0 && S - nst <= kSplitRows;
 
     ChanEnvDF E;
     E.tab = v.tabdf + tg.tab_off;
@@ -487,7 +502,46 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         // after a launch's first step the static rows' (rhs term, coupling
         // factor) are in kst (see k_stack)
         const bool fast = it > 0;
-        for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
+        const bool split = sp && fast;
+        bool bad = false;
+        if (SPLIT && wid == 1 && !split) goto step_end;   // the second warp works in split steps only
+        if (!split || wid == 1)
+            for (int k = 0; k < ty.nitot; ++k) NR.IT[k * LANES] = 0.0;   // hines_chip.c:134-136
+        if (SPLIT && wid == 1) {
+            // the rows above the static ones: channel phase into shared
+            // memory, then the pool phase (it reads Vm, fluxes and
+            // concentrations, never a row of the elimination)
+            ChanStateDF cs1;
+            chan_state_reset_df(cs1);
+            const int *pc1 = v.prog + ty.prog_off + 9 * nst;   // a passive row's program is 9 ints
+            for (int s = nst; s < S && !bad; ++s) {
+                double R, D;
+                if (!chan_compartment_df<GIV, LANES>(v, E, cs1, NR, pc1, Vw[s * LANES], step, R, D)) {
+                    bad = true;
+                } else {
+                    rdb[(2 * (s - nst)) * LANES] = R;
+                    rdb[(2 * (s - nst) + 1) * LANES] = D;
+                }
+            }
+            if (!bad) {
+                PoolLane PL;
+                PL.C = Cw;
+                PL.F = Fw;
+                PL.CR = v.CR ? v.CR + tl.pools * LANES + lane : nullptr;
+                PL.CD = NR.CD;
+                PL.S = v.S ? v.S + tl.scr * LANES + lane : nullptr;
+                PL.P = Pw;
+                PL.V = Vw;
+                PL.dt = v.dt;
+                PL.crank = ty.crank;
+                bad = !pool_phase<LANES>(v.prog + ty.pool_off, PL);
+            }
+            if (bad && v.status) atomicOr(v.status, ST_BAD_OP);
+            bar_named(1, 2 * LANES);   // (R, D) ready
+            goto step_end;
+        }
+        {
+        const int Send = split ? nst : S;   // the rows this warp sweeps before the barrier
         ChanStateDF cs;
         chan_state_reset_df(cs);
         const int *pc = v.prog + ty.prog_off;
@@ -534,16 +588,38 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             if (f & FL_CARRY_IN) R -= cr;
             reinterpret_cast<double *>(col + s * LANES)[0] = R;
             if (f & FL_PARENT) {
-                const double pd = (f & FL_PD) ? __ldg(&Bw[s * LANES]) * T : 0.0, pr = R * T;
+                // the diagonal contribution only for a parent above the static
+                // rows (a static parent never reads it)
+                const double pr = R * T;
                 if (f & FL_CARRY_OUT) {
-                    cd = pd;
                     cr = pr;
+                    if (f & FL_PD) cd = __ldg(&Bw[s * LANES]) * T;
                 } else {
-                    stk[(2 * top) * LANES] = pd;
+                    if (f & FL_PD) stk[(2 * top) * LANES] = __ldg(&Bw[s * LANES]) * T;
                     stk[(2 * top + 1) * LANES] = pr;
                     ++top;
                 }
             }
+        };
+        // fwd_static for types whose rows pop at most one stacked child: the
+        // same operations as selects and predicated stores instead of
+        // branches, so consecutive rows' independent work can overlap
+        auto fwd_static1 = [&](int s, double R, double T, int f) {
+            const bool pop = f & 1;
+            top -= pop ? 1 : 0;
+            const double sv = stk[(pop ? 2 * top + 1 : 1) * LANES];
+            R = pop ? R - sv : R;
+            R = (f & FL_CARRY_IN) ? R - cr : R;
+            reinterpret_cast<double *>(col + s * LANES)[0] = R;
+            const double pr = R * T;
+            if (f & FL_PD) {   // a parent above the static rows: its diagonal contribution
+                const double pd = __ldg(&Bw[s * LANES]) * T;
+                if (f & FL_CARRY_OUT) cd = pd;
+                else stk[(2 * top) * LANES] = pd;
+            }
+            cr = (f & FL_CARRY_OUT) ? pr : cr;
+            if (f & FL_PUSH) stk[(2 * top + 1) * LANES] = pr;
+            top += (f & FL_PUSH) ? 1 : 0;
         };
         // a passive row (M_BEGIN / M_END): its current term ichan * tbyc in
         // double-float, added to Vm in FP64 (part of the Vm update); the
@@ -554,13 +630,8 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             R = Vw[s * LANES] + K;
             D = df2d(ld_df(&Pw[ps[5] * LANES]));
         };
-        for (int s0 = 0; s0 < S; s0 += kCh) {
+        for (int s0 = 0; s0 < Send && !bad; s0 += kCh) {
             if (fast && s0 + kCh <= nst) {
-                for (int q = s0 + kCh; q < min(s0 + 2 * kCh, nst); ++q) {   // the next chunk's rows
-                    prefetch_l1(&Vw[q * LANES]);
-                    prefetch_l1(&lt[q * LANES]);
-                    prefetch_l1(&kst[q * LANES]);
-                }
                 double R[kCh], T[kCh];
                 int f[kCh];
 #pragma unroll
@@ -570,19 +641,24 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                     R[k] = Vw[(s0 + k) * LANES] + kt.x;
                     T[k] = kt.y;
                 }
+                if (ty.np1) {
 #pragma unroll
-                for (int k = 0; k < kCh; ++k) fwd_static(s0 + k, R[k], T[k], f[k]);
+                    for (int k = 0; k < kCh; ++k) fwd_static1(s0 + k, R[k], T[k], f[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kCh; ++k) fwd_static(s0 + k, R[k], T[k], f[k]);
+                }
                 pc += 9 * kCh;
                 continue;
             }
-            for (int q = s0 + kCh; q < min(s0 + 2 * kCh, S); ++q) {   // the next chunk's rows, into L1
+            for (int q = s0 + kCh; q < min(s0 + 2 * kCh, Send); ++q) {   // the next chunk's rows, into L1
                 for (int f = pf[6 * q]; f <= pf[6 * q + 1]; ++f) prefetch_l1(&Pw[f * LANES]);
                 prefetch_l1(&Vw[q * LANES]);
                 prefetch_l1(&lt[q * LANES]);
                 prefetch_l1(&Aw[q * LANES]);
                 prefetch_l1(&Bw[q * LANES]);
             }
-            bool all_passive = !GIV && s0 + kCh <= S;
+            bool all_passive = !GIV && s0 + kCh <= Send;
             for (int k = 0; k < kCh && all_passive; ++k) all_passive = pf[6 * (s0 + k) + 2] >= 0;
             if (all_passive) {
                 // every row's own terms first (independent of each other),
@@ -608,7 +684,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 pc += 9 * kCh;
                 continue;
             }
-            for (int s = s0; s < min(s0 + kCh, S); ++s) {
+            for (int s = s0; s < min(s0 + kCh, Send) && !bad; ++s) {
                 double R, D, K = 0.0;
                 const int *ps = pf + 6 * s;
                 if (fast && s < nst) {
@@ -622,12 +698,18 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                     pc += 9;
                 } else if (!chan_compartment_df<GIV, LANES>(v, E, cs, NR, pc, Vw[s * LANES], step, R, D)) {
                     if (v.status) atomicOr(v.status, ST_BAD_OP);
-                    return;
+                    bad = true;
+                    break;
                 }
                 fwd(s, R, D, __ldg(&lt[s * LANES]), __ldg(&Aw[s * LANES]), __ldg(&Bw[s * LANES]), K);
             }
         }
-        {
+        if (split) {
+            bar_named(1, 2 * LANES);   // the second warp's (R, D) of the rows above the static ones
+            for (int s = nst; s < S; ++s)
+                fwd(s, rdb[(2 * (s - nst)) * LANES], rdb[(2 * (s - nst) + 1) * LANES], __ldg(&lt[s * LANES]),
+                    __ldg(&Aw[s * LANES]), __ldg(&Bw[s * LANES]), 0.0);
+        } else if (!bad) {
             PoolLane PL;
             PL.C = Cw;
             PL.F = Fw;
@@ -640,33 +722,29 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             PL.crank = ty.crank;
             if (!pool_phase<LANES>(v.prog + ty.pool_off, PL)) {
                 if (v.status) atomicOr(v.status, ST_BAD_OP);
-                return;
+                bad = true;
             }
         }
+        if (!bad) {
         double xn = 0.0;
         top = 0;
         // back substitution of row s: its solution from the parent's (the row
         // after, or the branch point on the stack)
+        // (selects and predicated stack accesses instead of branches)
         auto bwd = [&](int s, int f, double2 rd, double c, double old) {
-            double r = rd.x;
-            if (f & FL_PARENT) {
-                const double xp = (f & FL_XLOAD) ? stk[(top - 1) * LANES] : xn;
-                if (f & FL_XPOP) --top;
-                r = fma(-c, xp, r);
-            }
+            const bool xl = f & FL_XLOAD;
+            const double sv = stk[(xl ? top - 1 : 0) * LANES];
+            const double xp = xl ? sv : xn;
+            top -= (f & FL_XPOP) ? 1 : 0;
+            double r = (f & FL_PARENT) ? fma(-c, xp, rd.x) : rd.x;
             r = r * rd.y;
-            if (f & FL_XPUSH) stk[(top++) * LANES] = r;
+            if (f & FL_XPUSH) stk[top * LANES] = r;
+            top += (f & FL_XPUSH) ? 1 : 0;
             xn = r;
             Vw[s * LANES] = ty.crank ? fma(2.0, r, -old) : r;
         };
         int s1 = S - 1;
         for (; s1 + 1 >= kCh; s1 -= kCh) {   // chunks: every row's loads, then the chain
-            for (int q = s1 - kCh; q > s1 - 2 * kCh && q >= 0; --q) {
-                prefetch_l1(&lt[q * LANES]);
-                prefetch_l1(&col[q * LANES]);
-                prefetch_l1(&Cbw[q * LANES]);
-                if (ty.crank) prefetch_l1(&Vw[q * LANES]);
-            }
             int f[kCh];
             double2 rd[kCh];
             double c[kCh], old[kCh];
@@ -685,19 +763,30 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             bwd(s1, __ldg(&lt[s1 * LANES]), col[s1 * LANES], __ldg(&Cbw[s1 * LANES]),
                 ty.crank ? Vw[s1 * LANES] : 0.0);
         finite_check(v, xn, active);   // row 0's solution
+        }
+        }
+    step_end:
+        if (SPLIT) {
+            if (bad) sbad = 1;
+            bar_named(2, 2 * LANES);   // the step's Vm is written before the next step reads it
+            if (sbad) return;
+        } else if (bad) {
+            return;
+        }
     }
 }
 
 inline cudaError_t stack_launch_mixed(const DevView &v, int tile0, int tile1, int cap, int nsteps, long long step,
-                                      bool giv, cudaStream_t st)
+                                      bool giv, bool split, cudaStream_t st)
 {
-    const size_t smem = (size_t)cap * LANES * sizeof(double);
-    auto fn = giv ? k_stack_mixed<true> : k_stack_mixed<false>;
+    split = split && !giv;
+    const size_t smem = ((size_t)cap + (split ? 2 * kSplitRows : 0)) * LANES * sizeof(double);
+    auto fn = giv ? k_stack_mixed<true, false> : split ? k_stack_mixed<false, true> : k_stack_mixed<false, false>;
     if (smem > 48 * 1024) {
         const cudaError_t ce = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (ce != cudaSuccess) return ce;
     }
-    fn<<<tile1 - tile0, LANES, smem, st>>>(v, tile0, tile1, cap, nsteps, step);
+    fn<<<tile1 - tile0, split ? 2 * LANES : LANES, smem, st>>>(v, tile0, tile1, cap, nsteps, step);
     return cudaGetLastError();
 }
 
