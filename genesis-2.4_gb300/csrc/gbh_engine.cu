@@ -2266,9 +2266,15 @@ gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, con
 // interpreted (the specialised kernels serve the small types the same way
 // under every candidate) at 16 steps per launch, times 32 steps after 16;
 // the fastest candidate is kept. Returns the chosen wide_min.
+// Also decides, when the kernel forms are autotuned (jit 0), whether the
+// specialised kernels pay on this batch: they run beside the stack or wide
+// launches and can slow the longest of them down (50,000 random trees: the
+// 24 specialised kernels of the small neurons made the step 15-30 % slower).
+// `no_jit` is set when the chosen mapping ran faster interpreted.
 int choose_mapping(gbh_engine *e, const gbh_batch_desc *desc, const gbh_synapses *syn,
-                   const gbh_remote_synapses *remote)
+                   const gbh_remote_synapses *remote, bool &no_jit)
 {
+    no_jit = false;
     int maxrows = 0;
     for (const Neuron &N : e->dec.neurons) maxrows = std::max(maxrows, N.nrows);
     std::vector<int> cand;
@@ -2278,10 +2284,11 @@ int choose_mapping(gbh_engine *e, const gbh_batch_desc *desc, const gbh_synapses
     cand.push_back(-1);
     int best = cand[0];
     double best_ms = 1e300;
-    for (int w : cand) {
+    // one trial: 32 steps after 16 on an engine built with the mapping w
+    auto trial = [&](int w, int jit) {
         gbh_options o = e->opt;
         o.wide_min = w;
-        o.jit = -1;
+        o.jit = jit;
         o.steps_per_launch = 16;
         o.use_graph = 0;
         gbh_error te{};
@@ -2292,21 +2299,27 @@ int choose_mapping(gbh_engine *e, const gbh_batch_desc *desc, const gbh_synapses
             if (made) gbh_destroy(made);
             t = nullptr;
         }
-        if (!t) continue;   // a candidate that cannot be built is not chosen
+        if (!t) return 1e300;   // a candidate that cannot be built is not chosen
         double ms = 1e300;
         if (gbh_run(t, 16) == GBH_OK) {
             const double ms0 = t->stats.device_ms;
             if (gbh_run(t, 32) == GBH_OK) ms = t->stats.device_ms - ms0;
         }
         if (getenv("GBH_VERBOSE"))
-            fprintf(stderr, "gbhsolve: mapping trial wide_min %d: %.2f us/step (%lld wide, %lld stack tiles)\n", w,
-                    ms / 32 * 1e3, (long long)t->stats.wide_tiles, (long long)t->stats.stack_tiles);
+            fprintf(stderr, "gbhsolve: mapping trial wide_min %d%s: %.2f us/step (%lld wide, %lld stack tiles)\n", w,
+                    jit < 0 ? "" : " specialised", ms / 32 * 1e3, (long long)t->stats.wide_tiles,
+                    (long long)t->stats.stack_tiles);
+        gbh_destroy(t);
+        return ms;
+    };
+    for (int w : cand) {
+        const double ms = trial(w, -1);
         if (ms < best_ms) {
             best_ms = ms;
             best = w;
         }
-        gbh_destroy(t);
     }
+    if (e->opt.jit == 0 && best_ms < 1e300) no_jit = trial(best, 0) > best_ms;
     return best;
 }
 
@@ -2336,7 +2349,11 @@ gbh_engine *create_dist(const gbh_batch_desc *desc, const gbh_synapses *syn, con
         delete e;
         return nullptr;
     }
-    if (!pre && e->opt.wide_min == 0) e->opt.wide_min = choose_mapping(e, desc, syn, remote);
+    if (!pre && e->opt.wide_min == 0) {
+        bool no_jit = false;
+        e->opt.wide_min = choose_mapping(e, desc, syn, remote, no_jit);
+        if (no_jit) e->opt.jit = -1;
+    }
     // keep the reference layout for state sync
     const int ns = desc->nsolvers;
     e->chip_start.assign(desc->chip_start, desc->chip_start + ns + 1);

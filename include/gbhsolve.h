@@ -179,7 +179,10 @@ typedef struct gbh_options {
                             lane, with the stack elimination. 0 = chosen by
                             trial at creation (candidates 32, 64, 128, never:
                             an interpreted engine per candidate times a few
-                            steps); < 0 = never (gbh_loss_gradient needs it) */
+                            steps; with jit 0 the chosen mapping is also timed
+                            specialised, and specialisation is turned off
+                            when it is slower); < 0 = never
+                            (gbh_loss_gradient needs it)                      */
 } gbh_options;
 
 typedef struct gbh_stats {
