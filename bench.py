@@ -452,9 +452,25 @@ def run_reference(args, ws, rank, dist):
                                    % (cores, per, nst)},
         "e2e": {"value": value, "unit": "compartment-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_cuda_backend": reference_cuda_backend(),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_cuda_backend():
+    """The reference's own GPU arm on the cables workload of 1,000 x 16
+    compartments (oracle/ref_cuda.py, its own process); beside the CPU arm,
+    not the headline."""
+    try:
+        r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "ref_cuda.py")], capture_output=True,
+                           text=True, timeout=900)
+        lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+        if not lines:
+            return {"unavailable": "no result (exit %d): %s" % (r.returncode, r.stderr.strip()[-300:])}
+        return json.loads(lines[-1])
+    except Exception as ex:  # noqa: BLE001 -- recorded in the line, never fatal to the arm
+        return {"unavailable": "%s: %s" % (type(ex).__name__, ex)}
 
 
 def main():
