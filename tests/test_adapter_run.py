@@ -111,3 +111,72 @@ def test_adapter_batch_equals_reference_step_code(tmp_path, oracle, gpu_engine):
     finally:
         arr = (C.c_void_p * len(ptrs))(*ptrs)
         host.ah_destroy_all(arr, len(ptrs))
+
+
+def _save2(s):
+    """The SAVE2 image of a solver (hines.c:553-558): n = nchips + ncompts +
+    nconcs as an int, then chip[], vm[], conc[] as doubles."""
+    nconc = s.s.nconcs
+    n = len(s.chip) + len(s.vm) + nconc
+    return (np.array([n], dtype=np.int32).tobytes() + s.chip.tobytes() + s.vm.tobytes() +
+            s.conc[:nconc].tobytes())
+
+
+def _restore2(s, image):
+    """RESTORE2 (hines.c:560-571) into the solver's arrays."""
+    nconc = s.s.nconcs
+    n = int(np.frombuffer(image[:4], dtype=np.int32)[0])
+    assert n == len(s.chip) + len(s.vm) + nconc
+    d = np.frombuffer(image[4:], dtype=np.float64)
+    s.chip[:] = d[:len(s.chip)]
+    s.vm[:] = d[len(s.chip):len(s.chip) + len(s.vm)]
+    s.conc[:nconc] = d[len(s.chip) + len(s.vm):]
+
+
+@pytest.mark.gpu
+def test_adapter_save2_restore2(tmp_path, oracle, gpu_engine):
+    """SAVE2 after gbh_sync_chip writes the same bytes as the reference's own
+    step code after the same steps; a RESTORE2 image (taken from the
+    reference run 60 steps earlier) pushed into the running batch with
+    gbh_push_state continues exactly as the reference continues from it."""
+    host = _host_lib(tmp_path)
+    n, dt = 12, None
+    hs = [model.build(m) for m in configs.random_trees(n, size_range=(8, 48), seed=35)]
+    mine = [oracle.Solver(h, i) for i, h in enumerate(hs)]
+    ref = [oracle.Solver(h, i) for i, h in enumerate(hs)]
+    zero = np.zeros(1, dtype=np.int32)
+    nov = np.zeros(1)
+    ptrs = []
+    try:
+        for i, s in enumerate(mine):
+            h = hs[i]
+            ncov = len(h.diff["covals0"]) if getattr(h, "diff", None) is not None and len(h.diff["nshells"]) else 0
+            ptrs.append(host.ah_create(C.addressof(s.s), b"/c%d" % i, len(s.stablist), ncov, 0, zero.ctypes.data,
+                                       nov.ctypes.data, 0))
+        for p in ptrs:
+            assert host.ah_init(p) == 0
+        dt = hs[0].dt
+        saved = None
+        for step in range(200):
+            for p in ptrs:
+                assert host.ah_process(p, step * dt) == 1
+            for o in ref:
+                o.run(1, "reference")
+            if step == 59:
+                saved = [_save2(o) for o in ref]          # the reference's SAVE2 at step 60
+            if step == 119:
+                for p in ptrs:
+                    host.ah_sync(p)                       # SAVE2 reads the host arrays
+                for s, o in zip(mine, ref):
+                    assert _save2(s) == _save2(o)
+                for i, (s, o) in enumerate(zip(mine, ref)):
+                    _restore2(s, saved[i])                # RESTORE2 of the step-60 image into both
+                    _restore2(o, saved[i])
+                    assert host.ah_push(ptrs[i]) == 0
+        for p in ptrs:
+            host.ah_sync(p)
+        for s, o in zip(mine, ref):
+            assert _save2(s) == _save2(o)
+    finally:
+        arr = (C.c_void_p * len(ptrs))(*ptrs)
+        host.ah_destroy_all(arr, len(ptrs))
