@@ -561,6 +561,36 @@ bool stack_plan(const std::vector<int> &parent, std::vector<int> &flags, int &ca
     return true;
 }
 
+// The stack entry of every row (TileType::slots), from its flags: forward,
+// the depth after its pops; backward, the entry it reads its parent's
+// solution from and the one it writes its own to. False when one is 32 or
+// more. `fdepth`: the largest forward entry index used.
+bool stack_slots(const std::vector<int> &flags, std::vector<int> &packed, int &fdepth)
+{
+    const int S = (int)flags.size();
+    packed.assign(S, 0);
+    fdepth = 0;
+    int top = 0;
+    for (int s = 0; s < S; ++s) {
+        const int f = flags[s];
+        top -= f & FL_NPOP;
+        if (top < 0 || top > 31) return false;
+        packed[s] |= top << FL_SLOT_F;
+        fdepth = std::max(fdepth, top);
+        if (f & FL_PUSH) ++top;
+    }
+    top = 0;
+    for (int s = S - 1; s >= 0; --s) {
+        const int f = flags[s];
+        const int rb = (f & FL_XLOAD) ? top - 1 : 0;
+        if (f & FL_XPOP) --top;
+        if (rb < 0 || rb > 31 || top < 0 || top > 31) return false;
+        packed[s] |= rb << FL_SLOT_R | top << FL_SLOT_W;
+        if (f & FL_XPUSH) ++top;
+    }
+    return true;
+}
+
 // Elimination schedule of one wide neuron (see k_wide): forward levels by
 // height (leaves 0), children of each row in ascending order, backward
 // levels by depth (root 0).
@@ -671,21 +701,25 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
         TileType &tt = e->types[ti];
         if (tt.wide || tt.sym || tt.nslots < kStackMin) continue;
         int cap = 2;   // at least one stack entry: the sweeps read an entry whether or not they use it
-        bool ok = true, np1 = true;
-        std::vector<int> fl;
+        bool ok = true, np1 = true, slots = true;
+        std::vector<int> fl, sl;
         for (int i : members[ti]) {
-            int c = 0;
+            int c = 0, fdepth = 0;
             if (!stack_plan(dec.neurons[i].parent, fl, c)) {
                 ok = false;
                 break;
             }
             cap = std::max(cap, c);
             for (int f : fl) np1 = np1 && (f & FL_NPOP) <= 1;
+            // the forward sweep reads its row's entry whether or not it pops
+            if (slots && stack_slots(fl, sl, fdepth)) cap = std::max(cap, 2 * fdepth + 2);
+            else slots = false;
         }
         if (ok && cap <= kStackCapMax) {
             tt.stack = 1;
             tt.scap = cap;
             tt.np1 = np1;
+            tt.slots = np1 && slots;
             const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
             tt.nstatic = 0;
             while (tt.nstatic < tt.nslots && pf[6 * tt.nstatic + 2] >= 0) ++tt.nstatic;
@@ -794,8 +828,11 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             int cap = 0;
             stack_plan(N.parent, fl, cap);
             const int nst = e->types[t.type].nstatic;
+            std::vector<int> sl(N.nrows, 0);
+            int fdepth = 0;
+            if (e->types[t.type].slots) stack_slots(fl, sl, fdepth);
             for (int s = 0; s < N.nrows; ++s)
-                LT[at(t.topo, s, l, false)] = fl[s] | (s < nst && N.parent[s] >= nst ? FL_PD : 0);
+                LT[at(t.topo, s, l, false)] = fl[s] | sl[s] | (s < nst && N.parent[s] >= nst ? FL_PD : 0);
         }
         for (size_t f = 0; f < N.fsrc.size(); ++f) P[at(t.fld, f, l, w)] = N.fval[f];
         for (size_t k = 0; k < N.rav.size(); ++k) RV[at(t.rav, k, l, w)] = N.rav[k];

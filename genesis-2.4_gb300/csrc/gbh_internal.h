@@ -131,6 +131,8 @@ struct TileType {
                      // their diagonals, reciprocals and coupling factors are the same every step
     int np1;         // stack: no row of any of its neurons has more than one stacked child (binary
                      // trees): the forward sweep pops at most one entry per row, without a loop
+    int slots;       // stack, np1: every row's stack entries are below 32 and packed in its flags
+                     // (FL_SLOT_*), so the sweeps index the stack without a running top
 };
 
 // Per-row flags of the stack elimination (DevView::ltop, topo rows, one word
@@ -156,6 +158,11 @@ enum StackFlag {
     FL_PD = 1 << 15          // a row below nstatic whose parent is at or above it: the parent's
                              // forward step needs this row's diagonal contribution
 };
+// TileType::slots: bits 16-20 the forward entry (the stack depth after the
+// row's pops: its stacked child is read there and its own contribution
+// written there), 21-25 the backward entry its parent's solution is read
+// from, 26-30 the backward entry its own solution is written to.
+constexpr int FL_SLOT_F = 16, FL_SLOT_R = 21, FL_SLOT_W = 26;
 
 struct Tile {
     int type;

@@ -553,6 +553,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         // a static row also keeps its rhs term K and its factor a / D
         auto fwd = [&](int s, double R, double D, int f, double a, double bb, double K) {
             const int np = f & FL_NPOP;
+            if (ty.slots) top = ((f >> FL_SLOT_F) & 31) + np;   // the static rows keep no running top
             top -= np;
             for (int j = 0; j < np; ++j) {
                 D -= stk[(2 * (top + j)) * LANES];
@@ -621,6 +622,29 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             if (f & FL_PUSH) stk[(2 * top + 1) * LANES] = pr;
             top += (f & FL_PUSH) ? 1 : 0;
         };
+        // fwd_static1 for TileType::slots: the row's stack entry comes with
+        // its flags, so no running top is kept
+        auto fwd_static2 = [&](int s, double R, double T, int f) {
+            const int sl = (f >> FL_SLOT_F) & 31;
+            const double sv = stk[(2 * sl + 1) * LANES];
+            R = (f & 1) ? R - sv : R;
+            R = (f & FL_CARRY_IN) ? R - cr : R;
+            reinterpret_cast<double *>(col + s * LANES)[0] = R;
+            const double pr = R * T;
+            if (f & FL_PD) {   // a parent above the static rows: its diagonal contribution
+                const double pd = __ldg(&Bw[s * LANES]) * T;
+                if (f & FL_CARRY_OUT) cd = pd;
+                else stk[(2 * sl) * LANES] = pd;
+            }
+            cr = (f & FL_CARRY_OUT) ? pr : cr;
+            if (f & FL_PUSH) stk[(2 * sl + 1) * LANES] = pr;
+        };
+        // a static row on a launch's later step, in the form its type allows
+        auto fwd_fast = [&](int s, double R, double T, int f) {
+            if (ty.slots) fwd_static2(s, R, T, f);
+            else if (ty.np1) fwd_static1(s, R, T, f);
+            else fwd_static(s, R, T, f);
+        };
         // a passive row (M_BEGIN / M_END): its current term ichan * tbyc in
         // double-float, added to Vm in FP64 (part of the Vm update); the
         // diagonal is the row's diagonal term (its conductance sum is zero)
@@ -641,7 +665,10 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                     R[k] = Vw[(s0 + k) * LANES] + kt.x;
                     T[k] = kt.y;
                 }
-                if (ty.np1) {
+                if (ty.slots) {
+#pragma unroll
+                    for (int k = 0; k < kCh; ++k) fwd_static2(s0 + k, R[k], T[k], f[k]);
+                } else if (ty.np1) {
 #pragma unroll
                     for (int k = 0; k < kCh; ++k) fwd_static1(s0 + k, R[k], T[k], f[k]);
                 } else {
@@ -676,7 +703,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 for (int k = 0; k < kCh; ++k) {
                     const int s = s0 + k;
                     if (fast && s < nst) {
-                        fwd_static(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
+                        fwd_fast(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
                     } else {
                         fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
                     }
@@ -689,7 +716,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 const int *ps = pf + 6 * s;
                 if (fast && s < nst) {
                     const double2 kt = kst[s * LANES];
-                    fwd_static(s, Vw[s * LANES] + kt.x, kt.y, __ldg(&lt[s * LANES]));
+                    fwd_fast(s, Vw[s * LANES] + kt.x, kt.y, __ldg(&lt[s * LANES]));
                     pc += 9;
                     continue;
                 }
@@ -731,15 +758,17 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         // back substitution of row s: its solution from the parent's (the row
         // after, or the branch point on the stack)
         // (selects and predicated stack accesses instead of branches)
+        // (TileType::slots: the stack entries come with the flags)
         auto bwd = [&](int s, int f, double2 rd, double c, double old) {
             const bool xl = f & FL_XLOAD;
-            const double sv = stk[(xl ? top - 1 : 0) * LANES];
+            const int rs = ty.slots ? (f >> FL_SLOT_R) & 31 : (xl ? top - 1 : 0);
+            const double sv = stk[rs * LANES];
             const double xp = xl ? sv : xn;
-            top -= (f & FL_XPOP) ? 1 : 0;
+            if (!ty.slots) top -= (f & FL_XPOP) ? 1 : 0;
             double r = (f & FL_PARENT) ? fma(-c, xp, rd.x) : rd.x;
             r = r * rd.y;
-            if (f & FL_XPUSH) stk[top * LANES] = r;
-            top += (f & FL_XPUSH) ? 1 : 0;
+            if (f & FL_XPUSH) stk[(ty.slots ? (f >> FL_SLOT_W) & 31 : top) * LANES] = r;
+            if (!ty.slots) top += (f & FL_XPUSH) ? 1 : 0;
             xn = r;
             Vw[s * LANES] = ty.crank ? fma(2.0, r, -old) : r;
         };

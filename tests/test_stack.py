@@ -165,3 +165,34 @@ def test_static_rows_follow_inputs_and_state_between_launches(oracle, gpu_engine
                 worst = max(worst, float(np.max(np.abs(vm[i] - r.vm))))
     assert worst <= 1e-9, worst
     eng.close()
+
+
+def _three_child_trees(n, size, seed):
+    """Random trees whose root gets a third child (a subtree moved under it),
+    so the forward sweep pops two stacked children at one row."""
+    ms = configs.random_trees(n, size_range=(size, size), seed=seed)
+    for m in ms:
+        comps = m.compartments
+        k = next(i for i in range(len(comps) - 1, 0, -1) if comps[i].parent not in (-1, 0))
+        comps[k].parent = 0
+    return [model.build(m) for m in ms]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_stack_rows_with_three_children(oracle, gpu_engine, prec):
+    """A type whose rows pop more than one stacked child takes the general
+    forward sweep (a loop over the popped entries, a running stack top) on
+    every step, including the static rows' rhs-only steps."""
+    hs = _three_child_trees(40, 64, seed=51)
+    p = gpu_engine.PREC_FP64 if prec == "fp64" else gpu_engine.PREC_MIXED
+    eng = gpu_engine.Engine(hs, precision=p, wide_min=-1, jit=False, steps_per_launch=25)
+    assert eng.stats().stack_tiles == eng.stats().tiles
+    eng.run(100)
+    vm = eng.get_state()["vm"]
+    for i in range(0, len(hs), 3):
+        ref = _oracle_run(oracle, hs[i], 100)
+        if prec == "fp64":
+            np.testing.assert_array_equal(vm[i], ref.vm)
+        else:
+            assert float(np.max(np.abs(vm[i] - ref.vm))) <= 1e-9
+    eng.close()
