@@ -79,6 +79,11 @@ struct DevView {
     const int *ltop;
     double2 *col;
     double2 *kst;
+    // stack tiles' kept factors: the fields' generation (bumped by state
+    // writes) and, per tile, the generation its kst / col were kept at
+    const unsigned *sgen;
+    unsigned *tgen;
+    const int *kref;  // nonzero: an input writes a static row's Em/Rm, inject or dt/Cm
     // synapses of weighted synchans (SynW): per synapse its bit's word for
     // slot 0 (-1 for a synchan of one weight) and bit | nwords << 5
     const int64_t *syn_out_mword;

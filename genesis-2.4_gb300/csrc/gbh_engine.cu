@@ -130,6 +130,12 @@ struct gbh_engine {
     DBuf<int> d_ltop;              // stack elimination: per-row flags (topo rows)
     DBuf<double2> d_col;           // stack elimination: (rhs, diagonal) per row
     DBuf<double2> d_kst;           // stack elimination: static rows' (rhs term, coupling factor)
+    DBuf<unsigned> d_sgen, d_tgen; // stack elimination: the fields' generation; each tile's kept one
+    unsigned sgen_host = 1;
+    std::vector<std::vector<char>> stack_dfield;   // per type: field rows that are a static row's diagonal term
+    std::vector<std::vector<char>> stack_kfield;   // per type: field rows of a static row's rhs term
+    bool stack_input_d = false;    // an input writes such a field: every launch redoes the kept factors
+    DBuf<int> d_kref;              // an input writes a static row's rhs fields: launches refresh them
     DBuf<unsigned> d_ring;
     DBuf<int64_t> d_out_start, d_out_base;
     DBuf<int> d_out_delay;
@@ -725,6 +731,15 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
             const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
             tt.nstatic = 0;
             while (tt.nstatic < tt.nslots && pf[6 * tt.nstatic + 2] >= 0) ++tt.nstatic;
+            e->stack_dfield.resize(e->types.size());
+            e->stack_kfield.resize(e->types.size());
+            e->stack_dfield[ti].assign(tt.nfields, 0);
+            e->stack_kfield[ti].assign(tt.nfields, 0);
+            for (int q = 0; q < tt.nstatic; ++q) {
+                if (pf[6 * q + 5] >= 0 && pf[6 * q + 5] < tt.nfields) e->stack_dfield[ti][pf[6 * q + 5]] = 1;
+                for (int c = 2; c <= 4; ++c)   // Em/Rm, inject, dt/Cm
+                    if (pf[6 * q + c] >= 0 && pf[6 * q + c] < tt.nfields) e->stack_kfield[ti][pf[6 * q + c]] = 1;
+            }
             tt.pf_off = (int)prog_pool.size();
             prog_pool.insert(prog_pool.end(), pf.begin(), pf.end());
         }
@@ -1094,7 +1109,12 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_I.upload(I);
     rc |= e->d_par.upload(par);
     rc |= e->d_ltop.upload(LT);
-    if (any_stack) rc |= e->d_col.alloc(e->rows_topo * L) | e->d_kst.alloc(e->rows_topo * L);
+    if (any_stack) {
+        rc |= e->d_col.alloc(e->rows_topo * L) | e->d_kst.alloc(e->rows_topo * L);
+        rc |= e->d_sgen.upload(std::vector<unsigned>(1, e->sgen_host));
+        rc |= e->d_tgen.upload(std::vector<unsigned>(std::max<size_t>(e->tiles.size(), 1), 0u));
+        rc |= e->d_kref.upload(std::vector<int>(1, 0));
+    }
     rc |= e->d_giv.upload(std::vector<double>(e->rows_giv * L, 0.0));
     rc |= e->d_stab.upload(stab);
     rc |= e->d_ring.upload(std::vector<unsigned>(e->rows_syn * L, 0u));
@@ -1300,6 +1320,9 @@ DevView view_of(gbh_engine *e)
     v.ltop = e->d_ltop.p;
     v.col = e->d_col.p;
     v.kst = e->d_kst.p;
+    v.sgen = e->d_sgen.p;
+    v.tgen = e->d_tgen.p;
+    v.kref = e->d_kref.p;
     v.A = e->d_A.p;
     v.B = e->d_B.p;
     v.Cb = e->d_Cb.p;
@@ -1506,8 +1529,24 @@ int run_coop(gbh_engine *e, int nsteps, cudaStream_t st)
     return GBH_OK;
 }
 
+__global__ void k_bump(unsigned *g) { *g += 1u; }
+
+// The stack tiles' kept factors are redone at their next launch (a field
+// they come from may have changed).
+int stack_invalidate(gbh_engine *e, cudaStream_t st)
+{
+    if (!e->d_sgen.p) return GBH_OK;
+    k_bump<<<1, 1, 0, st>>>(e->d_sgen.p);
+    CK(cudaGetLastError());
+    return GBH_OK;
+}
+
 int run_steps(gbh_engine *e, int nsteps, cudaStream_t st)
 {
+    if (e->stack_input_d) {   // inputs write a static row's diagonal term
+        const int rci = stack_invalidate(e, st);
+        if (rci) return rci;
+    }
     if (e->net_coop && !e->givals_enabled && e->nremote == 0) {
         e->dstep_valid = false;
         return run_coop(e, nsteps, st);
@@ -1838,6 +1877,7 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
         if (k == GBH_IN_FLUX) want_conc[e->conc_start[solver[i]] + index[i]].push_back(i);
         else want_chip[e->chip_start[solver[i]] + index[i]].push_back(i);
     }
+    bool kfield_input = false;   // an input writes a static row's rhs fields
     for (size_t q = 0; q < e->dec.neurons.size(); ++q) {
         const Neuron &N = e->dec.neurons[q];
         const Tile &t = e->tiles[e->neuron_tile[q]];
@@ -1847,6 +1887,12 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
             auto it = want_chip.find(e->chip_start[N.solver] + N.fsrc[f].idx);
             if (it == want_chip.end()) continue;
             const bool packed = !e->type_df[t.type].empty() && e->type_df[t.type][f];
+            if ((size_t)t.type < e->stack_dfield.size() && !e->stack_dfield[t.type].empty() &&
+                e->stack_dfield[t.type][f])
+                e->stack_input_d = true;
+            if ((size_t)t.type < e->stack_kfield.size() && !e->stack_kfield[t.type].empty() &&
+                e->stack_kfield[t.type][f])
+                kfield_input = true;
             for (int i : it->second) {
                 const bool add = kind && kind[i] == GBH_IN_ADD;
                 addrs[i].push_back(at(t.fld, (int64_t)f, l, e->types[t.type].wide != 0) |
@@ -1859,6 +1905,11 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
             for (int i : it->second)
                 addrs[i].push_back(at(t.pools, (int64_t)p, l, e->types[t.type].wide != 0) | kFluxFlag);
         }
+    }
+    if (kfield_input && e->d_kref.p) {   // the stack tiles then refresh those terms at every launch
+        const int one = 1;
+        CK(cudaStreamSynchronize(e->stream));
+        CK(cudaMemcpy(e->d_kref.p, &one, sizeof(int), cudaMemcpyHostToDevice));
     }
     std::map<int64_t, std::vector<int>> by_target;   // keyed by address without the add flag
     std::map<int64_t, int64_t> flags;
@@ -2595,6 +2646,11 @@ int gbh_set_state(gbh_engine *e, const double *vm, const double *chip, const dou
     if (!V.empty()) CK(cudaMemcpy(e->d_V.p, V.data(), V.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (!P.empty()) CK(cudaMemcpy(e->d_P.p, P.data(), P.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (!C.empty()) CK(cudaMemcpy(e->d_C.p, C.data(), C.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (chip) {   // the stack tiles' kept factors come from chip fields
+        const int rci = stack_invalidate(e, e->stream);
+        if (rci) return rci;
+        CK(cudaStreamSynchronize(e->stream));
+    }
     return GBH_OK;
 }
 
@@ -2958,6 +3014,9 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         }
         return GBH_OK;
     };
+    // the work copies' stack tiles keep their own factors (the engine's state
+    // is restored afterwards; its tiles redo theirs at their next launch)
+    if (stack_invalidate(e, st)) return GBH_ERR_CUDA;
     auto forward = [&](int n) { return issue_steps(e, fv, n, 0, false, st, nullptr); };
     // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed)
     CK(cudaEventRecord(e->ev0, st));
@@ -3079,7 +3138,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_kst.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_kst.release(); e->d_sgen.release(); e->d_tgen.release(); e->d_kref.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

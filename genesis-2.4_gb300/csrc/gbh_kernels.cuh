@@ -538,6 +538,13 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     const int nst = GIV ? 0 : ty.nstatic; // static rows (givals off: they would write Im)
     constexpr int kCh = 8;                // rows per chunk
     const bool sp = SPLIT && nst > 0 && S - nst <= kSplitRows;
+    // The static rows' kept factors outlive a launch: they are redone (a
+    // full first step) only when the fields they come from may have changed
+    // since this tile last kept them (a state write bumps *v.sgen); else the
+    // first step only refreshes the rhs terms (inputs may set an inject).
+    const unsigned sgen = nst > 0 ? *v.sgen : 0u;
+    const bool full = nst > 0 && v.tgen[t] != sgen;
+    const bool kref = nst > 0 && *v.kref != 0;   // an input writes a static row's rhs fields
 
     ChanEnv<G> E;
     E.tab = tab_ptr<G>(v, tg.tab_off);
@@ -566,7 +573,8 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         // factor) are in kst: their diagonals do not change within a launch
         // (nothing but channels changes a diagonal; inputs and state writes
         // come between launches), so they skip the diagonal's elimination
-        const bool fast = it > 0;
+        const bool fast = it > 0 || !full;
+        const bool refresh = it == 0 && kref;   // (fast) the rhs terms from the fields
         const bool split = sp && fast;
         bool bad = false;
         if (SPLIT && wid == 1 && !split) goto step_end;   // the second warp works in split steps only
@@ -712,6 +720,14 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
             else if (ty.np1) fwd_static1(s, R, T, f);
             else fwd_static(s, R, T, f);
         };
+        // a static row's rhs term from its fields (as `passive` forms it), kept
+        auto kterm = [&](int s) {
+            const int *ps = pf + 6 * s;
+            const double ichan = Pw[ps[2] * LANES] + Pw[ps[3] * LANES];
+            const double K = ichan * Pw[ps[4] * LANES];
+            kst[s * LANES].x = K;
+            return K;
+        };
         // the interpreter's M_BEGIN / M_END arithmetic of a passive row; K
         // is the rhs term ichan * tbyc
         auto passive = [&](int s, const int *ps, double &R, double &D, double &K) {
@@ -731,7 +747,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 for (int k = 0; k < kCh; ++k) {
                     const double2 kt = kst[(s0 + k) * LANES];
                     f[k] = lt[(s0 + k) * LANES];
-                    R[k] = Vw[(s0 + k) * LANES] + kt.x;
+                    R[k] = Vw[(s0 + k) * LANES] + (refresh ? kterm(s0 + k) : kt.x);
                     T[k] = kt.y;
                 }
                 if (ty.slots) {
@@ -772,7 +788,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 for (int k = 0; k < kCh; ++k) {
                     const int s = s0 + k;
                     if (fast && s < nst) {
-                        fwd_fast(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
+                        fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kst[s * LANES].x), kst[s * LANES].y, f[k]);
                     } else {
                         fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
                     }
@@ -785,7 +801,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 const int *ps = pf + 6 * s;
                 if (fast && s < nst) {
                     const double2 kt = kst[s * LANES];
-                    fwd_fast(s, Vw[s * LANES] + kt.x, kt.y, lt[s * LANES]);
+                    fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kt.x), kt.y, lt[s * LANES]);
                     pc += 9;
                     continue;
                 }
@@ -860,6 +876,10 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         for (; s1 >= 0; --s1)
             bwd(s1, lt[s1 * LANES], col[s1 * LANES], Cbw[s1 * LANES], ty.crank ? Vw[s1 * LANES] : 0.0);
         finite_check(v, xn, active);   // row 0's solution
+        if (full && it == 0) {   // this tile's kept factors now match the fields
+            __syncwarp();
+            if (lane == 0) v.tgen[t] = sgen;
+        }
         }
         }
     step_end:

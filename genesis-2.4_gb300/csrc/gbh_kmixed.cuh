@@ -474,6 +474,13 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
     const int nst = GIV ? 0 : ty.nstatic; // static rows (givals off: they would write Im)
     constexpr int kCh = 8;                // rows per chunk
     const bool sp = SPLIT && nst > 0 && S - nst <= kSplitRows;
+    // The static rows' kept factors outlive a launch: they are redone (a
+    // full first step) only when the fields they come from may have changed
+    // since this tile last kept them (a state write bumps *v.sgen); else the
+    // first step only refreshes the rhs terms (inputs may set an inject).
+    const unsigned sgen = nst > 0 ? *v.sgen : 0u;
+    const bool full = nst > 0 && v.tgen[t] != sgen;
+    const bool kref = nst > 0 && *v.kref != 0;   // an input writes a static row's rhs fields
 
     ChanEnvDF E;
     E.tab = v.tabdf + tg.tab_off;
@@ -501,7 +508,8 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         const long long step = sbase + step0 + it;
         // after a launch's first step the static rows' (rhs term, coupling
         // factor) are in kst (see k_stack)
-        const bool fast = it > 0;
+        const bool fast = it > 0 || !full;
+        const bool refresh = it == 0 && kref;   // (fast) the rhs terms from the fields
         const bool split = sp && fast;
         bool bad = false;
         if (SPLIT && wid == 1 && !split) goto step_end;   // the second warp works in split steps only
@@ -645,6 +653,14 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             else if (ty.np1) fwd_static1(s, R, T, f);
             else fwd_static(s, R, T, f);
         };
+        // a static row's rhs term from its fields (as `passive` forms it), kept
+        auto kterm = [&](int s) {
+            const int *ps = pf + 6 * s;
+            const df ichan = df_add(ld_df(&Pw[ps[2] * LANES]), ld_df(&Pw[ps[3] * LANES]));
+            const double K = df2d(df_mul(ichan, ld_df(&Pw[ps[4] * LANES])));
+            kst[s * LANES].x = K;
+            return K;
+        };
         // a passive row (M_BEGIN / M_END): its current term ichan * tbyc in
         // double-float, added to Vm in FP64 (part of the Vm update); the
         // diagonal is the row's diagonal term (its conductance sum is zero)
@@ -662,7 +678,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 for (int k = 0; k < kCh; ++k) {
                     const double2 kt = kst[(s0 + k) * LANES];
                     f[k] = __ldg(&lt[(s0 + k) * LANES]);
-                    R[k] = Vw[(s0 + k) * LANES] + kt.x;
+                    R[k] = Vw[(s0 + k) * LANES] + (refresh ? kterm(s0 + k) : kt.x);
                     T[k] = kt.y;
                 }
                 if (ty.slots) {
@@ -703,7 +719,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 for (int k = 0; k < kCh; ++k) {
                     const int s = s0 + k;
                     if (fast && s < nst) {
-                        fwd_fast(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
+                        fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kst[s * LANES].x), kst[s * LANES].y, f[k]);
                     } else {
                         fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
                     }
@@ -716,7 +732,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 const int *ps = pf + 6 * s;
                 if (fast && s < nst) {
                     const double2 kt = kst[s * LANES];
-                    fwd_fast(s, Vw[s * LANES] + kt.x, kt.y, __ldg(&lt[s * LANES]));
+                    fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kt.x), kt.y, __ldg(&lt[s * LANES]));
                     pc += 9;
                     continue;
                 }
@@ -792,6 +808,10 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             bwd(s1, __ldg(&lt[s1 * LANES]), col[s1 * LANES], __ldg(&Cbw[s1 * LANES]),
                 ty.crank ? Vw[s1 * LANES] : 0.0);
         finite_check(v, xn, active);   // row 0's solution
+        if (full && it == 0) {   // this tile's kept factors now match the fields
+            __syncwarp();
+            if (lane == 0) v.tgen[t] = sgen;
+        }
         }
         }
     step_end:

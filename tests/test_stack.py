@@ -197,3 +197,57 @@ def test_stack_rows_with_three_children(oracle, gpu_engine, prec):
         else:
             assert float(np.max(np.abs(vm[i] - ref.vm))) <= 1e-9
     eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_kept_factors_across_launches(oracle, gpu_engine, prec):
+    """The static rows' kept factors outlive a launch. One-step launches (the
+    hsolve-level ABI's use) take the fast path from the second launch on; a
+    state write of a static row's diagonal term, and an input that sets one
+    every launch, make the next launch redo them."""
+    hs = _trees(model.BEULER, seed=61)
+    p = gpu_engine.PREC_FP64 if prec == "fp64" else gpu_engine.PREC_MIXED
+    eng = gpu_engine.Engine(hs, precision=p, wide_min=-1, jit=False, steps_per_launch=1)
+    refs = [oracle.Solver(h) for h in hs]
+    worst = 0.0
+
+    def check():
+        nonlocal worst
+        vm = eng.get_state()["vm"]
+        for i, r in enumerate(refs):
+            if prec == "fp64":
+                np.testing.assert_array_equal(vm[i], r.vm)
+            else:
+                worst = max(worst, float(np.max(np.abs(vm[i] - r.vm))))
+
+    for _ in range(40):                           # 40 one-step launches
+        eng.run(1)
+    for r in refs:
+        r.run(40)
+    check()
+    st = eng.get_state()                          # row 5's diagonal term, written between launches
+    for i, h in enumerate(hs):
+        c = int(h.compchips[5]) + 3
+        st["chip"][i][c] *= 1.02
+        refs[i].chip[c] = st["chip"][i][c]
+    eng.set_state(chip=st["chip"])
+    for _ in range(20):
+        eng.run(1)
+    for r in refs:
+        r.run(20)
+    check()
+    # an input that sets row 3's diagonal term before every launch
+    rows = [(i, int(h.compchips[3]) + 3) for i, h in enumerate(hs)]
+    eng.register_inputs(np.array([r[0] for r in rows], np.int32), np.array([r[1] for r in rows]))
+    base = np.array([refs[i].chip[c] for i, c in rows])
+    for k in range(10):
+        v = base * (1.0 + 0.01 * (k % 3))
+        eng.set_inputs_async(v, 0)
+        for (i, c), x in zip(rows, v):
+            refs[i].chip[c] = x
+        eng.run(3)
+        for r in refs:
+            r.run(3)
+    check()
+    assert worst <= 1e-9, worst
+    eng.close()
