@@ -545,6 +545,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     const unsigned sgen = nst > 0 ? *v.sgen : 0u;
     const bool full = nst > 0 && v.tgen[t] != sgen;
     const bool kref = nst > 0 && *v.kref != 0;   // an input writes a static row's rhs fields
+    if (SPLIT) __syncthreads();   // both warps read tgen[t] before the sweeping warp rewrites it
 
     ChanEnv<G> E;
     E.tab = tab_ptr<G>(v, tg.tab_off);
