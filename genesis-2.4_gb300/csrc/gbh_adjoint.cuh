@@ -5,9 +5,9 @@
 // (do_chip_hh4_update, genesis/src/hines/hines_chip.c:157-600, followed by
 // do_euler_hsolve / do_crank_hsolve, genesis/src/hines/hines_solve.c:140-296).
 //
-// FP64 arithmetic on GB300 is bound by each SM sub-partition's FP64 unit,
-// and a warp occupies it for all 32 lanes whether they are active or not: a
-// batch of a few thousand neurons (one warp per 32) reaches a quarter of the
+// FP64 arithmetic on GB300: one warp issues at most ~0.47 lane-DFMA per clock
+// whether its lanes are active or not, an SM ~1.6 with four warps or more, so
+// a batch of a few thousand neurons (one warp per 32) reaches a quarter of the
 // GPU's FP64 rate in any kernel that walks the steps one after another. The
 // sweep therefore keeps the sequential kernels lean and moves the rest into
 // kernels that are parallel over steps as well as neurons:

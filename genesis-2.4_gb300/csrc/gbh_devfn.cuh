@@ -107,7 +107,6 @@ __device__ __forceinline__ void finite_check(const DevView &v, double x, bool ac
     if (!(fabs(x) <= 1.0e30) && active && v.status) atomicOr(v.status, ST_NONFINITE);
 }
 
-// Prefetch of the cache line holding *p into L1 (the loads of a later row).
 // Named barrier `id` (1-15; 0 is __syncthreads') over `n` threads, a
 // multiple of 32: warps that do different work in a step meet here from
 // different places in the code.
@@ -116,6 +115,7 @@ __device__ __forceinline__ void bar_named(int id, int n)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
+// Prefetch of the cache line holding *p into L1 (the loads of a later row).
 __device__ __forceinline__ void prefetch_l1(const void *p)
 {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
