@@ -260,9 +260,11 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
     """Gradient workload: 4,096 seeded random binary trees x 64 compartments
     with Na, K and leak on every compartment, dt 25 us, backward Euler; loss =
     summed squared somatic Vm error over 10,000 steps against traces of the
-    same trees with every gbar scaled by U(0.8, 1.2); checkpoints every 100
-    steps. Times gbh_loss_gradient against the plain FP64 forward
-    (gbh_run) of the same steps on the same engine."""
+    same trees with every gbar scaled by U(0.8, 1.2). Times gbh_loss_gradient
+    against the plain FP64 forward (gbh_run) of the same steps on the same
+    engine: every step's state kept in device memory (~84 GB), and with
+    checkpoints every 100 steps (each segment recomputed), which must give
+    the same bits."""
     import torch
     from gbhsolve import configs, engine, model
     t0 = time.time()
@@ -290,24 +292,39 @@ def adjoint_measure(device, n_neurons=GRAD_NEURONS, nsteps=GRAD_STEPS):
     eng.run(nsteps)
     fwd_ms = eng.stats().device_ms - ms0
     eng.set_state(vm=st0["vm"], chip=st0["chip"])
+    # every step's state kept in device memory (checkpoint_every 0), then
+    # checkpoints every GRAD_K steps with each segment recomputed: same bits
     launches0 = eng.stats().launches
     t1 = time.time()
-    loss, dchip, drav, dvm = eng.loss_gradient(nsteps, solver, soma, tr, GRAD_K)
+    loss, dchip, drav, dvm = eng.loss_gradient(nsteps, solver, soma, tr, 0)
     wall = time.time() - t1
     st = eng.stats()
     grad_ms = st.grad_forward_ms + st.grad_reverse_ms
+    kept = int(st.grad_kept_steps)
+    launches = int(st.launches - launches0)
+    loss_c, dchip_c, drav_c, dvm_c = eng.loss_gradient(nsteps, solver, soma, tr, GRAD_K)
+    stc = eng.stats()
+    grad_c_ms = stc.grad_forward_ms + stc.grad_reverse_ms
+    same = bool(loss_c == loss and np.array_equal(dchip_c, dchip) and np.array_equal(drav_c, drav)
+                and np.array_equal(dvm_c, dvm))
     eng.close()
     finite = bool(np.all(np.isfinite(dchip)) and np.all(np.isfinite(drav)) and np.all(np.isfinite(dvm)))
-    log("gradient: forward %.1f ms, gradient %.1f ms (checkpoint pass %.1f, reverse %.1f), ratio %.2f, "
-        "loss %.6g" % (fwd_ms, grad_ms, st.grad_forward_ms, st.grad_reverse_ms, grad_ms / fwd_ms, loss))
+    log("gradient: forward %.1f ms, gradient %.1f ms (forward pass %.1f, reverse %.1f, every step kept: %d), "
+        "ratio %.2f; checkpointed every %d: %.1f ms (ratio %.2f), same bits %s; loss %.6g"
+        % (fwd_ms, grad_ms, st.grad_forward_ms, st.grad_reverse_ms, kept, grad_ms / fwd_ms, GRAD_K, grad_c_ms,
+           grad_c_ms / fwd_ms, same, loss))
     return {"workload": "grad-trees-%dx%d: %d random binary trees x %d compartments, Na/K/leak on every "
                         "compartment, dt 25 us, backward Euler, somatic-trace loss" % (n_neurons, GRAD_NCOMP, n_neurons, GRAD_NCOMP),
-            "steps": nsteps, "checkpoint_every": GRAD_K, "dtype": "f64",
-            "forward_ms": fwd_ms, "gradient_ms": grad_ms, "checkpoint_pass_ms": st.grad_forward_ms,
+            "steps": nsteps, "checkpoint_every": 0, "every_step_kept": kept, "dtype": "f64",
+            "forward_ms": fwd_ms, "gradient_ms": grad_ms, "forward_pass_ms": st.grad_forward_ms,
             "reverse_pass_ms": st.grad_reverse_ms, "gradient_wall_s": wall,
             "ratio_gradient_over_forward": grad_ms / fwd_ms,
             "ratio_backward_over_forward": st.grad_reverse_ms / fwd_ms, "loss": loss, "gradients_finite": finite,
-            "launches": int(st.launches - launches0)}
+            "launches": launches,
+            "checkpointed": {"checkpoint_every": GRAD_K, "gradient_ms": grad_c_ms,
+                             "checkpoint_pass_ms": stc.grad_forward_ms, "reverse_pass_ms": stc.grad_reverse_ms,
+                             "ratio_gradient_over_forward": grad_c_ms / fwd_ms,
+                             "same_bits_as_every_step_kept": same}}
 
 
 def other_configs(device, n_trees=50_000):

@@ -22,6 +22,14 @@ cudaError_t launch_adj_copy(const AdjView &v, int ntiles, int maxrows, int c, in
     return cudaGetLastError();
 }
 
+cudaError_t launch_adj_ck_to_tape(const AdjView &v, int ntiles, int maxrows, int c0, int nk, cudaStream_t st)
+{
+    if (ntiles <= 0 || maxrows <= 0 || nk <= 0) return cudaSuccess;
+    const dim3 grid(ntiles, (maxrows + 31) / 32, nk);
+    k_adj_ck_to_tape<<<grid, LANES, 0, st>>>(v, c0);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adj_linearize(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st)
 {
     if (ntiles <= 0 || nk <= 0) return cudaSuccess;

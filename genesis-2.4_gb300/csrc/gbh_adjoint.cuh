@@ -100,6 +100,24 @@ k_adj_copy(AdjView v, int c, int dir, int to_tape)
     }
 }
 
+// Checkpoint c0 + k -> tape step k (blockIdx.z = k): the snapshot rows of a
+// segment whose every step was kept by the forward pass.
+__global__ void __launch_bounds__(LANES)
+k_adj_ck_to_tape(AdjView v, int c0)
+{
+    const int lane = threadIdx.x;
+    const int t = blockIdx.x;
+    const int k = blockIdx.z;
+    const Tile tl = v.tiles[t];
+    const AdjType at = v.atypes[tl.type];
+    const int rows = at.nslots + at.ngates;
+    const int r0 = blockIdx.y * 32;
+    const int r1 = min(rows, r0 + 32);
+    const double *src = v.ckpt + ((int64_t)(c0 + k) * v.ck_stride + v.ck_off[t]) * LANES + lane;
+    double *dst = adj_tape(v, k, t, lane);
+    for (int r = r0; r < r1; ++r) dst[r * LANES] = src[r * LANES];
+}
+
 // ---------------------------------------------------------------- linearisation
 // grid (tiles, steps), 32 threads. Shared memory: 2 * smax * 32 doubles.
 __global__ void __launch_bounds__(32)

@@ -115,6 +115,9 @@ struct AdjView {
 //   dir 1: checkpoint c -> work
 cudaError_t launch_adj_copy(const AdjView &v, int ntiles, int maxrows, int c, int dir, bool to_tape,
                             cudaStream_t st);
+// Checkpoints c0 .. c0+nk-1 (one per step, every step's state kept) -> tape
+// steps 0 .. nk-1.
+cudaError_t launch_adj_ck_to_tape(const AdjView &v, int ntiles, int maxrows, int c0, int nk, cudaStream_t st);
 // Per-step linearisation of tape steps [0, nk): recomputes each step from
 // its snapshot (parallel over steps and tiles) and fills the tape rows.
 cudaError_t launch_adj_linearize(const AdjView &v, int ntiles, int smax, int nk, cudaStream_t st);

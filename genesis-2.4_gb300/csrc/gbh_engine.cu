@@ -2867,6 +2867,7 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         if (dvm0) memset(dvm0, 0, e->vm_start.back() * sizeof(double));
         return GBH_OK;
     }
+    // K: the steps of one segment (tape); checkpoint_every <= 0 may keep every step instead
     const int K = std::max(1, std::min({checkpoint_every > 0 ? checkpoint_every : 100, nsteps, 65535}));
     const int nseg = (nsteps + K - 1) / K;
     // ---- target rows ----
@@ -2939,7 +2940,21 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         }
     } b;
     const int64_t nfld = e->rows_fld * L, nvm = e->rows_vm * L, ntopo = e->rows_topo * L;
-    if (b.P.alloc(nfld) || b.V.alloc(nvm) || b.ck.alloc((size_t)nseg * ck_stride * L) ||
+    // checkpoint_every <= 0: every step's state kept (one checkpoint per
+    // step) when it fits in 60% of the free memory beside the two tapes
+    bool keep = false;
+    if (checkpoint_every <= 0) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return fail_err(nullptr, GBH_ERR_CUDA, "cudaMemGetInfo");
+        const double need = (double)nsteps * ck_stride * L * sizeof(double);
+        const double tapes = 2.0 * K * tp_stride * L * sizeof(double);
+        keep = need <= 0.6 * ((double)free_b - tapes);
+        if (keep && b.ck.alloc((size_t)nsteps * ck_stride * L) != GBH_OK) {
+            cudaGetLastError();
+            keep = false;
+        }
+    }
+    if ((!keep && b.ck.alloc((size_t)nseg * ck_stride * L)) || b.P.alloc(nfld) || b.V.alloc(nvm) ||
         b.tape.alloc((size_t)K * tp_stride * L) || b.Vb.alloc(nvm) || b.Xb.alloc(xb_rows * L) ||
         b.Gf.alloc(nfld) || b.Gek.alloc(ch_rows * L) || b.Ggm.alloc(ch_rows * L) || b.GA.alloc(ntopo) ||
         b.GB.alloc(ntopo) || b.GC.alloc(ntopo) || b.loss.alloc((size_t)ntiles * L) ||
@@ -3018,20 +3033,29 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     // is restored afterwards; its tiles redo theirs at their next launch)
     if (stack_invalidate(e, st)) return GBH_ERR_CUDA;
     auto forward = [&](int n) { return issue_steps(e, fv, n, 0, false, st, nullptr); };
-    // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed)
+    // forward pass: checkpoints 0 .. nseg-1 (the last segment is recomputed),
+    // or the state before every step when every step is kept
     CK(cudaEventRecord(e->ev0, st));
-    for (int seg = 0; seg < nseg; ++seg) {
-        if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, seg, 0, false, st))) return GBH_ERR_CUDA;
-        if (seg + 1 < nseg && forward(K)) return GBH_ERR_CUDA;
+    if (keep) {
+        for (int n = 0; n < nsteps; ++n) {
+            if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, n, 0, false, st))) return GBH_ERR_CUDA;
+            if (n + 1 < nsteps && forward(1)) return GBH_ERR_CUDA;
+        }
+    } else {
+        for (int seg = 0; seg < nseg; ++seg) {
+            if (ck_launch(launch_adj_copy(v, ntiles, maxcopy, seg, 0, false, st))) return GBH_ERR_CUDA;
+            if (seg + 1 < nseg && forward(K)) return GBH_ERR_CUDA;
+        }
     }
     CK(cudaEventRecord(e->ev1, st));
     CK(cudaEventSynchronize(e->ev1));
     float ms_fwd = 0.f;
     CK(cudaEventElapsedTime(&ms_fwd, e->ev0, e->ev1));
-    // reverse pass, segment by segment, last first: recompute with snapshots
-    // (engine stream), then linearise, sweep back and sum the gradients (a
-    // second stream). With two tape buffers the recomputation of the next
-    // segment overlaps the adjoint kernels of this one; they share only the
+    // reverse pass, segment by segment, last first: the snapshots into the
+    // tape (recomputed from the checkpoint on the engine stream, or copied
+    // when every step was kept), the linearisation, then sweep back and sum
+    // the gradients (a second stream). With two tape buffers the next
+    // segment's snapshots overlap this one's sweep; they share only the
     // constant fields of the work copy.
     const bool overlap = b.tape2.alloc((size_t)K * tp_stride * L) == GBH_OK;
     if (!overlap) cudaGetLastError();
@@ -3050,14 +3074,24 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
         const int nk = std::min(K, nsteps - seg * K);
         // the buffer's previous segment must be through the adjoint kernels
         if (idx >= (overlap ? 2 : 1)) CK(cudaStreamWaitEvent(st, b.ev_done[buf], 0));
-        if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, seg, 1, false, st))) return GBH_ERR_CUDA;
-        for (int k = 0; k < nk; ++k) {
-            if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, k, 0, true, st))) return GBH_ERR_CUDA;
-            if (k + 1 < nk && forward(1)) return GBH_ERR_CUDA;
+        if (keep) {
+            if (ck_launch(launch_adj_ck_to_tape(w, ntiles, maxcopy, seg * K, nk, st))) return GBH_ERR_CUDA;
+        } else {
+            if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, seg, 1, false, st))) return GBH_ERR_CUDA;
+            for (int k = 0; k < nk; ++k) {
+                if (ck_launch(launch_adj_copy(w, ntiles, maxcopy, k, 0, true, st))) return GBH_ERR_CUDA;
+                if (k + 1 < nk && forward(1)) return GBH_ERR_CUDA;
+            }
         }
+        // the linearisation (parallel over steps): with every step kept, on
+        // the engine stream, so that it overlaps the previous segment's
+        // reverse sweep (a chain over steps on a few blocks); with segments
+        // recomputed, beside the sweep on the second stream (the engine
+        // stream runs the next segment's recomputation meanwhile)
+        if (keep && ck_launch(launch_adj_linearize(w, ntiles, smax, nk, st))) return GBH_ERR_CUDA;
         CK(cudaEventRecord(b.ev_tape[buf], st));
         CK(cudaStreamWaitEvent(b.ast, b.ev_tape[buf], 0));
-        if (ck_launch(launch_adj_linearize(w, ntiles, smax, nk, b.ast))) return GBH_ERR_CUDA;
+        if (!keep && ck_launch(launch_adj_linearize(w, ntiles, smax, nk, b.ast))) return GBH_ERR_CUDA;
         if (ck_launch(launch_adj_reverse(w, ntiles, smax, hmax, nk, seg * K, b.ast))) return GBH_ERR_CUDA;
         if (ck_launch(launch_adj_reduce(w, ntiles, smax, nk, b.ast))) return GBH_ERR_CUDA;
         CK(cudaEventRecord(b.ev_done[buf], b.ast));
@@ -3070,9 +3104,10 @@ int gbh_loss_gradient(gbh_engine *e, int nsteps, int checkpoint_every, const gbh
     CK(cudaEventElapsedTime(&ms_rev, e->ev0, e->ev1));
     e->stats.grad_forward_ms = ms_fwd;
     e->stats.grad_reverse_ms = ms_rev;
+    e->stats.grad_kept_steps = keep ? 1 : 0;
     // forward step launches are counted by launch_one; add the copies
     // (checkpoint saves and restores, snapshots) and three kernels per segment
-    e->stats.launches += 2 * (int64_t)nseg + nsteps + 3 * (int64_t)nseg;
+    e->stats.launches += (keep ? (int64_t)nsteps + nseg : 2 * (int64_t)nseg + nsteps) + 3 * (int64_t)nseg;
     int status = 0;
     CK(cudaMemcpy(&status, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (status) {

@@ -83,7 +83,8 @@ class GbhStats(C.Structure):
                 ("steps_per_launch", C.c_int), ("warps_per_block", C.c_int), ("precision", C.c_int),
                 ("jit_kernels", C.c_int), ("jit_min_blocks", C.c_int),
                 ("grad_forward_ms", C.c_double), ("grad_reverse_ms", C.c_double), ("jit_compact", C.c_int),
-                ("cooperative", C.c_int), ("wide_tiles", C.c_int64), ("stack_tiles", C.c_int64)]
+                ("cooperative", C.c_int), ("wide_tiles", C.c_int64), ("stack_tiles", C.c_int64),
+                ("grad_kept_steps", C.c_int64)]
 
 
 EXPORTED = ["gbh_jit_source", "gbh_validate", "gbh_create", "gbh_run", "gbh_run_async", "gbh_get_state", "gbh_set_state",

@@ -211,6 +211,10 @@ typedef struct gbh_stats {
                                   threads (level-by-level elimination)        */
     int64_t stack_tiles;       /* tiles of 32 large neurons, one per lane,
                                   eliminated with per-lane stacks             */
+    int64_t grad_kept_steps;   /* last gbh_loss_gradient: 1 if every step's
+                                  state stayed in device memory (no segment
+                                  recomputed), 0 if segments were recomputed
+                                  from checkpoints                            */
 } gbh_stats;
 
 typedef struct gbh_engine gbh_engine;
@@ -415,14 +419,21 @@ int gbh_run_noalloc(gbh_engine *e, int nsteps, void *stream);
  * are zero. The engine's own state is left unchanged.
  *
  * Method: hand-written adjoint (reverse-mode) kernels. A forward pass stores
- * Vm and the gate states every checkpoint_every steps (<= 0: 100); the
- * reverse pass recomputes each segment from its checkpoint, recording Vm,
- * the elimination's diagonals and right-hand sides, the solution and the
- * gate states of every step, and runs the transposed Hines sweep (reverse
+ * Vm and the gate states every checkpoint_every steps; the reverse pass
+ * recomputes each segment from its checkpoint, recording Vm, the
+ * elimination's diagonals and right-hand sides, the solution and the gate
+ * states of every step, and runs the transposed Hines sweep (reverse
  * elimination order) and the reverse of the gate updates and table
- * interpolations step by step back to the start. Device memory held during
- * the call: checkpoints ~ (nsteps / checkpoint_every) x (rows + gates) and
- * the tape ~ checkpoint_every x (4 rows + gates) doubles per neuron.
+ * interpolations step by step back to the start, one segment of
+ * checkpoint_every steps at a time. checkpoint_every <= 0: the forward pass
+ * keeps every step's Vm and gate states when nsteps x (rows + gates)
+ * doubles per neuron fit in 60% of the device memory left free beside the
+ * tapes, and no segment is recomputed (segments of 100 steps); otherwise as
+ * checkpoint_every = 100. The results are the same bits either way
+ * (gbh_stats.grad_kept_steps says which ran). Device memory held during
+ * the call: checkpoints ~ (nsteps / checkpoint_every) x (rows + gates)
+ * doubles per neuron (nsteps x when every step is kept) and two tapes of
+ * ~ checkpoint_every x (10 rows + 4 gates + channels) doubles per neuron.
  *
  * Supported programs (GBH_ERR_UNSUPPORTED otherwise): compartments with
  * voltage-tabulated channels (TABCHAN with IPOL1V gates of nonzero power,

@@ -254,8 +254,11 @@ def test_checkpoint_interval_invariance_and_state(oracle, gpu_engine):
     trace = np.concatenate(traces, axis=1)
     vm0 = eng.vm().copy()
     base = eng.loss_gradient(nsteps, solver, row, trace, 100)
-    for K in (1, 7, 600, 5000):
+    assert eng.stats().grad_kept_steps == 0
+    # 0: every step's state kept in device memory, no segment recomputed
+    for K in (1, 7, 600, 5000, 0):
         other = eng.loss_gradient(nsteps, solver, row, trace, K)
+        assert eng.stats().grad_kept_steps == (1 if K == 0 else 0)
         assert other[0] == base[0]
         for a, b in zip(other[1:], base[1:]):
             assert np.array_equal(a, b), K
