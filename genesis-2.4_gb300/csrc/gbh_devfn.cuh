@@ -83,7 +83,7 @@ struct DevView {
     // writes) and, per tile, the generation its kst / col were kept at
     const unsigned *sgen;
     unsigned *tgen;
-    const int *kref;  // nonzero: an input writes a static row's Em/Rm, inject or dt/Cm
+    const int *kref;  // 1: an input writes a static row's Em/Rm, inject or dt/Cm; 2: also its diagonal term
     // synapses of weighted synchans (SynW): per synapse its bit's word for
     // slot 0 (-1 for a synchan of one weight) and bit | nwords << 5
     const int64_t *syn_out_mword;

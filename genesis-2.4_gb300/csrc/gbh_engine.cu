@@ -1576,6 +1576,9 @@ int autotune(gbh_engine *e)
     e->opt.use_graph = use_graph;
     drop_graphs(e);
     e->dstep_valid = false;
+    // the trials' kernels kept the static rows' factors with their own
+    // arithmetic: the chosen kernels keep theirs at their first launch
+    if (rc_t == GBH_OK && stack_invalidate(e, e->stream)) return GBH_ERR_CUDA;
     return rc_t;
 }
 
@@ -1906,10 +1909,12 @@ int gbh_register_inputs_typed(gbh_engine *e, int n, const int *solver, const int
                 addrs[i].push_back(at(t.pools, (int64_t)p, l, e->types[t.type].wide != 0) | kFluxFlag);
         }
     }
-    if (kfield_input && e->d_kref.p) {   // the stack tiles then refresh those terms at every launch
-        const int one = 1;
+    // the stack tiles then refresh those terms at every launch, the specialised
+    // kernels at every step (2: a diagonal term, every step of theirs a full one)
+    if ((kfield_input || e->stack_input_d) && e->d_kref.p) {
+        const int kr = e->stack_input_d ? 2 : 1;
         CK(cudaStreamSynchronize(e->stream));
-        CK(cudaMemcpy(e->d_kref.p, &one, sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(e->d_kref.p, &kr, sizeof(int), cudaMemcpyHostToDevice));
     }
     std::map<int64_t, std::vector<int>> by_target;   // keyed by address without the add flag
     std::map<int64_t, int64_t> flags;
@@ -2305,6 +2310,15 @@ int64_t gbh_jit_source(const gbh_batch_desc *desc, int precision, int type_index
         }
     }
     if (type_index < 0 || type_index >= (int)types.size()) return GBH_ERR_ARG;
+    {   // the static rows as the engine plans them for a stack-eligible type
+        TileType &tt = types[type_index];
+        std::vector<int> fl;
+        int cap = 0;
+        if (!tt.sym && tt.nslots >= kStackMin && stack_plan(parents[type_index], fl, cap) && cap <= kStackCapMax) {
+            const std::vector<int> pf = slot_field_ranges(prog_pool, tt);
+            while (tt.nstatic < tt.nslots && pf[6 * tt.nstatic + 2] >= 0) ++tt.nstatic;
+        }
+    }
     std::vector<TableGeom> tg;
     std::vector<double> tab64, xy;
     build_tables(desc, tg, tab64, xy);

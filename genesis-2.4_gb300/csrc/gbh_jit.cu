@@ -20,6 +20,7 @@
 #include <nvrtc.h>
 
 #include <cstdio>
+#include <array>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -590,8 +591,46 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
         sstart[S] = off;
     }
+    // Static rows of the register form of a shared tree: the rows below the
+    // first compartment with channels (TileType::nstatic; programs of
+    // M_BEGIN + M_END alone). Their rhs term K = (Em/Rm + inject) * tbyc, D'
+    // and T = A / D' change only when a field they come from does, so a
+    // launch's first step after such a change (kfull) keeps them -- kst =
+    // (K, T), col.y = D' (FP64) or 1/D' (mixed), the stack kernels' layout --
+    // and the other steps eliminate only the rhs: R = Vm + K less R_child *
+    // T_child, with the arithmetic of the full step (FP64: the same bits).
+    // *v.kref: 1, an input writes a static row's Em/Rm, inject or dt/Cm, so K
+    // is formed from the fields every step; 2, an input writes a diagonal
+    // term, so every step is a full one.
+    int nst = 0;
+    std::vector<std::array<int, 3>> kf;   // per static row: Em/Rm, inject, tbyc fields
+    if (uniform_parent && !cols && !giv) {
+        nst = std::min(tt.nstatic, S);
+        for (int q = 0; q < nst; ++q) {
+            const int *a = prog.data() + sstart[q];
+            if (sstart[q + 1] - sstart[q] != 9 || a[0] != M_BEGIN || a[5] != M_END) {
+                nst = q;
+                break;
+            }
+            kf.push_back({a[1], a[2], a[6]});
+        }
+    }
+    if (nst > 0)
+        o << "  double2 *kst = v.kst + tl.topo * 32 + lane; double2 *col = v.col + tl.topo * 32 + lane;\n"
+          << "  const int kr = v.sgen ? *v.kref : 2; const unsigned sgen = v.sgen ? *v.sgen : 0u;\n"
+          << "  const bool full = kr > 1 || v.tgen[t] != sgen;\n";
+    // K of static row q from its fields, as the slot code forms it
+    auto kexpr = [&](int q) {
+        const std::string e = std::to_string(kf[q][0] * LANES), i = std::to_string(kf[q][1] * LANES),
+                          b = std::to_string(kf[q][2] * LANES);
+        if (mixed) return "df_mul(df_add(ld_df_ro(&Pw[" + e + "]), ld_df_cg(&Pw[" + i + "])), ld_df_ro(&Pw[" + b + "]))";
+        return "(__ldg(&Pw[" + e + "]) + Pw[" + i + "]) * __ldg(&Pw[" + b + "])";
+    };
     std::deque<std::string> pending;   // fused elimination blocks not yet emitted
     const int elim_lag = 1;   // measured: 1 beats 0, 2 and 3 on the 16-compartment cable
+    // the channel phase with the fused forward sweep; fast: the static rows
+    // from their kept factors
+    auto emit_phase = [&](bool fast) -> bool {
     // compact form: runs of four or more identical slot programs become one
     // loop (keeps the kernel inside the instruction cache)
     for (int s = 0; s < S;) {
@@ -604,13 +643,26 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 E.fx[x.first] = std::to_string(x.first) + " + " + std::to_string(x.second) + " * (s - " +
                                 std::to_string(s) + ")";
             o << "    for (int s = " << s << "; s < " << s + run << "; ++s) {\n";
-            if (!emit_slot(E, s, pc, tg)) return std::string();
+            if (!emit_slot(E, s, pc, tg)) return false;
             o << "    }\n";
             E.sidx.clear();
             E.fx.clear();
             s += run;
         } else {
-            if (!emit_slot(E, s, pc, tg)) return std::string();
+            const bool kept = s < nst;
+            if (fast && kept) {
+                const std::string ks = std::to_string(s * LANES), ss = std::to_string(s);
+                o << "    { // slot " << s << ": kept factors\n      const double Vm = Vw[" << ks << "];\n";
+                if (mixed)
+                    o << "      if (kr) R[" << ss << "] = df2d(df_add(d2df(Vm), " << kexpr(s) << "));\n"
+                      << "      else R[" << ss << "] = df2d(df_add(d2df(Vm), d2df(kst[" << ks << "].x)));\n";
+                else
+                    o << "      if (kr) R[" << ss << "] = Vm + " << kexpr(s) << ";\n"
+                      << "      else R[" << ss << "] = Vm + kst[" << ks << "].x;\n";
+                o << "      D[" << ss << "] = col[" << ks << "].y; T[" << ss << "] = kst[" << ks << "].y; }\n";
+            } else if (!emit_slot(E, s, pc, tg)) {
+                return false;
+            }
             if (uniform_parent) {
                 // forward elimination fused into the channel phase: row s pulls
                 // its children (ascending, the order the separate sweep pushes
@@ -621,7 +673,12 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 const std::vector<int> &par = *uniform_parent;
                 std::ostringstream el;
                 el << "    {";
-                for (int c = 0; c < s; ++c) {
+                for (int c = 0; c < s && fast && kept; ++c) {   // a kept row: the rhs only
+                    if (par[c] != s) continue;
+                    if (mixed) el << " R[" << s << "] = fma(-R[" << c << "], T[" << c << "], R[" << s << "]);";
+                    else el << " R[" << s << "] -= R[" << c << "] * T[" << c << "];";
+                }
+                for (int c = 0; c < s && !(fast && kept); ++c) {
                     if (par[c] != s) continue;
                     if (mixed)
                         el << " D[" << s << "] = fma(-Bw[" << c * LANES << "], T[" << c << "], D[" << s << "]); R[" << s
@@ -630,11 +687,20 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                         el << " D[" << s << "] -= Bw[" << c * LANES << "] * T[" << c << "]; R[" << s << "] -= R[" << c
                            << "] * T[" << c << "];";
                 }
-                if (mixed) {
+                if (fast && kept) {
+                } else if (mixed) {
                     el << " const double ri = rcp_newton(D[" << s << "]); D[" << s << "] = ri;";
                     if (par[s] >= 0) el << " T[" << s << "] = Aw[" << s * LANES << "] * ri;";
                 } else if (par[s] >= 0) {
                     el << " T[" << s << "] = Aw[" << s * LANES << "] / D[" << s << "];";
+                }
+                if (!fast && kept) {   // keep K, T and D' (1/D')
+                    const std::string ks = std::to_string(s * LANES);
+                    el << "\n      if (full) {";
+                    if (mixed) el << " kst[" << ks << "].x = df2d(" << kexpr(s) << ");";
+                    else el << " kst[" << ks << "].x = " << kexpr(s) << ";";
+                    el << " kst[" << ks << "].y = " << (par[s] >= 0 ? "T[" + std::to_string(s) + "]" : std::string("0.0"))
+                       << "; col[" << ks << "].y = D[" << s << "]; }";
                 }
                 el << " }\n";
                 pending.push_back(el.str());
@@ -647,6 +713,18 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         }
     }
     for (const std::string &x : pending) o << x;
+    pending.clear();
+    return true;
+    };
+    if (nst > 0) {
+        o << "    const bool kfull = full && (it == 0 || kr > 1);\n    if (kfull) {\n";
+        if (!emit_phase(false)) return std::string();
+        o << "    } else {\n";
+        if (!emit_phase(true)) return std::string();
+        o << "    }\n";
+    } else if (!emit_phase(false)) {
+        return std::string();
+    }
     std::string body = o.str();
     if (cols) {
         // rewrite D[s]/R[s] into the shared columns
@@ -720,6 +798,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         t << " }\n";
     }
     t << "    finite_check(v, Vw[0], active);\n";
+    if (nst > 0) t << "    if (kfull && it == 0) { __syncwarp(); if (lane == 0) v.tgen[t] = sgen; }\n";
     t << "    if (v.io_out) {   // this step's outputs\n"
       << "      __syncwarp(); double *dst = v.io_out + (step - v.io_step0) * v.io_nout; const double *Vt = v.V + tl.vm * 32;\n"
       << "      for (int q = v.tout_start[t] + lane; q < v.tout_start[t + 1]; q += 32) dst[v.tout_idx[q]] = Vt[v.tout_off[q]]; }\n";
