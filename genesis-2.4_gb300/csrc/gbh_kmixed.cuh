@@ -671,6 +671,10 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             R = Vw[s * LANES] + K;
             D = df2d(ld_df(&Pw[ps[5] * LANES]));
         };
+        // inputs on the static rows' rhs fields: their terms from the fields,
+        // once, before the sweep (not inside its chains)
+        if (refresh && fast)
+            for (int s = 0; s < nst; ++s) kterm(s);
         for (int s0 = 0; s0 < Send && !bad; s0 += kCh) {
             if (fast && s0 + kCh <= nst) {
                 double R[kCh], T[kCh];
@@ -679,7 +683,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 for (int k = 0; k < kCh; ++k) {
                     const double2 kt = kst[(s0 + k) * LANES];
                     f[k] = __ldg(&lt[(s0 + k) * LANES]);
-                    R[k] = Vw[(s0 + k) * LANES] + (refresh ? kterm(s0 + k) : kt.x);
+                    R[k] = Vw[(s0 + k) * LANES] + kt.x;
                     T[k] = kt.y;
                 }
                 if (ty.slots) {
@@ -720,7 +724,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 for (int k = 0; k < kCh; ++k) {
                     const int s = s0 + k;
                     if (fast && s < nst) {
-                        fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kst[s * LANES].x), kst[s * LANES].y, f[k]);
+                        fwd_fast(s, Vw[s * LANES] + kst[s * LANES].x, kst[s * LANES].y, f[k]);
                     } else {
                         fwd(s, R[k], D[k], f[k], a[k], bb[k], K[k]);
                     }
@@ -733,7 +737,7 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
                 const int *ps = pf + 6 * s;
                 if (fast && s < nst) {
                     const double2 kt = kst[s * LANES];
-                    fwd_fast(s, Vw[s * LANES] + (refresh ? kterm(s) : kt.x), kt.y, __ldg(&lt[s * LANES]));
+                    fwd_fast(s, Vw[s * LANES] + kt.x, kt.y, __ldg(&lt[s * LANES]));
                     pc += 9;
                     continue;
                 }
