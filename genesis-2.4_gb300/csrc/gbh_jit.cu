@@ -600,8 +600,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     // and the other steps eliminate only the rhs: R = Vm + K less R_child *
     // T_child, with the arithmetic of the full step (FP64: the same bits).
     // *v.kref: 1, an input writes a static row's Em/Rm, inject or dt/Cm, so K
-    // is formed from the fields every step; 2, an input writes a diagonal
-    // term, so every step is a full one.
+    // is formed from the fields every step (one pass before the chain); 2, an
+    // input writes a diagonal term, so every step is a full one.
     int nst = 0;
     std::vector<std::array<int, 3>> kf;   // per static row: Em/Rm, inject, tbyc fields
     if (uniform_parent && !cols && !giv) {
@@ -653,12 +653,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
             if (fast && kept) {
                 const std::string ks = std::to_string(s * LANES), ss = std::to_string(s);
                 o << "    { // slot " << s << ": kept factors\n      const double Vm = Vw[" << ks << "];\n";
-                if (mixed)
-                    o << "      if (kr) R[" << ss << "] = df2d(df_add(d2df(Vm), " << kexpr(s) << "));\n"
-                      << "      else R[" << ss << "] = df2d(df_add(d2df(Vm), d2df(kst[" << ks << "].x)));\n";
-                else
-                    o << "      if (kr) R[" << ss << "] = Vm + " << kexpr(s) << ";\n"
-                      << "      else R[" << ss << "] = Vm + kst[" << ks << "].x;\n";
+                if (mixed) o << "      R[" << ss << "] = df2d(df_add(d2df(Vm), d2df(kst[" << ks << "].x)));\n";
+                else o << "      R[" << ss << "] = Vm + kst[" << ks << "].x;\n";
                 o << "      D[" << ss << "] = col[" << ks << "].y; T[" << ss << "] = kst[" << ks << "].y; }\n";
             } else if (!emit_slot(E, s, pc, tg)) {
                 return false;
@@ -720,6 +716,12 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
         o << "    const bool kfull = full && (it == 0 || kr > 1);\n    if (kfull) {\n";
         if (!emit_phase(false)) return std::string();
         o << "    } else {\n";
+        // inputs on the static rows' rhs fields: this step's K of every
+        // static row from its fields, before the chain (not inside it)
+        o << "    if (kr) {";
+        for (int q = 0; q < nst; ++q)
+            o << " kst[" << q * LANES << "].x = " << (mixed ? "df2d(" + kexpr(q) + ")" : kexpr(q)) << ";";
+        o << " }\n";
         if (!emit_phase(true)) return std::string();
         o << "    }\n";
     } else if (!emit_phase(false)) {
