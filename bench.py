@@ -378,12 +378,26 @@ def other_configs(device, n_trees=50_000):
     for graph in (False, True):
         eng = engine.Engine(hs1, synapses=esyn, precision=engine.PREC_FP64, device=device, use_graph=graph)
         st = eng.stats()
-        ms = rate(eng, 5000, 100)
+        if graph:
+            # a graph is captured per step count: the untimed first 5,000-step
+            # run captures the one the timed run replays; its spike counts
+            # after the same 5,100 steps must equal the per-launch engine's
+            eng.run(100)
+            eng.run(5000)
+            same = bool(np.array_equal(eng.spike_counts(), fp64_counts))
+            ms0 = eng.stats().device_ms
+            eng.run(5000)
+            ms = eng.stats().device_ms - ms0
+        else:
+            ms = rate(eng, 5000, 100)
         key = "graph" if graph else "launches"
         net[key] = {"ms": ms, "steps_per_s": 5000 / (ms / 1e3), "value": 4000 * 5000 / (ms / 1e3),
                     "spikes": int(eng.spike_counts().sum()), "cooperative": int(st.cooperative),
                     "specialised_kernels": int(st.jit_kernels)}
-        if not graph:
+        if graph:
+            net[key].update({"timed": "replay of the captured 5,000-step graph (steps 5,100-10,100)",
+                             "spike_counts_equal_launches_at_5100": same})
+        else:
             fp64_counts, fp64_vm = eng.spike_counts(), eng.vm()
         eng.close()
     # the mixed form over the same 5,100 steps against the FP64 engine (which
