@@ -4,7 +4,7 @@
   chanmode 4, CPU FP64 -> RESULT_VM= -0.02143485882
   (cluster_bringup/accel_regression_golden.txt:4), reproduced by the SETUP
   restatement plus the oracle, and checked against the committed fixture;
-* where the reference sources are present (this build container), the
+* where the reference sources are present, the
   oracle is checked bit for bit against do_chip_hh4_update /
   do_h4_conc_chip_update / do_euler_hsolve / do_crank_hsolve compiled from
   them (oracle/_ref), on single solvers and on a spiking network.
