@@ -618,8 +618,8 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
             const bool pop = f & 1;
             top -= pop ? 1 : 0;
             const double sv = stk[(pop ? 2 * top + 1 : 1) * LANES];
-            R = pop ? R - sv : R;
-            R = (f & FL_CARRY_IN) ? R - cr : R;
+            R = (f & FL_CARRY_IN) ? R - cr : R;   // the carried child first: the stacked one's
+            R = pop ? R - sv : R;                  // shared-memory load overlaps that subtraction
             reinterpret_cast<double *>(col + s * LANES)[0] = R;
             const double pr = R * T;
             if (f & FL_PD) {   // a parent above the static rows: its diagonal contribution
@@ -636,8 +636,8 @@ k_stack_mixed(DevView v, int tile0, int tile1, int cap, int nsteps, long long st
         auto fwd_static2 = [&](int s, double R, double T, int f) {
             const int sl = (f >> FL_SLOT_F) & 31;
             const double sv = stk[(2 * sl + 1) * LANES];
+            R = (f & FL_CARRY_IN) ? R - cr : R;   // (as in fwd_static1)
             R = (f & 1) ? R - sv : R;
-            R = (f & FL_CARRY_IN) ? R - cr : R;
             reinterpret_cast<double *>(col + s * LANES)[0] = R;
             const double pr = R * T;
             if (f & FL_PD) {   // a parent above the static rows: its diagonal contribution
