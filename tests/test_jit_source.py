@@ -43,6 +43,7 @@ def compile_sm103a(src, fp64_exact):
 
 def _models():
     yield "cables-uniform", configs.cables_replicated(4, gk_dend=36.0)[0]
+    yield "cables-passive", configs.cables_replicated(4, gk_dend=0.0)[0]   # static rows kept across steps
     yield "single-hsolve", [model.build(configs.cables(3, gk_dend=36.0, method=model.CRANK)[0])]
     yield "trees-ca", [model.build(m) for m in configs.random_trees(3, size_range=(12, 12), seed=4)]
     ms, _ = configs.hh_network(6, p_conn=0.5)
@@ -81,3 +82,16 @@ def test_shared_rows_form_keeps_rows_out_of_registers():
     assert "double D[16]" not in cols and "double T[16]" in cols
     assert "Dc[(15) * 32]" in cols and "Rc[480]" in cols
     assert "dynamic_smem_size" in cols and "dynamic_smem_size" not in regs
+
+
+@pytest.mark.parametrize("prec", [engine.PREC_FP64, engine.PREC_MIXED])
+def test_static_rows_only_where_rows_are_passive(prec):
+    """The unrolled register form keeps the factors of the passive rows below
+    the first compartment with channels: passive dendrites get the kept-factor
+    phase (15 of 16 rows), active dendrites and the looped forms do not."""
+    passive = configs.cables_replicated(4, gk_dend=0.0)[0]
+    active = configs.cables_replicated(4, gk_dend=36.0)[0]
+    src = engine.jit_source(passive, precision=prec, type_index=0, compact=0)
+    assert src.count("kept factors") == 15 and "v.tgen[t] = sgen" in src
+    for hs, compact in ((active, 0), (passive, 1), (passive, 2)):
+        assert "kept factors" not in engine.jit_source(hs, precision=prec, type_index=0, compact=compact)
