@@ -79,6 +79,7 @@ struct DevView {
     const int *ltop;
     double2 *col;
     double2 *kst;
+    double *kri;   // FP64 form: the static rows' correctly rounded 1/D'
     // stack tiles' kept factors: the fields' generation (bumped by state
     // writes) and, per tile, the generation its kst / col were kept at
     const unsigned *sgen;

@@ -130,6 +130,7 @@ struct gbh_engine {
     DBuf<int> d_ltop;              // stack elimination: per-row flags (topo rows)
     DBuf<double2> d_col;           // stack elimination: (rhs, diagonal) per row
     DBuf<double2> d_kst;           // stack elimination: static rows' (rhs term, coupling factor)
+    DBuf<double> d_kri;            // stack elimination, FP64 form: static rows' 1/D'
     DBuf<unsigned> d_sgen, d_tgen; // stack elimination: the fields' generation; each tile's kept one
     unsigned sgen_host = 1;
     std::vector<std::vector<char>> stack_dfield;   // per type: field rows that are a static row's diagonal term
@@ -1110,7 +1111,7 @@ int build_layout(gbh_engine *e, const gbh_batch_desc *d, const gbh_synapses *syn
     rc |= e->d_par.upload(par);
     rc |= e->d_ltop.upload(LT);
     if (any_stack) {
-        rc |= e->d_col.alloc(e->rows_topo * L) | e->d_kst.alloc(e->rows_topo * L);
+        rc |= e->d_col.alloc(e->rows_topo * L) | e->d_kst.alloc(e->rows_topo * L) | e->d_kri.alloc(e->rows_topo * L);
         rc |= e->d_sgen.upload(std::vector<unsigned>(1, e->sgen_host));
         rc |= e->d_tgen.upload(std::vector<unsigned>(std::max<size_t>(e->tiles.size(), 1), 0u));
         rc |= e->d_kref.upload(std::vector<int>(1, 0));
@@ -1320,6 +1321,7 @@ DevView view_of(gbh_engine *e)
     v.ltop = e->d_ltop.p;
     v.col = e->d_col.p;
     v.kst = e->d_kst.p;
+    v.kri = e->d_kri.p;
     v.sgen = e->d_sgen.p;
     v.tgen = e->d_tgen.p;
     v.kref = e->d_kref.p;
@@ -3187,7 +3189,7 @@ void gbh_destroy(gbh_engine *e)
     if (e->stream) cudaStreamSynchronize(e->stream);
     e->d_tiles.release(); e->d_types.release(); e->d_prog.release(); e->d_tgeom.release();
     e->d_tab64.release(); e->d_tab32.release(); e->d_tabdf.release(); e->d_xy.release(); e->d_P.release();
-    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_kst.release(); e->d_sgen.release(); e->d_tgen.release(); e->d_kref.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
+    e->d_V.release(); e->d_C.release(); e->d_F.release(); e->d_CR.release(); e->d_CD.release(); e->d_S.release(); e->d_wtop.release(); e->d_RV.release(); e->d_IT.release(); e->d_A.release(); e->d_B.release(); e->d_ltop.release(); e->d_col.release(); e->d_kst.release(); e->d_kri.release(); e->d_sgen.release(); e->d_tgen.release(); e->d_kref.release(); e->d_out_mword.release(); e->d_rmword.release(); e->d_out_mbit.release(); e->d_rmbit.release(); e->d_synw.release(); e->d_wval.release(); e->d_wmask.release(); e->d_spike_src.release();
     e->d_Cb.release(); e->d_giv.release(); e->d_stab.release(); e->d_I.release();
     e->d_par.release(); e->d_ring.release(); e->d_out_start.release(); e->d_out_base.release();
     e->d_out_delay.release(); e->d_spikes.release(); e->d_status.release();

@@ -531,6 +531,7 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
     const double *Cbw = v.Cb + tl.topo * LANES + lane;
     double2 *col = v.col + tl.topo * LANES + lane;
     double2 *kst = v.kst + tl.topo * LANES + lane;
+    double *kri = v.kri + tl.topo * LANES + lane;
     double *stk = sm + lane;      // entry j at stk[j * 32]
     double *rdb = sm + cap * LANES + lane;  // SPLIT: (R, D) of the rows above the static ones
     const int S = ty.nslots;
@@ -652,7 +653,10 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                     ++top;
                 }
             }
-            if (s < nst) kst[s * LANES] = make_double2(K, temp);
+            if (s < nst) {
+                kst[s * LANES] = make_double2(K, temp);
+                kri[s * LANES] = 1.0 / D;   // IEEE: the correctly rounded reciprocal
+            }
         };
         // the same for a static row on later steps: its diagonal and factor
         // are those of the first step, so only the rhs is eliminated (the
@@ -849,21 +853,32 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
         // from the parent's (the row after, or the branch point on the stack)
         // (selects and predicated stack accesses instead of branches)
         // (TileType::slots: the stack entries come with the flags)
-        auto bwd = [&](int s, int f, double2 rd, double c, double old) {
+        // A static row divides by its kept D' with the correctly rounded y =
+        // 1/D' (kri): q = RN(r y), e = r - D' q (exact, FMA), RN(q + e y) is
+        // RN(r / D') (Markstein's theorem: y within half an ulp of 1/D', q
+        // within an ulp of r / D'), so the quotient is the division's bits.
+        auto bwd = [&](int s, int f, double2 rd, double c, double old, bool stat, double y) {
             const bool xl = f & FL_XLOAD;
             const int rs = ty.slots ? (f >> FL_SLOT_R) & 31 : (xl ? top - 1 : 0);
             const double sv = stk[rs * LANES];
             const double xp = xl ? sv : xn;
             if (!ty.slots) top -= (f & FL_XPOP) ? 1 : 0;
             double r = (f & FL_PARENT) ? rd.x - c * xp : rd.x;
-            r = r / rd.y;
+            if (stat) {
+                const double q = r * y;
+                r = fma(fma(-rd.y, q, r), y, q);
+            } else {
+                r = r / rd.y;
+            }
             if (f & FL_XPUSH) stk[(ty.slots ? (f >> FL_SLOT_W) & 31 : top) * LANES] = r;
             if (!ty.slots) top += (f & FL_XPUSH) ? 1 : 0;
             xn = r;
             Vw[s * LANES] = ty.crank ? r + r - old : r;
         };
         int s1 = S - 1;
-        for (; s1 + 1 >= kCh; s1 -= kCh) {   // chunks: every row's loads, then the chain
+        // chunks: every row's loads, then the chain; the rows above the
+        // static ones first (IEEE division), then the static rows
+        for (; s1 + 1 - nst >= kCh; s1 -= kCh) {
             int f[kCh];
             double2 rd[kCh];
             double c[kCh], old[kCh];
@@ -876,10 +891,29 @@ k_stack(DevView v, int tile0, int tile1, int cap, int nsteps, long long step0)
                 old[k] = ty.crank ? Vw[s * LANES] : 0.0;
             }
 #pragma unroll
-            for (int k = 0; k < kCh; ++k) bwd(s1 - k, f[k], rd[k], c[k], old[k]);
+            for (int k = 0; k < kCh; ++k) bwd(s1 - k, f[k], rd[k], c[k], old[k], false, 0.0);
+        }
+        for (; s1 >= nst; --s1)
+            bwd(s1, lt[s1 * LANES], col[s1 * LANES], Cbw[s1 * LANES], ty.crank ? Vw[s1 * LANES] : 0.0, false, 0.0);
+        for (; s1 + 1 >= kCh; s1 -= kCh) {
+            int f[kCh];
+            double2 rd[kCh];
+            double c[kCh], old[kCh], y[kCh];
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) {
+                const int s = s1 - k;
+                f[k] = lt[s * LANES];
+                rd[k] = col[s * LANES];
+                c[k] = Cbw[s * LANES];
+                old[k] = ty.crank ? Vw[s * LANES] : 0.0;
+                y[k] = kri[s * LANES];
+            }
+#pragma unroll
+            for (int k = 0; k < kCh; ++k) bwd(s1 - k, f[k], rd[k], c[k], old[k], true, y[k]);
         }
         for (; s1 >= 0; --s1)
-            bwd(s1, lt[s1 * LANES], col[s1 * LANES], Cbw[s1 * LANES], ty.crank ? Vw[s1 * LANES] : 0.0);
+            bwd(s1, lt[s1 * LANES], col[s1 * LANES], Cbw[s1 * LANES], ty.crank ? Vw[s1 * LANES] : 0.0, true,
+                kri[s1 * LANES]);
         finite_check(v, xn, active);   // row 0's solution
         if (full && it == 0) {   // this tile's kept factors now match the fields
             __syncwarp();
