@@ -615,6 +615,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
             kf.push_back({a[1], a[2], a[6]});
         }
     }
+    if (nst > 0 && !mixed)   // FP64: the static rows' correctly rounded 1/D' (Markstein's division below)
+        o << "  double *kri = v.kri + tl.topo * 32 + lane;\n";
     if (nst > 0)
         o << "  double2 *kst = v.kst + tl.topo * 32 + lane; double2 *col = v.col + tl.topo * 32 + lane;\n"
           << "  const int kr = v.sgen ? *v.kref : 2; const unsigned sgen = v.sgen ? *v.sgen : 0u;\n"
@@ -655,7 +657,9 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 o << "    { // slot " << s << ": kept factors\n      const double Vm = Vw[" << ks << "];\n";
                 if (mixed) o << "      R[" << ss << "] = df2d(df_add(d2df(Vm), d2df(kst[" << ks << "].x)));\n";
                 else o << "      R[" << ss << "] = Vm + kst[" << ks << "].x;\n";
-                o << "      D[" << ss << "] = col[" << ks << "].y; T[" << ss << "] = kst[" << ks << "].y; }\n";
+                o << "      D[" << ss << "] = col[" << ks << "].y; T[" << ss << "] = kst[" << ks << "].y;";
+                if (!mixed) o << " Y[" << ss << "] = kri[" << ks << "];";
+                o << " }\n";
             } else if (!emit_slot(E, s, pc, tg)) {
                 return false;
             }
@@ -697,6 +701,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                     else el << " kst[" << ks << "].x = " << kexpr(s) << ";";
                     el << " kst[" << ks << "].y = " << (par[s] >= 0 ? "T[" + std::to_string(s) + "]" : std::string("0.0"))
                        << "; col[" << ks << "].y = D[" << s << "]; }";
+                    if (!mixed) el << " Y[" << s << "] = 1.0 / D[" << s << "]; kri[" << ks << "] = Y[" << s << "];";
                 }
                 el << " }\n";
                 pending.push_back(el.str());
@@ -713,6 +718,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     return true;
     };
     if (nst > 0) {
+        if (!mixed) o << "    double Y[" << nst << "];\n";
         o << "    const bool kfull = full && (it == 0 || kr > 1);\n    if (kfull) {\n";
         if (!emit_phase(false)) return std::string();
         o << "    } else {\n";
@@ -769,8 +775,15 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 if (mixed) t << " r = fma(-Cbw[" << s * LANES << "], " << Rx(p) << ", r);";
                 else t << " r -= Cbw[" << s * LANES << "] * " << Rx(p) << ";";
             }
-            if (mixed) t << " r = r * " << Dx(s) << ";";
-            else t << " r = r / " << Dx(s) << ";";
+            if (mixed) {
+                t << " r = r * " << Dx(s) << ";";
+            } else if (s < nst) {
+                // a static row: RN(r / D') from the correctly rounded y = 1/D'
+                // by Markstein's correction, the division's bits (one DMUL, two DFMAs)
+                t << " { const double q = r * Y[" << s << "]; r = fma(fma(-" << Dx(s) << ", q, r), Y[" << s << "], q); }";
+            } else {
+                t << " r = r / " << Dx(s) << ";";
+            }
             t << " " << Rx(s) << " = r;";
             if (tt.crank) {
                 if (mixed) t << " Vw[" << s * LANES << "] = fma(2.0, r, -Vw[" << s * LANES << "]);";
