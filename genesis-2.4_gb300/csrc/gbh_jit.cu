@@ -691,8 +691,13 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                 } else if (mixed) {
                     el << " const double ri = rcp_newton(D[" << s << "]); D[" << s << "] = ri;";
                     if (par[s] >= 0) el << " T[" << s << "] = Aw[" << s * LANES << "] * ri;";
-                } else if (par[s] >= 0) {
-                    el << " T[" << s << "] = Aw[" << s * LANES << "] / D[" << s << "];";
+                } else {
+                    // FP64: one correctly rounded y = 1/D' per row; T = A/D' and the back
+                    // substitution's quotient by Markstein's correction (the divisions' bits)
+                    el << " Y[" << s << "] = 1.0 / D[" << s << "];";
+                    if (par[s] >= 0)
+                        el << " { const double a = Aw[" << s * LANES << "], qa = a * Y[" << s << "]; T[" << s
+                           << "] = fma(fma(-D[" << s << "], qa, a), Y[" << s << "], qa); }";
                 }
                 if (!fast && kept) {   // keep K, T and D' (1/D')
                     const std::string ks = std::to_string(s * LANES);
@@ -701,7 +706,7 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
                     else el << " kst[" << ks << "].x = " << kexpr(s) << ";";
                     el << " kst[" << ks << "].y = " << (par[s] >= 0 ? "T[" + std::to_string(s) + "]" : std::string("0.0"))
                        << "; col[" << ks << "].y = D[" << s << "]; }";
-                    if (!mixed) el << " Y[" << s << "] = 1.0 / D[" << s << "]; kri[" << ks << "] = Y[" << s << "];";
+                    if (!mixed) el << " kri[" << ks << "] = Y[" << s << "];";
                 }
                 el << " }\n";
                 pending.push_back(el.str());
@@ -717,8 +722,8 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
     pending.clear();
     return true;
     };
+    if (uniform_parent && !mixed) o << "    double Y[" << S << "];\n";   // FP64: each row's 1/D'
     if (nst > 0) {
-        if (!mixed) o << "    double Y[" << nst << "];\n";
         o << "    const bool kfull = full && (it == 0 || kr > 1);\n    if (kfull) {\n";
         if (!emit_phase(false)) return std::string();
         o << "    } else {\n";
@@ -777,12 +782,10 @@ std::string jit_source(const TileType &tt, const std::vector<int> &prog, const T
             }
             if (mixed) {
                 t << " r = r * " << Dx(s) << ";";
-            } else if (s < nst) {
-                // a static row: RN(r / D') from the correctly rounded y = 1/D'
-                // by Markstein's correction, the division's bits (one DMUL, two DFMAs)
-                t << " { const double q = r * Y[" << s << "]; r = fma(fma(-" << Dx(s) << ", q, r), Y[" << s << "], q); }";
             } else {
-                t << " r = r / " << Dx(s) << ";";
+                // RN(r / D') from the correctly rounded y = 1/D' by Markstein's
+                // correction, the division's bits (one DMUL, two DFMAs)
+                t << " { const double q = r * Y[" << s << "]; r = fma(fma(-" << Dx(s) << ", q, r), Y[" << s << "], q); }";
             }
             t << " " << Rx(s) << " = r;";
             if (tt.crank) {
